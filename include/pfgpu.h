@@ -1,0 +1,210 @@
+/*
+ * pfgpu.h - C ABI of the GB300-native CNF inprocessing engine.
+ *
+ * This header is the drop-in boundary for ParaFROST's GPU simplify phase.
+ * The reference has no C ABI for this path: its boundary is the C++ member
+ * function `void Solver::simplify(const bool& skip_transfer_to_host)`
+ * (src/gpu/solver.hpp:772, src/gpu/simplify.cu:57) whose body
+ * (`Solver::simplifying`, src/gpu/simplify.cu:136-241) uploads the clause
+ * database (`awaken`, simplify.cu:77-134), runs the round loop
+ * (simplify.cu:163-186) and writes results back (simplify.cu:190-240).
+ * The entry points below replace that body; the host adapter that a
+ * maintainer drops into `Solver::simplifying` is shown in INTEGRATION.md.
+ *
+ * Conventions
+ *  - Literals use the reference's internal encoding: lit = 2*v | sign,
+ *    v in [1, max_var] (src/gpu/constants.hpp:72-80).
+ *  - The caller owns every host buffer; the engine owns all device memory
+ *    (it replaces cuMM/cuArena, src/gpu/memory.cuh:54-180).
+ *  - No entry point exits, traps or throws. Calls on one context must come
+ *    from one host thread; contexts are independent.
+ *  - Return codes mirror the reference's `simpstate` values
+ *    (src/gpu/constants.cuh:28-31) plus engine-specific codes.
+ */
+#ifndef PFGPU_H
+#define PFGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* return codes: 0..3 keep the reference's simpstate meaning */
+#define PFG_OK             0  /* AWAKEN_SUCC                                  */
+#define PFG_AWAKEN_FAIL    1  /* AWAKEN_FAIL  (device pool could not be made) */
+#define PFG_CNFALLOC_FAIL  2  /* CNFALLOC_FAIL (clause store does not fit)    */
+#define PFG_OTALLOC_FAIL   3  /* OTALLOC_FAIL  (occurrence table does not fit)*/
+#define PFG_TIMEOUT        4  /* a bounded device-side loop gave up           */
+#define PFG_INVALID        5  /* invalid argument or input                    */
+#define PFG_CUDA_ERROR     6  /* a CUDA runtime call failed                   */
+
+/* solver status after pfg_simplify (same values as the reference CLI/IPASIR) */
+#define PFG_UNKNOWN        0
+#define PFG_SAT           10  /* every clause was removed                       */
+#define PFG_UNSAT         20  /* device unit propagation found a conflict       */
+
+/*
+ * Simplifier options. Names in comments are the reference's CLI option names
+ * and defaults (src/gpu/options.cpp:24-43, src/gpu/options.cu:33-60); the
+ * folding rules of OPTION::init (options.cpp:274-299) are applied by
+ * pfg_resolve_options().
+ */
+typedef struct pfg_options {
+    int32_t  phases;          /* "phases"            5     */
+    int32_t  shrink_rate;     /* "collectfreq"       2     */
+    int32_t  lcve_fast;       /* "lcvefast"          1 (Luby MIS) */
+    uint32_t lcve_min_vars;   /* "electionsmin"      2     */
+    uint32_t lcve_max_occurs; /* "electionsmax"      3000  */
+    int32_t  lcve_clause_max; /* "lcveclausemax"     30000 */
+    uint32_t phase_lits_min;  /* "eliminatedlitsmin" 500   */
+    uint32_t mu_pos;          /* "mupos"             32    */
+    uint32_t mu_neg;          /* "muneg"             32    */
+    double   lits_mul;        /* "literalsmul"       1.0   */
+    uint8_t  ve_en;           /* "ve"                1     */
+    uint8_t  ve_plus_en;      /* "veextend"          1     */
+    uint8_t  sub_en;          /* "sub"               1     */
+    uint8_t  ere_en;          /* "ere"               1     */
+    uint8_t  bce_en;          /* "bce"               0 (not implemented: must be 0) */
+    uint8_t  all_en;          /* "all"               0     */
+    uint8_t  ve_fun_en;       /* "vefunction"        1     */
+    uint8_t  ve_lbound_en;    /* "velitsbound"       0     */
+    uint8_t  proof_en;        /* "proof"             0 (not implemented: must be 0) */
+    uint8_t  ve_inprocess;    /* 1 when Solver::stats.sigma.calls > 1: BVE counts only
+                                 original clauses (in_ve_k_1, bounded.cuh:397)       */
+    uint8_t  _pad[6];
+    uint32_t ve_clause_max;   /* "resolventmax"      100   */
+    uint32_t xor_max_arity;   /* "xormaxarity"       10    */
+    uint32_t sub_max_occurs;  /* "submaxoccurs"      3000  */
+    uint32_t ere_max_occurs;  /* "eremaxoccurs"      3000  */
+    uint32_t ere_clause_max;  /* "ereclausemax"      250 (clamped to 250)  */
+    uint32_t bce_max_occurs;  /* "bcemaxoccurs"      3000  */
+} pfg_options;
+
+/* Per-call statistics (the reference's stats.sigma / inf counters). */
+typedef struct pfg_stats {
+    int32_t  status;          /* PFG_UNKNOWN / PFG_SAT / PFG_UNSAT                 */
+    int32_t  rounds;          /* SUB+BVE rounds executed (reference `phase`)       */
+    int32_t  ere_ran;         /* 1 if the final ERE pass ran                       */
+    int32_t  simpstate;       /* reference simpstate at exit                       */
+    uint64_t clauses_in;      /* live clauses uploaded                              */
+    uint64_t literals_in;
+    uint64_t clauses_out;     /* live clauses after simplification                  */
+    uint64_t literals_out;
+    uint64_t clauses_processed; /* sum over rounds of live clauses entering SUB+BVE */
+    uint64_t literals_processed;
+    uint64_t eliminated;      /* variables eliminated (MELTING bit, not FORCED)     */
+    uint64_t forced;          /* variables assigned by device unit propagation      */
+    uint64_t resolvents;      /* clauses added by BVE                               */
+    uint64_t stack_words;     /* model-reconstruction words produced                */
+    double   device_ms;       /* cudaEvent time of all rounds (upload/download excluded) */
+    double   pass_ms[8];      /* per pass: ot, bcp, lcve, sub, ve, ere, gc/count, other */
+    uint64_t alg_bytes;       /* algorithmic bytes of all rounds (byte model in the design doc) */
+    uint64_t kernel_launches; /* kernels launched by pfg_simplify                   */
+} pfg_stats;
+
+/* Sizes of the results of the last pfg_simplify call. */
+typedef struct pfg_result_sizes {
+    uint64_t clauses;         /* live clauses in the simplified CNF                */
+    uint64_t literals;        /* their literals                                     */
+    uint64_t units;           /* units assigned on the device (set, sorted)         */
+    uint64_t pending_units;   /* units produced by the last round and not propagated */
+    uint64_t stack_words;     /* model-reconstruction stack words                   */
+    uint64_t rounds;          /* entries of round_ends                              */
+    uint32_t max_var;
+    uint32_t _pad;
+} pfg_result_sizes;
+
+typedef struct pfg_ctx pfg_ctx;
+
+/* Fill `o` with the reference defaults. */
+void pfg_default_options(pfg_options* o);
+
+/* Apply OPTION::init's folding rules (src/gpu/options.cpp:283-297). */
+void pfg_resolve_options(pfg_options* o);
+
+/*
+ * Create a context on the current CUDA device with a device pool of
+ * `arena_bytes` (0 = size it from the free device memory, as
+ * cuMM::initDeviceArena does, src/gpu/memory.cu:99-176).
+ * Replaces: Solver::optSimp + cuMM::init (simplify.cu:243, memory.cu:99).
+ */
+int  pfg_create(pfg_ctx** ctx, const pfg_options* opts, size_t arena_bytes);
+
+/*
+ * Upload one CNF instance (host buffers, internal literal encoding).
+ *   lits[cls_off[i] .. cls_off[i+1])  literals of clause i (any order, no duplicates,
+ *                                     size >= 2);
+ *   cls_learnt[i]  0 = original, 1 = learnt (nullable: all original)
+ *   cls_lbd[i], cls_usage[i]  learnt metadata (nullable)
+ *   var_state[v]   non-zero VSTATE.state excludes v from elections (nullable)
+ *   assumed[v]     non-zero excludes v from elections (nullable)
+ *   vorg[v]        original variable of v used in the model stack (nullable: identity)
+ * Clause order is preserved: originals are expected first, then learnts, as
+ * Solver::extractCNF appends them (simplify.cu:108-109, cnf.cu:176-184).
+ * Replaces: Solver::awaken (simplify.cu:77-134): extractCNF/reflectCNF and
+ * prepareCNFAsync (cnf.cu:108).
+ */
+int  pfg_upload(pfg_ctx* ctx, uint32_t max_var, uint64_t num_clauses,
+                const uint32_t* lits, const uint64_t* cls_off,
+                const uint8_t* cls_learnt, const uint32_t* cls_lbd,
+                const uint8_t* cls_usage, const uint8_t* var_state,
+                const uint8_t* assumed, const uint32_t* vorg);
+
+/*
+ * Run simplification rounds until the reference's stop rule
+ * (Solver::stop, solver.hpp:748-753).
+ * Replaces: the round loop of Solver::simplifying (simplify.cu:159-186).
+ */
+int  pfg_simplify(pfg_ctx* ctx, pfg_stats* stats);
+
+/* Sizes needed by pfg_download. */
+int  pfg_result_sizes_get(pfg_ctx* ctx, pfg_result_sizes* sizes);
+
+/*
+ * Copy results to host buffers sized by pfg_result_sizes_get (any pointer
+ * may be NULL to skip that item).
+ *   lits/cls_off/cls_learnt/cls_lbd/cls_usage: simplified CNF in clause order
+ *       (Solver::cacheCNF, cnf.cu:200-236)
+ *   eliminated[max_var+1]: MELTING 0x1 | ADDING 0x2 | FORCED 0x4 bytes
+ *       (Solver::cacheEliminated, transfer.cu:69)
+ *   units: literals assigned by device propagation, sorted ascending
+ *       (what Solver::prop enqueues on the host trail, elimbcp.cu:193-203)
+ *   pending_units: units produced in the last round that no later round
+ *       propagated (the reference leaves them in vars->units)
+ *   stack: model-reconstruction words [lit_w, l2..lk, k]* [w, 1] in original
+ *       variable numbering (Solver::cacheResolved, transfer.cu:83)
+ *   round_ends[r]: stack length after round r
+ */
+int  pfg_download(pfg_ctx* ctx, uint32_t* lits, uint64_t* cls_off,
+                  uint8_t* cls_learnt, uint32_t* cls_lbd, uint8_t* cls_usage,
+                  uint8_t* eliminated, uint32_t* units, uint32_t* pending_units,
+                  uint32_t* stack, uint64_t* round_ends);
+
+/* Release all device memory of the context. Replaces Solver::freeSimp (simplify.cu:254). */
+void pfg_destroy(pfg_ctx* ctx);
+
+/* Last CUDA or engine error message of the context (never NULL). */
+const char* pfg_last_error(pfg_ctx* ctx);
+
+/* Number of this library's kernels launched since the context was created. */
+uint64_t pfg_kernel_launches(pfg_ctx* ctx);
+
+/*
+ * Host-side synthetic CNF generators (the seeded families used by the
+ * benchmark and the tests). They write into caller buffers; call once with
+ * lits == NULL to get the sizes.
+ *   family 0: uniform random k-SAT   (a = vars, b = clauses, c = k)
+ *   family 1: Tseitin circuit        (a = gates, b = primary inputs, c = outputs)
+ *   family 2: scale-free CNF         (a = vars, b = clauses, c unused)
+ */
+int  pfg_generate(int family, uint64_t a, uint64_t b, uint64_t c, uint64_t seed,
+                  uint32_t* max_var, uint64_t* num_clauses, uint64_t* num_lits,
+                  uint32_t* lits, uint64_t* cls_off);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFGPU_H */

@@ -1,0 +1,61 @@
+"""Loader of the engine library `libpfgpu.so` (ctypes, C ABI of include/pfgpu.h).
+
+The library is built in-tree by `parafrost_gb300.build`; there is no other
+implementation to fall back to, so a missing or broken library raises.
+"""
+import ctypes as C
+import os
+
+from ._abi import PfgOptions, PfgResultSizes, PfgStats
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpfgpu.so")
+_lib = None
+
+u8p = C.POINTER(C.c_uint8)
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build the CUDA engine first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    L = C.CDLL(LIB_PATH)
+    L.pfg_default_options.argtypes = [C.POINTER(PfgOptions)]
+    L.pfg_default_options.restype = None
+    L.pfg_resolve_options.argtypes = [C.POINTER(PfgOptions)]
+    L.pfg_resolve_options.restype = None
+    L.pfg_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(PfgOptions), C.c_size_t]
+    L.pfg_create.restype = C.c_int
+    L.pfg_upload.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, u32p, u64p, u8p, u32p, u8p, u8p, u8p, u32p]
+    L.pfg_upload.restype = C.c_int
+    L.pfg_simplify.argtypes = [C.c_void_p, C.POINTER(PfgStats)]
+    L.pfg_simplify.restype = C.c_int
+    L.pfg_result_sizes_get.argtypes = [C.c_void_p, C.POINTER(PfgResultSizes)]
+    L.pfg_result_sizes_get.restype = C.c_int
+    L.pfg_download.argtypes = [C.c_void_p, u32p, u64p, u8p, u32p, u8p, u8p, u32p, u32p, u32p, u64p]
+    L.pfg_download.restype = C.c_int
+    L.pfg_destroy.argtypes = [C.c_void_p]
+    L.pfg_destroy.restype = None
+    L.pfg_last_error.argtypes = [C.c_void_p]
+    L.pfg_last_error.restype = C.c_char_p
+    L.pfg_kernel_launches.argtypes = [C.c_void_p]
+    L.pfg_kernel_launches.restype = C.c_uint64
+    L.pfg_generate.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64,
+                               u32p, u64p, u64p, u32p, u64p]
+    L.pfg_generate.restype = C.c_int
+    _lib = L
+    return L
+
+
+# C-ABI entry points declared in include/pfgpu.h (checked by the CPU tests)
+EXPORTED = (
+    "pfg_default_options", "pfg_resolve_options", "pfg_create", "pfg_upload", "pfg_simplify",
+    "pfg_result_sizes_get", "pfg_download", "pfg_destroy", "pfg_last_error", "pfg_kernel_launches",
+    "pfg_generate",
+)

@@ -1,0 +1,141 @@
+"""CNF containers, DIMACS I/O and the seeded instance generators.
+
+Literals use the reference's internal encoding lit = 2*v | sign
+(src/gpu/constants.hpp:72-80); clauses are stored flat with uint64 offsets.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Iterable, List, Optional
+
+import numpy as np
+
+from . import _lib
+
+FAMILY_KSAT = 0
+FAMILY_TSEITIN = 1
+FAMILY_SCALEFREE = 2
+
+
+@dataclass
+class Cnf:
+    max_var: int
+    lits: np.ndarray                      # uint32, internal literals
+    off: np.ndarray                       # uint64, num_clauses + 1
+    learnt: Optional[np.ndarray] = None   # uint8 per clause (1 = learnt)
+    lbd: Optional[np.ndarray] = None      # uint32 per clause
+    usage: Optional[np.ndarray] = None    # uint8 per clause
+
+    def __post_init__(self):
+        self.lits = np.ascontiguousarray(self.lits, dtype=np.uint32)
+        self.off = np.ascontiguousarray(self.off, dtype=np.uint64)
+        if self.learnt is not None:
+            self.learnt = np.ascontiguousarray(self.learnt, dtype=np.uint8)
+        if self.lbd is not None:
+            self.lbd = np.ascontiguousarray(self.lbd, dtype=np.uint32)
+        if self.usage is not None:
+            self.usage = np.ascontiguousarray(self.usage, dtype=np.uint8)
+
+    @property
+    def num_clauses(self) -> int:
+        return len(self.off) - 1
+
+    @property
+    def num_literals(self) -> int:
+        return int(self.off[-1]) if len(self.off) else 0
+
+    def clause(self, i: int) -> np.ndarray:
+        return self.lits[int(self.off[i]):int(self.off[i + 1])]
+
+    def clauses(self) -> List[List[int]]:
+        """Clauses as lists of DIMACS integers."""
+        out = []
+        for i in range(self.num_clauses):
+            out.append([lit_to_int(int(l)) for l in self.clause(i)])
+        return out
+
+    @staticmethod
+    def from_ints(max_var: int, clauses: Iterable[Iterable[int]], learnt: Optional[Iterable[int]] = None) -> "Cnf":
+        lits, off = [], [0]
+        for c in clauses:
+            for x in c:
+                lits.append(int_to_lit(int(x)))
+            off.append(len(lits))
+        lr = None if learnt is None else np.asarray(list(learnt), dtype=np.uint8)
+        return Cnf(max_var, np.asarray(lits, dtype=np.uint32), np.asarray(off, dtype=np.uint64), lr)
+
+
+def int_to_lit(x: int) -> int:
+    return (abs(x) << 1) | (1 if x < 0 else 0)
+
+
+def lit_to_int(lit: int) -> int:
+    v = lit >> 1
+    return -v if lit & 1 else v
+
+
+def generate(family: int, a: int, b: int, c: int, seed: int) -> Cnf:
+    """Seeded instance from the engine's C generators (pfg_generate)."""
+    lib = _lib.lib()
+    mv = C.c_uint32()
+    nc = C.c_uint64()
+    nl = C.c_uint64()
+    rc = lib.pfg_generate(family, a, b, c, seed, C.byref(mv), C.byref(nc), C.byref(nl), None, None)
+    if rc != 0:
+        raise ValueError(f"pfg_generate failed ({rc})")
+    lits = np.empty(nl.value, dtype=np.uint32)
+    off = np.empty(nc.value + 1, dtype=np.uint64)
+    rc = lib.pfg_generate(family, a, b, c, seed, None, None, None,
+                          lits.ctypes.data_as(C.POINTER(C.c_uint32)), off.ctypes.data_as(C.POINTER(C.c_uint64)))
+    if rc != 0:
+        raise ValueError(f"pfg_generate failed ({rc})")
+    return Cnf(int(mv.value), lits, off)
+
+
+def random_ksat(num_vars: int, num_clauses: int, k: int = 3, seed: int = 1) -> Cnf:
+    return generate(FAMILY_KSAT, num_vars, num_clauses, k, seed)
+
+
+def tseitin(gates: int, inputs: int, outputs: int, seed: int = 1) -> Cnf:
+    return generate(FAMILY_TSEITIN, gates, inputs, outputs, seed)
+
+
+def scale_free(num_vars: int, num_clauses: int, seed: int = 1) -> Cnf:
+    return generate(FAMILY_SCALEFREE, num_vars, num_clauses, 0, seed)
+
+
+def write_dimacs(cnf: Cnf, path: str, extra_units: Iterable[int] = ()) -> None:
+    units = list(extra_units)
+    with open(path, "w") as f:
+        f.write(f"p cnf {cnf.max_var} {cnf.num_clauses + len(units)}\n")
+        lits = cnf.lits
+        off = cnf.off
+        ints = np.where(lits & 1, -(lits >> 1).astype(np.int64), (lits >> 1).astype(np.int64))
+        for i in range(cnf.num_clauses):
+            f.write(" ".join(map(str, ints[int(off[i]):int(off[i + 1])].tolist())) + " 0\n")
+        for u in units:
+            f.write(f"{u} 0\n")
+
+
+def read_dimacs(path: str) -> Cnf:
+    max_var = 0
+    clauses = []
+    cur = []
+    with open(path) as f:
+        for line in f:
+            line = line.strip()
+            if not line or line[0] in "c%":
+                continue
+            if line[0] == "p":
+                max_var = int(line.split()[2])
+                continue
+            for tok in line.split():
+                x = int(tok)
+                if x == 0:
+                    clauses.append(cur)
+                    cur = []
+                else:
+                    cur.append(x)
+                    max_var = max(max_var, abs(x))
+    return Cnf.from_ints(max_var, clauses)

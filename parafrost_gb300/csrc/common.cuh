@@ -1,0 +1,99 @@
+// Shared device definitions of the GB300 CNF inprocessing engine.
+//
+// Clause store (structure of arrays, replaces SCLAUSE + S_REF, src/gpu/sclause.cuh:37,
+// src/gpu/cnf.cuh:35):
+//   ClsHdr hdr[c]  = {off, size, sig, meta}: one 16-byte vector load per clause
+//   lits[off .. off+size)  literals 2v|s, ascending inside a clause
+// meta packs the reference's header bits: status (2), molten (1), added (1),
+// usage (2), lbd (26).
+// Clause ids follow the reference's ref order (upload order, then resolvents in
+// elected order), so every ordering tie-break of the reference holds.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define PFG_HD __host__ __device__ __forceinline__
+#define PFG_D __device__ __forceinline__
+
+namespace pfg {
+
+// clause status (src/gpu/constants.hpp:69-71)
+constexpr uint32_t ST_ORIGINAL = 0u;
+constexpr uint32_t ST_LEARNT = 1u;
+constexpr uint32_t ST_DELETED = 2u;
+// eliminated-variable bits (src/gpu/constants.cuh:34-36)
+constexpr uint8_t MELTING_MASK = 0x01u;
+constexpr uint8_t ADDING_MASK = 0x02u;
+constexpr uint8_t FORCED_MASK = 0x04u;
+// BVE type word (src/gpu/constants.cuh:38-63)
+constexpr uint32_t RES_MASK = 1u;
+constexpr uint32_t AOIX_MASK = 2u;
+constexpr uint32_t CORE_MASK = 3u;
+constexpr uint32_t ADDEDCLS_MAX = 0x3FFFu;
+constexpr uint32_t ADDEDLITS_MAX = 0xFFFFu;
+// reference arena accounting: a clause occupies 3 header buckets + its literals
+constexpr uint32_t NBUCKETS = 3u;
+// kernel limits of an EXTSHMEM build (the reference's install.sh enables it on cc >= 7)
+constexpr uint32_t SH_MAX_BVE_OUT1 = 250u;
+constexpr uint32_t SH_MAX_ERE_OUT = 250u;
+constexpr uint32_t SUB_MAX_CL_SIZE = 1000u;
+constexpr uint32_t LBD_TIER1 = 2u;
+constexpr uint32_t USAGET3 = 1u;
+constexpr uint32_t NOREF = 0xFFFFFFFFu;
+constexpr uint32_t ERE_LANES = 32u;  // blockDim.x of the reference's ere_k
+
+struct __align__(16) ClsHdr {
+    uint32_t off;
+    uint32_t size;
+    uint32_t sig;
+    uint32_t meta;
+};
+
+PFG_HD uint32_t m_st(uint32_t m) { return m & 3u; }
+PFG_HD bool m_orig(uint32_t m) { return (m & 3u) == ST_ORIGINAL; }
+PFG_HD bool m_learnt(uint32_t m) { return (m & ST_LEARNT) != 0; }
+PFG_HD bool m_deleted(uint32_t m) { return (m & ST_DELETED) != 0; }
+PFG_HD bool m_molten(uint32_t m) { return (m >> 2) & 1u; }
+PFG_HD uint32_t m_usage(uint32_t m) { return (m >> 4) & 3u; }
+PFG_HD uint32_t m_lbd(uint32_t m) { return m >> 6; }
+PFG_HD uint32_t m_make(uint32_t st, uint32_t molten, uint32_t added, uint32_t usage, uint32_t lbd) {
+    return st | (molten << 2) | (added << 3) | (usage << 4) | (lbd << 6);
+}
+PFG_HD uint32_t m_set_st(uint32_t m, uint32_t st) { return (m & ~3u) | st; }
+PFG_HD uint32_t m_set_molten(uint32_t m, uint32_t f) { return (m & ~4u) | (f << 2); }
+
+PFG_HD uint32_t ABSV(uint32_t l) { return l >> 1; }
+PFG_HD uint32_t SIGNL(uint32_t l) { return l & 1u; }
+PFG_HD uint32_t FLIPL(uint32_t l) { return l ^ 1u; }
+PFG_HD uint32_t MAPHASH(uint32_t l) { return 1u << (l & 31u); }
+PFG_HD bool SUBSIG(uint32_t a, uint32_t b) { return !(a & ~b); }
+
+// Device counters shared between kernels and the host (one pinned mirror).
+struct DevCounters {
+    unsigned long long nstack;     // model-stack words
+    unsigned long long live_cls;   // live clauses (count kernel)
+    unsigned long long live_lits;
+    unsigned long long err_info;   // first error detail
+    uint32_t nunits;               // vars->units size
+    uint32_t err;                  // error flags (ERR_*)
+    uint32_t nwork;                // MIS worklist size
+    uint32_t nwin;                 // winners in the current MIS round
+    uint32_t nelected;
+    uint32_t nfrozen;
+    uint32_t conflict;             // BCP conflict flag
+    uint32_t bcp_curr, bcp_next, bcp_level;
+    uint32_t ntrail;
+    int32_t last_elim;             // lastEliminatedID
+    uint32_t survivors;
+    uint32_t big_lists;
+    uint32_t pad[3];
+};
+
+constexpr uint32_t ERR_UNITS_OVERFLOW = 1u;
+constexpr uint32_t ERR_STACK_OVERFLOW = 2u;
+constexpr uint32_t ERR_SLOT_MISMATCH = 4u;
+constexpr uint32_t ERR_BAD_LIT = 8u;
+constexpr uint32_t ERR_OT_OVERFLOW = 16u;
+
+}  // namespace pfg

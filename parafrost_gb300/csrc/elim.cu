@@ -1,0 +1,1102 @@
+// Per-variable elimination passes: SUB (+ self-subsuming strengthening),
+// BVE phase 1 (gate detection + resolvent counting), BVE phase 3 (resolvent
+// emission into prefix-summed slots) and ERE.
+//
+// Elected variables share no clause (LCVE freezes every neighbour), so each
+// thread owns the clauses of its variable; reads of neighbouring occurrence
+// lists never match a clause that another thread is changing. The
+// per-variable semantics follow the reference kernels:
+//   sub_k        src/gpu/subsume.cuh:402-484
+//   ve_k_1       src/gpu/bounded.cuh:282-473 (+ and/xor/ifthenelse/function/equivalence.cuh)
+//   ve_k_2       src/gpu/bounded.cuh:69-258, 488-544
+//   ere_k        src/gpu/redundancy.cuh:27-175
+#include "engine.cuh"
+
+namespace pfg {
+namespace {
+
+struct EK {
+    ClsHdr* hdr;
+    uint32_t* lits;
+    const uint32_t* ot_off;
+    uint32_t* ot_size;
+    uint32_t* ot_ids;
+    uint8_t* elim;
+    const uint32_t* varcore;
+    int varcore_on;
+    const uint32_t* vorg;
+    uint32_t* units;
+    uint32_t units_cap;
+    uint32_t* stack;
+    unsigned long long stack_cap;
+    DevCounters* dc;
+    uint32_t ve_clause_max, xor_max_arity, sub_max_occurs, ere_max_occurs, ere_clause_max;
+    int ve_lbound_en, ve_inprocess;
+};
+
+PFG_D uint32_t* OLp(const EK& k, uint32_t lit) { return k.ot_ids + k.ot_off[lit]; }
+PFG_D uint32_t OLs(const EK& k, uint32_t lit) { return k.ot_size[lit]; }
+PFG_D uint32_t* CLp(const EK& k, uint32_t c) { return k.lits + k.hdr[c].off; }
+PFG_D uint32_t META(const EK& k, uint32_t c) { return k.hdr[c].meta; }
+PFG_D uint32_t SIZE(const EK& k, uint32_t c) { return k.hdr[c].size; }
+PFG_D void SET_MOLTEN(const EK& k, uint32_t c, uint32_t f) { k.hdr[c].meta = m_set_molten(k.hdr[c].meta, f); }
+PFG_D void SET_DELETED(const EK& k, uint32_t c) { k.hdr[c].meta = m_set_st(k.hdr[c].meta, ST_DELETED); }
+
+PFG_D void push_unit(const EK& k, uint32_t lit) {
+    const uint32_t i = atomicAdd(&k.dc->nunits, 1u);
+    if (i < k.units_cap) k.units[i] = lit;
+    else atomicOr(&k.dc->err, ERR_UNITS_OVERFLOW);
+}
+
+PFG_D void sort_small(uint32_t* d, uint32_t n) {
+    for (uint32_t i = 1; i < n; i++) {
+        const uint32_t t = d[i];
+        uint32_t j = i;
+        while (j > 0 && t < d[j - 1]) { d[j] = d[j - 1]; j--; }
+        d[j] = t;
+    }
+}
+
+PFG_D void calc_sig(const EK& k, uint32_t c) {   // calcSig(SCLAUSE&): only for size > 1
+    const uint32_t sz = SIZE(k, c);
+    if (sz <= 1) return;
+    const uint32_t* l = CLp(k, c);
+    uint32_t s = 0;
+    for (uint32_t i = 0; i < sz; i++) s |= MAPHASH(l[i]);
+    k.hdr[c].sig = s;
+}
+
+PFG_D bool selfsub_sig(uint32_t A, uint32_t B) {
+    const uint32_t Bt = B | ((B & 0xAAAAAAAAu) >> 1) | ((B & 0x55555555u) << 1);
+    return !(A & ~Bt);
+}
+
+PFG_D void freeze_binaries(const EK& k, uint32_t lit) {
+    const uint32_t* ol = OLp(k, lit);
+    const uint32_t n = OLs(k, lit);
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t c = ol[i];
+        const ClsHdr h = k.hdr[c];
+        if (m_orig(h.meta) && h.size == 2) SET_MOLTEN(k, c, 0);
+    }
+}
+
+PFG_D void freeze_clauses(const EK& k, uint32_t p, uint32_t n) {
+    for (int s = 0; s < 2; s++) {
+        const uint32_t lit = s ? n : p;
+        const uint32_t* ol = OLp(k, lit);
+        const uint32_t sz = OLs(k, lit);
+        for (uint32_t i = 0; i < sz; i++) {
+            const uint32_t m = META(k, ol[i]);
+            if (m_orig(m) && m_molten(m)) SET_MOLTEN(k, ol[i], 0);
+        }
+    }
+}
+
+PFG_D void append_units(const EK& k, uint32_t lit) {
+    const uint32_t* ol = OLp(k, lit);
+    const uint32_t n = OLs(k, lit);
+    for (uint32_t i = 0; i < n; i++) {
+        const ClsHdr h = k.hdr[ol[i]];
+        if (h.size == 1) push_unit(k, k.lits[h.off]);
+    }
+}
+
+PFG_D bool is_equal(const EK& k, uint32_t c, const uint32_t* d, uint32_t n) {
+    const uint32_t* l = CLp(k, c);
+    for (uint32_t i = 0; i < n; i++) if (l[i] != d[i]) return false;
+    return true;
+}
+
+// merge(x, c1, c2, unit) counting version (elimination.cuh:242-270)
+PFG_D int merge_cnt(const EK& k, uint32_t x, uint32_t c1, uint32_t c2, uint32_t& unit) {
+    const ClsHdr h1 = k.hdr[c1], h2 = k.hdr[c2];
+    const uint32_t* a = k.lits + h1.off;
+    const uint32_t* b = k.lits + h2.off;
+    const int n1 = (int)h1.size, n2 = (int)h2.size;
+    int i = 0, j = 0, len = n1 + n2 - 2;
+    unit = 0;
+    while (i < n1 && j < n2) {
+        const uint32_t l1 = a[i], l2 = b[j], v1 = ABSV(l1), v2 = ABSV(l2);
+        if (v1 == x) i++;
+        else if (v2 == x) j++;
+        else if ((l1 ^ l2) == 1u) return 0;
+        else if (v1 < v2) i++;
+        else if (v2 < v1) j++;
+        else { i++; j++; len--; if (len == 1) unit = l1; }
+    }
+    return len;
+}
+
+// merge(x, c1, c2, out_c) (elimination.cuh:302-331)
+PFG_D int merge_out(const EK& k, uint32_t x, uint32_t c1, uint32_t c2, uint32_t* out) {
+    const ClsHdr h1 = k.hdr[c1], h2 = k.hdr[c2];
+    const uint32_t* a = k.lits + h1.off;
+    const uint32_t* b = k.lits + h2.off;
+    const int n1 = (int)h1.size, n2 = (int)h2.size;
+    int i = 0, j = 0, len = 0;
+    while (i < n1 && j < n2) {
+        const uint32_t l1 = a[i], l2 = b[j], v1 = ABSV(l1), v2 = ABSV(l2);
+        if (v1 == x) i++;
+        else if (v2 == x) j++;
+        else if ((l1 ^ l2) == 1u) return 0;
+        else if (v1 < v2) { i++; out[len++] = l1; }
+        else if (v2 < v1) { j++; out[len++] = l2; }
+        else { i++; j++; out[len++] = l1; }
+    }
+    while (i < n1) { const uint32_t l1 = a[i++]; if (ABSV(l1) != x) out[len++] = l1; }
+    while (j < n2) { const uint32_t l2 = b[j++]; if (ABSV(l2) != x) out[len++] = l2; }
+    return len;
+}
+
+PFG_D uint32_t count_lits_before(const EK& k, uint32_t lit) {
+    const uint32_t* ol = OLp(k, lit);
+    const uint32_t n = OLs(k, lit);
+    uint32_t s = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const ClsHdr h = k.hdr[ol[i]];
+        if (m_orig(h.meta)) s += h.size;
+    }
+    return s;
+}
+
+constexpr int PAIR_RES = 0, PAIR_SUBS = 1, PAIR_CORE = 2;
+
+PFG_D bool pair_ok(int kind, uint32_t mi, uint32_t mj) {
+    if (kind == PAIR_RES) return !m_learnt(mj);
+    if (kind == PAIR_SUBS) return m_orig(mj) && (m_molten(mi) != m_molten(mj));
+    return m_orig(mj) && (!m_molten(mi) || !m_molten(mj));
+}
+
+// countSubstituted / countCoreSubstituted: true = cannot substitute
+PFG_D bool count_subst(const EK& k, int kind, uint32_t x, uint32_t nClsBefore, uint32_t me, uint32_t other,
+                       uint32_t& nE, uint32_t& nC, uint32_t& nL) {
+    const int rlimit = (int)k.ve_clause_max;
+    const uint32_t* ml = OLp(k, me);
+    const uint32_t* ot = OLp(k, other);
+    const uint32_t ms = OLs(k, me), os = OLs(k, other);
+    for (uint32_t i = 0; i < ms; i++) {
+        const uint32_t ci = ml[i];
+        const uint32_t mi = META(k, ci);
+        if (m_learnt(mi)) continue;
+        for (uint32_t j = 0; j < os; j++) {
+            const uint32_t cj = ot[j];
+            if (!pair_ok(kind, mi, META(k, cj))) continue;
+            uint32_t u;
+            const int rsize = merge_cnt(k, x, ci, cj, u);
+            if (rsize == 1) nE++;
+            else if (rsize) {
+                if (++nC > nClsBefore || (rlimit && rsize > rlimit)) return true;
+                nL += (uint32_t)rsize;
+            }
+        }
+    }
+    if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return true;
+    if (k.ve_lbound_en) {
+        const uint32_t before = count_lits_before(k, me) + count_lits_before(k, other);
+        if (nL > before) return true;
+    }
+    return false;
+}
+
+// countResolvents, unbounded (resolve.cuh:28-109): true = can resolve
+PFG_D bool count_res_unbounded(const EK& k, uint32_t x, uint32_t me, uint32_t other, uint32_t& nE, uint32_t& nC,
+                               uint32_t& nL) {
+    const int rlimit = (int)k.ve_clause_max;
+    const uint32_t* ml = OLp(k, me);
+    const uint32_t* ot = OLp(k, other);
+    const uint32_t ms = OLs(k, me), os = OLs(k, other);
+    for (uint32_t i = 0; i < ms; i++) {
+        const uint32_t ci = ml[i];
+        if (m_learnt(META(k, ci))) continue;
+        for (uint32_t j = 0; j < os; j++) {
+            const uint32_t cj = ot[j];
+            if (m_learnt(META(k, cj))) continue;
+            uint32_t u;
+            const int rsize = merge_cnt(k, x, ci, cj, u);
+            if (rsize == 1) nE++;
+            else if (rsize) {
+                if (rlimit && rsize > rlimit) return false;
+                ++nC;
+                nL += (uint32_t)rsize;
+            }
+        }
+    }
+    if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return false;
+    return true;
+}
+
+// countResolvents, bounded (resolve.cuh:111-198): true = can resolve
+PFG_D bool count_res_bounded(const EK& k, uint32_t x, uint32_t nClsBefore, uint32_t me, uint32_t other,
+                             uint32_t& nE, uint32_t& nC, uint32_t& nL) {
+    nE = 0; nC = 0; nL = 0;
+    const int rlimit = (int)k.ve_clause_max;
+    const uint32_t* ml = OLp(k, me);
+    const uint32_t* ot = OLp(k, other);
+    const uint32_t ms = OLs(k, me), os = OLs(k, other);
+    for (uint32_t i = 0; i < ms; i++) {
+        const uint32_t ci = ml[i];
+        if (m_learnt(META(k, ci))) continue;
+        for (uint32_t j = 0; j < os; j++) {
+            const uint32_t cj = ot[j];
+            if (m_learnt(META(k, cj))) continue;
+            uint32_t u;
+            const int rsize = merge_cnt(k, x, ci, cj, u);
+            if (rsize == 1) nE++;
+            else if (rsize) {
+                if (++nC > nClsBefore || (rlimit && rsize > rlimit)) return false;
+                nL += (uint32_t)rsize;
+            }
+        }
+    }
+    if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return false;
+    if (k.ve_lbound_en) {
+        const uint32_t before = count_lits_before(k, me) + count_lits_before(k, other);
+        if (nL > before) return false;
+    }
+    return true;
+}
+
+// ---- model stack (model.cuh:29-49) ----
+PFG_D uint32_t org_lit(const EK& k, uint32_t lit) { return (k.vorg[ABSV(lit)] << 1) | SIGNL(lit); }
+
+// original clauses of `side` (witness literal first) followed by [w, 1]
+PFG_D void save_side(const EK& k, uint32_t side, uint32_t witlit, uint32_t w) {
+    const uint32_t* ol = OLp(k, side);
+    const uint32_t n = OLs(k, side);
+    unsigned long long words = 2;
+    for (uint32_t i = 0; i < n; i++) {
+        const ClsHdr h = k.hdr[ol[i]];
+        if (m_orig(h.meta)) words += h.size + 1ull;
+    }
+    const unsigned long long base = atomicAdd(&k.dc->nstack, words);
+    if (base + words > k.stack_cap) { atomicOr(&k.dc->err, ERR_STACK_OVERFLOW); return; }
+    uint32_t* s = k.stack + base;
+    for (uint32_t i = 0; i < n; i++) {
+        const ClsHdr h = k.hdr[ol[i]];
+        if (!m_orig(h.meta)) continue;
+        const uint32_t* l = k.lits + h.off;
+        uint32_t wpos = 0;
+        for (uint32_t t = 0; t < h.size; t++) {
+            if (l[t] == witlit) wpos = t;
+            s[t] = org_lit(k, l[t]);
+        }
+        if (wpos) { const uint32_t tmp = s[0]; s[0] = s[wpos]; s[wpos] = tmp; }
+        s[h.size] = h.size;
+        s += h.size + 1;
+    }
+    s[0] = org_lit(k, w);
+    s[1] = 1;
+}
+
+PFG_D void save_resolved_orgs(const EK& k, uint32_t p, uint32_t n, uint32_t pOrgs, uint32_t nOrgs) {
+    if (pOrgs > nOrgs) save_side(k, n, n, p);
+    else save_side(k, p, p, n);
+}
+
+PFG_D void save_resolved_lists(const EK& k, uint32_t p, uint32_t n) {
+    if (OLs(k, p) > OLs(k, n)) save_side(k, n, n, p);
+    else save_side(k, p, p, n);
+}
+
+PFG_D void delete_list(const EK& k, uint32_t lit) {
+    const uint32_t* ol = OLp(k, lit);
+    const uint32_t n = OLs(k, lit);
+    for (uint32_t i = 0; i < n; i++) SET_DELETED(k, ol[i]);
+}
+
+PFG_D void toblivion(const EK& k, uint32_t p, uint32_t n) {
+    delete_list(k, p);
+    delete_list(k, n);
+    k.ot_size[p] = 0;
+    k.ot_size[n] = 0;
+}
+
+// ---- gates ----
+PFG_D int find_fanin(const EK& k, uint32_t gate_out, uint32_t* out, uint32_t& sig) {
+    sig = 0;
+    int nImps = 0;
+    const uint32_t* ol = OLp(k, gate_out);
+    const uint32_t n = OLs(k, gate_out);
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t c = ol[i];
+        const ClsHdr h = k.hdr[c];
+        if (m_orig(h.meta) && h.size == 2) {
+            const uint32_t* l = k.lits + h.off;
+            const uint32_t imp = FLIPL(l[0] ^ l[1] ^ gate_out);
+            out[nImps++] = imp;
+            sig |= MAPHASH(imp);
+            SET_MOLTEN(k, c, 1);
+        }
+    }
+    return nImps;
+}
+
+// find_ao_gate (and.cuh:46-113)
+PFG_D bool find_ao_gate(const EK& k, uint32_t dx, uint32_t fx, uint32_t nOrgCls, uint32_t* out, uint32_t& nE,
+                        uint32_t& nC, uint32_t& nL) {
+    const uint32_t* dl = OLp(k, dx);
+    const uint32_t* fl = OLp(k, fx);
+    const uint32_t fsz = OLs(k, fx);
+    if (SIZE(k, dl[0]) > 2 || SIZE(k, fl[fsz - 1]) < 3) return false;
+    uint32_t sig;
+    int nImps = find_fanin(k, dx, out, sig);
+    if (nImps > 1) {
+        const uint32_t x = ABSV(dx);
+        out[nImps++] = fx;
+        sig |= MAPHASH(fx);
+        sort_small(out, (uint32_t)nImps);
+        for (uint32_t i = 0; i < fsz; i++) {
+            const uint32_t c = fl[i];
+            const ClsHdr h = k.hdr[c];
+            if (m_orig(h.meta) && h.size == (uint32_t)nImps && SUBSIG(h.sig, sig) && is_equal(k, c, out, (uint32_t)nImps)) {
+                SET_MOLTEN(k, c, 1);
+                nE = 0; nC = 0; nL = 0;
+                if (count_subst(k, PAIR_SUBS, x, nOrgCls, dx, fx, nE, nC, nL)) { SET_MOLTEN(k, c, 0); break; }
+                return true;
+            }
+        }
+    }
+    freeze_binaries(k, dx);
+    return false;
+}
+
+// fast_equality_check (ifthenelse.cuh:27-48)
+PFG_D uint32_t fast_equality_check(const EK& k, uint32_t x, uint32_t y, uint32_t z) {
+    uint32_t t;
+    if (OLs(k, y) > OLs(k, z)) { t = y; y = z; z = t; }
+    if (OLs(k, x) > OLs(k, y)) { t = x; x = y; y = t; }
+    const uint32_t lst = x;
+    if (z < y) { t = y; y = z; z = t; }
+    if (z < x) { t = x; x = z; z = t; }
+    if (y < x) { t = x; x = y; y = t; }
+    const uint32_t* ol = OLp(k, lst);
+    const uint32_t n = OLs(k, lst);
+    for (uint32_t i = 0; i < n; i++) {
+        const ClsHdr h = k.hdr[ol[i]];
+        if (m_molten(h.meta)) continue;
+        if (m_orig(h.meta) && h.size == 3) {
+            const uint32_t* l = k.lits + h.off;
+            if (l[0] == x && l[1] == y && l[2] == z) return ol[i];
+        }
+    }
+    return NOREF;
+}
+
+// find_ite_gate (ifthenelse.cuh:50-123)
+PFG_D bool find_ite_gate(const EK& k, uint32_t dx, uint32_t fx, uint32_t nOrgCls, uint32_t& nE, uint32_t& nC,
+                         uint32_t& nL) {
+    const uint32_t* dl = OLp(k, dx);
+    const uint32_t dsz = OLs(k, dx);
+    if (SIZE(k, dl[dsz - 1]) == 2) return false;
+    const uint32_t v = ABSV(dx);
+    for (uint32_t i = 0; i < dsz; i++) {
+        const uint32_t ci = dl[i];
+        const ClsHdr hi = k.hdr[ci];
+        if (!(m_orig(hi.meta) && hi.size == 3)) continue;
+        const uint32_t* li = k.lits + hi.off;
+        uint32_t xi = li[0], yi = li[1], zi = li[2], t;
+        if (yi == dx) { t = xi; xi = yi; yi = t; }
+        if (zi == dx) { t = xi; xi = zi; zi = t; }
+        for (uint32_t j = i + 1; j < dsz; j++) {
+            const uint32_t cj = dl[j];
+            const ClsHdr hj = k.hdr[cj];
+            if (!(m_orig(hj.meta) && hj.size == 3)) continue;
+            const uint32_t* lj = k.lits + hj.off;
+            uint32_t xj = lj[0], yj = lj[1], zj = lj[2];
+            if (yj == dx) { t = xj; xj = yj; yj = t; }
+            if (zj == dx) { t = xj; xj = zj; zj = t; }
+            if (ABSV(yi) == ABSV(zj)) { t = yj; yj = zj; zj = t; }
+            if (ABSV(zi) == ABSV(zj)) continue;
+            if (yi != FLIPL(yj)) continue;
+            const uint32_t r1 = fast_equality_check(k, fx, yi, FLIPL(zi));
+            if (r1 == NOREF) continue;
+            const uint32_t r2 = fast_equality_check(k, fx, yj, FLIPL(zj));
+            if (r2 == NOREF) continue;
+            SET_MOLTEN(k, ci, 1); SET_MOLTEN(k, cj, 1);
+            SET_MOLTEN(k, r1, 1); SET_MOLTEN(k, r2, 1);
+            nE = 0; nC = 0; nL = 0;
+            if (count_subst(k, PAIR_SUBS, v, nOrgCls, dx, fx, nE, nC, nL)) {
+                SET_MOLTEN(k, ci, 0); SET_MOLTEN(k, cj, 0);
+                SET_MOLTEN(k, r1, 0); SET_MOLTEN(k, r2, 0);
+                return false;
+            }
+            return true;
+        }
+    }
+    return false;
+}
+
+PFG_D void freeze_arities(const EK& k, uint32_t me, uint32_t other) {
+    for (int s = 0; s < 2; s++) {
+        const uint32_t lit = s ? other : me;
+        const uint32_t* ol = OLp(k, lit);
+        const uint32_t n = OLs(k, lit);
+        for (uint32_t i = 0; i < n; i++) {
+            const ClsHdr h = k.hdr[ol[i]];
+            if (h.size > 2 && m_molten(h.meta)) SET_MOLTEN(k, ol[i], 0);
+        }
+    }
+}
+
+PFG_D bool check_arity(const EK& k, const ClsHdr& h, const uint32_t* lits, uint32_t size) {
+    const uint32_t* l = k.lits + h.off;
+    for (uint32_t i = 0; i < h.size; i++) {
+        uint32_t j;
+        for (j = 0; j < size; j++) if (l[i] == lits[j]) break;
+        if (j == size) return false;
+    }
+    return true;
+}
+
+// makeArity (xor.cuh:69-100)
+PFG_D bool make_arity(const EK& k, uint32_t& parity, uint32_t* lits, uint32_t size) {
+    const uint32_t old = parity;
+    do { parity++; } while (__popc(parity) & 1);
+    for (uint32_t q = 0; q < size; q++) {
+        const uint32_t bit = 1u << q;
+        if ((parity & bit) != (old & bit)) lits[q] = FLIPL(lits[q]);
+    }
+    uint32_t best = lits[0];
+    uint32_t minsize = OLs(k, best);
+    for (uint32_t q = 1; q < size; q++) {
+        const uint32_t ls = OLs(k, lits[q]);
+        if (ls < minsize) { minsize = ls; best = lits[q]; }
+    }
+    const uint32_t* ol = OLp(k, best);
+    const uint32_t n = OLs(k, best);
+    for (uint32_t i = 0; i < n; i++) {
+        const ClsHdr h = k.hdr[ol[i]];
+        if (m_orig(h.meta) && h.size == size && check_arity(k, h, lits, size)) { SET_MOLTEN(k, ol[i], 1); return true; }
+    }
+    return false;
+}
+
+// find_xor_gate (xor.cuh:102-178)
+PFG_D bool find_xor_gate(const EK& k, uint32_t dx, uint32_t fx, uint32_t nOrgCls, uint32_t* out, uint32_t& nE,
+                         uint32_t& nC, uint32_t& nL) {
+    const uint32_t* dl = OLp(k, dx);
+    const uint32_t* fl = OLp(k, fx);
+    const uint32_t dsz = OLs(k, dx), fsz = OLs(k, fx);
+    if (SIZE(k, dl[dsz - 1]) == 2 || SIZE(k, fl[fsz - 1]) == 2) return false;
+    const int maxarity = (int)k.xor_max_arity;
+    const int arity0 = (int)SIZE(k, dl[0]) - 1;
+    if (arity0 > maxarity) return false;
+    const uint32_t v = ABSV(dx);
+    for (uint32_t i = 0; i < dsz; i++) {
+        const uint32_t ci = dl[i];
+        const ClsHdr h = k.hdr[ci];
+        if (!m_orig(h.meta)) continue;
+        const int size = (int)h.size, arity = size - 1;
+        if (size < 3 || arity > maxarity) continue;
+        const uint32_t* l = k.lits + h.off;
+        for (int q = 0; q < size; q++) out[q] = l[q];
+        uint32_t parity = 0;
+        int itargets = 1 << arity;
+        while (--itargets && make_arity(k, parity, out, (uint32_t)size)) {}
+        if (itargets) freeze_arities(k, dx, fx);
+        else {
+            SET_MOLTEN(k, ci, 1);
+            nE = 0; nC = 0; nL = 0;
+            if (count_subst(k, PAIR_SUBS, v, nOrgCls, dx, fx, nE, nC, nL)) {
+                freeze_arities(k, dx, fx);
+                break;
+            }
+            return true;
+        }
+    }
+    return false;
+}
+
+// ---- function tables (function.cuh) ----
+constexpr int FUNTABLEN = 64;
+constexpr uint32_t MAXFUNVAR = 12;
+__constant__ uint64_t MAGIC[6] = {
+    0xaaaaaaaaaaaaaaaaULL, 0xccccccccccccccccULL, 0xf0f0f0f0f0f0f0f0ULL,
+    0xff00ff00ff00ff00ULL, 0xffff0000ffff0000ULL, 0xffffffff00000000ULL,
+};
+
+PFG_D void clause2fun(uint32_t v, uint32_t sign, uint64_t* f) {
+    if (v < 6) {
+        uint64_t val = MAGIC[v];
+        if (sign) val = ~val;
+        for (int i = 0; i < FUNTABLEN; i++) f[i] |= val;
+    } else {
+        uint64_t val = sign ? ~0ULL : 0ULL;
+        int j = 0;
+        const int sv = 1 << (v - 6);
+        for (int i = 0; i < FUNTABLEN; i++) {
+            f[i] |= val;
+            if (++j >= sv) { val = ~val; j = 0; }
+        }
+    }
+}
+
+PFG_D bool build_funtab(const EK& k, uint32_t lit, uint64_t* f, uint64_t* cls) {
+    for (int i = 0; i < FUNTABLEN; i++) f[i] = ~0ULL;
+    const uint32_t* ol = OLp(k, lit);
+    const uint32_t n = OLs(k, lit);
+    for (uint32_t i = 0; i < n; i++) {
+        const ClsHdr h = k.hdr[ol[i]];
+        if (m_learnt(h.meta)) continue;
+        for (int q = 0; q < FUNTABLEN; q++) cls[q] = 0;
+        const uint32_t* l = k.lits + h.off;
+        for (uint32_t t = 0; t < h.size; t++) {
+            const uint32_t other = l[t];
+            if (other == lit) continue;
+            const uint32_t mvar = k.varcore[ABSV(other)];
+            if (mvar >= MAXFUNVAR) return false;
+            clause2fun(mvar, SIGNL(other), cls);
+        }
+        for (int q = 0; q < FUNTABLEN; q++) f[q] &= cls[q];
+    }
+    return true;
+}
+
+PFG_D void build_funtab_core(const EK& k, uint32_t lit, uint32_t tail, uint64_t* fun, uint64_t* cls, bool& core) {
+    const uint32_t* ol = OLp(k, lit);
+    for (uint32_t j = 0; j < tail; j++) {
+        const ClsHdr h = k.hdr[ol[j]];
+        if (m_learnt(h.meta)) continue;
+        for (int q = 0; q < FUNTABLEN; q++) cls[q] = 0;
+        const uint32_t* l = k.lits + h.off;
+        for (uint32_t t = 0; t < h.size; t++) {
+            const uint32_t other = l[t];
+            if (other == lit) continue;
+            clause2fun(k.varcore[ABSV(other)], SIGNL(other), cls);
+        }
+        for (int q = 0; q < FUNTABLEN; q++) fun[q] &= cls[q];
+    }
+    bool isfalse = true;
+    for (int q = 0; q < FUNTABLEN; q++) if (fun[q]) { isfalse = false; break; }
+    if (isfalse) { SET_MOLTEN(k, ol[tail], 1); core = true; }
+}
+
+// find_fun_gate (function.cuh:275-325)
+PFG_D bool find_fun_gate(const EK& k, uint32_t p, uint32_t n, uint32_t nOrgCls, uint64_t* pos, uint64_t* neg,
+                         uint64_t* cls, uint32_t& nE, uint32_t& nC, uint32_t& nL) {
+    if (!build_funtab(k, p, pos, cls) || !build_funtab(k, n, neg, cls)) return false;
+    uint64_t allzero = 0;
+    for (int i = 0; i < FUNTABLEN; i++) allzero |= pos[i] & neg[i];
+    if (allzero) return false;
+    bool core = false;
+    const uint32_t* pl = OLp(k, p);
+    for (int i = (int)OLs(k, p) - 1; i >= 0; i--) {
+        for (int q = 0; q < FUNTABLEN; q++) pos[q] = neg[q];
+        if (m_orig(META(k, pl[i]))) build_funtab_core(k, p, (uint32_t)i, pos, cls, core);
+    }
+    const uint32_t* nl = OLp(k, n);
+    for (int i = (int)OLs(k, n) - 1; i >= 0; i--) {
+        for (int q = 0; q < FUNTABLEN; q++) pos[q] = ~0ULL;
+        if (m_orig(META(k, nl[i]))) build_funtab_core(k, n, (uint32_t)i, pos, cls, core);
+    }
+    nE = 0; nC = 0; nL = 0;
+    if (count_subst(k, PAIR_CORE, ABSV(p), nOrgCls, p, n, nE, nC, nL)) {
+        if (core) freeze_clauses(k, p, n);
+        return false;
+    }
+    return true;
+}
+
+// ---- equivalences (equivalence.cuh) ----
+PFG_D bool has_lit(const EK& k, uint32_t c, uint32_t lit) {
+    const ClsHdr h = k.hdr[c];
+    const uint32_t* l = k.lits + h.off;
+    for (uint32_t i = 0; i < h.size; i++) if (l[i] == lit) return true;
+    return false;
+}
+
+PFG_D void substitute_one(const EK& k, uint32_t dx, uint32_t def, uint32_t c, uint32_t& nUnits) {
+    const ClsHdr h = k.hdr[c];
+    uint32_t* l = k.lits + h.off;
+    uint32_t j = 0;
+    for (uint32_t i = 0; i < h.size; i++) {
+        const uint32_t lit = l[i];
+        if (lit == dx) l[j++] = def;
+        else if (lit != def) l[j++] = lit;
+    }
+    k.hdr[c].size = j;
+    if (j == 1) nUnits++;
+    else { sort_small(l, j); calc_sig(k, c); }
+}
+
+PFG_D void substitute_single(const EK& k, uint32_t p, uint32_t n, uint32_t def) {
+    const uint32_t def_f = FLIPL(def);
+    uint32_t nNeg = 0, nPos = 0;
+    const uint32_t* nl = OLp(k, n);
+    const uint32_t ns = OLs(k, n);
+    for (uint32_t i = 0; i < ns; i++) {
+        const uint32_t c = nl[i];
+        const uint32_t m = META(k, c);
+        if (m_learnt(m) || m_molten(m) || has_lit(k, c, def)) SET_DELETED(k, c);
+        else substitute_one(k, n, def_f, c, nNeg);
+    }
+    const uint32_t* pl = OLp(k, p);
+    const uint32_t ps = OLs(k, p);
+    for (uint32_t i = 0; i < ps; i++) {
+        const uint32_t c = pl[i];
+        const uint32_t m = META(k, c);
+        if (m_learnt(m) || m_molten(m) || has_lit(k, c, def_f)) SET_DELETED(k, c);
+        else substitute_one(k, p, def, c, nPos);
+    }
+    if (nPos || nNeg) {
+        if (nNeg) append_units(k, n);
+        if (nPos) append_units(k, p);
+    }
+}
+
+PFG_D uint32_t find_sfanin(const EK& k, uint32_t gate_out) {
+    uint32_t imp = 0;
+    int nImps = 0;
+    const uint32_t* ol = OLp(k, gate_out);
+    const uint32_t n = OLs(k, gate_out);
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t c = ol[i];
+        const ClsHdr h = k.hdr[c];
+        if (m_orig(h.meta) && h.size == 2) {
+            const uint32_t* l = k.lits + h.off;
+            imp = FLIPL(l[0] ^ l[1] ^ gate_out);
+            SET_MOLTEN(k, c, 1);
+            nImps++;
+        }
+        if (nImps > 1) return 0;
+    }
+    return imp;
+}
+
+PFG_D uint32_t find_equ_gate(const EK& k, uint32_t p, uint32_t n) {
+    const uint32_t* pl = OLp(k, p);
+    const uint32_t* nl = OLp(k, n);
+    if (SIZE(k, pl[0]) > 2 || SIZE(k, nl[0]) > 2) return 0;
+    uint32_t first = find_sfanin(k, p);
+    if (first) {
+        uint32_t second = n, def = first;
+        if (second < def) { first = second; second = def; }
+        const uint32_t ns = OLs(k, n);
+        for (uint32_t i = 0; i < ns; i++) {
+            const uint32_t c = nl[i];
+            const ClsHdr h = k.hdr[c];
+            const uint32_t* l = k.lits + h.off;
+            if (m_orig(h.meta) && h.size == 2 && l[0] == first && l[1] == second) {
+                SET_MOLTEN(k, c, 1);
+                return def;
+            }
+        }
+    }
+    freeze_binaries(k, p);
+    return 0;
+}
+
+// ---- SUB (subsume.cuh) ----
+PFG_D bool sub_c(const EK& k, const ClsHdr& s, const ClsHdr& t) {
+    const uint32_t* d1 = k.lits + s.off;
+    const uint32_t* d2 = k.lits + t.off;
+    uint32_t i = 0, j = 0, sub = 0;
+    while (i < s.size && j < t.size) {
+        if (d1[i] < d2[j]) i++;
+        else if (d2[j] < d1[i]) j++;
+        else { sub++; i++; j++; }
+    }
+    return sub == s.size;
+}
+
+PFG_D bool selfsub_c(const EK& k, uint32_t x, uint32_t fx, const ClsHdr& s, const ClsHdr& t) {
+    const uint32_t* d1 = k.lits + s.off;
+    const uint32_t* d2 = k.lits + t.off;
+    uint32_t i = 0, j = 0, sub = 0;
+    bool self = false;
+    while (i < s.size && j < t.size) {
+        const uint32_t l1 = d1[i], l2 = d2[j];
+        if (l1 == fx) i++;
+        else if (l2 == x) { self = true; j++; }
+        else if (l1 < l2) i++;
+        else if (l2 < l1) j++;
+        else { sub++; i++; j++; }
+    }
+    if (sub + 1 == s.size) {
+        if (self) return true;
+        while (j < t.size) { if (d2[j] == x) return true; j++; }
+    }
+    return false;
+}
+
+PFG_D void strengthen(const EK& k, uint32_t c, uint32_t self) {
+    ClsHdr h = k.hdr[c];
+    uint32_t* l = k.lits + h.off;
+    uint32_t j = 0;
+    for (uint32_t i = 0; i < h.size; i++) if (l[i] != self) l[j++] = l[i];
+    h.size--;
+    k.hdr[c].size = h.size;
+    if (h.size > 1) {
+        calc_sig(k, c);
+        if (m_learnt(h.meta)) {   // bumpShrunken (subsume.cuh:216-231)
+            const int old_lbd = (int)m_lbd(h.meta);
+            if (old_lbd > (int)LBD_TIER1) {
+                const int sz1 = (int)h.size - 1;
+                const int new_lbd = sz1 < old_lbd ? sz1 : old_lbd;
+                if (new_lbd < old_lbd) {
+                    const uint32_t m = k.hdr[c].meta;
+                    k.hdr[c].meta = (m & 0xFu) | (USAGET3 << 4) | ((uint32_t)new_lbd << 6);
+                }
+            }
+        }
+    }
+}
+
+PFG_D void update_ol(const EK& k, uint32_t lit) {
+    uint32_t* ol = OLp(k, lit);
+    const uint32_t n = OLs(k, lit);
+    uint32_t j = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t c = ol[i];
+        const uint32_t m = META(k, c);
+        if (m_molten(m)) SET_MOLTEN(k, c, 0);
+        else if (!m_deleted(m)) ol[j++] = c;
+    }
+    k.ot_size[lit] = j;
+}
+
+PFG_D void subsume_cand(const EK& k, uint32_t lit, uint32_t end, uint32_t cand) {
+    const ClsHdr ch = k.hdr[cand];
+    const uint32_t* ol = OLp(k, lit);
+    for (uint32_t j = 0; j < end; j++) {
+        const uint32_t sc = ol[j];
+        const ClsHdr s = k.hdr[sc];
+        if (m_deleted(s.meta)) continue;
+        if (m_molten(ch.meta) && s.size > ch.size) continue;
+        if (s.size > 1 && SUBSIG(s.sig, ch.sig) && sub_c(k, s, ch)) {
+            if (m_learnt(s.meta) && m_orig(ch.meta)) k.hdr[sc].meta = m_set_st(s.meta, ST_ORIGINAL);
+            SET_DELETED(k, cand);
+            break;
+        }
+    }
+}
+
+PFG_D void self_subsume(const EK& k, uint32_t x, uint32_t fx, uint32_t lit, uint32_t cand, uint32_t& nUnits) {
+    const ClsHdr ch = k.hdr[cand];
+    const uint32_t* ol = OLp(k, lit);
+    const uint32_t n = OLs(k, lit);
+    for (uint32_t j = 0; j < n; j++) {
+        const ClsHdr s = k.hdr[ol[j]];
+        if (s.size > ch.size) break;
+        if (m_deleted(s.meta) || m_molten(s.meta)) continue;
+        if (s.size > 1 && selfsub_sig(s.sig, ch.sig) && selfsub_c(k, x, fx, s, ch)) {
+            strengthen(k, cand, x);
+            SET_MOLTEN(k, cand, 1);
+            if (SIZE(k, cand) == 1) nUnits++;
+            break;
+        }
+    }
+}
+
+__global__ void sub_k(EK k, const uint32_t* elected, uint32_t nelected) {
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < nelected; e += gridDim.x * blockDim.x) {
+        const uint32_t x = elected[e];
+        const uint32_t p = 2 * x, n = p | 1;
+        if (OLs(k, p) > k.sub_max_occurs || OLs(k, n) > k.sub_max_occurs) continue;
+        uint32_t nPos = 0, nNeg = 0;
+        const uint32_t* pl = OLp(k, p);
+        const uint32_t ps = OLs(k, p);
+        for (uint32_t i = 0; i < ps; i++) {
+            const uint32_t c = pl[i];
+            const ClsHdr h = k.hdr[c];
+            if (h.size > SUB_MAX_CL_SIZE) break;
+            if (m_deleted(h.meta)) continue;
+            self_subsume(k, p, n, n, c, nPos);
+            subsume_cand(k, p, i, c);
+        }
+        const uint32_t* nl = OLp(k, n);
+        const uint32_t ns = OLs(k, n);
+        for (uint32_t i = 0; i < ns; i++) {
+            const uint32_t c = nl[i];
+            const ClsHdr h = k.hdr[c];
+            if (h.size > SUB_MAX_CL_SIZE) break;
+            if (m_deleted(h.meta)) continue;
+            self_subsume(k, n, p, p, c, nNeg);
+            subsume_cand(k, n, i, c);
+        }
+        if (nPos || nNeg) {
+            if (nPos) append_units(k, p);
+            if (nNeg) append_units(k, n);
+        }
+        update_ol(k, p);
+        update_ol(k, n);
+    }
+}
+
+// ---- BVE phase 1 ----
+__global__ void __launch_bounds__(64) ve1_k(EK k, const uint32_t* elected, uint32_t nelected, uint32_t* type,
+                                            uint32_t* ucnt, unsigned long long* rpos, unsigned long long* rref) {
+    uint32_t outs[SH_MAX_BVE_OUT1 + 2];
+    uint64_t fpos[FUNTABLEN], fneg[FUNTABLEN], fcls[FUNTABLEN];
+    for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < nelected; tid += gridDim.x * blockDim.x) {
+        const uint32_t x = elected[tid];
+        const uint32_t p = 2 * x, n = p | 1;
+        uint32_t pOrgs = 0, nOrgs = 0;
+        if (k.ve_inprocess) {
+            const uint32_t* pl = OLp(k, p);
+            const uint32_t* nl = OLp(k, n);
+            for (uint32_t i = 0; i < OLs(k, p); i++) if (m_orig(META(k, pl[i]))) pOrgs++;
+            for (uint32_t i = 0; i < OLs(k, n); i++) if (m_orig(META(k, nl[i]))) nOrgs++;
+        } else {
+            pOrgs = OLs(k, p);
+            nOrgs = OLs(k, n);
+        }
+        uint32_t elimType = 0, nE = 0, nC = 0, nL = 0;
+        type[tid] = 0; ucnt[tid] = 0; rpos[tid] = 0; rref[tid] = 0;
+        if (!pOrgs || !nOrgs) {
+            save_resolved_orgs(k, p, n, pOrgs, nOrgs);
+            toblivion(k, p, n);
+            k.elim[x] |= MELTING_MASK;
+            continue;
+        }
+        const uint32_t def = find_equ_gate(k, p, n);
+        if (def) {
+            save_resolved_orgs(k, p, n, pOrgs, nOrgs);
+            substitute_single(k, p, n, def);
+            k.elim[x] |= MELTING_MASK;
+            continue;
+        }
+        if ((pOrgs == 1 || nOrgs == 1) && count_res_unbounded(k, x, p, n, nE, nC, nL)) {
+            if (nC) {
+                type[tid] = RES_MASK | (nC << 2) | (nL << 16);
+                ucnt[tid] = nE; rpos[tid] = nC; rref[tid] = nL + (unsigned long long)NBUCKETS * nC;
+            } else {
+                save_resolved_orgs(k, p, n, pOrgs, nOrgs);
+                toblivion(k, p, n);
+                k.elim[x] |= MELTING_MASK;
+            }
+            continue;
+        }
+        const uint32_t nClsBefore = pOrgs + nOrgs;
+        elimType = 0; nE = 0; nC = 0; nL = 0;
+        if (nClsBefore > 2) {
+            if (nOrgs < SH_MAX_BVE_OUT1 && find_ao_gate(k, n, p, nClsBefore, outs, nE, nC, nL)) elimType = AOIX_MASK;
+            else if (!nC && pOrgs < SH_MAX_BVE_OUT1 && find_ao_gate(k, p, n, nClsBefore, outs, nE, nC, nL)) elimType = AOIX_MASK;
+        }
+        if (!elimType && nClsBefore > 3) {
+            if (find_ite_gate(k, p, n, nClsBefore, nE, nC, nL)) elimType = AOIX_MASK;
+            else if (!nC && find_ite_gate(k, n, p, nClsBefore, nE, nC, nL)) elimType = AOIX_MASK;
+            else if (find_xor_gate(k, p, n, nClsBefore, outs, nE, nC, nL)) elimType = AOIX_MASK;
+            else if (!nC && find_xor_gate(k, n, p, nClsBefore, outs, nE, nC, nL)) elimType = AOIX_MASK;
+        }
+        if (k.varcore_on && !elimType && nClsBefore > 2 &&
+            find_fun_gate(k, p, n, nClsBefore, fpos, fneg, fcls, nE, nC, nL))
+            elimType = CORE_MASK;
+        else if (!elimType && !nC && count_res_bounded(k, x, nClsBefore, p, n, nE, nC, nL))
+            elimType = RES_MASK;
+        if (!nC) {
+            save_resolved_orgs(k, p, n, pOrgs, nOrgs);
+            toblivion(k, p, n);
+            k.elim[x] |= MELTING_MASK;
+        } else if (elimType) {
+            type[tid] = elimType | (nC << 2) | (nL << 16);
+            ucnt[tid] = nE; rpos[tid] = nC; rref[tid] = nL + (unsigned long long)NBUCKETS * nC;
+        }
+    }
+}
+
+// ---- BVE phase 3 ----
+__global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint32_t nelected, const uint32_t* type,
+                                             const unsigned long long* rpos, const unsigned long long* rref,
+                                             unsigned long long cs_cap, unsigned long long data_cap, uint8_t* keep) {
+    for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < nelected; tid += gridDim.x * blockDim.x) {
+        const uint32_t x = elected[tid];
+        const uint32_t xinfo = type[tid];
+        const uint32_t et = xinfo & 3u;
+        if (et) {
+            const uint32_t p = 2 * x, n = p | 1;
+            const uint32_t nAddedCls = (xinfo & 0xFFFCu) >> 2, nAddedLits = xinfo >> 16;
+            const unsigned long long addedPos = rpos[tid], addedRef = rref[tid];
+            if (addedPos + nAddedCls <= cs_cap &&
+                addedRef + nAddedLits + (unsigned long long)NBUCKETS * nAddedCls <= data_cap) {
+                save_resolved_lists(k, p, n);
+                const int kind = et == RES_MASK ? PAIR_RES : (et == CORE_MASK ? PAIR_CORE : PAIR_SUBS);
+                // resolvents go to slots addedPos.. ; literals packed at ref - 3 * index
+                unsigned long long slot = addedPos;
+                unsigned long long woff = addedRef - (unsigned long long)NBUCKETS * addedPos;
+                const unsigned long long checksum = addedPos + nAddedCls;
+                const uint32_t* ml = OLp(k, p);
+                const uint32_t* ol = OLp(k, n);
+                const uint32_t ms = OLs(k, p), os = OLs(k, n);
+                for (uint32_t i = 0; i < ms && slot < checksum; i++) {
+                    const uint32_t ci = ml[i];
+                    const uint32_t mi = META(k, ci);
+                    if (m_learnt(mi)) continue;
+                    for (uint32_t j = 0; j < os && slot < checksum; j++) {
+                        const uint32_t cj = ol[j];
+                        const uint32_t mj = META(k, cj);
+                        if (m_learnt(mj)) continue;
+                        if (kind == PAIR_SUBS && m_molten(mi) == m_molten(mj)) continue;
+                        if (kind == PAIR_CORE && m_molten(mi) && m_molten(mj)) continue;
+                        uint32_t unit;
+                        const int rsize = merge_cnt(k, x, ci, cj, unit);
+                        if (!rsize) continue;
+                        if (rsize == 1) { push_unit(k, unit); continue; }
+                        uint32_t* out = k.lits + woff;
+                        merge_out(k, x, ci, cj, out);
+                        uint32_t sig = 0;
+                        for (int q = 0; q < rsize; q++) sig |= MAPHASH(out[q]);
+                        ClsHdr h;
+                        h.off = (uint32_t)woff;
+                        h.size = (uint32_t)rsize;
+                        h.sig = sig;
+                        h.meta = m_make(ST_ORIGINAL, 0, 1, 0, 0);
+                        k.hdr[slot] = h;
+                        slot++;
+                        woff += (unsigned long long)rsize;
+                    }
+                }
+                if (slot != checksum) atomicOr(&k.dc->err, ERR_SLOT_MISMATCH);
+                toblivion(k, p, n);
+                k.elim[x] |= MELTING_MASK | ADDING_MASK;
+                atomicMax(&k.dc->last_elim, (int)tid);
+            } else if (et != RES_MASK) {
+                freeze_clauses(k, p, n);
+            }
+        }
+        keep[tid] = k.elim[x] ? 0 : 1;
+    }
+}
+
+// ---- ERE: one warp per elected variable ----
+__global__ void __launch_bounds__(128) ere_k(EK k, const uint32_t* elected, uint32_t nelected) {
+    __shared__ uint32_t bufs[4][SH_MAX_ERE_OUT + 8];
+    const uint32_t wib = threadIdx.x >> 5;
+    const unsigned lane = threadIdx.x & 31u;
+    uint32_t* buf = bufs[wib];
+    const uint32_t cmax = k.ere_clause_max;
+    for (uint32_t e = blockIdx.x * 4 + wib; e < nelected; e += gridDim.x * 4) {
+        const uint32_t v = elected[e], p = 2 * v, n = p | 1;
+        const uint32_t ds = OLs(k, p), fs = OLs(k, n);
+        if (!(ds && fs && ds <= k.ere_max_occurs && fs <= k.ere_max_occurs)) continue;
+        const uint32_t* pl = OLp(k, p);
+        const uint32_t* nl = OLp(k, n);
+        if (!(SIZE(k, pl[0]) <= cmax && SIZE(k, nl[0]) <= cmax)) continue;
+        for (uint32_t i = 0; i < ds; i++) {
+            const uint32_t pc = pl[i];
+            const ClsHdr ph = k.hdr[pc];
+            if (m_deleted(ph.meta)) continue;
+            for (uint32_t j = 0; j < fs; j++) {
+                const uint32_t nc = nl[j];
+                const ClsHdr nh = k.hdr[nc];
+                if (m_deleted(nh.meta) || ph.size + nh.size - 2 > cmax) continue;
+                int mlen = 0;
+                if (lane == 0) mlen = merge_out(k, v, pc, nc, buf);
+                mlen = __shfl_sync(0xFFFFFFFFu, mlen, 0);
+                __syncwarp();
+                if (mlen > 1) {
+                    const uint32_t type = (m_learnt(ph.meta) || m_learnt(nh.meta)) ? ST_LEARNT : ST_ORIGINAL;
+                    uint32_t best = buf[0], msig = MAPHASH(best);
+                    uint32_t minsize = OLs(k, best);
+                    for (int q = 1; q < mlen; q++) {
+                        const uint32_t ls = OLs(k, buf[q]);
+                        if (ls < minsize) { minsize = ls; best = buf[q]; }
+                        msig |= MAPHASH(buf[q]);
+                    }
+                    const uint32_t* ml = OLp(k, best);
+                    for (uint32_t ii = lane; ii < minsize; ii += 32) {
+                        const uint32_t c = ml[ii];
+                        const ClsHdr h = k.hdr[c];
+                        if ((uint32_t)mlen == h.size && (m_learnt(h.meta) || m_st(h.meta) == type) &&
+                            SUBSIG(msig, h.sig) && !m_deleted(h.meta) && is_equal(k, c, buf, (uint32_t)mlen)) {
+                            // claim: the first non-deleted match of this lane's stride is deleted
+                            unsigned int* mp = (unsigned int*)&k.hdr[c].meta;
+                            unsigned int old = h.meta;
+                            bool won = false;
+                            for (int it = 0; it < 8; it++) {
+                                if (m_deleted(old)) break;
+                                const unsigned int prev = atomicCAS(mp, old, m_set_st(old, ST_DELETED));
+                                if (prev == old) { won = true; break; }
+                                old = prev;
+                            }
+                            if (won) break;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    }
+}
+
+EK make_ek(Ctx& c) {
+    EK k;
+    k.hdr = c.hdr;
+    k.lits = c.lits;
+    k.ot_off = c.ot_off;
+    k.ot_size = c.ot_size;
+    k.ot_ids = c.ot_ids;
+    k.elim = c.elim;
+    k.varcore = c.varcore;
+    k.varcore_on = c.varcore_on ? 1 : 0;
+    k.vorg = c.vorg;
+    k.units = c.units;
+    k.units_cap = c.units_cap;
+    k.stack = c.stack;
+    k.stack_cap = c.stack_cap;
+    k.dc = c.dc;
+    k.ve_clause_max = c.o.ve_clause_max;
+    k.xor_max_arity = c.o.xor_max_arity;
+    k.sub_max_occurs = c.o.sub_max_occurs;
+    k.ere_max_occurs = c.o.ere_max_occurs;
+    k.ere_clause_max = c.o.ere_clause_max;
+    k.ve_lbound_en = c.o.ve_lbound_en;
+    k.ve_inprocess = c.o.ve_inprocess;
+    return k;
+}
+
+__global__ void keep_u32_k(const uint8_t* keep, uint32_t n, uint32_t* out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = keep[i];
+}
+
+}  // namespace
+
+void sub_pass(Ctx& c) {
+    if (!c.nelected) return;
+    sub_k<<<grid_for(c.nelected, 64), 64, 0, c.s>>>(make_ek(c), c.elected, c.nelected);
+    g_launches += 1;
+}
+
+bool ve_pass(Ctx& c) {
+    const uint32_t E = c.nelected;
+    if (!E) return true;
+    const EK k = make_ek(c);
+    ve1_k<<<grid_for(E, 64), 64, 0, c.s>>>(k, c.elected, E, c.type, c.ucnt, c.rpos, c.rref);
+    g_launches += 1;
+    if (!ensure_tmp(c, scan_temp_bytes(E))) return false;
+    exclusive_scan_u64(c.rpos, c.rpos, E, (unsigned long long)c.ncls, nullptr, c.tmp, c.s);
+    exclusive_scan_u64(c.rref, c.rref, E, (unsigned long long)c.data_size, nullptr, c.tmp, c.s);
+    cudaMemsetAsync(&c.dc->last_elim, 0xFF, sizeof(int32_t), c.s);   // -1
+    ve3_k<<<grid_for(E, 128), 128, 0, c.s>>>(k, c.elected, E, c.type, c.rpos, c.rref, c.cs_cap, c.data_cap, c.flag8);
+    g_launches += 1;
+    // postVE: keep surviving elected variables in order (elimination.cu:249-267)
+    select_flagged(c.elected, c.flag8, c.work, E, &c.dc->survivors, c.vscan, c.tmp, c.s);
+    sync_counters(c);
+    if (!c.err.empty()) return false;
+    const int32_t last = c.hc->last_elim;
+    const uint32_t survivors = c.hc->survivors;
+    cudaMemcpyAsync(c.elected, c.work, survivors * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+    if (last >= 0) {   // resizeCNF_k (cnf.cu:55-80)
+        uint32_t lt = 0;
+        unsigned long long lp = 0, lr = 0;
+        cudaMemcpyAsync(&lt, c.type + last, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+        cudaMemcpyAsync(&lp, c.rpos + last, sizeof(lp), cudaMemcpyDeviceToHost, c.s);
+        cudaMemcpyAsync(&lr, c.rref + last, sizeof(lr), cudaMemcpyDeviceToHost, c.s);
+        if (!cuda_ok(c, cudaStreamSynchronize(c.s), "ve resize")) return false;
+        const uint64_t nC = (lt & 0xFFFCu) >> 2, nL = lt >> 16;
+        c.ncls = lp + nC;
+        c.data_size = lr + nL + NBUCKETS * nC;
+        c.lits_used = c.data_size - NBUCKETS * c.ncls;
+    }
+    c.nelected = survivors;
+    return cuda_ok(c, cudaGetLastError(), "ve");
+}
+
+void ere_pass(Ctx& c) {
+    if (!c.nelected) return;
+    ere_k<<<grid_for((uint64_t)c.nelected * 32, 128), 128, 0, c.s>>>(make_ek(c), c.elected, c.nelected);
+    g_launches += 1;
+}
+
+}  // namespace pfg

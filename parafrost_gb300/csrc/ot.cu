@@ -1,0 +1,295 @@
+// Occurrence-table construction and sorting.
+//
+// Replaces histSimp (full sort of all literals, histogram.cu:54-71),
+// resizeOTAsync/assignListPtrs (memory.cu:421-466), create_ot_k
+// (occurrence.cu:50-62) and the moderngpu segmented sort of sortOT
+// (segsort.cu:37-47) with:
+//   1. a literal histogram by atomics over live clauses,
+//   2. an exclusive scan into CSR offsets,
+//   3. an atomic scatter of clause ids,
+//   4. a size-tiered segmented sort by the OLIST_CMP key (key.cuh:67-85):
+//      thread-per-list insertion sort (<= 16), block bitonic sort in shared
+//      memory (<= 2048), chunk sort + merge-path passes for longer lists.
+#include <algorithm>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace pfg {
+namespace {
+
+constexpr uint32_t SMALL_MAX = 16;
+constexpr uint32_t MID_MAX = 2048;
+constexpr int MID_THREADS = 256;
+
+__global__ void hist_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
+                       uint32_t* hist) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        const ClsHdr h = hdr[c];
+        if (m_deleted(h.meta)) continue;
+        for (uint32_t k = 0; k < h.size; k++) atomicAdd(&hist[lits[h.off + k]], 1u);
+    }
+}
+
+__global__ void fill_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
+                       uint32_t* fill, uint32_t* ids) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        const ClsHdr h = hdr[c];
+        if (m_deleted(h.meta)) continue;
+        for (uint32_t k = 0; k < h.size; k++) {
+            const uint32_t pos = atomicAdd(&fill[lits[h.off + k]], 1u);
+            ids[pos] = (uint32_t)c;
+        }
+    }
+}
+
+PFG_D uint4 ckey(const ClsHdr* hdr, const uint32_t* lits, uint32_t c, bool by_id) {
+    if (by_id) return make_uint4(0, 0, 0, 0);
+    const ClsHdr h = hdr[c];
+    return make_uint4(h.size, lits[h.off], lits[h.off + h.size - 1], h.sig);
+}
+
+// OLIST_CMP: (size, first, last, sig, ref)
+PFG_D bool kless(const uint4& a, uint32_t ia, const uint4& b, uint32_t ib) {
+    if (a.x != b.x) return a.x < b.x;
+    if (a.y != b.y) return a.y < b.y;
+    if (a.z != b.z) return a.z < b.z;
+    if (a.w != b.w) return a.w < b.w;
+    return ia < ib;
+}
+
+__global__ void sort_small_k(const ClsHdr* hdr, const uint32_t* lits, uint64_t nlist,
+                             const uint32_t* off, const uint32_t* size, uint32_t* ids, bool by_id,
+                             uint32_t* mid_desc, uint32_t* mid_cnt, uint32_t* big_lists, uint32_t* big_cnt) {
+    for (uint64_t l = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlist; l += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t n = size[l];
+        if (n < 2) continue;
+        if (n > SMALL_MAX) {
+            if (n <= MID_MAX) {
+                const uint32_t q = atomicAdd(mid_cnt, 1u);
+                mid_desc[2 * q] = off[l];
+                mid_desc[2 * q + 1] = n;
+            } else {
+                big_lists[atomicAdd(big_cnt, 1u)] = (uint32_t)l;
+            }
+            continue;
+        }
+        uint32_t* L = ids + off[l];
+        uint4 k[SMALL_MAX];
+        uint32_t id[SMALL_MAX];
+        for (uint32_t i = 0; i < n; i++) { id[i] = L[i]; k[i] = ckey(hdr, lits, id[i], by_id); }
+        for (uint32_t i = 1; i < n; i++) {
+            const uint4 tk = k[i];
+            const uint32_t ti = id[i];
+            uint32_t j = i;
+            while (j > 0 && kless(tk, ti, k[j - 1], id[j - 1])) { k[j] = k[j - 1]; id[j] = id[j - 1]; j--; }
+            k[j] = tk; id[j] = ti;
+        }
+        for (uint32_t i = 0; i < n; i++) L[i] = id[i];
+    }
+}
+
+// Bitonic sort of one segment (<= MID_MAX) in shared memory.
+PFG_D void bitonic_smem(uint4* sk, uint32_t* sid, uint32_t P) {
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const bool asc = (i & k) == 0;
+                    const bool gt = kless(sk[ixj], sid[ixj], sk[i], sid[i]);
+                    if (gt == asc) {
+                        const uint4 tk = sk[i]; sk[i] = sk[ixj]; sk[ixj] = tk;
+                        const uint32_t ti = sid[i]; sid[i] = sid[ixj]; sid[ixj] = ti;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(MID_THREADS) sort_mid_k(const ClsHdr* hdr, const uint32_t* lits,
+                                                         const uint32_t* desc, uint32_t* ids, bool by_id) {
+    __shared__ uint4 sk[MID_MAX];
+    __shared__ uint32_t sid[MID_MAX];
+    const uint32_t o = desc[2 * blockIdx.x], n = desc[2 * blockIdx.x + 1];
+    uint32_t P = 1;
+    while (P < n) P <<= 1;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+        if (i < n) { sid[i] = ids[o + i]; sk[i] = ckey(hdr, lits, sid[i], by_id); }
+        else { sid[i] = 0xFFFFFFFFu; sk[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu); }
+    }
+    __syncthreads();
+    bitonic_smem(sk, sid, P);
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) ids[o + i] = sid[i];
+}
+
+// Big lists: gather into a contiguous area with precomputed keys.
+__global__ void big_gather_k(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* big_lists, uint32_t nbig,
+                             const uint32_t* off, const uint32_t* size, const uint32_t* boff,
+                             const uint32_t* ids, uint4* bk, uint32_t* bid, bool by_id) {
+    for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+        const uint32_t l = big_lists[b], n = size[l], o = off[l], a = boff[b];
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const uint32_t c = ids[o + i];
+            bid[a + i] = c;
+            bk[a + i] = ckey(hdr, lits, c, by_id);
+        }
+    }
+}
+
+// chunk sort of big lists: block (b, chunk)
+__global__ void __launch_bounds__(MID_THREADS) big_chunk_k(const uint32_t* big_lists, const uint32_t* size,
+                                                          const uint32_t* boff, uint4* bk, uint32_t* bid) {
+    __shared__ uint4 sk[MID_MAX];
+    __shared__ uint32_t sid[MID_MAX];
+    const uint32_t b = blockIdx.y;
+    const uint32_t n = size[big_lists[b]];
+    const uint32_t cs = blockIdx.x * MID_MAX;
+    if (cs >= n) return;
+    const uint32_t m = min(MID_MAX, n - cs);
+    const uint32_t a = boff[b] + cs;
+    uint32_t P = 1;
+    while (P < m) P <<= 1;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+        if (i < m) { sid[i] = bid[a + i]; sk[i] = bk[a + i]; }
+        else { sid[i] = 0xFFFFFFFFu; sk[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu); }
+    }
+    __syncthreads();
+    bitonic_smem(sk, sid, P);
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) { bid[a + i] = sid[i]; bk[a + i] = sk[i]; }
+}
+
+// one merge pass: runs of length R merged pairwise (element-parallel binary search)
+__global__ void big_merge_k(const uint32_t* big_lists, const uint32_t* size, const uint32_t* boff, uint32_t R,
+                            const uint4* bk, const uint32_t* bid, uint4* bk2, uint32_t* bid2) {
+    const uint32_t b = blockIdx.y;
+    const uint32_t n = size[big_lists[b]];
+    const uint32_t a = boff[b];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t r = i / R, s = r * R;
+        uint32_t ps, pe;
+        if (r & 1u) { ps = s - R; pe = s; }
+        else { ps = s + R; pe = min(s + 2 * R, n); if (ps > n) ps = n; }
+        const uint4 mk = bk[a + i];
+        const uint32_t mi = bid[a + i];
+        // count partner elements less than me
+        uint32_t lo = ps, hi = pe;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (kless(bk[a + mid], bid[a + mid], mk, mi)) lo = mid + 1;
+            else hi = mid;
+        }
+        const uint32_t pair = (r & ~1u) * R;
+        const uint32_t dst = pair + (i - s) + (lo - ps);
+        bk2[a + dst] = mk;
+        bid2[a + dst] = mi;
+    }
+}
+
+__global__ void big_scatter_k(const uint32_t* big_lists, uint32_t nbig, const uint32_t* off, const uint32_t* size,
+                              const uint32_t* boff, const uint32_t* bid, uint32_t* ids) {
+    for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+        const uint32_t l = big_lists[b], n = size[l], o = off[l], a = boff[b];
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) ids[o + i] = bid[a + i];
+    }
+}
+
+__global__ void big_sizes_k(const uint32_t* big_lists, uint32_t nbig, const uint32_t* size, uint32_t* out) {
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nbig; b += gridDim.x * blockDim.x)
+        out[b] = size[big_lists[b]];
+}
+
+}  // namespace
+
+bool ot_build(Ctx& c) {
+    const uint64_t nl = c.nlist;
+    if (c.numLiterals > 0xFFFFFFF0ull) { c.simpstate = PFG_OTALLOC_FAIL; c.err = "occurrence table exceeds 2^32 entries"; return false; }
+    if (c.ot_cap < c.numLiterals) {
+        dfree(c, c.ot_ids);
+        c.ot_ids = nullptr;
+        const uint64_t cap = c.numLiterals + c.numLiterals / 4 + 1024;
+        if (!dalloc_t(c, &c.ot_ids, cap)) { c.simpstate = PFG_OTALLOC_FAIL; c.ot_cap = 0; return false; }
+        c.ot_cap = cap;
+    }
+    cudaMemsetAsync(c.hist, 0, nl * sizeof(uint32_t), c.s);
+    hist_k<<<grid_for(c.ncls, 256), 256, 0, c.s>>>(c.hdr, c.lits, c.ncls, c.hist);
+    if (!ensure_tmp(c, scan_temp_bytes(nl))) return false;
+    exclusive_scan_u32(c.hist, c.ot_off, nl, 0u, c.ot_off + nl, c.tmp, c.s);
+    cudaMemcpyAsync(c.ot_fill, c.ot_off, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+    cudaMemcpyAsync(c.ot_size, c.hist, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+    fill_k<<<grid_for(c.ncls, 256), 256, 0, c.s>>>(c.hdr, c.lits, c.ncls, c.ot_fill, c.ot_ids);
+    g_launches += 2;
+    return cuda_ok(c, cudaGetLastError(), "ot_build");
+}
+
+bool ot_sort(Ctx& c, bool by_id) {
+    const uint64_t nl = c.nlist;
+    // worst case: every list is mid-sized
+    const uint64_t want_desc = std::max<uint64_t>(1024, c.numLiterals / (SMALL_MAX + 1) + 1);
+    if (c.mid_desc_cap < want_desc) {
+        dfree(c, c.mid_desc);
+        c.mid_desc = nullptr;
+        if (!dalloc_t(c, &c.mid_desc, 2 * want_desc)) { c.simpstate = PFG_OTALLOC_FAIL; return false; }
+        c.mid_desc_cap = want_desc;
+    }
+    cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
+    cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
+    sort_small_k<<<grid_for(nl, 256), 256, 0, c.s>>>(c.hdr, c.lits, nl, c.ot_off, c.ot_size, c.ot_ids, by_id,
+                                                     c.mid_desc, &c.dc->nwin, c.big_lists, &c.dc->big_lists);
+    g_launches += 1;
+    sync_counters(c);
+    const uint32_t nmid = c.hc->nwin, nbig = c.hc->big_lists;
+    if (nmid) {
+        sort_mid_k<<<nmid, MID_THREADS, 0, c.s>>>(c.hdr, c.lits, c.mid_desc, c.ot_ids, by_id);
+        g_launches += 1;
+    }
+    if (nbig) {
+        // sizes and area offsets of the big lists
+        uint32_t* bsz = c.tmp_u32;  // nbig + 1 entries needed twice
+        if (!ensure_tmp_u32(c, 2ull * nbig + 4)) return false;
+        bsz = c.tmp_u32;
+        uint32_t* boff = c.tmp_u32 + nbig + 2;
+        big_sizes_k<<<grid_for(nbig, 256), 256, 0, c.s>>>(c.big_lists, nbig, c.ot_size, bsz);
+        if (!ensure_tmp(c, scan_temp_bytes(nbig))) return false;
+        exclusive_scan_u32(bsz, boff, nbig, 0u, boff + nbig, c.tmp, c.s);
+        std::vector<uint32_t> hs(nbig + 1);
+        cudaMemcpyAsync(hs.data(), bsz, nbig * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+        cudaMemcpyAsync(&hs[nbig], boff + nbig, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+        if (!cuda_ok(c, cudaStreamSynchronize(c.s), "ot_sort big sizes")) return false;
+        const uint64_t total = hs[nbig];
+        uint32_t maxn = 0;
+        for (uint32_t i = 0; i < nbig; i++) maxn = std::max(maxn, hs[i]);
+        if (c.big_cap < total) {
+            dfree(c, c.big_keys); dfree(c, c.big_keys_alt); dfree(c, c.big_ids); dfree(c, c.big_ids_alt);
+            c.big_keys = c.big_keys_alt = nullptr; c.big_ids = c.big_ids_alt = nullptr;
+            const uint64_t cap = total + total / 4 + 1024;
+            if (!dalloc_t(c, &c.big_keys, cap) || !dalloc_t(c, &c.big_keys_alt, cap) ||
+                !dalloc_t(c, &c.big_ids, cap) || !dalloc_t(c, &c.big_ids_alt, cap)) {
+                c.simpstate = PFG_OTALLOC_FAIL; c.big_cap = 0; return false;
+            }
+            c.big_cap = cap;
+        }
+        big_gather_k<<<std::min<uint32_t>(nbig, 4096), 256, 0, c.s>>>(c.hdr, c.lits, c.big_lists, nbig, c.ot_off,
+                                                                     c.ot_size, boff, c.ot_ids, c.big_keys,
+                                                                     c.big_ids, by_id);
+        const uint32_t nchunks = (maxn + MID_MAX - 1) / MID_MAX;
+        big_chunk_k<<<dim3(nchunks, nbig), MID_THREADS, 0, c.s>>>(c.big_lists, c.ot_size, boff, c.big_keys, c.big_ids);
+        g_launches += 3;
+        uint4* k0 = c.big_keys; uint4* k1 = c.big_keys_alt;
+        uint32_t* i0 = c.big_ids; uint32_t* i1 = c.big_ids_alt;
+        for (uint32_t R = MID_MAX; R < maxn; R <<= 1) {
+            const uint32_t gx = std::min<uint32_t>((maxn + 255) / 256, 1024);
+            big_merge_k<<<dim3(gx, nbig), 256, 0, c.s>>>(c.big_lists, c.ot_size, boff, R, k0, i0, k1, i1);
+            g_launches += 1;
+            std::swap(k0, k1); std::swap(i0, i1);
+        }
+        big_scatter_k<<<std::min<uint32_t>(nbig, 4096), 256, 0, c.s>>>(c.big_lists, nbig, c.ot_off, c.ot_size,
+                                                                      boff, i0, c.ot_ids);
+        g_launches += 1;
+    }
+    return cuda_ok(c, cudaGetLastError(), "ot_sort");
+}
+
+}  // namespace pfg

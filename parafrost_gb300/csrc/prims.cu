@@ -1,0 +1,254 @@
+// Device-wide scan, stable radix sort and compaction (see prims.cuh).
+#include "prims.cuh"
+
+namespace pfg {
+
+thread_local uint64_t g_launches = 0;
+
+namespace {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
+    const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        T o = __shfl_up_sync(0xFFFFFFFFu, v, d);
+        if (lane >= (unsigned)d) v += o;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+template <typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T& total) {
+    __shared__ T warp_tot[SCAN_THREADS / 32];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    T incl = warp_incl_scan(v);
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        T w = (lane < SCAN_THREADS / 32) ? warp_tot[lane] : T(0);
+        T wi = warp_incl_scan(w);
+        if (lane < SCAN_THREADS / 32) warp_tot[lane] = wi - w;
+    }
+    __syncthreads();
+    T excl = incl - v + warp_tot[warp];
+    // block total = last thread's inclusive value
+    __shared__ T tot;
+    if (threadIdx.x == SCAN_THREADS - 1) tot = excl + v;
+    __syncthreads();
+    total = tot;
+    __syncthreads();
+    return excl;
+}
+
+// Phase 1: scan each tile locally, emit tile totals.
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_tiles_k(const T* in, T* out, uint64_t n, T* tile_sums) {
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    __shared__ T sh[SCAN_TILE];
+    // coalesced striped load into shared memory
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
+        sh[i * SCAN_THREADS + threadIdx.x] = idx < n ? in[idx] : T(0);
+    }
+    __syncthreads();
+    T loc[SCAN_ITEMS];
+    T sum = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        loc[i] = sum;
+        sum += sh[threadIdx.x * SCAN_ITEMS + i];
+    }
+    T total;
+    const T excl = block_excl_scan<T>(sum, total);
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) sh[threadIdx.x * SCAN_ITEMS + i] = loc[i] + excl;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
+        if (idx < n) out[idx] = sh[i * SCAN_THREADS + threadIdx.x];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// Phase 2: one block scans the tile totals sequentially in chunks.
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_sums_k(T* sums, uint64_t nt, T init, T* total_out) {
+    T carry = init;
+    for (uint64_t b = 0; b < nt; b += SCAN_THREADS) {
+        const uint64_t i = b + threadIdx.x;
+        const T v = i < nt ? sums[i] : T(0);
+        T tot;
+        const T ex = block_excl_scan<T>(v, tot);
+        if (i < nt) sums[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0 && total_out) *total_out = carry;
+}
+
+// Phase 3: add the tile offsets.
+template <typename T>
+__global__ void scan_add_k(T* out, uint64_t n, const T* sums) {
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    const T add = sums[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
+        if (idx < n) out[idx] += add;
+    }
+}
+
+template <typename T>
+void excl_scan(const T* in, T* out, uint64_t n, T init, T* total_out, void* tmp, cudaStream_t s) {
+    if (n == 0) {
+        if (total_out) cudaMemcpyAsync(total_out, &init, sizeof(T), cudaMemcpyHostToDevice, s);
+        return;
+    }
+    const uint64_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
+    T* sums = (T*)tmp;
+    scan_tiles_k<T><<<(unsigned)nt, SCAN_THREADS, 0, s>>>(in, out, n, sums);
+    scan_sums_k<T><<<1, SCAN_THREADS, 0, s>>>(sums, nt, init, total_out);
+    scan_add_k<T><<<(unsigned)nt, SCAN_THREADS, 0, s>>>(out, n, sums);
+    g_launches += 3;
+}
+
+// ---------------- radix sort ----------------
+constexpr int RS_THREADS = 256;
+constexpr int RS_ROUNDS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
+constexpr int RS_WARPS = RS_THREADS / 32;
+
+__global__ void __launch_bounds__(RS_THREADS) radix_hist_k(const uint32_t* keys, uint64_t n, int shift,
+                                                          uint32_t* hist, uint32_t nblocks) {
+    __shared__ uint32_t cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t base = (uint64_t)blockIdx.x * RS_TILE;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const uint64_t idx = base + (uint64_t)r * RS_THREADS + threadIdx.x;
+        if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(RS_THREADS) radix_scatter_k(const uint32_t* keys, const uint32_t* vals,
+                                                             uint32_t* kout, uint32_t* vout, uint64_t n,
+                                                             int shift, const uint32_t* offs, uint32_t nblocks) {
+    __shared__ uint32_t tab[RS_WARPS][257];
+    __shared__ uint32_t run[256];
+    __shared__ uint32_t gbase[256];
+    gbase[threadIdx.x] = offs[(uint64_t)threadIdx.x * nblocks + blockIdx.x];
+    run[threadIdx.x] = 0;
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    const uint64_t base = (uint64_t)blockIdx.x * RS_TILE;
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        for (int i = threadIdx.x; i < RS_WARPS * 257; i += RS_THREADS) (&tab[0][0])[i] = 0;
+        __syncthreads();
+        const uint64_t idx = base + (uint64_t)r * RS_THREADS + threadIdx.x;
+        const bool valid = idx < n;
+        uint32_t k = 0, v = 0, d = 256;
+        if (valid) { k = keys[idx]; v = vals[idx]; d = (k >> shift) & 0xFFu; }
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const unsigned wrank = __popc(peers & lt);
+        if (wrank == 0 && d != 256) tab[warp][d] = __popc(peers);
+        __syncthreads();
+        {   // per-digit exclusive prefix over warps, continuing the running totals
+            const uint32_t dg = threadIdx.x;
+            uint32_t acc = run[dg];
+#pragma unroll
+            for (int w = 0; w < RS_WARPS; w++) {
+                const uint32_t t = tab[w][dg];
+                tab[w][dg] = acc;
+                acc += t;
+            }
+            run[dg] = acc;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t dst = gbase[d] + tab[warp][d] + wrank;
+            kout[dst] = k;
+            vout[dst] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------- compaction ----------------
+__global__ void flags_to_u32_k(const uint8_t* flags, uint32_t* out, uint64_t n) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = flags[i] ? 1u : 0u;
+}
+
+__global__ void select_scatter_k(const uint32_t* in, const uint8_t* flags, const uint32_t* pos, uint32_t* out, uint64_t n) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        if (flags[i]) out[pos[i]] = in ? in[i] : (uint32_t)i;
+}
+
+}  // namespace
+
+size_t scan_temp_bytes(uint64_t n) {
+    return ((n + SCAN_TILE - 1) / SCAN_TILE + 1) * sizeof(unsigned long long) + 256;
+}
+
+size_t radix_temp_bytes(uint64_t n) {
+    const uint64_t nb = (n + RS_TILE - 1) / RS_TILE;
+    const uint64_t h = 256 * nb;
+    return h * sizeof(uint32_t) + scan_temp_bytes(h) + 512;
+}
+
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t init,
+                        uint32_t* total_out, void* tmp, cudaStream_t s) {
+    excl_scan<uint32_t>(in, out, n, init, total_out, tmp, s);
+}
+
+void exclusive_scan_u64(const unsigned long long* in, unsigned long long* out, uint64_t n,
+                        unsigned long long init, unsigned long long* total_out, void* tmp,
+                        cudaStream_t s) {
+    excl_scan<unsigned long long>(in, out, n, init, total_out, tmp, s);
+}
+
+int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint64_t n,
+                     int begin_bit, int end_bit, void* tmp, cudaStream_t s) {
+    if (n <= 1) return 0;
+    const uint64_t nb = (n + RS_TILE - 1) / RS_TILE;
+    uint32_t* hist = (uint32_t*)tmp;
+    void* stmp = (void*)(((uintptr_t)(hist + 256 * nb) + 255) & ~(uintptr_t)255);
+    int cur = 0;
+    for (int sh = begin_bit; sh < end_bit; sh += 8) {
+        const uint32_t* ki = cur ? k1 : k0;
+        const uint32_t* vi = cur ? v1 : v0;
+        uint32_t* ko = cur ? k0 : k1;
+        uint32_t* vo = cur ? v0 : v1;
+        radix_hist_k<<<(unsigned)nb, RS_THREADS, 0, s>>>(ki, n, sh, hist, (uint32_t)nb);
+        excl_scan<uint32_t>(hist, hist, 256 * nb, 0u, nullptr, stmp, s);
+        radix_scatter_k<<<(unsigned)nb, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n, sh, hist, (uint32_t)nb);
+        g_launches += 2;
+        cur ^= 1;
+    }
+    return cur;
+}
+
+void select_flagged(const uint32_t* in, const uint8_t* flags, uint32_t* out, uint64_t n,
+                    uint32_t* count_out, uint32_t* scan_buf, void* tmp, cudaStream_t s) {
+    if (n == 0) {
+        cudaMemsetAsync(count_out, 0, sizeof(uint32_t), s);
+        return;
+    }
+    flags_to_u32_k<<<grid_for(n, 256), 256, 0, s>>>(flags, scan_buf, n);
+    excl_scan<uint32_t>(scan_buf, scan_buf, n, 0u, count_out, tmp, s);
+    select_scatter_k<<<grid_for(n, 256), 256, 0, s>>>(in, flags, scan_buf, out, n);
+    g_launches += 2;
+}
+
+}  // namespace pfg

@@ -1,0 +1,49 @@
+// Device-wide primitives of the engine: exclusive scans, stable LSD radix
+// sort and stream compaction. They replace the reference's CUB/Thrust calls
+// (DeviceScan: elimination.cu:85-92, memory.cu:429-430, recycle.cu:84-93;
+// DeviceSelect: elimination.cu:253-256, cnf.cu:218-222; thrust::sort:
+// lcve.cu:294, histogram.cu:65).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pfg {
+
+// Every launcher counts its kernel launches here (per host thread).
+extern thread_local uint64_t g_launches;
+
+// Scratch bytes needed by the scans / sorts below for n elements.
+size_t scan_temp_bytes(uint64_t n);
+size_t radix_temp_bytes(uint64_t n);
+
+// out[i] = init + sum(in[0..i)); optional *total_out (device) = init + sum(in).
+// in and out may alias.
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t init,
+                        uint32_t* total_out, void* tmp, cudaStream_t s);
+void exclusive_scan_u64(const unsigned long long* in, unsigned long long* out, uint64_t n,
+                        unsigned long long init, unsigned long long* total_out, void* tmp,
+                        cudaStream_t s);
+
+// Stable LSD radix sort of (key, value) pairs on bits [begin_bit, end_bit).
+// Ping-pongs between (k0, v0) and (k1, v1); returns 0 if the result is in
+// (k0, v0), 1 if in (k1, v1).
+int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint64_t n,
+                     int begin_bit, int end_bit, void* tmp, cudaStream_t s);
+
+// Stable compaction: out[j] = in[i] for flags[i] != 0 in order; *count_out
+// (device) = number kept. `scan_buf` holds n+1 uint32.
+void select_flagged(const uint32_t* in, const uint8_t* flags, uint32_t* out, uint64_t n,
+                    uint32_t* count_out, uint32_t* scan_buf, void* tmp, cudaStream_t s);
+
+// Grid size helper: enough blocks to cover n with `threads`, capped at 152 SMs x `per_sm`.
+inline unsigned grid_for(uint64_t n, unsigned threads, unsigned per_sm = 32) {
+    uint64_t b = (n + threads - 1) / threads;
+    const uint64_t cap = 152ull * per_sm;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+}  // namespace pfg

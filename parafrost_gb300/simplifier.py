@@ -1,0 +1,139 @@
+"""Host-side mirror of ParaFROST's GPU simplify entry point.
+
+`Simplifier.simplify(cnf)` does what `Solver::simplify` (src/gpu/simplify.cu:57)
+does for one clause database: upload (awaken, simplify.cu:77-134), run the
+simplification rounds until the reference's stop rule (simplify.cu:163-186),
+and return the simplified CNF, the eliminated-variable bytes, the units fixed
+by device propagation and the model-reconstruction stack (simplify.cu:190-240).
+Options use the reference's CLI names (`phases`, `electionsmax`, `ere`, ...).
+
+Every call goes through the C ABI of include/pfgpu.h into the CUDA engine.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from . import _abi, _lib
+from .cnf import Cnf
+
+
+class SimplifyError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{_abi.RETURN_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+def _ptr(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+@dataclass
+class SimplifyResult:
+    status: int                      # 0 unknown, 10 SAT (no clause left), 20 UNSAT
+    cnf: Cnf                         # simplified clause database (clause order kept)
+    eliminated: np.ndarray           # uint8[max_var+1]: MELTING 1 | ADDING 2 | FORCED 4
+    units: np.ndarray                # literals fixed by device propagation (sorted)
+    pending_units: np.ndarray        # units of the last round not yet propagated (sorted)
+    stack: np.ndarray                # model-reconstruction words
+    round_ends: np.ndarray           # stack length after each SUB+BVE round
+    stats: dict = field(default_factory=dict)
+
+    def eliminated_vars(self) -> np.ndarray:
+        e = self.eliminated
+        return np.nonzero((e & 1) & ~((e >> 2) & 1))[0].astype(np.uint32)
+
+
+class Simplifier:
+    """One device-resident instance at a time (a `pfg_ctx`)."""
+
+    def __init__(self, arena_bytes: int = 0, **options):
+        self.lib = _lib.lib()
+        self.options = _abi.options_from(**options)
+        self._ctx = C.c_void_p()
+        rc = self.lib.pfg_create(C.byref(self._ctx), C.byref(self.options), arena_bytes)
+        if rc != 0:
+            raise SimplifyError(rc, "pfg_create failed (is a CUDA device visible?)")
+        self.last_stats: Optional[_abi.PfgStats] = None
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.lib.pfg_last_error(self._ctx)
+            raise SimplifyError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def upload(self, cnf: Cnf, var_state: Optional[np.ndarray] = None, assumed: Optional[np.ndarray] = None,
+               vorg: Optional[np.ndarray] = None) -> None:
+        vs = None if var_state is None else np.ascontiguousarray(var_state, dtype=np.uint8)
+        asd = None if assumed is None else np.ascontiguousarray(assumed, dtype=np.uint8)
+        vo = None if vorg is None else np.ascontiguousarray(vorg, dtype=np.uint32)
+        rc = self.lib.pfg_upload(self._ctx, cnf.max_var, cnf.num_clauses, _ptr(cnf.lits, C.c_uint32),
+                                 _ptr(cnf.off, C.c_uint64), _ptr(cnf.learnt, C.c_uint8), _ptr(cnf.lbd, C.c_uint32),
+                                 _ptr(cnf.usage, C.c_uint8), _ptr(vs, C.c_uint8), _ptr(asd, C.c_uint8),
+                                 _ptr(vo, C.c_uint32))
+        self._check(rc, "pfg_upload")
+
+    def run(self) -> _abi.PfgStats:
+        st = _abi.PfgStats()
+        rc = self.lib.pfg_simplify(self._ctx, C.byref(st))
+        self.last_stats = st
+        self._check(rc, "pfg_simplify")
+        return st
+
+    def download(self) -> SimplifyResult:
+        sz = _abi.PfgResultSizes()
+        self._check(self.lib.pfg_result_sizes_get(self._ctx, C.byref(sz)), "pfg_result_sizes_get")
+        lits = np.empty(sz.literals, dtype=np.uint32)
+        off = np.empty(sz.clauses + 1, dtype=np.uint64)
+        learnt = np.empty(sz.clauses, dtype=np.uint8)
+        lbd = np.empty(sz.clauses, dtype=np.uint32)
+        usage = np.empty(sz.clauses, dtype=np.uint8)
+        elim = np.empty(sz.max_var + 1, dtype=np.uint8)
+        units = np.empty(sz.units, dtype=np.uint32)
+        pend = np.empty(sz.pending_units, dtype=np.uint32)
+        stack = np.empty(sz.stack_words, dtype=np.uint32)
+        rends = np.empty(sz.rounds, dtype=np.uint64)
+        rc = self.lib.pfg_download(self._ctx, _ptr(lits, C.c_uint32), _ptr(off, C.c_uint64), _ptr(learnt, C.c_uint8),
+                                   _ptr(lbd, C.c_uint32), _ptr(usage, C.c_uint8), _ptr(elim, C.c_uint8),
+                                   _ptr(units, C.c_uint32), _ptr(pend, C.c_uint32), _ptr(stack, C.c_uint32),
+                                   _ptr(rends, C.c_uint64))
+        self._check(rc, "pfg_download")
+        st = self.last_stats
+        stats = {}
+        if st is not None:
+            stats = {f[0]: getattr(st, f[0]) for f in _abi.PfgStats._fields_ if f[0] != "pass_ms"}
+            stats["pass_ms"] = dict(zip(_abi.PASS_NAMES, list(st.pass_ms)))
+        return SimplifyResult(int(st.status) if st is not None else 0,
+                              Cnf(sz.max_var, lits, off, learnt, lbd, usage), elim, units, pend, stack, rends, stats)
+
+    def simplify(self, cnf: Cnf, var_state=None, assumed=None, vorg=None) -> SimplifyResult:
+        self.upload(cnf, var_state, assumed, vorg)
+        self.run()
+        return self.download()
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.pfg_kernel_launches(self._ctx))
+
+    def close(self) -> None:
+        if self._ctx:
+            self.lib.pfg_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def simplify(cnf: Cnf, **options) -> SimplifyResult:
+    with Simplifier(**options) as s:
+        return s.simplify(cnf)
