@@ -517,6 +517,12 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
             c.multiplier += (c.phase == c.o.phases);
             if (!c.err.empty()) break;
         }
+        if (c.err.empty()) {   // ERE deletes after the last count (the write-back recounts, cnf.cu:211-224)
+            count_live(c);
+            sync_counters(c);
+            c.numClauses = c.hc->live_cls;
+            c.numLiterals = c.hc->live_lits;
+        }
         if (c.status != PFG_UNSAT && c.err.empty() && !c.numClauses) c.status = PFG_SAT;
     }
     cudaEventRecord(c.ev_end, c.s);

@@ -140,14 +140,14 @@ __global__ void big_gather_k(const ClsHdr* hdr, const uint32_t* lits, const uint
 }
 
 // chunk sort of big lists: block (b, chunk)
-__global__ void __launch_bounds__(MID_THREADS) big_chunk_k(const uint32_t* big_lists, const uint32_t* size,
+__global__ void __launch_bounds__(MID_THREADS) big_chunk_k(const uint32_t* big_lists, uint32_t nbig, const uint32_t* size,
                                                           const uint32_t* boff, uint4* bk, uint32_t* bid) {
     __shared__ uint4 sk[MID_MAX];
     __shared__ uint32_t sid[MID_MAX];
-    const uint32_t b = blockIdx.y;
+    for (uint32_t b = blockIdx.y; b < nbig; b += gridDim.y) {
     const uint32_t n = size[big_lists[b]];
     const uint32_t cs = blockIdx.x * MID_MAX;
-    if (cs >= n) return;
+    if (cs >= n) continue;
     const uint32_t m = min(MID_MAX, n - cs);
     const uint32_t a = boff[b] + cs;
     uint32_t P = 1;
@@ -159,12 +159,14 @@ __global__ void __launch_bounds__(MID_THREADS) big_chunk_k(const uint32_t* big_l
     __syncthreads();
     bitonic_smem(sk, sid, P);
     for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) { bid[a + i] = sid[i]; bk[a + i] = sk[i]; }
+    __syncthreads();
+    }
 }
 
 // one merge pass: runs of length R merged pairwise (element-parallel binary search)
-__global__ void big_merge_k(const uint32_t* big_lists, const uint32_t* size, const uint32_t* boff, uint32_t R,
-                            const uint4* bk, const uint32_t* bid, uint4* bk2, uint32_t* bid2) {
-    const uint32_t b = blockIdx.y;
+__global__ void big_merge_k(const uint32_t* big_lists, uint32_t nbig, const uint32_t* size, const uint32_t* boff,
+                            uint32_t R, const uint4* bk, const uint32_t* bid, uint4* bk2, uint32_t* bid2) {
+    for (uint32_t b = blockIdx.y; b < nbig; b += gridDim.y) {
     const uint32_t n = size[big_lists[b]];
     const uint32_t a = boff[b];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -185,6 +187,7 @@ __global__ void big_merge_k(const uint32_t* big_lists, const uint32_t* size, con
         const uint32_t dst = pair + (i - s) + (lo - ps);
         bk2[a + dst] = mk;
         bid2[a + dst] = mi;
+    }
     }
 }
 
@@ -275,13 +278,14 @@ bool ot_sort(Ctx& c, bool by_id) {
                                                                      c.ot_size, boff, c.ot_ids, c.big_keys,
                                                                      c.big_ids, by_id);
         const uint32_t nchunks = (maxn + MID_MAX - 1) / MID_MAX;
-        big_chunk_k<<<dim3(nchunks, nbig), MID_THREADS, 0, c.s>>>(c.big_lists, c.ot_size, boff, c.big_keys, c.big_ids);
+        const uint32_t gy = std::min<uint32_t>(nbig, 65535);
+        big_chunk_k<<<dim3(nchunks, gy), MID_THREADS, 0, c.s>>>(c.big_lists, nbig, c.ot_size, boff, c.big_keys, c.big_ids);
         g_launches += 3;
         uint4* k0 = c.big_keys; uint4* k1 = c.big_keys_alt;
         uint32_t* i0 = c.big_ids; uint32_t* i1 = c.big_ids_alt;
         for (uint32_t R = MID_MAX; R < maxn; R <<= 1) {
             const uint32_t gx = std::min<uint32_t>((maxn + 255) / 256, 1024);
-            big_merge_k<<<dim3(gx, nbig), 256, 0, c.s>>>(c.big_lists, c.ot_size, boff, R, k0, i0, k1, i1);
+            big_merge_k<<<dim3(gx, gy), 256, 0, c.s>>>(c.big_lists, nbig, c.ot_size, boff, R, k0, i0, k1, i1);
             g_launches += 1;
             std::swap(k0, k1); std::swap(i0, i1);
         }

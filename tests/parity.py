@@ -7,16 +7,25 @@ from oracle import pyoracle as po
 
 
 def canon(res):
+    """Canonical outputs. Units are sets. When device propagation finds a
+    conflict (UNSAT) the reference stops the solver on the spot
+    (src/gpu/elimbcp.cu:180, simplify.cu:168): the CNF is left untouched, and
+    which units were assigned before the conflict was seen depends on the
+    propagation schedule, so forced units are not compared then."""
     lits, off, learnt, lbd, usage = po.canon_cnf(res.cnf)
-    return {
+    unsat = int(res.status) == pg.PFG_UNSAT
+    elim = np.asarray(res.eliminated)
+    out = {
         "lits": lits, "off": off, "learnt": learnt, "lbd": lbd, "usage": usage,
-        "eliminated": np.asarray(res.eliminated),
-        "units": np.asarray(res.units),
-        "pending": np.asarray(res.pending_units),
+        "eliminated": (elim & 0x3) if unsat else elim,
         "stack": po.canon_stack(res.stack, res.round_ends),
         "rounds": len(res.round_ends),
         "status": int(res.status),
     }
+    if not unsat:
+        out["units"] = np.unique(np.asarray(res.units))
+        out["pending"] = np.unique(np.asarray(res.pending_units))
+    return out
 
 
 def diff(a, b):
