@@ -1,0 +1,328 @@
+#!/usr/bin/env python3
+"""Benchmark of the GPU simplify path: inprocessing clauses/s (SUB + BVE rounds).
+
+One step = one full `Solver::simplify`-equivalent call (all rounds until the
+reference's stop rule) on one seeded synthetic instance. The metric counts,
+per step, the live clauses entering every SUB+BVE round (sum of C_in).
+
+  value : clauses/s with the instance resident in HBM when timing starts
+          (CUDA events around the engine's rounds on its own stream);
+  e2e   : the same metric through the C ABI with host buffers: upload (H2D),
+          simplify and download (D2H) inside the timed region.
+
+`--impl reference` times the CPU restatement of the same passes (the oracle
+port; the reference's GPU simplifier cannot run here) on all host cores, one
+independent replica per core.
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # configs[1]: plain GPU method on a Tseitin circuit (the default bench line)
+    "tseitin": dict(family=1, a=1_000_000, b=50_000, c=1_000, seed=1,
+                    desc="Tseitin circuit: 1M 2-input gates (40% AND, 30% OR, 30% XOR) over 50k inputs, "
+                         "1k outputs asserted and root-propagated"),
+    # configs[0]: uniform random 3-SAT, 20k vars, 85.2k clauses
+    "ksat": dict(family=0, a=20_000, b=85_200, c=3, seed=1,
+                 desc="uniform random 3-SAT, 20,000 vars, 85,200 clauses"),
+    # configs[2]: scale-free, 4M vars, 16M clauses, planted model so all 5 rounds run
+    "scalefree": dict(family=2, a=4_000_000, b=16_000_000, c=1, seed=1,
+                      desc="scale-free CNF, 4M vars, 16M clauses, power-law exponent 2.5, "
+                           "geometric lengths on [2,50] mean 4, planted model"),
+}
+
+METRIC = "inprocessing clauses/s (BVE+SUB)"
+UNIT = "clauses/s"
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_cnf(w):
+    import parafrost_gb300 as pg
+    return pg.generate(w["family"], w["a"], w["b"], w["c"], w["seed"])
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.path = tempfile.mktemp(prefix="clocks", suffix=".csv")
+        self.p = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx = max(mx, float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def oracle_run(args):
+    """One replica of the CPU restatement (run in a spawned worker)."""
+    wname, opts = args
+    sys.path.insert(0, ROOT)
+    import parafrost_gb300 as pg
+    from oracle import pyoracle as po
+    cnf = make_cnf(WORKLOADS[wname])
+    t0 = time.perf_counter()
+    r = po.simplify(cnf, pg.options_from(**opts))
+    dt = time.perf_counter() - t0
+    processed = sum(s["clauses_before"] for s in r.round_stats)
+    return processed, dt
+
+
+def cpu_baseline(wname, opts, cores):
+    """Oracle port timed on host cores: `cores` independent replicas at once."""
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(oracle_run, [(wname, opts)] * cores)
+        wall = time.perf_counter() - t0
+    processed = sum(r[0] for r in res)
+    return processed, wall, res
+
+
+def run_reference(a, world, rank):
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    opts = {}
+    for _ in range(a.warmup):
+        cpu_baseline(a.workload, opts, cores)
+    times, proc = [], 0
+    for _ in range(a.steps):
+        p, wall, _ = cpu_baseline(a.workload, opts, cores)
+        proc += p
+        times.append(wall)
+    total = sum(times)
+    value = proc / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1000.0 * total / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator)",
+        "config": {"workload": a.workload, "desc": WORKLOADS[a.workload]["desc"], "options": "reference defaults"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} concurrent replicas of the full workload per step (oracle/pfo.c, "
+                                   f"single-threaded each)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(a, world, rank, local):
+    import numpy as np
+    import torch
+    import parafrost_gb300 as pg
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+
+    w = WORKLOADS[a.workload]
+    cnf = make_cnf(w)
+    sim = pg.Simplifier()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    for _ in range(a.warmup):
+        sim.upload(cnf)
+        sim.run()
+        sim.download()
+    # ---- device-timed region: HBM-resident input, rounds timed with CUDA events ----
+    sim.profile(True)
+    sim.profile_reset()
+    clocks = Clocks(local)
+    barrier()
+    clocks.start()
+    dev_ms, processed, launches, alg = 0.0, 0, 0, 0
+    last = None
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        sim.upload(cnf)
+        flush.fill_(1.0)
+        st = sim.run()
+        dev_ms += st.device_ms
+        processed += st.clauses_processed
+        launches += st.kernel_launches
+        alg += st.alg_bytes
+        last = st
+    barrier()
+    wall_ms = (time.perf_counter() - t0) * 1000
+    clk = clocks.stop()
+    prof = sim.profile_report()
+    sim.profile(False)
+    # ---- end-to-end through the C ABI with host buffers ----
+    barrier()
+    e2e_s, e2e_proc, h2d, d2h = 0.0, 0, 0, 0
+    for _ in range(a.steps):
+        t1 = time.perf_counter()
+        sim.upload(cnf)
+        st = sim.run()
+        res = sim.download()
+        e2e_s += time.perf_counter() - t1
+        e2e_proc += st.clauses_processed
+        h2d = cnf.lits.nbytes + cnf.off.nbytes
+        d2h = (res.cnf.lits.nbytes + res.cnf.off.nbytes + res.cnf.learnt.nbytes + res.cnf.lbd.nbytes +
+               res.cnf.usage.nbytes + res.eliminated.nbytes + res.units.nbytes + res.pending_units.nbytes +
+               res.stack.nbytes)
+    barrier()
+    dev_ms_max = max_over_ranks(dev_ms)
+    total_proc = sum_over_ranks(processed)
+    e2e_max = max_over_ranks(e2e_s)
+    e2e_total = sum_over_ranks(e2e_proc)
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    value = total_proc / (dev_ms_max / 1000.0)
+    # roofline of the dominant kernel group (most device time in the timed region)
+    peak, peak_kind = load_peaks()
+    dom_name, dom = max(((k, v) for k, v in prof.items() if v["ms"] > 0), key=lambda kv: kv[1]["ms"])
+    achieved = (dom["alg_bytes"] / 1e9) / (dom["ms"] / 1e3) if dom["ms"] > 0 else 0.0
+    roofline = {
+        "bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_kind, "traffic": TRAFFIC.get((a.workload, dom_name)),
+        "launches": dom["launches"], "ms_per_launch": dom["ms"] / max(1, dom["launches"]),
+        "alg_bytes_per_launch": dom["alg_bytes"] / max(1, dom["launches"]),
+        "share": dom["ms"] / sum(v["ms"] for v in prof.values()),
+        "all_alg_bytes_gbs": (alg / 1e9) / (dev_ms / 1e3),
+    }
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": dev_ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic (seeded generator)",
+        "config": {"workload": a.workload, "desc": WORKLOADS[a.workload]["desc"],
+                   "options": "reference defaults (phases=5, ERE on)",
+                   "clauses_in": int(cnf.num_clauses), "literals_in": int(cnf.num_literals),
+                   "clauses_out": int(last.clauses_out), "rounds": int(last.rounds),
+                   "l2": "256 MB buffer written between steps; instance working set > L2",
+                   "parallelism": "replicas only" if world > 1 else "single GPU",
+                   "wall_ms_per_step_incl_upload": wall_ms / a.steps},
+        "e2e": {"value": e2e_total / e2e_max, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_max / a.steps},
+        "roofline": roofline,
+        "gpu_launches": int(launches),
+        "kernel_ms": {k: round(v["ms"] / a.steps, 4) for k, v in prof.items() if v["launches"]},
+        "clocks": clk,
+    }
+    if not a.no_cpu_baseline:
+        p, wall, _ = cpu_baseline(a.workload, {}, 1)
+        line["cpu_baseline"] = {"value": p / wall, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": "the full workload once (oracle/pfo.c, one thread)"}
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+# DRAM traffic per launch of the dominant kernel group from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (workload, group).
+TRAFFIC = {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="tseitin", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--single-step", action="store_true",
+                    help="one simplify call of the workload, nothing timed (the command profiled by ncu)")
+    a = ap.parse_args()
+    world, rank, local = dist_setup()
+    if a.single_step:
+        import parafrost_gb300 as pg
+        cnf = make_cnf(WORKLOADS[a.workload])
+        with pg.Simplifier() as sim:
+            res = sim.simplify(cnf)
+        print(json.dumps({"workload": a.workload, "clauses_out": int(res.cnf.num_clauses),
+                          "launches": int(res.stats["kernel_launches"])}))
+        return 0
+    if a.impl == "reference":
+        return run_reference(a, world, rank)
+    return run_gpu(a, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -192,12 +192,24 @@ const char* pfg_last_error(pfg_ctx* ctx);
 uint64_t pfg_kernel_launches(pfg_ctx* ctx);
 
 /*
+ * Per-kernel profiling of pfg_simplify. Launch counts are always kept; with
+ * profiling enabled every launch is also bracketed by CUDA events on the
+ * context's stream. Kernel groups are numbered 0 .. pfg_profile_count()-1;
+ * alg_bytes is the algorithmic byte count of the group (byte model in the design doc).
+ */
+int  pfg_profile_enable(pfg_ctx* ctx, int on);
+void pfg_profile_reset(pfg_ctx* ctx);
+int  pfg_profile_count(void);
+const char* pfg_profile_name(int id);
+int  pfg_profile_get(pfg_ctx* ctx, int id, uint64_t* launches, double* ms, uint64_t* alg_bytes);
+
+/*
  * Host-side synthetic CNF generators (the seeded families used by the
  * benchmark and the tests). They write into caller buffers; call once with
  * lits == NULL to get the sizes.
  *   family 0: uniform random k-SAT   (a = vars, b = clauses, c = k)
  *   family 1: Tseitin circuit        (a = gates, b = primary inputs, c = outputs)
- *   family 2: scale-free CNF         (a = vars, b = clauses, c unused)
+ *   family 2: scale-free CNF         (a = vars, b = clauses, c = 1: planted model)
  */
 int  pfg_generate(int family, uint64_t a, uint64_t b, uint64_t c, uint64_t seed,
                   uint32_t* max_var, uint64_t* num_clauses, uint64_t* num_lits,

@@ -46,6 +46,16 @@ def lib():
     L.pfg_last_error.restype = C.c_char_p
     L.pfg_kernel_launches.argtypes = [C.c_void_p]
     L.pfg_kernel_launches.restype = C.c_uint64
+    L.pfg_profile_enable.argtypes = [C.c_void_p, C.c_int]
+    L.pfg_profile_enable.restype = C.c_int
+    L.pfg_profile_reset.argtypes = [C.c_void_p]
+    L.pfg_profile_reset.restype = None
+    L.pfg_profile_count.argtypes = []
+    L.pfg_profile_count.restype = C.c_int
+    L.pfg_profile_name.argtypes = [C.c_int]
+    L.pfg_profile_name.restype = C.c_char_p
+    L.pfg_profile_get.argtypes = [C.c_void_p, C.c_int, u64p, C.POINTER(C.c_double), u64p]
+    L.pfg_profile_get.restype = C.c_int
     L.pfg_generate.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64,
                                u32p, u64p, u64p, u32p, u64p]
     L.pfg_generate.restype = C.c_int
@@ -57,5 +67,6 @@ def lib():
 EXPORTED = (
     "pfg_default_options", "pfg_resolve_options", "pfg_create", "pfg_upload", "pfg_simplify",
     "pfg_result_sizes_get", "pfg_download", "pfg_destroy", "pfg_last_error", "pfg_kernel_launches",
-    "pfg_generate",
+    "pfg_generate", "pfg_profile_enable", "pfg_profile_reset", "pfg_profile_count", "pfg_profile_name",
+    "pfg_profile_get",
 )

@@ -101,8 +101,9 @@ def tseitin(gates: int, inputs: int, outputs: int, seed: int = 1) -> Cnf:
     return generate(FAMILY_TSEITIN, gates, inputs, outputs, seed)
 
 
-def scale_free(num_vars: int, num_clauses: int, seed: int = 1) -> Cnf:
-    return generate(FAMILY_SCALEFREE, num_vars, num_clauses, 0, seed)
+def scale_free(num_vars: int, num_clauses: int, seed: int = 1, planted: bool = False) -> Cnf:
+    """Scale-free CNF; `planted` keeps it satisfiable with a hidden model."""
+    return generate(FAMILY_SCALEFREE, num_vars, num_clauses, 1 if planted else 0, seed)
 
 
 def write_dimacs(cnf: Cnf, path: str, extra_units: Iterable[int] = ()) -> None:

@@ -126,21 +126,19 @@ bool bcp_prop(Ctx& c, bool& ok) {
     cudaMemsetAsync(&c.dc->bcp_curr, 0, 3 * sizeof(uint32_t), c.s);
     const uint32_t trail_before = c.hc->ntrail;
     // seed: assigned literals go to front_a through bcp_next, then advance to level 0
-    bcp_seed_k<<<grid_for(c.nUnits, 256), 256, 0, c.s>>>(c.bstate, c.elim, c.units, (uint32_t)c.nUnits, c.front_a,
+    PFG_LAUNCH(K_BCP, bcp_seed_k, grid_for(c.nUnits, 256), 256, 0, c.s, c.bstate, c.elim, c.units, (uint32_t)c.nUnits, c.front_a,
                                                         c.dc, c.trail, c.trail_cap, c.V);
-    bcp_advance_k<<<1, 1, 0, c.s>>>(c.dc);   // curr = seeded, level = 1
+    PFG_LAUNCH(K_BCP, bcp_advance_k, 1, 1, 0, c.s, c.dc);   // curr = seeded, level = 1
     // make level parity start at 0 with the seeds in front_a
     cudaMemsetAsync(&c.dc->bcp_level, 0, sizeof(uint32_t), c.s);
-    g_launches += 2;
     const unsigned grid = 152 * 8;
     uint32_t levels = 0;
     const uint32_t max_levels = c.V + 2;   // every level assigns at least one new variable
     for (int batch = 1;; batch = std::min(batch << 1, 64)) {
         for (int b = 0; b < batch; b++) {
-            bcp_propagate_k<<<grid, 256, 0, c.s>>>(c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids, c.bstate, c.elim,
+            PFG_LAUNCH(K_BCP, bcp_propagate_k, grid, 256, 0, c.s, c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids, c.bstate, c.elim,
                                                    c.front_a, c.front_b, c.dc, c.trail, c.trail_cap, c.V);
-            bcp_advance_k<<<1, 1, 0, c.s>>>(c.dc);
-            g_launches += 2;
+            PFG_LAUNCH(K_BCP, bcp_advance_k, 1, 1, 0, c.s, c.dc);
         }
         levels += batch;
         sync_counters(c);
@@ -150,8 +148,7 @@ bool bcp_prop(Ctx& c, bool& ok) {
     }
     if (c.hc->err) { c.err = "device error during unit propagation"; return false; }
     if (c.hc->conflict) { ok = false; return true; }
-    bcp_apply_k<<<grid_for(c.ncls, 256), 256, 0, c.s>>>(c.hdr, c.lits, c.ncls, c.bstate);
-    g_launches += 1;
+    PFG_LAUNCH(K_BCP, bcp_apply_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.bstate);
     (void)trail_before;
     return cuda_ok(c, cudaGetLastError(), "bcp");
 }

@@ -1054,22 +1054,19 @@ __global__ void keep_u32_k(const uint8_t* keep, uint32_t n, uint32_t* out) {
 
 void sub_pass(Ctx& c) {
     if (!c.nelected) return;
-    sub_k<<<grid_for(c.nelected, 64), 64, 0, c.s>>>(make_ek(c), c.elected, c.nelected);
-    g_launches += 1;
+    PFG_LAUNCH(K_SUB, sub_k, grid_for(c.nelected, 64), 64, 0, c.s, make_ek(c), c.elected, c.nelected);
 }
 
 bool ve_pass(Ctx& c) {
     const uint32_t E = c.nelected;
     if (!E) return true;
     const EK k = make_ek(c);
-    ve1_k<<<grid_for(E, 64), 64, 0, c.s>>>(k, c.elected, E, c.type, c.ucnt, c.rpos, c.rref);
-    g_launches += 1;
+    PFG_LAUNCH(K_VE1, ve1_k, grid_for(E, 64), 64, 0, c.s, k, c.elected, E, c.type, c.ucnt, c.rpos, c.rref);
     if (!ensure_tmp(c, scan_temp_bytes(E))) return false;
     exclusive_scan_u64(c.rpos, c.rpos, E, (unsigned long long)c.ncls, nullptr, c.tmp, c.s);
     exclusive_scan_u64(c.rref, c.rref, E, (unsigned long long)c.data_size, nullptr, c.tmp, c.s);
     cudaMemsetAsync(&c.dc->last_elim, 0xFF, sizeof(int32_t), c.s);   // -1
-    ve3_k<<<grid_for(E, 128), 128, 0, c.s>>>(k, c.elected, E, c.type, c.rpos, c.rref, c.cs_cap, c.data_cap, c.flag8);
-    g_launches += 1;
+    PFG_LAUNCH(K_VE3, ve3_k, grid_for(E, 128), 128, 0, c.s, k, c.elected, E, c.type, c.rpos, c.rref, c.cs_cap, c.data_cap, c.flag8);
     // postVE: keep surviving elected variables in order (elimination.cu:249-267)
     select_flagged(c.elected, c.flag8, c.work, E, &c.dc->survivors, c.vscan, c.tmp, c.s);
     sync_counters(c);
@@ -1095,8 +1092,7 @@ bool ve_pass(Ctx& c) {
 
 void ere_pass(Ctx& c) {
     if (!c.nelected) return;
-    ere_k<<<grid_for((uint64_t)c.nelected * 32, 128), 128, 0, c.s>>>(make_ek(c), c.elected, c.nelected);
-    g_launches += 1;
+    PFG_LAUNCH(K_ERE, ere_k, grid_for((uint64_t)c.nelected * 32, 128), 128, 0, c.s, make_ek(c), c.elected, c.nelected);
 }
 
 }  // namespace pfg

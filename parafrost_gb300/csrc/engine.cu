@@ -195,6 +195,7 @@ void free_all(pfg_ctx* o) {
     fresh.ev_begin = c.ev_begin; fresh.ev_end = c.ev_end; fresh.ev_a = c.ev_a; fresh.ev_b = c.ev_b;
     fresh.dc = nullptr; fresh.hc = c.hc;
     fresh.launches = c.launches;
+    fresh.prof = c.prof;
     c = fresh;
 }
 
@@ -322,6 +323,7 @@ extern "C" int pfg_upload(pfg_ctx* o, uint32_t max_var, uint64_t num_clauses, co
     }
     const uint64_t base_launches = g_launches;
     free_all(o);
+    g_prof = &c.prof;
     c.V = max_var;
     c.nlist = 2ull * max_var + 2;
     uint64_t orgCls = 0, orgLits = 0;
@@ -387,21 +389,21 @@ extern "C" int pfg_upload(pfg_ctx* o, uint32_t max_var, uint64_t num_clauses, co
     if (cls_lbd) cudaMemcpyAsync(d_lbd, cls_lbd, num_clauses * sizeof(uint32_t), cudaMemcpyHostToDevice, c.s);
     if (cls_usage) cudaMemcpyAsync(d_usage, cls_usage, num_clauses, cudaMemcpyHostToDevice, c.s);
     if (num_clauses) {
-        init_hdr_k<<<grid_for(num_clauses, 256), 256, 0, c.s>>>(c.hdr, d_off, num_clauses, d_learnt, d_lbd, d_usage);
-        prep_k<<<grid_for(num_clauses, 128), 128, 0, c.s>>>(c.hdr, c.lits, num_clauses);
-        g_launches += 2;
+        PFG_LAUNCH(K_UPLOAD, init_hdr_k, grid_for(num_clauses, 256), 256, 0, c.s, c.hdr, d_off, num_clauses, d_learnt, d_lbd, d_usage);
+        PFG_LAUNCH(K_UPLOAD, prep_k, grid_for(num_clauses, 128), 128, 0, c.s, c.hdr, c.lits, num_clauses);
     }
     if (var_state) cudaMemcpyAsync(c.vstate, var_state, V1, cudaMemcpyHostToDevice, c.s);
     else cudaMemsetAsync(c.vstate, 0, V1, c.s);
     if (assumed) cudaMemcpyAsync(c.assumed, assumed, V1, cudaMemcpyHostToDevice, c.s);
     if (vorg) cudaMemcpyAsync(c.vorg, vorg, V1 * sizeof(uint32_t), cudaMemcpyHostToDevice, c.s);
-    else { identity_k<<<grid_for(V1, 256), 256, 0, c.s>>>(c.vorg, (uint32_t)V1); g_launches += 1; }
+    else { PFG_LAUNCH(K_UPLOAD, identity_k, grid_for(V1, 256), 256, 0, c.s, c.vorg, (uint32_t)V1); }
     cudaMemsetAsync(c.elim, 0, V1, c.s);
     cudaMemsetAsync(c.varcore, 0, V1 * sizeof(uint32_t), c.s);
     cudaMemsetAsync(c.dc, 0, sizeof(DevCounters), c.s);
     dfree(c, d_off); dfree(c, d_learnt); dfree(c, d_lbd); dfree(c, d_usage);
     sync_counters(c);
     c.launches += g_launches - base_launches;
+    g_prof = nullptr;
     if (!c.err.empty()) return PFG_CUDA_ERROR;
     c.uploaded = true;
     c.simplified = false;
@@ -414,6 +416,8 @@ extern "C" int pfg_upload(pfg_ctx* o, uint32_t max_var, uint64_t num_clauses, co
 }
 
 static int finish(Ctx& c, pfg_stats* st, uint64_t base_launches, int rc) {
+    if (c.prof.on) c.prof.resolve();
+    g_prof = nullptr;
     c.launches += g_launches - base_launches;
     if (st) *st = c.stats;
     return rc;
@@ -425,6 +429,7 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
     if (!c.uploaded) { c.err = "no instance uploaded"; return PFG_INVALID; }
     if (c.simplified) { c.err = "instance already simplified; upload again"; return PFG_INVALID; }
     const uint64_t base_launches = g_launches;
+    g_prof = &c.prof;
     c.err.clear();
     for (double& x : c.pass_ms) x = 0;
     c.phase = c.multiplier = c.simpstate = 0;
@@ -474,6 +479,11 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
             if (c.phase == c.o.phases || (cdiff == 0 && ldiff == 0) ||
                 (c.phase > 2 && ldiff <= (int64_t)c.o.phase_lits_min)) {
                 if (c.o.ere_en && c.nelected) {
+                    cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
+                    PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected,
+                               c.hdr, c.ot_off, c.ot_size, c.ot_ids, &c.dc->live_cls);
+                    sync_counters(c);
+                    c.prof.bytes[K_ERE] += 4 * (c.hc->live_cls + c.hc->live_lits);
                     PassTimer t(c, 5);
                     ere_pass(c);
                     c.stats.ere_ran = 1;
@@ -482,12 +492,13 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
             }
             // byte model: C_E, L_E of this round
             cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
-            elected_volume_k<<<grid_for(c.nelected, 256), 256, 0, c.s>>>(c.elected, c.nelected, c.hdr, c.ot_off,
+            PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected, c.hdr, c.ot_off,
                                                                          c.ot_size, c.ot_ids, &c.dc->live_cls);
-            g_launches += 1;
             sync_counters(c);
             const uint64_t CE = c.hc->live_cls, LE = c.hc->live_lits;
             const uint64_t Cin = c.numClauses, Lin = c.numLiterals;
+            c.prof.bytes[K_SUB] += 4 * (LE + CE);
+            c.prof.bytes[K_VE1] += 4 * (LE + CE);
             const uint64_t ncls0 = c.ncls, lits0 = c.lits_used;
             c.stats.clauses_processed += Cin;
             c.stats.literals_processed += Lin;
@@ -510,6 +521,7 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
             c.nUnits = c.hc->nunits;
             const uint64_t Cres = c.ncls - ncls0, Lres = c.lits_used - lits0;
             c.stats.resolvents += Cres;
+            c.prof.bytes[K_VE3] += 4 * (LE + CE) + 4 * (Lres + Cres);
             alg += 4 * (Lin + Cin) + 8 * Lin + 8 * (LE + CE) + 4 * (Lres + Cres) + 4 * (c.numLiterals + c.numClauses);
             cdiff = clsbefore - (int64_t)c.numClauses; clsbefore = (int64_t)c.numClauses;
             ldiff = litsbefore - (int64_t)c.numLiterals; litsbefore = (int64_t)c.numLiterals;
@@ -582,6 +594,7 @@ extern "C" int pfg_download(pfg_ctx* o, uint32_t* lits, uint64_t* cls_off, uint8
     Ctx& c = o->c;
     if (!c.uploaded) return PFG_INVALID;
     const uint64_t base_launches = g_launches;
+    g_prof = &c.prof;
     sync_counters(c);
     const uint64_t n = c.ncls;
     if (lits || cls_off || cls_learnt || cls_lbd || cls_usage) {
@@ -598,11 +611,10 @@ extern "C" int pfg_download(pfg_ctx* o, uint32_t* lits, uint64_t* cls_off, uint8
                   dalloc_t(c, &ousage, C + 1) && ensure_tmp(c, scan_temp_bytes(n + 1));
         if (!ok) { dfree(c, flag); dfree(c, sz); dfree(c, olits); dfree(c, ooff); dfree(c, olearnt); dfree(c, olbd); dfree(c, ousage); return PFG_CNFALLOC_FAIL; }
         if (n) {
-            out_flags_k<<<grid_for(n, 256), 256, 0, c.s>>>(c.hdr, n, flag, sz);
+            PFG_LAUNCH(K_DOWNLOAD, out_flags_k, grid_for(n, 256), 256, 0, c.s, c.hdr, n, flag, sz);
             exclusive_scan_u32(flag, flag, n, 0u, nullptr, c.tmp, c.s);
             exclusive_scan_u64(sz, sz, n, 0ull, ooff + C, c.tmp, c.s);
-            out_pack_k<<<grid_for(n * 32, 256), 256, 0, c.s>>>(c.hdr, c.lits, n, flag, sz, olits, ooff, olearnt, olbd, ousage);
-            g_launches += 2;
+            PFG_LAUNCH(K_DOWNLOAD, out_pack_k, grid_for(n * 32, 256), 256, 0, c.s, c.hdr, c.lits, n, flag, sz, olits, ooff, olearnt, olbd, ousage);
         } else {
             cudaMemsetAsync(ooff, 0, sizeof(unsigned long long), c.s);
         }
@@ -625,6 +637,28 @@ extern "C" int pfg_download(pfg_ctx* o, uint32_t* lits, uint64_t* cls_off, uint8
     return finish(c, nullptr, base_launches, PFG_OK);
 }
 
+extern "C" int pfg_profile_enable(pfg_ctx* o, int on) {
+    if (!o) return PFG_INVALID;
+    o->c.prof.on = on != 0;
+    return PFG_OK;
+}
+
+extern "C" void pfg_profile_reset(pfg_ctx* o) {
+    if (o) o->c.prof.reset();
+}
+
+extern "C" int pfg_profile_count(void) { return K_NUM; }
+
+extern "C" const char* pfg_profile_name(int id) { return (id >= 0 && id < K_NUM) ? kKernelNames[id] : ""; }
+
+extern "C" int pfg_profile_get(pfg_ctx* o, int id, uint64_t* launches, double* ms, uint64_t* alg_bytes) {
+    if (!o || id < 0 || id >= K_NUM) return PFG_INVALID;
+    if (launches) *launches = o->c.prof.launches[id];
+    if (ms) *ms = o->c.prof.ms[id];
+    if (alg_bytes) *alg_bytes = o->c.prof.bytes[id];
+    return PFG_OK;
+}
+
 extern "C" void pfg_destroy(pfg_ctx* o) {
     if (!o) return;
     Ctx& c = o->c;
@@ -637,6 +671,7 @@ extern "C" void pfg_destroy(pfg_ctx* o) {
     if (c.ev_a) cudaEventDestroy(c.ev_a);
     if (c.ev_b) cudaEventDestroy(c.ev_b);
     if (c.hc) cudaFreeHost(c.hc);
+    c.prof.destroy();
     cudaGetLastError();
     delete o;
 }

@@ -101,6 +101,9 @@ struct Ctx {
     void* tmp = nullptr; size_t tmp_cap = 0;
     uint32_t* tmp_u32 = nullptr; uint64_t tmp_u32_cap = 0;   // generic u32 scratch
 
+    // per-kernel profiler (launch counts always; CUDA-event timing when enabled)
+    Profiler prof;
+
     // round state
     int phase = 0, multiplier = 0, simpstate = 0, status = PFG_UNKNOWN;
     uint32_t mis_rounds = 0;

@@ -59,9 +59,9 @@ __global__ void compact_k(const ClsHdr* __restrict__ hdr, const uint32_t* __rest
 
 void count_live(Ctx& c) {
     cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
+    c.prof.bytes[K_COUNT] += 8 * c.ncls;
     if (c.ncls) {
-        count_k<<<grid_for(c.ncls, 256, 8), 256, 0, c.s>>>(c.hdr, c.ncls, c.dc);
-        g_launches += 1;
+        PFG_LAUNCH(K_COUNT, count_k, grid_for(c.ncls, 256, 8), 256, 0, c.s, c.hdr, c.ncls, c.dc);
     }
 }
 
@@ -90,12 +90,12 @@ bool compact_cnf(Ctx& c) {
         return false;
     }
     if (!ensure_tmp(c, scan_temp_bytes(n))) return false;
-    live_flags_k<<<grid_for(n, 256), 256, 0, c.s>>>(c.hdr, n, pos, loff);
+    PFG_LAUNCH(K_COMPACT, live_flags_k, grid_for(n, 256), 256, 0, c.s, c.hdr, n, pos, loff);
     exclusive_scan_u32(pos, pos, n, 0u, nullptr, c.tmp, c.s);
     exclusive_scan_u64(loff, loff, n, 0ull, nullptr, c.tmp, c.s);
-    compact_k<<<grid_for(n * 32, 256), 256, 0, c.s>>>(c.hdr, c.lits, n, pos, loff, nhdr, nlits);
-    g_launches += 2;
+    PFG_LAUNCH(K_COMPACT, compact_k, grid_for(n * 32, 256), 256, 0, c.s, c.hdr, c.lits, n, pos, loff, nhdr, nlits);
     dfree(c, pos); dfree(c, loff);
+    c.prof.bytes[K_COMPACT] += 8 * (c.numLiterals + c.numClauses);
     dfree(c, c.hdr); dfree(c, c.lits);
     c.hdr = nhdr; c.lits = nlits;
     c.hdr_cap = clsCap + 1; c.lits_cap = phys_lits;

@@ -195,9 +195,16 @@ void gen_tseitin(uint64_t gates, uint64_t P, uint64_t outs, uint64_t seed, Cnf& 
 // beta = 2.5, by the continuous inverse CDF rank = ceil(V * u^3); ranks are
 // scattered over variable ids by an affine bijection; clause length is
 // 2 + Geometric(p = 1/3) truncated to [2, 50] (mean ~4); distinct variables
-// within a clause; random polarity.
-void gen_scalefree(uint32_t V, uint64_t C, uint64_t seed, Cnf& out) {
+// within a clause; random polarity. With `planted`, a hidden random
+// assignment is drawn first and a clause that it falsifies gets the polarity
+// of one random literal flipped, so the instance stays satisfiable.
+void gen_scalefree(uint32_t V, uint64_t C, uint64_t seed, bool planted, Cnf& out) {
     Rng r(seed);
+    std::vector<uint8_t> hidden;
+    if (planted) {
+        hidden.resize((size_t)V + 1);
+        for (uint32_t v = 1; v <= V; v++) hidden[v] = (uint8_t)r.bit();
+    }
     out.maxVar = V;
     out.lits.reserve(C * 4 + C / 8);
     out.off.reserve(C + 1);
@@ -228,6 +235,14 @@ void gen_scalefree(uint32_t V, uint64_t C, uint64_t seed, Cnf& out) {
             } while (dup);
             c[j] = mklit(v, r.bit());
         }
+        if (planted) {
+            bool sat = false;
+            for (int j = 0; j < len && !sat; j++) sat = ((c[j] & 1u) ^ 1u) == hidden[c[j] >> 1];
+            if (!sat) {
+                const int j = (int)r.below((uint64_t)len);
+                c[j] ^= 1u;
+            }
+        }
         out.add(c, len);
     }
 }
@@ -256,7 +271,7 @@ extern "C" int pfg_generate(int family, uint64_t a, uint64_t b, uint64_t c, uint
                 break;
             case 2:
                 if (a < 2 || a > 0x7FFFFFFEULL) return PFG_INVALID;
-                gen_scalefree((uint32_t)a, b, seed, cnf);
+                gen_scalefree((uint32_t)a, b, seed, c != 0, cnf);
                 break;
             default:
                 return PFG_INVALID;

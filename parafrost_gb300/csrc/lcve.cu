@@ -192,8 +192,7 @@ bool lcve(Ctx& c) {
     const uint32_t V = c.V;
     // scores and the (score, var) order
     cudaMemsetAsync(&c.dc->nfrozen, 0, sizeof(uint32_t), c.s);
-    scores_k<<<grid_for(V, 256), 256, 0, c.s>>>(c.hist, V, c.scores, c.keys_a, c.eligible, c.dc);
-    g_launches += 1;
+    PFG_LAUNCH(K_LCVE, scores_k, grid_for(V, 256), 256, 0, c.s, c.hist, V, c.scores, c.keys_a, c.eligible, c.dc);
     sync_counters(c);
     const uint32_t maxscore = c.hc->nfrozen;
     int bits = 0;
@@ -212,10 +211,9 @@ bool lcve(Ctx& c) {
     c.mis_rounds = 0;
     uint32_t nfrozen = 0;
     if (c.o.lcve_fast) {
-        mis_init_k<<<grid_for(V, 256), 256, 0, c.s>>>(c.eligible, V, c.rank, c.mstate, c.vstate, c.assumed, c.hist,
+        PFG_LAUNCH(K_LCVE, mis_init_k, grid_for(V, 256), 256, 0, c.s, c.eligible, V, c.rank, c.mstate, c.vstate, c.assumed, c.hist,
                                                       c.hdr, c.ot_off, c.ot_size, c.ot_ids, pmax, nmax, maxoccurs,
                                                       maxcsize, c.flag8);
-        g_launches += 1;
         if (!ensure_tmp(c, scan_temp_bytes(V + 1))) return false;
         select_flagged(c.eligible, c.flag8, c.work, V, &c.dc->nwork, c.vscan, c.tmp, c.s);
         sync_counters(c);
@@ -224,15 +222,14 @@ bool lcve(Ctx& c) {
         uint32_t* wb = c.work_b;
         while (nwork) {
             // round: winners among the undecided (mis_round_k), then elect + freeze (mis_freeze_k)
-            mis_win_k<<<grid_for(nwork, 128), 128, 0, c.s>>>(w, nwork, c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids,
+            PFG_LAUNCH(K_MIS_WIN, mis_win_k, grid_for(nwork, 128), 128, 0, c.s, w, nwork, c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids,
                                                              c.rank, c.mstate, c.flag8);
-            win_u32_k<<<grid_for(nwork, 256), 256, 0, c.s>>>(c.flag8, nwork, c.vscan);
+            PFG_LAUNCH(K_LCVE, win_u32_k, grid_for(nwork, 256), 256, 0, c.s, c.flag8, nwork, c.vscan);
             exclusive_scan_u32(c.vscan, c.vscan, nwork, 0u, &c.dc->nwin, c.tmp, c.s);
-            mis_apply_k<<<grid_for(nwork, 128), 128, 0, c.s>>>(w, nwork, c.flag8, c.vscan, c.nelected, c.elected,
+            PFG_LAUNCH(K_MIS_APPLY, mis_apply_k, grid_for(nwork, 128), 128, 0, c.s, w, nwork, c.flag8, c.vscan, c.nelected, c.elected,
                                                                c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids,
                                                                c.frozen, c.mstate);
-            undecided_flags_k<<<grid_for(nwork, 256), 256, 0, c.s>>>(w, nwork, c.mstate, c.flag8);
-            g_launches += 4;
+            PFG_LAUNCH(K_LCVE, undecided_flags_k, grid_for(nwork, 256), 256, 0, c.s, w, nwork, c.mstate, c.flag8);
             select_flagged(w, c.flag8, wb, nwork, &c.dc->nwork, c.keys_b, c.tmp, c.s);
             sync_counters(c);
             if (!c.err.empty()) return false;
@@ -245,25 +242,22 @@ bool lcve(Ctx& c) {
         }
         c.mis_rounds++;   // the reference's final round that finds nothing undecided
         if (c.varcore_on) {
-            frozen_u32_k<<<grid_for(V + 1, 256), 256, 0, c.s>>>(c.frozen, V, c.vscan);
+            PFG_LAUNCH(K_LCVE, frozen_u32_k, grid_for(V + 1, 256), 256, 0, c.s, c.frozen, V, c.vscan);
             exclusive_scan_u32(c.vscan, c.vscan, V + 1, 0u, &c.dc->nfrozen, c.tmp, c.s);
-            varcore_k<<<grid_for(V, 256), 256, 0, c.s>>>(c.frozen, V, c.vscan, c.varcore);
-            g_launches += 2;
+            PFG_LAUNCH(K_LCVE, varcore_k, grid_for(V, 256), 256, 0, c.s, c.frozen, V, c.vscan, c.varcore);
             sync_counters(c);
             nfrozen = c.hc->nfrozen;
         }
     } else {
         // flist in keys_b
-        lcve_seq_k<<<1, 1, 0, c.s>>>(c.eligible, V, c.elected, c.keys_b, c.frozen, c.vstate, c.assumed, c.hist,
+        PFG_LAUNCH(K_LCVE, lcve_seq_k, 1, 1, 0, c.s, c.eligible, V, c.elected, c.keys_b, c.frozen, c.vstate, c.assumed, c.hist,
                                      c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids, pmax, nmax, maxoccurs, maxcsize,
                                      c.dc);
-        g_launches += 1;
         sync_counters(c);
         c.nelected = c.hc->nelected;
         nfrozen = c.hc->nfrozen;
         if (c.varcore_on && nfrozen) {
-            mapfrozen_k<<<grid_for(nfrozen, 256), 256, 0, c.s>>>(c.keys_b, nfrozen, c.varcore);
-            g_launches += 1;
+            PFG_LAUNCH(K_LCVE, mapfrozen_k, grid_for(nfrozen, 256), 256, 0, c.s, c.keys_b, nfrozen, c.varcore);
         }
     }
     if (c.varcore_on && !nfrozen) c.varcore_on = false;   // vars->varcore = NULL (lcve.cu:403)

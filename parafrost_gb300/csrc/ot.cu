@@ -216,14 +216,15 @@ bool ot_build(Ctx& c) {
         if (!dalloc_t(c, &c.ot_ids, cap)) { c.simpstate = PFG_OTALLOC_FAIL; c.ot_cap = 0; return false; }
         c.ot_cap = cap;
     }
+    c.prof.bytes[K_HIST] += 4 * (c.numLiterals + c.numClauses);
+    c.prof.bytes[K_FILL] += 4 * (c.numLiterals + c.numClauses) + 4 * c.numLiterals;
     cudaMemsetAsync(c.hist, 0, nl * sizeof(uint32_t), c.s);
-    hist_k<<<grid_for(c.ncls, 256), 256, 0, c.s>>>(c.hdr, c.lits, c.ncls, c.hist);
+    PFG_LAUNCH(K_HIST, hist_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.hist);
     if (!ensure_tmp(c, scan_temp_bytes(nl))) return false;
     exclusive_scan_u32(c.hist, c.ot_off, nl, 0u, c.ot_off + nl, c.tmp, c.s);
     cudaMemcpyAsync(c.ot_fill, c.ot_off, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
     cudaMemcpyAsync(c.ot_size, c.hist, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
-    fill_k<<<grid_for(c.ncls, 256), 256, 0, c.s>>>(c.hdr, c.lits, c.ncls, c.ot_fill, c.ot_ids);
-    g_launches += 2;
+    PFG_LAUNCH(K_FILL, fill_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.ot_fill, c.ot_ids);
     return cuda_ok(c, cudaGetLastError(), "ot_build");
 }
 
@@ -239,14 +240,12 @@ bool ot_sort(Ctx& c, bool by_id) {
     }
     cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
-    sort_small_k<<<grid_for(nl, 256), 256, 0, c.s>>>(c.hdr, c.lits, nl, c.ot_off, c.ot_size, c.ot_ids, by_id,
+    PFG_LAUNCH(K_SORT_SMALL, sort_small_k, grid_for(nl, 256), 256, 0, c.s, c.hdr, c.lits, nl, c.ot_off, c.ot_size, c.ot_ids, by_id,
                                                      c.mid_desc, &c.dc->nwin, c.big_lists, &c.dc->big_lists);
-    g_launches += 1;
     sync_counters(c);
     const uint32_t nmid = c.hc->nwin, nbig = c.hc->big_lists;
     if (nmid) {
-        sort_mid_k<<<nmid, MID_THREADS, 0, c.s>>>(c.hdr, c.lits, c.mid_desc, c.ot_ids, by_id);
-        g_launches += 1;
+        PFG_LAUNCH(K_SORT_MID, sort_mid_k, nmid, MID_THREADS, 0, c.s, c.hdr, c.lits, c.mid_desc, c.ot_ids, by_id);
     }
     if (nbig) {
         // sizes and area offsets of the big lists
@@ -254,7 +253,7 @@ bool ot_sort(Ctx& c, bool by_id) {
         if (!ensure_tmp_u32(c, 2ull * nbig + 4)) return false;
         bsz = c.tmp_u32;
         uint32_t* boff = c.tmp_u32 + nbig + 2;
-        big_sizes_k<<<grid_for(nbig, 256), 256, 0, c.s>>>(c.big_lists, nbig, c.ot_size, bsz);
+        PFG_LAUNCH(K_SORT_BIG, big_sizes_k, grid_for(nbig, 256), 256, 0, c.s, c.big_lists, nbig, c.ot_size, bsz);
         if (!ensure_tmp(c, scan_temp_bytes(nbig))) return false;
         exclusive_scan_u32(bsz, boff, nbig, 0u, boff + nbig, c.tmp, c.s);
         std::vector<uint32_t> hs(nbig + 1);
@@ -274,24 +273,21 @@ bool ot_sort(Ctx& c, bool by_id) {
             }
             c.big_cap = cap;
         }
-        big_gather_k<<<std::min<uint32_t>(nbig, 4096), 256, 0, c.s>>>(c.hdr, c.lits, c.big_lists, nbig, c.ot_off,
+        PFG_LAUNCH(K_SORT_BIG, big_gather_k, std::min<uint32_t>(nbig, 4096), 256, 0, c.s, c.hdr, c.lits, c.big_lists, nbig, c.ot_off,
                                                                      c.ot_size, boff, c.ot_ids, c.big_keys,
                                                                      c.big_ids, by_id);
         const uint32_t nchunks = (maxn + MID_MAX - 1) / MID_MAX;
         const uint32_t gy = std::min<uint32_t>(nbig, 65535);
-        big_chunk_k<<<dim3(nchunks, gy), MID_THREADS, 0, c.s>>>(c.big_lists, nbig, c.ot_size, boff, c.big_keys, c.big_ids);
-        g_launches += 3;
+        PFG_LAUNCH(K_SORT_BIG, big_chunk_k, dim3(nchunks, gy), MID_THREADS, 0, c.s, c.big_lists, nbig, c.ot_size, boff, c.big_keys, c.big_ids);
         uint4* k0 = c.big_keys; uint4* k1 = c.big_keys_alt;
         uint32_t* i0 = c.big_ids; uint32_t* i1 = c.big_ids_alt;
         for (uint32_t R = MID_MAX; R < maxn; R <<= 1) {
             const uint32_t gx = std::min<uint32_t>((maxn + 255) / 256, 1024);
-            big_merge_k<<<dim3(gx, gy), 256, 0, c.s>>>(c.big_lists, nbig, c.ot_size, boff, R, k0, i0, k1, i1);
-            g_launches += 1;
+            PFG_LAUNCH(K_SORT_BIG, big_merge_k, dim3(gx, gy), 256, 0, c.s, c.big_lists, nbig, c.ot_size, boff, R, k0, i0, k1, i1);
             std::swap(k0, k1); std::swap(i0, i1);
         }
-        big_scatter_k<<<std::min<uint32_t>(nbig, 4096), 256, 0, c.s>>>(c.big_lists, nbig, c.ot_off, c.ot_size,
+        PFG_LAUNCH(K_SORT_BIG, big_scatter_k, std::min<uint32_t>(nbig, 4096), 256, 0, c.s, c.big_lists, nbig, c.ot_off, c.ot_size,
                                                                       boff, i0, c.ot_ids);
-        g_launches += 1;
     }
     return cuda_ok(c, cudaGetLastError(), "ot_sort");
 }

@@ -4,6 +4,53 @@
 namespace pfg {
 
 thread_local uint64_t g_launches = 0;
+thread_local Profiler* g_prof = nullptr;
+
+const char* const kKernelNames[K_NUM] = {
+    "ot_hist", "ot_fill", "ot_sort_small", "ot_sort_mid", "ot_sort_big", "scan", "radix_sort", "select",
+    "lcve", "mis_win", "mis_apply", "sub", "ve_phase1", "ve_phase3", "ere", "bcp", "count", "compact",
+    "upload", "download", "misc",
+};
+
+cudaEvent_t Profiler::next_event() {
+    if (used == pool.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        pool.push_back(e);
+    }
+    return pool[used++];
+}
+
+void Profiler::begin(int id, cudaStream_t s) {
+    marks.push_back(id);
+    cudaEventRecord(next_event(), s);
+}
+
+void Profiler::end(int, cudaStream_t s) { cudaEventRecord(next_event(), s); }
+
+void Profiler::resolve() {
+    if (used) cudaEventSynchronize(pool[used - 1]);
+    for (size_t i = 0; i < marks.size(); i++) {
+        float t = 0;
+        if (cudaEventElapsedTime(&t, pool[2 * i], pool[2 * i + 1]) == cudaSuccess) ms[marks[i]] += t;
+        else cudaGetLastError();
+    }
+    marks.clear();
+    used = 0;
+}
+
+void Profiler::reset() {
+    marks.clear();
+    used = 0;
+    for (int i = 0; i < K_NUM; i++) { ms[i] = 0; launches[i] = 0; bytes[i] = 0; }
+}
+
+void Profiler::destroy() {
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+    pool.clear();
+    marks.clear();
+    used = 0;
+}
 
 namespace {
 
@@ -113,10 +160,9 @@ void excl_scan(const T* in, T* out, uint64_t n, T init, T* total_out, void* tmp,
     }
     const uint64_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
     T* sums = (T*)tmp;
-    scan_tiles_k<T><<<(unsigned)nt, SCAN_THREADS, 0, s>>>(in, out, n, sums);
-    scan_sums_k<T><<<1, SCAN_THREADS, 0, s>>>(sums, nt, init, total_out);
-    scan_add_k<T><<<(unsigned)nt, SCAN_THREADS, 0, s>>>(out, n, sums);
-    g_launches += 3;
+    PFG_LAUNCH(K_SCAN, scan_tiles_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, in, out, n, sums);
+    PFG_LAUNCH(K_SCAN, scan_sums_k<T>, 1, SCAN_THREADS, 0, s, sums, nt, init, total_out);
+    PFG_LAUNCH(K_SCAN, scan_add_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, out, n, sums);
 }
 
 // ---------------- radix sort ----------------
@@ -230,10 +276,9 @@ int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uin
         const uint32_t* vi = cur ? v1 : v0;
         uint32_t* ko = cur ? k0 : k1;
         uint32_t* vo = cur ? v0 : v1;
-        radix_hist_k<<<(unsigned)nb, RS_THREADS, 0, s>>>(ki, n, sh, hist, (uint32_t)nb);
+        PFG_LAUNCH(K_RADIX, radix_hist_k, (unsigned)nb, RS_THREADS, 0, s, ki, n, sh, hist, (uint32_t)nb);
         excl_scan<uint32_t>(hist, hist, 256 * nb, 0u, nullptr, stmp, s);
-        radix_scatter_k<<<(unsigned)nb, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n, sh, hist, (uint32_t)nb);
-        g_launches += 2;
+        PFG_LAUNCH(K_RADIX, radix_scatter_k, (unsigned)nb, RS_THREADS, 0, s, ki, vi, ko, vo, n, sh, hist, (uint32_t)nb);
         cur ^= 1;
     }
     return cur;
@@ -245,10 +290,9 @@ void select_flagged(const uint32_t* in, const uint8_t* flags, uint32_t* out, uin
         cudaMemsetAsync(count_out, 0, sizeof(uint32_t), s);
         return;
     }
-    flags_to_u32_k<<<grid_for(n, 256), 256, 0, s>>>(flags, scan_buf, n);
+    PFG_LAUNCH(K_SELECT, flags_to_u32_k, grid_for(n, 256), 256, 0, s, flags, scan_buf, n);
     excl_scan<uint32_t>(scan_buf, scan_buf, n, 0u, count_out, tmp, s);
-    select_scatter_k<<<grid_for(n, 256), 256, 0, s>>>(in, flags, scan_buf, out, n);
-    g_launches += 2;
+    PFG_LAUNCH(K_SELECT, select_scatter_k, grid_for(n, 256), 256, 0, s, in, flags, scan_buf, out, n);
 }
 
 }  // namespace pfg

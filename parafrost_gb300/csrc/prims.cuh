@@ -7,12 +7,49 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 namespace pfg {
 
-// Every launcher counts its kernel launches here (per host thread).
+// Kernel groups timed by the profiler (one CUDA-event pair per launch).
+enum KernelId : int {
+    K_HIST = 0, K_FILL, K_SORT_SMALL, K_SORT_MID, K_SORT_BIG, K_SCAN, K_RADIX, K_SELECT,
+    K_LCVE, K_MIS_WIN, K_MIS_APPLY, K_SUB, K_VE1, K_VE3, K_ERE, K_BCP, K_COUNT, K_COMPACT,
+    K_UPLOAD, K_DOWNLOAD, K_MISC, K_NUM
+};
+extern const char* const kKernelNames[K_NUM];
+
+struct Profiler {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    std::vector<int> marks;          // kernel id per recorded event pair
+    double ms[K_NUM] = {0};
+    uint64_t launches[K_NUM] = {0};
+    uint64_t bytes[K_NUM] = {0};
+    cudaEvent_t next_event();
+    void begin(int id, cudaStream_t s);
+    void end(int id, cudaStream_t s);
+    void resolve();                  // synchronizes and accumulates recorded pairs
+    void reset();
+    void destroy();
+};
+
+// Every launcher counts its kernel launches here (per host thread) and, when
+// a profiler is installed for the calling thread, brackets the launch with events.
 extern thread_local uint64_t g_launches;
+extern thread_local Profiler* g_prof;
+
+#define PFG_LAUNCH(ID, KERNEL, GRID, BLOCK, SMEM, STREAM, ...)                  \
+    do {                                                                        \
+        ::pfg::Profiler* _pp = ::pfg::g_prof;                                   \
+        if (_pp && _pp->on) _pp->begin(::pfg::ID, (STREAM));                    \
+        KERNEL<<<(GRID), (BLOCK), (SMEM), (STREAM)>>>(__VA_ARGS__);             \
+        ::pfg::g_launches++;                                                    \
+        if (_pp) { _pp->launches[::pfg::ID]++;                                  \
+                   if (_pp->on) _pp->end(::pfg::ID, (STREAM)); }                \
+    } while (0)
 
 // Scratch bytes needed by the scans / sorts below for n elements.
 size_t scan_temp_bytes(uint64_t n);

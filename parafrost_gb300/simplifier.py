@@ -113,6 +113,24 @@ class Simplifier:
         self.run()
         return self.download()
 
+    def profile(self, on: bool = True) -> None:
+        """Per-kernel CUDA-event timing of the following simplify calls."""
+        self.lib.pfg_profile_enable(self._ctx, 1 if on else 0)
+
+    def profile_reset(self) -> None:
+        self.lib.pfg_profile_reset(self._ctx)
+
+    def profile_report(self) -> dict:
+        """{kernel group: {launches, ms, alg_bytes}} accumulated since the last reset."""
+        out = {}
+        for i in range(self.lib.pfg_profile_count()):
+            n = C.c_uint64()
+            ms = C.c_double()
+            b = C.c_uint64()
+            self.lib.pfg_profile_get(self._ctx, i, C.byref(n), C.byref(ms), C.byref(b))
+            out[self.lib.pfg_profile_name(i).decode()] = {"launches": n.value, "ms": ms.value, "alg_bytes": b.value}
+        return out
+
     def kernel_launches(self) -> int:
         return int(self.lib.pfg_kernel_launches(self._ctx))
 

@@ -39,3 +39,16 @@ def test_config1_random_3sat_full_size():
     cnf = pg.random_ksat(20000, 85200, 3, seed=1)
     assert_parity(cnf, phases=1, ere=False)
     assert_parity(cnf)
+
+
+def test_config2_tseitin_full_size():
+    # 1M gates, 50k inputs, 1k outputs: ~3.25M clauses, 5 rounds of gate-definition BVE
+    cnf = pg.tseitin(1_000_000, 50_000, 1_000, seed=1)
+    res, ref = assert_parity(cnf)
+    assert res.stats["rounds"] == 5 and res.cnf.num_clauses < cnf.num_clauses // 5
+
+
+def test_config3_scalefree_reduced():
+    # the scale-free family at 1/10 of its full size (planted model: all rounds run)
+    cnf = pg.scale_free(400_000, 1_600_000, seed=1, planted=True)
+    assert_parity(cnf)
