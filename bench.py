@@ -185,19 +185,13 @@ def run_gpu(a, world, rank, local):
             dist.barrier()
         torch.cuda.synchronize()
 
+    from parafrost_gb300.dist import allreduce_max, allreduce_sum
+
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return allreduce_max(x, device="cuda")
 
     def sum_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        return float(t.item())
+        return allreduce_sum(x, device="cuda")
 
     w = WORKLOADS[a.workload]
     cnf = make_cnf(w)

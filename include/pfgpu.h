@@ -118,6 +118,9 @@ typedef struct pfg_result_sizes {
 
 typedef struct pfg_ctx pfg_ctx;
 
+/* sizeof of the ABI structs as compiled into the library (FFI layout check). */
+void pfg_abi_sizes(size_t* options, size_t* stats, size_t* result_sizes);
+
 /* Fill `o` with the reference defaults. */
 void pfg_default_options(pfg_options* o);
 

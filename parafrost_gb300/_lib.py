@@ -26,6 +26,8 @@ def lib():
             f"{LIB_PATH} is missing: build the CUDA engine first "
             "(python -c 'import __graft_entry__ as g; g.build()')")
     L = C.CDLL(LIB_PATH)
+    L.pfg_abi_sizes.argtypes = [C.POINTER(C.c_size_t)] * 3
+    L.pfg_abi_sizes.restype = None
     L.pfg_default_options.argtypes = [C.POINTER(PfgOptions)]
     L.pfg_default_options.restype = None
     L.pfg_resolve_options.argtypes = [C.POINTER(PfgOptions)]
@@ -65,7 +67,7 @@ def lib():
 
 # C-ABI entry points declared in include/pfgpu.h (checked by the CPU tests)
 EXPORTED = (
-    "pfg_default_options", "pfg_resolve_options", "pfg_create", "pfg_upload", "pfg_simplify",
+    "pfg_abi_sizes", "pfg_default_options", "pfg_resolve_options", "pfg_create", "pfg_upload", "pfg_simplify",
     "pfg_result_sizes_get", "pfg_download", "pfg_destroy", "pfg_last_error", "pfg_kernel_launches",
     "pfg_generate", "pfg_profile_enable", "pfg_profile_reset", "pfg_profile_count", "pfg_profile_name",
     "pfg_profile_get",

@@ -217,6 +217,12 @@ struct PassTimer {
 
 using namespace pfg;
 
+extern "C" void pfg_abi_sizes(size_t* options, size_t* stats, size_t* result_sizes) {
+    if (options) *options = sizeof(pfg_options);
+    if (stats) *stats = sizeof(pfg_stats);
+    if (result_sizes) *result_sizes = sizeof(pfg_result_sizes);
+}
+
 extern "C" void pfg_default_options(pfg_options* o) {
     std::memset(o, 0, sizeof(*o));
     o->phases = 5;
