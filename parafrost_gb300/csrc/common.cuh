@@ -87,7 +87,7 @@ struct DevCounters {
     int32_t last_elim;             // lastEliminatedID
     uint32_t survivors;
     uint32_t big_lists;
-    uint32_t pad[3];
+    uint32_t nbig_sub, nbig_ve1, nbig_ve3;   // variables too large for the warp stage
 };
 
 constexpr uint32_t ERR_UNITS_OVERFLOW = 1u;

@@ -516,88 +516,6 @@ __constant__ uint64_t MAGIC[6] = {
     0xff00ff00ff00ff00ULL, 0xffff0000ffff0000ULL, 0xffffffff00000000ULL,
 };
 
-PFG_D void clause2fun(uint32_t v, uint32_t sign, uint64_t* f) {
-    if (v < 6) {
-        uint64_t val = MAGIC[v];
-        if (sign) val = ~val;
-        for (int i = 0; i < FUNTABLEN; i++) f[i] |= val;
-    } else {
-        uint64_t val = sign ? ~0ULL : 0ULL;
-        int j = 0;
-        const int sv = 1 << (v - 6);
-        for (int i = 0; i < FUNTABLEN; i++) {
-            f[i] |= val;
-            if (++j >= sv) { val = ~val; j = 0; }
-        }
-    }
-}
-
-PFG_D bool build_funtab(const EK& k, uint32_t lit, uint64_t* f, uint64_t* cls) {
-    for (int i = 0; i < FUNTABLEN; i++) f[i] = ~0ULL;
-    const uint32_t* ol = OLp(k, lit);
-    const uint32_t n = OLs(k, lit);
-    for (uint32_t i = 0; i < n; i++) {
-        const ClsHdr h = k.hdr[ol[i]];
-        if (m_learnt(h.meta)) continue;
-        for (int q = 0; q < FUNTABLEN; q++) cls[q] = 0;
-        const uint32_t* l = k.lits + h.off;
-        for (uint32_t t = 0; t < h.size; t++) {
-            const uint32_t other = l[t];
-            if (other == lit) continue;
-            const uint32_t mvar = k.varcore[ABSV(other)];
-            if (mvar >= MAXFUNVAR) return false;
-            clause2fun(mvar, SIGNL(other), cls);
-        }
-        for (int q = 0; q < FUNTABLEN; q++) f[q] &= cls[q];
-    }
-    return true;
-}
-
-PFG_D void build_funtab_core(const EK& k, uint32_t lit, uint32_t tail, uint64_t* fun, uint64_t* cls, bool& core) {
-    const uint32_t* ol = OLp(k, lit);
-    for (uint32_t j = 0; j < tail; j++) {
-        const ClsHdr h = k.hdr[ol[j]];
-        if (m_learnt(h.meta)) continue;
-        for (int q = 0; q < FUNTABLEN; q++) cls[q] = 0;
-        const uint32_t* l = k.lits + h.off;
-        for (uint32_t t = 0; t < h.size; t++) {
-            const uint32_t other = l[t];
-            if (other == lit) continue;
-            clause2fun(k.varcore[ABSV(other)], SIGNL(other), cls);
-        }
-        for (int q = 0; q < FUNTABLEN; q++) fun[q] &= cls[q];
-    }
-    bool isfalse = true;
-    for (int q = 0; q < FUNTABLEN; q++) if (fun[q]) { isfalse = false; break; }
-    if (isfalse) { SET_MOLTEN(k, ol[tail], 1); core = true; }
-}
-
-// find_fun_gate (function.cuh:275-325)
-PFG_D bool find_fun_gate(const EK& k, uint32_t p, uint32_t n, uint32_t nOrgCls, uint64_t* pos, uint64_t* neg,
-                         uint64_t* cls, uint32_t& nE, uint32_t& nC, uint32_t& nL) {
-    if (!build_funtab(k, p, pos, cls) || !build_funtab(k, n, neg, cls)) return false;
-    uint64_t allzero = 0;
-    for (int i = 0; i < FUNTABLEN; i++) allzero |= pos[i] & neg[i];
-    if (allzero) return false;
-    bool core = false;
-    const uint32_t* pl = OLp(k, p);
-    for (int i = (int)OLs(k, p) - 1; i >= 0; i--) {
-        for (int q = 0; q < FUNTABLEN; q++) pos[q] = neg[q];
-        if (m_orig(META(k, pl[i]))) build_funtab_core(k, p, (uint32_t)i, pos, cls, core);
-    }
-    const uint32_t* nl = OLp(k, n);
-    for (int i = (int)OLs(k, n) - 1; i >= 0; i--) {
-        for (int q = 0; q < FUNTABLEN; q++) pos[q] = ~0ULL;
-        if (m_orig(META(k, nl[i]))) build_funtab_core(k, n, (uint32_t)i, pos, cls, core);
-    }
-    nE = 0; nC = 0; nL = 0;
-    if (count_subst(k, PAIR_CORE, ABSV(p), nOrgCls, p, n, nE, nC, nL)) {
-        if (core) freeze_clauses(k, p, n);
-        return false;
-    }
-    return true;
-}
-
 // ---- equivalences (equivalence.cuh) ----
 PFG_D bool has_lit(const EK& k, uint32_t c, uint32_t lit) {
     const ClsHdr h = k.hdr[c];
@@ -789,8 +707,14 @@ PFG_D void self_subsume(const EK& k, uint32_t x, uint32_t fx, uint32_t lit, uint
     }
 }
 
-__global__ void sub_k(EK k, const uint32_t* elected, uint32_t nelected) {
-    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < nelected; e += gridDim.x * blockDim.x) {
+// Thread-per-variable kernels below take an optional device-side index list
+// (the variables the warp kernels could not stage); nelected bounds the grid.
+PFG_D uint32_t list_count(const uint32_t* list, const uint32_t* count, uint32_t n) { return list ? *count : n; }
+
+__global__ void sub_k(EK k, const uint32_t* elected, uint32_t nelected, const uint32_t* list, const uint32_t* count) {
+    const uint32_t nn = list_count(list, count, nelected);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += gridDim.x * blockDim.x) {
+        const uint32_t e = list ? list[q] : q;
         const uint32_t x = elected[e];
         const uint32_t p = 2 * x, n = p | 1;
         if (OLs(k, p) > k.sub_max_occurs || OLs(k, n) > k.sub_max_occurs) continue;
@@ -825,11 +749,33 @@ __global__ void sub_k(EK k, const uint32_t* elected, uint32_t nelected) {
 }
 
 // ---- BVE phase 1 ----
-__global__ void __launch_bounds__(64) ve1_k(EK k, const uint32_t* elected, uint32_t nelected, uint32_t* type,
-                                            uint32_t* ucnt, unsigned long long* rpos, unsigned long long* rref) {
+// Phase 1 runs in two kernels so that the rarely reached function-table gate
+// (64-word truth tables) does not set the register budget of the common path:
+// ve1a_k takes every decision up to that gate; variables that reach it are
+// flagged and finished by ve1b_k with the same state (pOrgs, nOrgs, nC).
+
+PFG_D void elim_no_resolvents(const EK& k, uint32_t x, uint32_t p, uint32_t n, uint32_t pOrgs, uint32_t nOrgs) {
+    save_resolved_orgs(k, p, n, pOrgs, nOrgs);
+    toblivion(k, p, n);
+    k.elim[x] |= MELTING_MASK;
+}
+
+PFG_D void store_elim_info(uint32_t tid, uint32_t elimType, uint32_t nE, uint32_t nC, uint32_t nL, uint32_t* type,
+                           uint32_t* ucnt, unsigned long long* rpos, unsigned long long* rref) {
+    type[tid] = elimType | (nC << 2) | (nL << 16);
+    ucnt[tid] = nE;
+    rpos[tid] = nC;
+    rref[tid] = nL + (unsigned long long)NBUCKETS * nC;
+}
+
+__global__ void __launch_bounds__(128) ve1a_k(EK k, const uint32_t* elected, uint32_t nelected, uint32_t* type,
+                                              uint32_t* ucnt, unsigned long long* rpos, unsigned long long* rref,
+                                              uint32_t* dlist, uint32_t* dcount, const uint32_t* list,
+                                              const uint32_t* count) {
     uint32_t outs[SH_MAX_BVE_OUT1 + 2];
-    uint64_t fpos[FUNTABLEN], fneg[FUNTABLEN], fcls[FUNTABLEN];
-    for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < nelected; tid += gridDim.x * blockDim.x) {
+    const uint32_t nn = list_count(list, count, nelected);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += gridDim.x * blockDim.x) {
+        const uint32_t tid = list ? list[q] : q;
         const uint32_t x = elected[tid];
         const uint32_t p = 2 * x, n = p | 1;
         uint32_t pOrgs = 0, nOrgs = 0;
@@ -844,12 +790,7 @@ __global__ void __launch_bounds__(64) ve1_k(EK k, const uint32_t* elected, uint3
         }
         uint32_t elimType = 0, nE = 0, nC = 0, nL = 0;
         type[tid] = 0; ucnt[tid] = 0; rpos[tid] = 0; rref[tid] = 0;
-        if (!pOrgs || !nOrgs) {
-            save_resolved_orgs(k, p, n, pOrgs, nOrgs);
-            toblivion(k, p, n);
-            k.elim[x] |= MELTING_MASK;
-            continue;
-        }
+        if (!pOrgs || !nOrgs) { elim_no_resolvents(k, x, p, n, pOrgs, nOrgs); continue; }
         const uint32_t def = find_equ_gate(k, p, n);
         if (def) {
             save_resolved_orgs(k, p, n, pOrgs, nOrgs);
@@ -858,14 +799,8 @@ __global__ void __launch_bounds__(64) ve1_k(EK k, const uint32_t* elected, uint3
             continue;
         }
         if ((pOrgs == 1 || nOrgs == 1) && count_res_unbounded(k, x, p, n, nE, nC, nL)) {
-            if (nC) {
-                type[tid] = RES_MASK | (nC << 2) | (nL << 16);
-                ucnt[tid] = nE; rpos[tid] = nC; rref[tid] = nL + (unsigned long long)NBUCKETS * nC;
-            } else {
-                save_resolved_orgs(k, p, n, pOrgs, nOrgs);
-                toblivion(k, p, n);
-                k.elim[x] |= MELTING_MASK;
-            }
+            if (nC) store_elim_info(tid, RES_MASK, nE, nC, nL, type, ucnt, rpos, rref);
+            else elim_no_resolvents(k, x, p, n, pOrgs, nOrgs);
             continue;
         }
         const uint32_t nClsBefore = pOrgs + nOrgs;
@@ -880,27 +815,153 @@ __global__ void __launch_bounds__(64) ve1_k(EK k, const uint32_t* elected, uint3
             else if (find_xor_gate(k, p, n, nClsBefore, outs, nE, nC, nL)) elimType = AOIX_MASK;
             else if (!nC && find_xor_gate(k, n, p, nClsBefore, outs, nE, nC, nL)) elimType = AOIX_MASK;
         }
-        if (k.varcore_on && !elimType && nClsBefore > 2 &&
-            find_fun_gate(k, p, n, nClsBefore, fpos, fneg, fcls, nE, nC, nL))
-            elimType = CORE_MASK;
-        else if (!elimType && !nC && count_res_bounded(k, x, nClsBefore, p, n, nE, nC, nL))
-            elimType = RES_MASK;
-        if (!nC) {
-            save_resolved_orgs(k, p, n, pOrgs, nOrgs);
-            toblivion(k, p, n);
-            k.elim[x] |= MELTING_MASK;
-        } else if (elimType) {
-            type[tid] = elimType | (nC << 2) | (nL << 16);
-            ucnt[tid] = nE; rpos[tid] = nC; rref[tid] = nL + (unsigned long long)NBUCKETS * nC;
+        if (k.varcore_on && !elimType && nClsBefore > 2) {
+            // function-table stage (and what follows it) is finished by ve1b_k
+            dlist[atomicAdd(dcount, 1u)] = tid;
+            ucnt[tid] = nC;
+            rpos[tid] = (unsigned long long)pOrgs | ((unsigned long long)nOrgs << 32);
+            continue;
         }
+        if (!elimType && !nC && count_res_bounded(k, x, nClsBefore, p, n, nE, nC, nL)) elimType = RES_MASK;
+        if (!nC) elim_no_resolvents(k, x, p, n, pOrgs, nOrgs);
+        else if (elimType) store_elim_info(tid, elimType, nE, nC, nL, type, ucnt, rpos, rref);
+    }
+}
+
+// ---- function-table stage, one warp per deferred variable ----
+// Lane l owns words 2l and 2l+1 of each 64-word truth table (function.cuh:27-115);
+// list walks run redundantly on all lanes (broadcast loads), writes by lane 0.
+
+struct WFun { uint64_t w0, w1; };
+
+PFG_D void wf_set(WFun& f, uint64_t v) { f.w0 = v; f.w1 = v; }
+
+// clause2fun for the lane's two words (function.cuh:91-114): variable v < 6 uses
+// the magic constant; v >= 6 alternates all-ones/zero every 2^(v-6) words.
+PFG_D void wf_clause2fun(uint32_t v, uint32_t sign, WFun& f, unsigned lane) {
+    if (v < 6) {
+        uint64_t val = MAGIC[v];
+        if (sign) val = ~val;
+        f.w0 |= val;
+        f.w1 |= val;
+    } else {
+        const uint64_t base = sign ? ~0ULL : 0ULL;
+        const uint32_t sh = v - 6;
+        const uint32_t i0 = 2 * lane, i1 = 2 * lane + 1;
+        f.w0 |= ((i0 >> sh) & 1u) ? ~base : base;
+        f.w1 |= ((i1 >> sh) & 1u) ? ~base : base;
+    }
+}
+
+PFG_D bool wf_build(const EK& k, uint32_t lit, WFun& f, unsigned lane) {
+    wf_set(f, ~0ULL);
+    const uint32_t* ol = OLp(k, lit);
+    const uint32_t n = OLs(k, lit);
+    for (uint32_t i = 0; i < n; i++) {
+        const ClsHdr h = k.hdr[ol[i]];
+        if (m_learnt(h.meta)) continue;
+        WFun cls{0, 0};
+        const uint32_t* l = k.lits + h.off;
+        for (uint32_t t = 0; t < h.size; t++) {
+            const uint32_t other = l[t];
+            if (other == lit) continue;
+            const uint32_t mvar = k.varcore[ABSV(other)];
+            if (mvar >= MAXFUNVAR) return false;
+            wf_clause2fun(mvar, SIGNL(other), cls, lane);
+        }
+        f.w0 &= cls.w0;
+        f.w1 &= cls.w1;
+    }
+    return true;
+}
+
+PFG_D void wf_build_core(const EK& k, uint32_t lit, uint32_t tail, WFun& fun, bool& core, unsigned lane) {
+    const uint32_t* ol = OLp(k, lit);
+    for (uint32_t j = 0; j < tail; j++) {
+        const ClsHdr h = k.hdr[ol[j]];
+        if (m_learnt(h.meta)) continue;
+        WFun cls{0, 0};
+        const uint32_t* l = k.lits + h.off;
+        for (uint32_t t = 0; t < h.size; t++) {
+            const uint32_t other = l[t];
+            if (other == lit) continue;
+            wf_clause2fun(k.varcore[ABSV(other)], SIGNL(other), cls, lane);
+        }
+        fun.w0 &= cls.w0;
+        fun.w1 &= cls.w1;
+    }
+    const bool isfalse = __all_sync(0xFFFFFFFFu, (fun.w0 | fun.w1) == 0);
+    if (isfalse) {
+        if (lane == 0) SET_MOLTEN(k, ol[tail], 1);   // non-gate clause
+        core = true;
+    }
+    __syncwarp();
+}
+
+// find_fun_gate (function.cuh:275-325) for one warp
+PFG_D bool wf_find_fun_gate(const EK& k, uint32_t p, uint32_t n, uint32_t nOrgCls, uint32_t& nE, uint32_t& nC,
+                            uint32_t& nL, unsigned lane) {
+    WFun pos, neg;
+    if (!wf_build(k, p, pos, lane) || !wf_build(k, n, neg, lane)) return false;
+    const bool nonzero = __any_sync(0xFFFFFFFFu, ((pos.w0 & neg.w0) | (pos.w1 & neg.w1)) != 0);
+    if (nonzero) return false;
+    bool core = false;
+    const uint32_t* pl = OLp(k, p);
+    for (int i = (int)OLs(k, p) - 1; i >= 0; i--) {
+        WFun fun = neg;
+        if (m_orig(META(k, pl[i]))) wf_build_core(k, p, (uint32_t)i, fun, core, lane);
+    }
+    const uint32_t* nl = OLp(k, n);
+    for (int i = (int)OLs(k, n) - 1; i >= 0; i--) {
+        WFun fun;
+        wf_set(fun, ~0ULL);
+        if (m_orig(META(k, nl[i]))) wf_build_core(k, n, (uint32_t)i, fun, core, lane);
+    }
+    nE = 0; nC = 0; nL = 0;
+    if (count_subst(k, PAIR_CORE, ABSV(p), nOrgCls, p, n, nE, nC, nL)) {
+        __syncwarp();
+        if (core && lane == 0) freeze_clauses(k, p, n);
+        __syncwarp();
+        return false;
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(128) ve1b_k(EK k, const uint32_t* elected, const uint32_t* dlist,
+                                              const uint32_t* dcount, uint32_t* type, uint32_t* ucnt,
+                                              unsigned long long* rpos, unsigned long long* rref) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t nd = *dcount;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nd; w += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t tid = dlist[w];
+        const uint32_t x = elected[tid];
+        const uint32_t p = 2 * x, n = p | 1;
+        uint32_t nC = ucnt[tid];
+        const unsigned long long po = rpos[tid];
+        const uint32_t pOrgs = (uint32_t)po, nOrgs = (uint32_t)(po >> 32);
+        const uint32_t nClsBefore = pOrgs + nOrgs;
+        uint32_t elimType = 0, nE = 0, nL = 0;
+        if (wf_find_fun_gate(k, p, n, nClsBefore, nE, nC, nL, lane)) elimType = CORE_MASK;
+        else if (!nC && count_res_bounded(k, x, nClsBefore, p, n, nE, nC, nL)) elimType = RES_MASK;
+        __syncwarp();
+        if (lane == 0) {
+            ucnt[tid] = 0;
+            rpos[tid] = 0;
+            if (!nC) elim_no_resolvents(k, x, p, n, pOrgs, nOrgs);
+            else if (elimType) store_elim_info(tid, elimType, nE, nC, nL, type, ucnt, rpos, rref);
+        }
+        __syncwarp();
     }
 }
 
 // ---- BVE phase 3 ----
 __global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint32_t nelected, const uint32_t* type,
                                              const unsigned long long* rpos, const unsigned long long* rref,
-                                             unsigned long long cs_cap, unsigned long long data_cap, uint8_t* keep) {
-    for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < nelected; tid += gridDim.x * blockDim.x) {
+                                             unsigned long long cs_cap, unsigned long long data_cap, uint8_t* keep,
+                                             const uint32_t* list, const uint32_t* count) {
+    const uint32_t nn = list_count(list, count, nelected);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += gridDim.x * blockDim.x) {
+        const uint32_t tid = list ? list[q] : q;
         const uint32_t x = elected[tid];
         const uint32_t xinfo = type[tid];
         const uint32_t et = xinfo & 3u;
@@ -1020,6 +1081,8 @@ __global__ void __launch_bounds__(128) ere_k(EK k, const uint32_t* elected, uint
     }
 }
 
+#include "elimw.cuh"
+
 EK make_ek(Ctx& c) {
     EK k;
     k.hdr = c.hdr;
@@ -1053,20 +1116,37 @@ __global__ void keep_u32_k(const uint8_t* keep, uint32_t n, uint32_t* out) {
 }  // namespace
 
 void sub_pass(Ctx& c) {
-    if (!c.nelected) return;
-    PFG_LAUNCH(K_SUB, sub_k, grid_for(c.nelected, 64), 64, 0, c.s, make_ek(c), c.elected, c.nelected);
+    const uint32_t E = c.nelected;
+    if (!E) return;
+    const EK k = make_ek(c);
+    cudaMemsetAsync(&c.dc->nbig_sub, 0, sizeof(uint32_t), c.s);
+    // warp per variable on the shared-memory stage; larger variables by one thread each
+    PFG_LAUNCH(K_SUB, subw_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.elected, E,
+               c.work_b, &c.dc->nbig_sub);
+    PFG_LAUNCH(K_SUB, sub_k, grid_for(E, 64, 8), 64, 0, c.s, k, c.elected, E, c.work_b, &c.dc->nbig_sub);
 }
 
 bool ve_pass(Ctx& c) {
     const uint32_t E = c.nelected;
     if (!E) return true;
     const EK k = make_ek(c);
-    PFG_LAUNCH(K_VE1, ve1_k, grid_for(E, 64), 64, 0, c.s, k, c.elected, E, c.type, c.ucnt, c.rpos, c.rref);
+    cudaMemsetAsync(&c.dc->nwork, 0, sizeof(uint32_t), c.s);
+    cudaMemsetAsync(&c.dc->nbig_ve1, 0, 2 * sizeof(uint32_t), c.s);
+    PFG_LAUNCH(K_VE1, ve1w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.elected, E,
+               c.type, c.ucnt, c.rpos, c.rref, c.work, &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
+    PFG_LAUNCH(K_VE1, ve1a_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.elected, E, c.type, c.ucnt, c.rpos, c.rref, c.work,
+               &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
+    if (c.varcore_on)   // one warp per deferred variable; the grid walks the device-side count
+        PFG_LAUNCH(K_VE1B, ve1b_k, grid_for((uint64_t)E * 32, 128, 16), 128, 0, c.s, k, c.elected, c.work,
+                   &c.dc->nwork, c.type, c.ucnt, c.rpos, c.rref);
     if (!ensure_tmp(c, scan_temp_bytes(E))) return false;
     exclusive_scan_u64(c.rpos, c.rpos, E, (unsigned long long)c.ncls, nullptr, c.tmp, c.s);
     exclusive_scan_u64(c.rref, c.rref, E, (unsigned long long)c.data_size, nullptr, c.tmp, c.s);
     cudaMemsetAsync(&c.dc->last_elim, 0xFF, sizeof(int32_t), c.s);   // -1
-    PFG_LAUNCH(K_VE3, ve3_k, grid_for(E, 128), 128, 0, c.s, k, c.elected, E, c.type, c.rpos, c.rref, c.cs_cap, c.data_cap, c.flag8);
+    PFG_LAUNCH(K_VE3, ve3w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.elected, E,
+               c.type, c.rpos, c.rref, c.cs_cap, c.data_cap, c.flag8, c.eligible_b, &c.dc->nbig_ve3);
+    PFG_LAUNCH(K_VE3, ve3_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.elected, E, c.type, c.rpos, c.rref, c.cs_cap,
+               c.data_cap, c.flag8, c.eligible_b, &c.dc->nbig_ve3);
     // postVE: keep surviving elected variables in order (elimination.cu:249-267)
     select_flagged(c.elected, c.flag8, c.work, E, &c.dc->survivors, c.vscan, c.tmp, c.s);
     sync_counters(c);

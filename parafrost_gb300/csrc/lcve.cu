@@ -119,6 +119,50 @@ __global__ void mis_apply_k(const uint32_t* work, uint32_t nwork, const uint8_t*
     }
 }
 
+// round kernel 1: winners among the undecided; counts the undecided (mis_round_k, lcve.cu:171-191)
+__global__ void mis_win2_k(const uint32_t* work, uint32_t nwork, const ClsHdr* hdr, const uint32_t* lits,
+                           const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids,
+                           const uint32_t* rank, const uint8_t* mstate, uint8_t* win, uint32_t* undecided) {
+    uint32_t cnt = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x) {
+        const uint32_t v = work[i];
+        uint8_t w = 0;
+        if (mstate[v] == MIS_UNDECIDED) {
+            cnt++;
+            const uint32_t r = rank[v];
+            w = !(blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, v, r, rank, mstate) ||
+                  blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v + 1, v, r, rank, mstate));
+        }
+        win[i] = w;
+    }
+    for (int d = 16; d > 0; d >>= 1) cnt += __shfl_down_sync(0xFFFFFFFFu, cnt, d);
+    if ((threadIdx.x & 31u) == 0 && cnt) atomicAdd(undecided, cnt);
+}
+
+// round kernel 2: winners are elected in round r and freeze their neighbours (mis_freeze_k, lcve.cu:193-209)
+__global__ void mis_apply2_k(const uint32_t* work, uint32_t nwork, const uint8_t* win, uint32_t r,
+                             uint32_t* mround, const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off,
+                             const uint32_t* ot_size, const uint32_t* ot_ids, uint8_t* frozen, uint8_t* mstate) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x) {
+        if (!win[i]) continue;
+        const uint32_t v = work[i];
+        mstate[v] = MIS_ELECTED;
+        mround[v] = r;
+        freeze_list(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, v, frozen, mstate);
+        freeze_list(hdr, lits, ot_off, ot_size, ot_ids, 2 * v + 1, v, frozen, mstate);
+    }
+}
+
+__global__ void elected_flags_k(const uint32_t* work, uint32_t nwork, const uint8_t* mstate, uint8_t* flag) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x)
+        flag[i] = mstate[work[i]] == MIS_ELECTED;
+}
+
+__global__ void round_keys_k(const uint32_t* elected, uint32_t n, const uint32_t* mround, uint32_t* keys) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        keys[i] = mround[elected[i]];
+}
+
 __global__ void undecided_flags_k(const uint32_t* work, uint32_t nwork, const uint8_t* mstate, uint8_t* flag) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x)
         flag[i] = mstate[work[i]] == MIS_UNDECIDED;
@@ -217,30 +261,41 @@ bool lcve(Ctx& c) {
         if (!ensure_tmp(c, scan_temp_bytes(V + 1))) return false;
         select_flagged(c.eligible, c.flag8, c.work, V, &c.dc->nwork, c.vscan, c.tmp, c.s);
         sync_counters(c);
-        uint32_t nwork = c.hc->nwork;
-        uint32_t* w = c.work;
-        uint32_t* wb = c.work_b;
-        while (nwork) {
-            // round: winners among the undecided (mis_round_k), then elect + freeze (mis_freeze_k)
-            PFG_LAUNCH(K_MIS_WIN, mis_win_k, grid_for(nwork, 128), 128, 0, c.s, w, nwork, c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids,
-                                                             c.rank, c.mstate, c.flag8);
-            PFG_LAUNCH(K_LCVE, win_u32_k, grid_for(nwork, 256), 256, 0, c.s, c.flag8, nwork, c.vscan);
-            exclusive_scan_u32(c.vscan, c.vscan, nwork, 0u, &c.dc->nwin, c.tmp, c.s);
-            PFG_LAUNCH(K_MIS_APPLY, mis_apply_k, grid_for(nwork, 128), 128, 0, c.s, w, nwork, c.flag8, c.vscan, c.nelected, c.elected,
-                                                               c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids,
-                                                               c.frozen, c.mstate);
-            PFG_LAUNCH(K_LCVE, undecided_flags_k, grid_for(nwork, 256), 256, 0, c.s, w, nwork, c.mstate, c.flag8);
-            select_flagged(w, c.flag8, wb, nwork, &c.dc->nwork, c.keys_b, c.tmp, c.s);
+        const uint32_t nwork = c.hc->nwork;
+        // Rounds run without compaction; each winner records its round. The host
+        // reads the undecided count only every 1, 2, 4 .. 16 rounds.
+        uint32_t* mround = c.scores;     // scores are dead once the order is sorted
+        uint32_t r = 0;
+        bool done = nwork == 0;
+        for (int batch = 1; !done; batch = std::min(batch * 2, 16)) {
+            for (int b = 0; b < batch; b++, r++) {
+                cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
+                PFG_LAUNCH(K_MIS_WIN, mis_win2_k, grid_for(nwork, 128), 128, 0, c.s, c.work, nwork, c.hdr, c.lits,
+                           c.ot_off, c.ot_size, c.ot_ids, c.rank, c.mstate, c.flag8, &c.dc->nwin);
+                PFG_LAUNCH(K_MIS_APPLY, mis_apply2_k, grid_for(nwork, 128), 128, 0, c.s, c.work, nwork, c.flag8, r,
+                           mround, c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids, c.frozen, c.mstate);
+            }
             sync_counters(c);
             if (!c.err.empty()) return false;
-            c.nelected += c.hc->nwin;
-            c.mis_rounds++;
-            const uint32_t next = c.hc->nwork;
-            if (next >= nwork && c.hc->nwin == 0) { c.err = "MIS made no progress"; c.simpstate = PFG_TIMEOUT; return false; }
-            nwork = next;
-            std::swap(w, wb);
+            if (c.hc->nwin == 0) done = true;          // the last round found nothing undecided
+            else if (r > nwork + 2) { c.err = "MIS did not converge"; c.simpstate = PFG_TIMEOUT; return false; }
         }
-        c.mis_rounds++;   // the reference's final round that finds nothing undecided
+        c.mis_rounds = r;
+        // elected in (round, rank) order: select in rank order, then stable sort by round
+        PFG_LAUNCH(K_LCVE, elected_flags_k, grid_for(nwork, 256), 256, 0, c.s, c.work, nwork, c.mstate, c.flag8);
+        select_flagged(c.work, c.flag8, c.elected, nwork, &c.dc->nelected, c.vscan, c.tmp, c.s);
+        sync_counters(c);
+        c.nelected = c.hc->nelected;
+        if (c.nelected > 1) {
+            int rbits = 0;
+            while (rbits < 32 && (r >> rbits)) rbits += 8;
+            PFG_LAUNCH(K_LCVE, round_keys_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected, mround,
+                       c.keys_a);
+            if (!ensure_tmp(c, radix_temp_bytes(c.nelected))) return false;
+            const int which = radix_sort_pairs(c.keys_a, c.elected, c.keys_b, c.work_b, c.nelected, 0, rbits, c.tmp, c.s);
+            if (which) cudaMemcpyAsync(c.elected, c.work_b, c.nelected * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+        }
+
         if (c.varcore_on) {
             PFG_LAUNCH(K_LCVE, frozen_u32_k, grid_for(V + 1, 256), 256, 0, c.s, c.frozen, V, c.vscan);
             exclusive_scan_u32(c.vscan, c.vscan, V + 1, 0u, &c.dc->nfrozen, c.tmp, c.s);

@@ -8,7 +8,7 @@ thread_local Profiler* g_prof = nullptr;
 
 const char* const kKernelNames[K_NUM] = {
     "ot_hist", "ot_fill", "ot_sort_small", "ot_sort_mid", "ot_sort_big", "scan", "radix_sort", "select",
-    "lcve", "mis_win", "mis_apply", "sub", "ve_phase1", "ve_phase3", "ere", "bcp", "count", "compact",
+    "lcve", "mis_win", "mis_apply", "sub", "ve_phase1", "ve_phase1_fun", "ve_phase3", "ere", "bcp", "count", "compact",
     "upload", "download", "misc",
 };
 
@@ -152,6 +152,43 @@ __global__ void scan_add_k(T* out, uint64_t n, const T* sums) {
     }
 }
 
+// Small arrays: one block walks the tiles in order, carrying the prefix (one launch).
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_single_k(const T* in, T* out, uint64_t n, T init, T* total_out) {
+    __shared__ T sh[SCAN_TILE];
+    T carry = init;
+    for (uint64_t base = 0; base < n; base += SCAN_TILE) {
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; i++) {
+            const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
+            sh[i * SCAN_THREADS + threadIdx.x] = idx < n ? in[idx] : T(0);
+        }
+        __syncthreads();
+        T loc[SCAN_ITEMS];
+        T sum = 0;
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; i++) {
+            loc[i] = sum;
+            sum += sh[threadIdx.x * SCAN_ITEMS + i];
+        }
+        T total;
+        const T excl = block_excl_scan<T>(sum, total);
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; i++) sh[threadIdx.x * SCAN_ITEMS + i] = carry + loc[i] + excl;
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; i++) {
+            const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
+            if (idx < n) out[idx] = sh[i * SCAN_THREADS + threadIdx.x];
+        }
+        carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && total_out) *total_out = carry;
+}
+
+constexpr uint64_t SCAN_SINGLE_MAX_TILES = 16;
+
 template <typename T>
 void excl_scan(const T* in, T* out, uint64_t n, T init, T* total_out, void* tmp, cudaStream_t s) {
     if (n == 0) {
@@ -159,6 +196,10 @@ void excl_scan(const T* in, T* out, uint64_t n, T init, T* total_out, void* tmp,
         return;
     }
     const uint64_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nt <= SCAN_SINGLE_MAX_TILES) {
+        PFG_LAUNCH(K_SCAN, scan_single_k<T>, 1, SCAN_THREADS, 0, s, in, out, n, init, total_out);
+        return;
+    }
     T* sums = (T*)tmp;
     PFG_LAUNCH(K_SCAN, scan_tiles_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, in, out, n, sums);
     PFG_LAUNCH(K_SCAN, scan_sums_k<T>, 1, SCAN_THREADS, 0, s, sums, nt, init, total_out);
