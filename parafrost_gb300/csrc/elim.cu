@@ -1027,7 +1027,8 @@ __global__ void __launch_bounds__(128) ere_k(EK k, const uint32_t* elected, uint
     const unsigned lane = threadIdx.x & 31u;
     uint32_t* buf = bufs[wib];
     const uint32_t cmax = k.ere_clause_max;
-    for (uint32_t e = blockIdx.x * 4 + wib; e < nelected; e += gridDim.x * 4) {
+    for (uint32_t q = blockIdx.x * 4 + wib; q < nelected; q += gridDim.x * 4) {
+        const uint32_t e = q;
         const uint32_t v = elected[e], p = 2 * v, n = p | 1;
         const uint32_t ds = OLs(k, p), fs = OLs(k, n);
         if (!(ds && fs && ds <= k.ere_max_occurs && fs <= k.ere_max_occurs)) continue;
@@ -1123,7 +1124,7 @@ void sub_pass(Ctx& c) {
     // warp per variable on the shared-memory stage; larger variables by one thread each
     PFG_LAUNCH(K_SUB, subw_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.elected, E,
                c.work_b, &c.dc->nbig_sub);
-    PFG_LAUNCH(K_SUB, sub_k, grid_for(E, 64, 8), 64, 0, c.s, k, c.elected, E, c.work_b, &c.dc->nbig_sub);
+    PFG_LAUNCH(K_BIGVAR, sub_k, grid_for(E, 64, 8), 64, 0, c.s, k, c.elected, E, c.work_b, &c.dc->nbig_sub);
 }
 
 bool ve_pass(Ctx& c) {
@@ -1134,7 +1135,7 @@ bool ve_pass(Ctx& c) {
     cudaMemsetAsync(&c.dc->nbig_ve1, 0, 2 * sizeof(uint32_t), c.s);
     PFG_LAUNCH(K_VE1, ve1w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.elected, E,
                c.type, c.ucnt, c.rpos, c.rref, c.work, &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
-    PFG_LAUNCH(K_VE1, ve1a_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.elected, E, c.type, c.ucnt, c.rpos, c.rref, c.work,
+    PFG_LAUNCH(K_BIGVAR, ve1a_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.elected, E, c.type, c.ucnt, c.rpos, c.rref, c.work,
                &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
     if (c.varcore_on)   // one warp per deferred variable; the grid walks the device-side count
         PFG_LAUNCH(K_VE1B, ve1b_k, grid_for((uint64_t)E * 32, 128, 16), 128, 0, c.s, k, c.elected, c.work,
@@ -1145,7 +1146,7 @@ bool ve_pass(Ctx& c) {
     cudaMemsetAsync(&c.dc->last_elim, 0xFF, sizeof(int32_t), c.s);   // -1
     PFG_LAUNCH(K_VE3, ve3w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.elected, E,
                c.type, c.rpos, c.rref, c.cs_cap, c.data_cap, c.flag8, c.eligible_b, &c.dc->nbig_ve3);
-    PFG_LAUNCH(K_VE3, ve3_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.elected, E, c.type, c.rpos, c.rref, c.cs_cap,
+    PFG_LAUNCH(K_BIGVAR, ve3_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.elected, E, c.type, c.rpos, c.rref, c.cs_cap,
                c.data_cap, c.flag8, c.eligible_b, &c.dc->nbig_ve3);
     // postVE: keep surviving elected variables in order (elimination.cu:249-267)
     select_flagged(c.elected, c.flag8, c.work, E, &c.dc->survivors, c.vscan, c.tmp, c.s);

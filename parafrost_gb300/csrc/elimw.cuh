@@ -709,8 +709,9 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve1w_k(EK k, const uint32_t* el
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
-    for (uint32_t tid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tid < nelected;
-         tid += (gridDim.x * blockDim.x) >> 5) {
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected;
+         q += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t tid = q;
         const uint32_t x = elected[tid];
         if (!ws_stage(k, w, 2 * x, 2 * x + 1, lane)) {
             if (lane == 0) big[atomicAdd(nbig, 1u)] = tid;
@@ -730,8 +731,9 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
-    for (uint32_t tid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tid < nelected;
-         tid += (gridDim.x * blockDim.x) >> 5) {
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected;
+         q += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t tid = q;
         const uint32_t x = elected[tid];
         const uint32_t xinfo = type[tid];
         const uint32_t et = xinfo & 3u;
@@ -958,8 +960,9 @@ __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* el
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
-    for (uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < nelected;
-         e += (gridDim.x * blockDim.x) >> 5) {
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected;
+         q += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t e = q;
         const uint32_t x = elected[e];
         const uint32_t p = 2 * x, n = p | 1;
         if (OLs(k, p) > k.sub_max_occurs || OLs(k, n) > k.sub_max_occurs) continue;

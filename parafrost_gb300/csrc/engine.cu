@@ -370,6 +370,7 @@ extern "C" int pfg_upload(pfg_ctx* o, uint32_t max_var, uint64_t num_clauses, co
          dalloc_t(c, &c.keys_b, V1) && dalloc_t(c, &c.eligible, V1) && dalloc_t(c, &c.eligible_b, V1) &&
          dalloc_t(c, &c.rank, V1) && dalloc_t(c, &c.varcore, V1) && dalloc_t(c, &c.elected, V1) &&
          dalloc_t(c, &c.work, V1) && dalloc_t(c, &c.work_b, V1) && dalloc_t(c, &c.vscan, V1 + 1) &&
+         dalloc_t(c, &c.winv, V1 + 8) &&
          dalloc_t(c, &c.type, V1) && dalloc_t(c, &c.ucnt, V1) && dalloc_t(c, &c.rpos, V1) &&
          dalloc_t(c, &c.rref, V1) && dalloc_t(c, &c.units, c.units_cap) && dalloc_t(c, &c.trail, c.trail_cap) &&
          dalloc_t(c, &c.stack, c.stack_cap) && dalloc_t(c, &c.front_a, V1) && dalloc_t(c, &c.front_b, V1);

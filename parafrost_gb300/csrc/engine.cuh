@@ -72,6 +72,9 @@ struct Ctx {
     uint32_t* work = nullptr;    // V+1 MIS worklist
     uint32_t* work_b = nullptr;  // V+1
     uint32_t* vscan = nullptr;   // V+2 scan scratch
+    uint8_t* winv = nullptr;     // V+1 MIS round winners
+    uint4* ckeys = nullptr;      // per-clause sort key (size, first, last, sig)
+    uint64_t ckeys_cap = 0;
     uint32_t nelected = 0;
     bool varcore_on = false;
 

@@ -35,23 +35,18 @@ __global__ void live_flags_k(const ClsHdr* __restrict__ hdr, uint64_t ncls, uint
     }
 }
 
-// one warp per clause: copy header and literals into the new store
+// thread per clause: copy header and literals into the new store (clauses are short)
 __global__ void compact_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
                           const uint32_t* __restrict__ pos, const unsigned long long* __restrict__ loff,
                           ClsHdr* nhdr, uint32_t* nlits) {
-    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const unsigned lane = threadIdx.x & 31u;
-    for (uint64_t c = warp; c < ncls; c += nwarps) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         const ClsHdr h = hdr[c];
         if (m_deleted(h.meta)) continue;
         const uint64_t o = loff[c];
-        for (uint32_t k = lane; k < h.size; k += 32) nlits[o + k] = lits[h.off + k];
-        if (lane == 0) {
-            ClsHdr nh = h;
-            nh.off = (uint32_t)o;
-            nhdr[pos[c]] = nh;
-        }
+        for (uint32_t k = 0; k < h.size; k++) nlits[o + k] = lits[h.off + k];
+        ClsHdr nh = h;
+        nh.off = (uint32_t)o;
+        nhdr[pos[c]] = nh;
     }
 }
 
@@ -93,7 +88,7 @@ bool compact_cnf(Ctx& c) {
     PFG_LAUNCH(K_COMPACT, live_flags_k, grid_for(n, 256), 256, 0, c.s, c.hdr, n, pos, loff);
     exclusive_scan_u32(pos, pos, n, 0u, nullptr, c.tmp, c.s);
     exclusive_scan_u64(loff, loff, n, 0ull, nullptr, c.tmp, c.s);
-    PFG_LAUNCH(K_COMPACT, compact_k, grid_for(n * 32, 256), 256, 0, c.s, c.hdr, c.lits, n, pos, loff, nhdr, nlits);
+    PFG_LAUNCH(K_COMPACT, compact_k, grid_for(n, 256), 256, 0, c.s, c.hdr, c.lits, n, pos, loff, nhdr, nlits);
     dfree(c, pos); dfree(c, loff);
     c.prof.bytes[K_COMPACT] += 8 * (c.numLiterals + c.numClauses);
     dfree(c, c.hdr); dfree(c, c.lits);

@@ -77,17 +77,6 @@ PFG_D bool blocked(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_o
     return false;
 }
 
-__global__ void mis_win_k(const uint32_t* work, uint32_t nwork, const ClsHdr* hdr, const uint32_t* lits,
-                          const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids,
-                          const uint32_t* rank, const uint8_t* mstate, uint8_t* win) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x) {
-        const uint32_t v = work[i];
-        const uint32_t r = rank[v];
-        win[i] = !(blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, v, r, rank, mstate) ||
-                   blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v + 1, v, r, rank, mstate));
-    }
-}
-
 PFG_D void freeze_list(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
                        const uint32_t* ot_ids, uint32_t lit, uint32_t cand, uint8_t* frozen, uint8_t* mstate) {
     const uint32_t o = ot_off[lit], n = ot_size[lit];
@@ -104,48 +93,27 @@ PFG_D void freeze_list(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* 
     }
 }
 
-// winners: mark elected, append in worklist (rank) order, freeze neighbours
-__global__ void mis_apply_k(const uint32_t* work, uint32_t nwork, const uint8_t* win, const uint32_t* pos,
-                            uint32_t base, uint32_t* elected, const ClsHdr* hdr, const uint32_t* lits,
-                            const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids,
-                            uint8_t* frozen, uint8_t* mstate) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x) {
-        if (!win[i]) continue;
-        const uint32_t v = work[i];
-        mstate[v] = MIS_ELECTED;
-        elected[base + pos[i]] = v;
-        freeze_list(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, v, frozen, mstate);
-        freeze_list(hdr, lits, ot_off, ot_size, ot_ids, 2 * v + 1, v, frozen, mstate);
-    }
-}
-
-// round kernel 1: winners among the undecided; counts the undecided (mis_round_k, lcve.cu:171-191)
-__global__ void mis_win2_k(const uint32_t* work, uint32_t nwork, const ClsHdr* hdr, const uint32_t* lits,
-                           const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids,
-                           const uint32_t* rank, const uint8_t* mstate, uint8_t* win, uint32_t* undecided) {
+// var-order round kernels: every variable checks its own state (coalesced)
+__global__ void mis_win3_k(uint32_t V, const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off,
+                           const uint32_t* ot_size, const uint32_t* ot_ids, const uint32_t* rank,
+                           const uint8_t* mstate, uint8_t* winv, uint32_t* undecided) {
     uint32_t cnt = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x) {
-        const uint32_t v = work[i];
-        uint8_t w = 0;
-        if (mstate[v] == MIS_UNDECIDED) {
-            cnt++;
-            const uint32_t r = rank[v];
-            w = !(blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, v, r, rank, mstate) ||
-                  blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v + 1, v, r, rank, mstate));
-        }
-        win[i] = w;
+    for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
+        if (mstate[v] != MIS_UNDECIDED) continue;
+        cnt++;
+        const uint32_t r = rank[v];
+        winv[v] = !(blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, v, r, rank, mstate) ||
+                    blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v + 1, v, r, rank, mstate));
     }
     for (int d = 16; d > 0; d >>= 1) cnt += __shfl_down_sync(0xFFFFFFFFu, cnt, d);
     if ((threadIdx.x & 31u) == 0 && cnt) atomicAdd(undecided, cnt);
 }
 
-// round kernel 2: winners are elected in round r and freeze their neighbours (mis_freeze_k, lcve.cu:193-209)
-__global__ void mis_apply2_k(const uint32_t* work, uint32_t nwork, const uint8_t* win, uint32_t r,
-                             uint32_t* mround, const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off,
-                             const uint32_t* ot_size, const uint32_t* ot_ids, uint8_t* frozen, uint8_t* mstate) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x) {
-        if (!win[i]) continue;
-        const uint32_t v = work[i];
+__global__ void mis_apply3_k(uint32_t V, const uint8_t* winv, uint32_t r, uint32_t* mround, const ClsHdr* hdr,
+                             const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
+                             const uint32_t* ot_ids, uint8_t* frozen, uint8_t* mstate) {
+    for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
+        if (mstate[v] != MIS_UNDECIDED || !winv[v]) continue;
         mstate[v] = MIS_ELECTED;
         mround[v] = r;
         freeze_list(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, v, frozen, mstate);
@@ -161,15 +129,6 @@ __global__ void elected_flags_k(const uint32_t* work, uint32_t nwork, const uint
 __global__ void round_keys_k(const uint32_t* elected, uint32_t n, const uint32_t* mround, uint32_t* keys) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         keys[i] = mround[elected[i]];
-}
-
-__global__ void undecided_flags_k(const uint32_t* work, uint32_t nwork, const uint8_t* mstate, uint8_t* flag) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x)
-        flag[i] = mstate[work[i]] == MIS_UNDECIDED;
-}
-
-__global__ void win_u32_k(const uint8_t* win, uint32_t n, uint32_t* out) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = win[i];
 }
 
 __global__ void frozen_u32_k(const uint8_t* frozen, uint32_t V, uint32_t* out) {
@@ -270,10 +229,10 @@ bool lcve(Ctx& c) {
         for (int batch = 1; !done; batch = std::min(batch * 2, 16)) {
             for (int b = 0; b < batch; b++, r++) {
                 cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
-                PFG_LAUNCH(K_MIS_WIN, mis_win2_k, grid_for(nwork, 128), 128, 0, c.s, c.work, nwork, c.hdr, c.lits,
-                           c.ot_off, c.ot_size, c.ot_ids, c.rank, c.mstate, c.flag8, &c.dc->nwin);
-                PFG_LAUNCH(K_MIS_APPLY, mis_apply2_k, grid_for(nwork, 128), 128, 0, c.s, c.work, nwork, c.flag8, r,
-                           mround, c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids, c.frozen, c.mstate);
+                PFG_LAUNCH(K_MIS_WIN, mis_win3_k, grid_for(V, 128), 128, 0, c.s, V, c.hdr, c.lits, c.ot_off,
+                           c.ot_size, c.ot_ids, c.rank, c.mstate, c.winv, &c.dc->nwin);
+                PFG_LAUNCH(K_MIS_APPLY, mis_apply3_k, grid_for(V, 128), 128, 0, c.s, V, c.winv, r, mround, c.hdr,
+                           c.lits, c.ot_off, c.ot_size, c.ot_ids, c.frozen, c.mstate);
             }
             sync_counters(c);
             if (!c.err.empty()) return false;

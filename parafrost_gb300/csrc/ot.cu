@@ -43,11 +43,17 @@ __global__ void fill_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restric
     }
 }
 
-PFG_D uint4 ckey(const ClsHdr* hdr, const uint32_t* lits, uint32_t c, bool by_id) {
-    if (by_id) return make_uint4(0, 0, 0, 0);
-    const ClsHdr h = hdr[c];
-    return make_uint4(h.size, lits[h.off], lits[h.off + h.size - 1], h.sig);
+// OLIST_CMP key of every live clause, computed once per sort in clause order
+__global__ void ckeys_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
+                        uint4* keys, bool by_id) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        const ClsHdr h = hdr[c];
+        if (m_deleted(h.meta)) continue;
+        keys[c] = by_id ? make_uint4(0, 0, 0, 0) : make_uint4(h.size, lits[h.off], lits[h.off + h.size - 1], h.sig);
+    }
 }
+
+PFG_D uint4 ckey(const uint4* keys, uint32_t c) { return keys[c]; }
 
 // OLIST_CMP: (size, first, last, sig, ref)
 PFG_D bool kless(const uint4& a, uint32_t ia, const uint4& b, uint32_t ib) {
@@ -58,8 +64,8 @@ PFG_D bool kless(const uint4& a, uint32_t ia, const uint4& b, uint32_t ib) {
     return ia < ib;
 }
 
-__global__ void sort_small_k(const ClsHdr* hdr, const uint32_t* lits, uint64_t nlist,
-                             const uint32_t* off, const uint32_t* size, uint32_t* ids, bool by_id,
+__global__ void sort_small_k(const uint4* keys, uint64_t nlist,
+                             const uint32_t* off, const uint32_t* size, uint32_t* ids,
                              uint32_t* mid_desc, uint32_t* mid_cnt, uint32_t* big_lists, uint32_t* big_cnt) {
     for (uint64_t l = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlist; l += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t n = size[l];
@@ -77,7 +83,7 @@ __global__ void sort_small_k(const ClsHdr* hdr, const uint32_t* lits, uint64_t n
         uint32_t* L = ids + off[l];
         uint4 k[SMALL_MAX];
         uint32_t id[SMALL_MAX];
-        for (uint32_t i = 0; i < n; i++) { id[i] = L[i]; k[i] = ckey(hdr, lits, id[i], by_id); }
+        for (uint32_t i = 0; i < n; i++) { id[i] = L[i]; k[i] = ckey(keys, id[i]); }
         for (uint32_t i = 1; i < n; i++) {
             const uint4 tk = k[i];
             const uint32_t ti = id[i];
@@ -109,15 +115,14 @@ PFG_D void bitonic_smem(uint4* sk, uint32_t* sid, uint32_t P) {
     }
 }
 
-__global__ void __launch_bounds__(MID_THREADS) sort_mid_k(const ClsHdr* hdr, const uint32_t* lits,
-                                                         const uint32_t* desc, uint32_t* ids, bool by_id) {
+__global__ void __launch_bounds__(MID_THREADS) sort_mid_k(const uint4* keys, const uint32_t* desc, uint32_t* ids) {
     __shared__ uint4 sk[MID_MAX];
     __shared__ uint32_t sid[MID_MAX];
     const uint32_t o = desc[2 * blockIdx.x], n = desc[2 * blockIdx.x + 1];
     uint32_t P = 1;
     while (P < n) P <<= 1;
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
-        if (i < n) { sid[i] = ids[o + i]; sk[i] = ckey(hdr, lits, sid[i], by_id); }
+        if (i < n) { sid[i] = ids[o + i]; sk[i] = ckey(keys, sid[i]); }
         else { sid[i] = 0xFFFFFFFFu; sk[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu); }
     }
     __syncthreads();
@@ -126,15 +131,15 @@ __global__ void __launch_bounds__(MID_THREADS) sort_mid_k(const ClsHdr* hdr, con
 }
 
 // Big lists: gather into a contiguous area with precomputed keys.
-__global__ void big_gather_k(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* big_lists, uint32_t nbig,
+__global__ void big_gather_k(const uint4* keys, const uint32_t* big_lists, uint32_t nbig,
                              const uint32_t* off, const uint32_t* size, const uint32_t* boff,
-                             const uint32_t* ids, uint4* bk, uint32_t* bid, bool by_id) {
+                             const uint32_t* ids, uint4* bk, uint32_t* bid) {
     for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
         const uint32_t l = big_lists[b], n = size[l], o = off[l], a = boff[b];
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
             const uint32_t c = ids[o + i];
             bid[a + i] = c;
-            bk[a + i] = ckey(hdr, lits, c, by_id);
+            bk[a + i] = ckey(keys, c);
         }
     }
 }
@@ -238,14 +243,22 @@ bool ot_sort(Ctx& c, bool by_id) {
         if (!dalloc_t(c, &c.mid_desc, 2 * want_desc)) { c.simpstate = PFG_OTALLOC_FAIL; return false; }
         c.mid_desc_cap = want_desc;
     }
+    if (c.ckeys_cap < c.ncls) {
+        dfree(c, c.ckeys);
+        c.ckeys = nullptr;
+        const uint64_t cap = c.hdr_cap > c.ncls ? c.hdr_cap : c.ncls;
+        if (!dalloc_t(c, &c.ckeys, cap)) { c.simpstate = PFG_OTALLOC_FAIL; c.ckeys_cap = 0; return false; }
+        c.ckeys_cap = cap;
+    }
+    PFG_LAUNCH(K_SORT_SMALL, ckeys_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.ckeys, by_id);
     cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_SORT_SMALL, sort_small_k, grid_for(nl, 256), 256, 0, c.s, c.hdr, c.lits, nl, c.ot_off, c.ot_size, c.ot_ids, by_id,
-                                                     c.mid_desc, &c.dc->nwin, c.big_lists, &c.dc->big_lists);
+    PFG_LAUNCH(K_SORT_SMALL, sort_small_k, grid_for(nl, 256), 256, 0, c.s, c.ckeys, nl, c.ot_off, c.ot_size, c.ot_ids,
+               c.mid_desc, &c.dc->nwin, c.big_lists, &c.dc->big_lists);
     sync_counters(c);
     const uint32_t nmid = c.hc->nwin, nbig = c.hc->big_lists;
     if (nmid) {
-        PFG_LAUNCH(K_SORT_MID, sort_mid_k, nmid, MID_THREADS, 0, c.s, c.hdr, c.lits, c.mid_desc, c.ot_ids, by_id);
+        PFG_LAUNCH(K_SORT_MID, sort_mid_k, nmid, MID_THREADS, 0, c.s, c.ckeys, c.mid_desc, c.ot_ids);
     }
     if (nbig) {
         // sizes and area offsets of the big lists
@@ -273,9 +286,8 @@ bool ot_sort(Ctx& c, bool by_id) {
             }
             c.big_cap = cap;
         }
-        PFG_LAUNCH(K_SORT_BIG, big_gather_k, std::min<uint32_t>(nbig, 4096), 256, 0, c.s, c.hdr, c.lits, c.big_lists, nbig, c.ot_off,
-                                                                     c.ot_size, boff, c.ot_ids, c.big_keys,
-                                                                     c.big_ids, by_id);
+        PFG_LAUNCH(K_SORT_BIG, big_gather_k, std::min<uint32_t>(nbig, 4096), 256, 0, c.s, c.ckeys, c.big_lists, nbig,
+                   c.ot_off, c.ot_size, boff, c.ot_ids, c.big_keys, c.big_ids);
         const uint32_t nchunks = (maxn + MID_MAX - 1) / MID_MAX;
         const uint32_t gy = std::min<uint32_t>(nbig, 65535);
         PFG_LAUNCH(K_SORT_BIG, big_chunk_k, dim3(nchunks, gy), MID_THREADS, 0, c.s, c.big_lists, nbig, c.ot_size, boff, c.big_keys, c.big_ids);
