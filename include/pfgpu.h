@@ -185,6 +185,38 @@ int  pfg_download(pfg_ctx* ctx, uint32_t* lits, uint64_t* cls_off,
                   uint8_t* eliminated, uint32_t* units, uint32_t* pending_units,
                   uint32_t* stack, uint64_t* round_ends);
 
+/*
+ * Batched simplification: n independent instances in one device clause store,
+ * every pass launched once for all of them. Each instance keeps its own round
+ * counter, stop rule, capacities and results, so its output is the one a
+ * single pfg_upload/pfg_simplify of that instance gives. pfg_upload is the
+ * n = 1 case. (No counterpart in the reference, which simplifies one CNF.)
+ */
+typedef struct pfg_instance {
+    uint32_t        max_var;
+    uint32_t        _pad;
+    uint64_t        num_clauses;
+    const uint32_t* lits;
+    const uint64_t* cls_off;
+    const uint8_t*  cls_learnt;   /* nullable */
+    const uint32_t* cls_lbd;      /* nullable */
+    const uint8_t*  cls_usage;    /* nullable */
+    const uint8_t*  var_state;    /* nullable */
+    const uint8_t*  assumed;      /* nullable */
+    const uint32_t* vorg;         /* nullable: identity */
+} pfg_instance;
+
+int  pfg_batch_upload(pfg_ctx* ctx, uint32_t n, const pfg_instance* instances);
+/* number of instances of the last upload */
+uint32_t pfg_batch_size(pfg_ctx* ctx);
+/* statistics of instance i of the last pfg_simplify (totals come from pfg_simplify itself) */
+int  pfg_batch_stats(pfg_ctx* ctx, uint32_t i, pfg_stats* stats);
+int  pfg_batch_result_sizes(pfg_ctx* ctx, uint32_t i, pfg_result_sizes* sizes);
+int  pfg_batch_download(pfg_ctx* ctx, uint32_t i, uint32_t* lits, uint64_t* cls_off,
+                        uint8_t* cls_learnt, uint32_t* cls_lbd, uint8_t* cls_usage,
+                        uint8_t* eliminated, uint32_t* units, uint32_t* pending_units,
+                        uint32_t* stack, uint64_t* round_ends);
+
 /* Release all device memory of the context. Replaces Solver::freeSimp (simplify.cu:254). */
 void pfg_destroy(pfg_ctx* ctx);
 

@@ -92,6 +92,23 @@ class PfgResultSizes(C.Structure):
     ]
 
 
+class PfgInstance(C.Structure):
+    """One instance of a batch (pfg_instance)."""
+    _fields_ = [
+        ("max_var", C.c_uint32),
+        ("_pad", C.c_uint32),
+        ("num_clauses", C.c_uint64),
+        ("lits", C.POINTER(C.c_uint32)),
+        ("cls_off", C.POINTER(C.c_uint64)),
+        ("cls_learnt", C.POINTER(C.c_uint8)),
+        ("cls_lbd", C.POINTER(C.c_uint32)),
+        ("cls_usage", C.POINTER(C.c_uint8)),
+        ("var_state", C.POINTER(C.c_uint8)),
+        ("assumed", C.POINTER(C.c_uint8)),
+        ("vorg", C.POINTER(C.c_uint32)),
+    ]
+
+
 PASS_NAMES = ("ot", "bcp", "lcve", "sub", "ve", "ere", "gc", "other")
 
 # Reference option names (src/gpu/options.cpp:24-43, options.cu:33-60) -> struct fields.

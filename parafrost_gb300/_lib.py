@@ -6,7 +6,7 @@ implementation to fall back to, so a missing or broken library raises.
 import ctypes as C
 import os
 
-from ._abi import PfgOptions, PfgResultSizes, PfgStats
+from ._abi import PfgInstance, PfgOptions, PfgResultSizes, PfgStats
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libpfgpu.so")
@@ -42,6 +42,16 @@ def lib():
     L.pfg_result_sizes_get.restype = C.c_int
     L.pfg_download.argtypes = [C.c_void_p, u32p, u64p, u8p, u32p, u8p, u8p, u32p, u32p, u32p, u64p]
     L.pfg_download.restype = C.c_int
+    L.pfg_batch_upload.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(PfgInstance)]
+    L.pfg_batch_upload.restype = C.c_int
+    L.pfg_batch_size.argtypes = [C.c_void_p]
+    L.pfg_batch_size.restype = C.c_uint32
+    L.pfg_batch_stats.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(PfgStats)]
+    L.pfg_batch_stats.restype = C.c_int
+    L.pfg_batch_result_sizes.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(PfgResultSizes)]
+    L.pfg_batch_result_sizes.restype = C.c_int
+    L.pfg_batch_download.argtypes = [C.c_void_p, C.c_uint32, u32p, u64p, u8p, u32p, u8p, u8p, u32p, u32p, u32p, u64p]
+    L.pfg_batch_download.restype = C.c_int
     L.pfg_destroy.argtypes = [C.c_void_p]
     L.pfg_destroy.restype = None
     L.pfg_last_error.argtypes = [C.c_void_p]
@@ -70,5 +80,6 @@ EXPORTED = (
     "pfg_abi_sizes", "pfg_default_options", "pfg_resolve_options", "pfg_create", "pfg_upload", "pfg_simplify",
     "pfg_result_sizes_get", "pfg_download", "pfg_destroy", "pfg_last_error", "pfg_kernel_launches",
     "pfg_generate", "pfg_profile_enable", "pfg_profile_reset", "pfg_profile_count", "pfg_profile_name",
-    "pfg_profile_get",
+    "pfg_profile_get", "pfg_batch_upload", "pfg_batch_size", "pfg_batch_stats", "pfg_batch_result_sizes",
+    "pfg_batch_download",
 )

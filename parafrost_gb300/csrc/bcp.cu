@@ -5,13 +5,29 @@
 // literal's occurrence list. Assignments are claimed with atomicCAS, so the
 // fixpoint (and a conflict) is independent of the schedule. Every level is a
 // kernel launch; the host reads the frontier size only every 1, 2, 4 .. 64
-// levels, and the level loop is bounded.
+// levels, and the level loop is bounded. With several instances, each one
+// seeds from its own unit region, records its own trail and conflict, and a
+// conflicting instance is left unchanged (its clauses are not rewritten), as
+// the reference leaves the CNF of an instance whose propagation conflicted.
 #include "engine.cuh"
 
 namespace pfg {
 namespace {
 
 constexpr uint8_t BCP_UNSET = 0, BCP_TRUE = 1, BCP_FALSE = 2;
+
+struct BK {
+    uint8_t* st;
+    uint8_t* elim;
+    const uint32_t* vinst;
+    const unsigned long long* tbase;
+    const uint32_t* tcap;
+    uint32_t* tcount;
+    uint32_t* conflict;
+    uint32_t* trail;
+    DevCounters* dc;
+    uint32_t V;
+};
 
 PFG_D uint32_t litval(const uint8_t* st, uint32_t lit) {
     const uint8_t s = st[ABSV(lit)];
@@ -20,38 +36,49 @@ PFG_D uint32_t litval(const uint8_t* st, uint32_t lit) {
     return sat ? BCP_TRUE : BCP_FALSE;
 }
 
-PFG_D void assign_unit(uint8_t* st, uint8_t* elim, uint32_t unit, uint32_t* front_next, DevCounters* dc,
-                       uint32_t* trail, uint32_t trail_cap, uint32_t V) {
+PFG_D void set_conflict(const BK& k, uint32_t inst) {
+    k.conflict[inst] = 1;
+    k.dc->conflict = 1;
+}
+
+PFG_D void assign_unit(const BK& k, uint32_t unit, uint32_t* front_next) {
     const uint32_t v = ABSV(unit);
-    if (v == 0 || v > V) { atomicOr(&dc->err, ERR_BAD_LIT); return; }
+    if (v == 0 || v > k.V) { atomicOr(&k.dc->err, ERR_BAD_LIT); return; }
+    const uint32_t inst = k.vinst[v];
     const uint8_t desired = SIGNL(unit) ? BCP_FALSE : BCP_TRUE;
     // byte-granular CAS through the containing word
-    unsigned int* word = (unsigned int*)((uintptr_t)(st + v) & ~(uintptr_t)3);
-    const unsigned int shift = (unsigned int)(((uintptr_t)(st + v) & 3u) * 8u);
+    unsigned int* word = (unsigned int*)((uintptr_t)(k.st + v) & ~(uintptr_t)3);
+    const unsigned int shift = (unsigned int)(((uintptr_t)(k.st + v) & 3u) * 8u);
     unsigned int old = *((volatile unsigned int*)word);
     for (int it = 0; it < 64; it++) {  // bounded: 4 bytes can change at most 4 times
         const uint8_t cur = (uint8_t)((old >> shift) & 0xFFu);
         if (cur != BCP_UNSET) {
-            if (cur != desired) dc->conflict = 1;
+            if (cur != desired) set_conflict(k, inst);
             return;
         }
         const unsigned int nw = (old & ~(0xFFu << shift)) | ((unsigned int)desired << shift);
         const unsigned int prev = atomicCAS(word, old, nw);
         if (prev == old) {
-            elim[v] |= FORCED_MASK;
-            const uint32_t t = atomicAdd(&dc->ntrail, 1u);
-            if (t < trail_cap) trail[t] = unit; else atomicOr(&dc->err, ERR_UNITS_OVERFLOW);
-            front_next[atomicAdd(&dc->bcp_next, 1u)] = FLIPL(unit);
+            k.elim[v] |= FORCED_MASK;
+            const uint32_t t = atomicAdd(&k.tcount[inst], 1u);
+            if (t < k.tcap[inst]) k.trail[k.tbase[inst] + t] = unit; else atomicOr(&k.dc->err, ERR_UNITS_OVERFLOW);
+            front_next[atomicAdd(&k.dc->bcp_next, 1u)] = FLIPL(unit);
             return;
         }
         old = prev;
     }
 }
 
-__global__ void bcp_seed_k(uint8_t* st, uint8_t* elim, const uint32_t* units, uint32_t nunits, uint32_t* front,
-                           DevCounters* dc, uint32_t* trail, uint32_t trail_cap, uint32_t V) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nunits; i += gridDim.x * blockDim.x)
-        assign_unit(st, elim, units[i], front, dc, trail, trail_cap, V);
+// grid.y walks the instances, grid.x strides the units of one instance
+__global__ void bcp_seed_k(BK k, const uint32_t* units, const unsigned long long* ubase, const uint32_t* ucount,
+                           const uint8_t* bcp, uint32_t ninst, uint32_t* front) {
+    for (uint32_t i = blockIdx.y; i < ninst; i += gridDim.y) {
+        if (!bcp[i]) continue;
+        const uint32_t n = ucount[i];
+        const uint32_t* u = units + ubase[i];
+        for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+            assign_unit(k, u[j], front);
+    }
 }
 
 __global__ void bcp_advance_k(DevCounters* dc) {
@@ -61,11 +88,10 @@ __global__ void bcp_advance_k(DevCounters* dc) {
 }
 
 // warp per frontier literal, lanes stride its occurrence list
-__global__ void bcp_propagate_k(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off,
-                                const uint32_t* ot_size, const uint32_t* ot_ids, uint8_t* st, uint8_t* elim,
-                                const uint32_t* front_a, uint32_t* front_b, DevCounters* dc,
-                                uint32_t* trail, uint32_t trail_cap, uint32_t V) {
-    if (dc->conflict) return;
+__global__ void bcp_propagate_k(BK k, const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off,
+                                const uint32_t* ot_size, const uint32_t* ot_ids, const uint32_t* front_a,
+                                uint32_t* front_b) {
+    DevCounters* dc = k.dc;
     const uint32_t level = dc->bcp_level;
     const uint32_t* cur = (level & 1u) ? front_b : (uint32_t*)front_a;
     uint32_t* nxt = (level & 1u) ? (uint32_t*)front_a : front_b;
@@ -75,6 +101,8 @@ __global__ void bcp_propagate_k(const ClsHdr* hdr, const uint32_t* lits, const u
     const unsigned lane = threadIdx.x & 31u;
     for (uint32_t fi = warp; fi < n; fi += nwarps) {
         const uint32_t f = cur[fi];
+        const uint32_t inst = k.vinst[ABSV(f)];
+        if (k.conflict[inst]) continue;       // this instance is UNSAT: stop propagating it
         const uint32_t o = ot_off[f], sz = ot_size[f];
         for (uint32_t j = lane; j < sz; j += 32) {
             const ClsHdr h = hdr[ot_ids[o + j]];
@@ -82,28 +110,32 @@ __global__ void bcp_propagate_k(const ClsHdr* hdr, const uint32_t* lits, const u
             uint32_t unit = 0;
             int nunset = 0;
             bool sat = false;
-            for (uint32_t k = 0; k < h.size; k++) {
-                const uint32_t l = lits[h.off + k];
-                const uint32_t ve = litval(st, l);
+            for (uint32_t q = 0; q < h.size; q++) {
+                const uint32_t l = lits[h.off + q];
+                const uint32_t ve = litval(k.st, l);
                 if (ve == BCP_TRUE) { sat = true; break; }
                 if (ve == BCP_UNSET) { unit = l; if (++nunset > 1) break; }
             }
             if (sat) continue;
-            if (!nunset) dc->conflict = 1;
-            else if (nunset == 1) assign_unit(st, elim, unit, nxt, dc, trail, trail_cap, V);
+            if (!nunset) set_conflict(k, inst);
+            else if (nunset == 1) assign_unit(k, unit, nxt);
         }
     }
 }
 
-__global__ void bcp_apply_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls, const uint8_t* st) {
+// strip false literals, delete satisfied clauses of the propagating, conflict-free instances
+__global__ void bcp_apply_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls, const uint8_t* st, const uint32_t* vinst,
+                            const uint8_t* bcp, const uint32_t* conflict) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         ClsHdr h = hdr[c];
-        if (m_deleted(h.meta)) continue;
+        if (m_deleted(h.meta) || !h.size) continue;
         uint32_t* l = lits + h.off;
+        const uint32_t inst = vinst[ABSV(l[0])];
+        if (!bcp[inst] || conflict[inst]) continue;
         uint32_t sig = 0, n = 0;
         bool sat = false;
-        for (uint32_t k = 0; k < h.size; k++) {
-            const uint32_t lit = l[k];
+        for (uint32_t q = 0; q < h.size; q++) {
+            const uint32_t lit = l[q];
             const uint32_t ve = litval(st, lit);
             if (ve == BCP_TRUE) { sat = true; break; }
             if (ve == BCP_FALSE) continue;
@@ -117,39 +149,48 @@ __global__ void bcp_apply_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls, const ui
 
 }  // namespace
 
-// Returns false on a CUDA/engine error; `ok` = false on a conflict (UNSAT).
-bool bcp_prop(Ctx& c, bool& ok) {
-    ok = true;
-    if (!c.nUnits) return true;
+// Propagates the units of the instances flagged in di.bcp (their counts are in
+// dout.ucount). Returns false on a CUDA/engine error; conflicts are reported
+// per instance in dout.conflict.
+bool bcp_prop(Ctx& c) {
     cudaMemsetAsync(c.bstate, 0, c.V + 1, c.s);
     cudaMemsetAsync(&c.dc->conflict, 0, sizeof(uint32_t), c.s);
+    cudaMemsetAsync(c.dout.conflict, 0, c.ninst * sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->bcp_curr, 0, 3 * sizeof(uint32_t), c.s);
-    const uint32_t trail_before = c.hc->ntrail;
-    // seed: assigned literals go to front_a through bcp_next, then advance to level 0
-    PFG_LAUNCH(K_BCP, bcp_seed_k, grid_for(c.nUnits, 256), 256, 0, c.s, c.bstate, c.elim, c.units, (uint32_t)c.nUnits, c.front_a,
-                                                        c.dc, c.trail, c.trail_cap, c.V);
-    PFG_LAUNCH(K_BCP, bcp_advance_k, 1, 1, 0, c.s, c.dc);   // curr = seeded, level = 1
+    BK k;
+    k.st = c.bstate; k.elim = c.elim; k.vinst = c.vinst;
+    k.tbase = c.di.tbase; k.tcap = c.di.tcap; k.tcount = c.dout.tcount;
+    k.conflict = c.dout.conflict; k.trail = c.trail; k.dc = c.dc; k.V = c.V;
+    uint64_t maxu = 0;
+    for (uint32_t i = 0; i < c.ninst; i++)
+        if (c.hi.bcp[i]) maxu = std::max<uint64_t>(maxu, c.ih[i].nUnits);
+    // seed: assigned literals go to front_a through bcp_next, then advance
+    const dim3 sgrid(grid_for(maxu, 256, 8), std::min<uint32_t>(c.ninst, 65535u));
+    PFG_LAUNCH(K_BCP, bcp_seed_k, sgrid, 256, 0, c.s, k, c.units, c.di.ubase, c.dout.ucount, c.di.bcp, c.ninst,
+               c.front_a);
+    PFG_LAUNCH(K_BCP, bcp_advance_k, 1, 1, 0, c.s, c.dc);
     // make level parity start at 0 with the seeds in front_a
     cudaMemsetAsync(&c.dc->bcp_level, 0, sizeof(uint32_t), c.s);
     const unsigned grid = 152 * 8;
     uint32_t levels = 0;
     const uint32_t max_levels = c.V + 2;   // every level assigns at least one new variable
+    const bool single = c.ninst == 1;
     for (int batch = 1;; batch = std::min(batch << 1, 64)) {
         for (int b = 0; b < batch; b++) {
-            PFG_LAUNCH(K_BCP, bcp_propagate_k, grid, 256, 0, c.s, c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids, c.bstate, c.elim,
-                                                   c.front_a, c.front_b, c.dc, c.trail, c.trail_cap, c.V);
+            PFG_LAUNCH(K_BCP, bcp_propagate_k, grid, 256, 0, c.s, k, c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids,
+                       c.front_a, c.front_b);
             PFG_LAUNCH(K_BCP, bcp_advance_k, 1, 1, 0, c.s, c.dc);
         }
         levels += batch;
         sync_counters(c);
         if (!c.err.empty()) return false;
-        if (c.hc->conflict || !c.hc->bcp_curr) break;
+        if ((single && c.hc->conflict) || !c.hc->bcp_curr) break;
         if (levels > max_levels) { c.err = "device unit propagation did not converge"; c.simpstate = PFG_TIMEOUT; return false; }
     }
     if (c.hc->err) { c.err = "device error during unit propagation"; return false; }
-    if (c.hc->conflict) { ok = false; return true; }
-    PFG_LAUNCH(K_BCP, bcp_apply_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.bstate);
-    (void)trail_before;
+    if (!(single && c.hc->conflict))
+        PFG_LAUNCH(K_BCP, bcp_apply_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.bstate, c.vinst,
+                   c.di.bcp, c.dout.conflict);
     return cuda_ok(c, cudaGetLastError(), "bcp");
 }
 

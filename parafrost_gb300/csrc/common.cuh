@@ -69,13 +69,12 @@ PFG_HD uint32_t FLIPL(uint32_t l) { return l ^ 1u; }
 PFG_HD uint32_t MAPHASH(uint32_t l) { return 1u << (l & 31u); }
 PFG_HD bool SUBSIG(uint32_t a, uint32_t b) { return !(a & ~b); }
 
-// Device counters shared between kernels and the host (one pinned mirror).
+// Device counters shared between kernels and the host (one pinned mirror);
+// per-instance counters live in the engine's InstOut arrays.
 struct DevCounters {
-    unsigned long long nstack;     // model-stack words
     unsigned long long live_cls;   // live clauses (count kernel)
     unsigned long long live_lits;
     unsigned long long err_info;   // first error detail
-    uint32_t nunits;               // vars->units size
     uint32_t err;                  // error flags (ERR_*)
     uint32_t nwork;                // MIS worklist size
     uint32_t nwin;                 // winners in the current MIS round
@@ -83,11 +82,9 @@ struct DevCounters {
     uint32_t nfrozen;
     uint32_t conflict;             // BCP conflict flag
     uint32_t bcp_curr, bcp_next, bcp_level;
-    uint32_t ntrail;
-    int32_t last_elim;             // lastEliminatedID
-    uint32_t survivors;
     uint32_t big_lists;
     uint32_t nbig_sub, nbig_ve1, nbig_ve3;   // variables too large for the warp stage
+    unsigned long long ve_cls, ve_lits;      // store size after the last BVE emission
 };
 
 constexpr uint32_t ERR_UNITS_OVERFLOW = 1u;

@@ -23,12 +23,17 @@ struct EK {
     uint32_t* ot_ids;
     uint8_t* elim;
     const uint32_t* varcore;
-    int varcore_on;
     const uint32_t* vorg;
-    uint32_t* units;
-    uint32_t units_cap;
-    uint32_t* stack;
-    unsigned long long stack_cap;
+    const uint32_t* vinst;               // instance of a variable
+    const uint8_t* vc_on;                // per instance: function-table gates on
+    uint32_t* units;                     // per-instance unit regions
+    const unsigned long long* ubase;
+    const uint32_t* ucap;
+    uint32_t* ucount;
+    uint32_t* stack;                     // per-instance model-stack regions
+    const unsigned long long* sbase;
+    const unsigned long long* scap;
+    unsigned long long* scount;
     DevCounters* dc;
     uint32_t ve_clause_max, xor_max_arity, sub_max_occurs, ere_max_occurs, ere_clause_max;
     int ve_lbound_en, ve_inprocess;
@@ -43,10 +48,21 @@ PFG_D void SET_MOLTEN(const EK& k, uint32_t c, uint32_t f) { k.hdr[c].meta = m_s
 PFG_D void SET_DELETED(const EK& k, uint32_t c) { k.hdr[c].meta = m_set_st(k.hdr[c].meta, ST_DELETED); }
 
 PFG_D void push_unit(const EK& k, uint32_t lit) {
-    const uint32_t i = atomicAdd(&k.dc->nunits, 1u);
-    if (i < k.units_cap) k.units[i] = lit;
+    const uint32_t inst = k.vinst[ABSV(lit)];
+    const uint32_t i = atomicAdd(&k.ucount[inst], 1u);
+    if (i < k.ucap[inst]) k.units[k.ubase[inst] + i] = lit;
     else atomicOr(&k.dc->err, ERR_UNITS_OVERFLOW);
 }
+
+// reserve `words` of the model stack of variable v's instance; ~0 on overflow
+PFG_D unsigned long long stack_reserve(const EK& k, uint32_t v, unsigned long long words) {
+    const uint32_t inst = k.vinst[v];
+    const unsigned long long base = atomicAdd(&k.scount[inst], words);
+    if (base + words > k.scap[inst]) { atomicOr(&k.dc->err, ERR_STACK_OVERFLOW); return ~0ull; }
+    return k.sbase[inst] + base;
+}
+
+PFG_D bool vc_on(const EK& k, uint32_t x) { return k.vc_on[k.vinst[x]] != 0; }
 
 PFG_D void sort_small(uint32_t* d, uint32_t n) {
     for (uint32_t i = 1; i < n; i++) {
@@ -269,8 +285,8 @@ PFG_D void save_side(const EK& k, uint32_t side, uint32_t witlit, uint32_t w) {
         const ClsHdr h = k.hdr[ol[i]];
         if (m_orig(h.meta)) words += h.size + 1ull;
     }
-    const unsigned long long base = atomicAdd(&k.dc->nstack, words);
-    if (base + words > k.stack_cap) { atomicOr(&k.dc->err, ERR_STACK_OVERFLOW); return; }
+    const unsigned long long base = stack_reserve(k, ABSV(w), words);
+    if (base == ~0ull) return;
     uint32_t* s = k.stack + base;
     for (uint32_t i = 0; i < n; i++) {
         const ClsHdr h = k.hdr[ol[i]];
@@ -815,7 +831,7 @@ __global__ void __launch_bounds__(128) ve1a_k(EK k, const uint32_t* elected, uin
             else if (find_xor_gate(k, p, n, nClsBefore, outs, nE, nC, nL)) elimType = AOIX_MASK;
             else if (!nC && find_xor_gate(k, n, p, nClsBefore, outs, nE, nC, nL)) elimType = AOIX_MASK;
         }
-        if (k.varcore_on && !elimType && nClsBefore > 2) {
+        if (vc_on(k, x) && !elimType && nClsBefore > 2) {
             // function-table stage (and what follows it) is finished by ve1b_k
             dlist[atomicAdd(dcount, 1u)] = tid;
             ucnt[tid] = nC;
@@ -956,9 +972,8 @@ __global__ void __launch_bounds__(128) ve1b_k(EK k, const uint32_t* elected, con
 
 // ---- BVE phase 3 ----
 __global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint32_t nelected, const uint32_t* type,
-                                             const unsigned long long* rpos, const unsigned long long* rref,
-                                             unsigned long long cs_cap, unsigned long long data_cap, uint8_t* keep,
-                                             const uint32_t* list, const uint32_t* count) {
+                                             const unsigned long long* rslot, const unsigned long long* rlit,
+                                             const uint8_t* fits, const uint32_t* list, const uint32_t* count) {
     const uint32_t nn = list_count(list, count, nelected);
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += gridDim.x * blockDim.x) {
         const uint32_t tid = list ? list[q] : q;
@@ -968,15 +983,14 @@ __global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint
         if (et) {
             const uint32_t p = 2 * x, n = p | 1;
             const uint32_t nAddedCls = (xinfo & 0xFFFCu) >> 2, nAddedLits = xinfo >> 16;
-            const unsigned long long addedPos = rpos[tid], addedRef = rref[tid];
-            if (addedPos + nAddedCls <= cs_cap &&
-                addedRef + nAddedLits + (unsigned long long)NBUCKETS * nAddedCls <= data_cap) {
+            (void)nAddedLits;
+            if (fits[tid]) {
                 save_resolved_lists(k, p, n);
                 const int kind = et == RES_MASK ? PAIR_RES : (et == CORE_MASK ? PAIR_CORE : PAIR_SUBS);
-                // resolvents go to slots addedPos.. ; literals packed at ref - 3 * index
-                unsigned long long slot = addedPos;
-                unsigned long long woff = addedRef - (unsigned long long)NBUCKETS * addedPos;
-                const unsigned long long checksum = addedPos + nAddedCls;
+                // resolvents go to physical slots rslot.. with literals packed from rlit
+                unsigned long long slot = rslot[tid];
+                unsigned long long woff = rlit[tid];
+                const unsigned long long checksum = slot + nAddedCls;
                 const uint32_t* ml = OLp(k, p);
                 const uint32_t* ol = OLp(k, n);
                 const uint32_t ms = OLs(k, p), os = OLs(k, n);
@@ -1011,12 +1025,10 @@ __global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint
                 if (slot != checksum) atomicOr(&k.dc->err, ERR_SLOT_MISMATCH);
                 toblivion(k, p, n);
                 k.elim[x] |= MELTING_MASK | ADDING_MASK;
-                atomicMax(&k.dc->last_elim, (int)tid);
             } else if (et != RES_MASK) {
                 freeze_clauses(k, p, n);
             }
         }
-        keep[tid] = k.elim[x] ? 0 : 1;
     }
 }
 
@@ -1093,12 +1105,17 @@ EK make_ek(Ctx& c) {
     k.ot_ids = c.ot_ids;
     k.elim = c.elim;
     k.varcore = c.varcore;
-    k.varcore_on = c.varcore_on ? 1 : 0;
     k.vorg = c.vorg;
+    k.vinst = c.vinst;
+    k.vc_on = c.di.vc_on;
     k.units = c.units;
-    k.units_cap = c.units_cap;
+    k.ubase = c.di.ubase;
+    k.ucap = c.di.ucap;
+    k.ucount = c.dout.ucount;
     k.stack = c.stack;
-    k.stack_cap = c.stack_cap;
+    k.sbase = c.di.sbase;
+    k.scap = c.di.scap;
+    k.scount = c.dout.scount;
     k.dc = c.dc;
     k.ve_clause_max = c.o.ve_clause_max;
     k.xor_max_arity = c.o.xor_max_arity;
@@ -1110,70 +1127,107 @@ EK make_ek(Ctx& c) {
     return k;
 }
 
-__global__ void keep_u32_k(const uint8_t* keep, uint32_t n, uint32_t* out) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = keep[i];
+// MEMORY_SAFE (bounded.cuh:279) per instance: gpos / gref are the exclusive
+// scans of added clauses / buckets over the whole BVE set; an instance's own
+// scan is the difference to its first entry, offset by its reference clause
+// count and data size. Slots that fit get their physical size counted in
+// cslot / clit (scanned next); the rest stay out of the store.
+__global__ void ve_place_k(const uint32_t* veset, uint32_t E, const uint32_t* type,
+                           const unsigned long long* gpos, const unsigned long long* gref, const uint32_t* vinst,
+                           const uint32_t* seg, const unsigned long long* acc, uint8_t* fits,
+                           unsigned long long* cslot, unsigned long long* clit) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < E; t += gridDim.x * blockDim.x) {
+        const uint32_t xinfo = type[t];
+        const uint32_t et = xinfo & 3u;
+        const unsigned long long nC = (xinfo & 0xFFFCu) >> 2, nL = xinfo >> 16;
+        bool ok = false;
+        if (et) {
+            const uint32_t i = vinst[veset[t]];
+            const uint32_t s0 = seg[i];
+            const unsigned long long* a = acc + 4 * (uint64_t)i;
+            const unsigned long long vpos = a[0] + gpos[t] - gpos[s0];
+            const unsigned long long vref = a[1] + gref[t] - gref[s0];
+            ok = vpos + nC <= a[2] && vref + nL + (unsigned long long)NBUCKETS * nC <= a[3];
+        }
+        fits[t] = ok ? 1 : 0;
+        cslot[t] = ok ? nC : 0ull;
+        clit[t] = ok ? nL : 0ull;
+    }
+}
+
+// clauses / literal words each instance added (differences of the physical scans)
+__global__ void inst_add_k(const unsigned long long* cslot, const unsigned long long* clit, const uint32_t* seg,
+                           uint32_t ninst, unsigned long long* add) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ninst; i += gridDim.x * blockDim.x) {
+        const uint32_t b = seg[i], e = seg[i + 1];
+        add[2 * i] = e > b ? cslot[e] - cslot[b] : 0ull;
+        add[2 * i + 1] = e > b ? clit[e] - clit[b] : 0ull;
+    }
 }
 
 }  // namespace
 
 void sub_pass(Ctx& c) {
-    const uint32_t E = c.nelected;
+    const uint32_t E = c.nve;
     if (!E) return;
     const EK k = make_ek(c);
     cudaMemsetAsync(&c.dc->nbig_sub, 0, sizeof(uint32_t), c.s);
     // warp per variable on the shared-memory stage; larger variables by one thread each
-    PFG_LAUNCH(K_SUB, subw_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.elected, E,
+    PFG_LAUNCH(K_SUB, subw_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.veset, E,
                c.work_b, &c.dc->nbig_sub);
-    PFG_LAUNCH(K_BIGVAR, sub_k, grid_for(E, 64, 8), 64, 0, c.s, k, c.elected, E, c.work_b, &c.dc->nbig_sub);
+    PFG_LAUNCH(K_BIGVAR, sub_k, grid_for(E, 64, 8), 64, 0, c.s, k, c.veset, E, c.work_b, &c.dc->nbig_sub);
 }
 
 bool ve_pass(Ctx& c) {
-    const uint32_t E = c.nelected;
+    const uint32_t E = c.nve;
     if (!E) return true;
     const EK k = make_ek(c);
+    bool any_vc = false;
+    for (uint32_t i = 0; i < c.ninst; i++) any_vc |= c.ih[i].mode == 1 && c.ih[i].varcore_on;
     cudaMemsetAsync(&c.dc->nwork, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->nbig_ve1, 0, 2 * sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_VE1, ve1w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.elected, E,
+    PFG_LAUNCH(K_VE1, ve1w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.veset, E,
                c.type, c.ucnt, c.rpos, c.rref, c.work, &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
-    PFG_LAUNCH(K_BIGVAR, ve1a_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.elected, E, c.type, c.ucnt, c.rpos, c.rref, c.work,
+    PFG_LAUNCH(K_BIGVAR, ve1a_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.veset, E, c.type, c.ucnt, c.rpos, c.rref, c.work,
                &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
-    if (c.varcore_on)   // one warp per deferred variable; the grid walks the device-side count
-        PFG_LAUNCH(K_VE1B, ve1b_k, grid_for((uint64_t)E * 32, 128, 16), 128, 0, c.s, k, c.elected, c.work,
+    if (any_vc)   // one warp per deferred variable; the grid walks the device-side count
+        PFG_LAUNCH(K_VE1B, ve1b_k, grid_for((uint64_t)E * 32, 128, 16), 128, 0, c.s, k, c.veset, c.work,
                    &c.dc->nwork, c.type, c.ucnt, c.rpos, c.rref);
     if (!ensure_tmp(c, scan_temp_bytes(E))) return false;
-    exclusive_scan_u64(c.rpos, c.rpos, E, (unsigned long long)c.ncls, nullptr, c.tmp, c.s);
-    exclusive_scan_u64(c.rref, c.rref, E, (unsigned long long)c.data_size, nullptr, c.tmp, c.s);
-    cudaMemsetAsync(&c.dc->last_elim, 0xFF, sizeof(int32_t), c.s);   // -1
-    PFG_LAUNCH(K_VE3, ve3w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.elected, E,
-               c.type, c.rpos, c.rref, c.cs_cap, c.data_cap, c.flag8, c.eligible_b, &c.dc->nbig_ve3);
-    PFG_LAUNCH(K_BIGVAR, ve3_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.elected, E, c.type, c.rpos, c.rref, c.cs_cap,
-               c.data_cap, c.flag8, c.eligible_b, &c.dc->nbig_ve3);
-    // postVE: keep surviving elected variables in order (elimination.cu:249-267)
-    select_flagged(c.elected, c.flag8, c.work, E, &c.dc->survivors, c.vscan, c.tmp, c.s);
-    sync_counters(c);
+    // vePhase2 (elimination.cu:74-100) per instance, then physical placement
+    exclusive_scan_u64(c.rpos, c.rpos, E, 0ull, nullptr, c.tmp, c.s);
+    exclusive_scan_u64(c.rref, c.rref, E, 0ull, nullptr, c.tmp, c.s);
+    PFG_LAUNCH(K_SCAN, ve_place_k, grid_for(E, 256), 256, 0, c.s, c.veset, E, c.type, c.rpos, c.rref, c.vinst,
+               c.di.seg, c.di.acc, c.winv, c.rslot, c.rlit);
+    exclusive_scan_u64(c.rslot, c.rslot, E, (unsigned long long)c.ncls, c.rslot + E, c.tmp, c.s);
+    exclusive_scan_u64(c.rlit, c.rlit, E, (unsigned long long)c.lits_used, c.rlit + E, c.tmp, c.s);
+    PFG_LAUNCH(K_SCAN, inst_add_k, grid_for(c.ninst, 256), 256, 0, c.s, c.rslot, c.rlit, c.di.seg, c.ninst,
+               c.dout.add);
+    cudaMemcpyAsync(&c.dc->ve_cls, c.rslot + E, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c.s);
+    cudaMemcpyAsync(&c.dc->ve_lits, c.rlit + E, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c.s);
+    PFG_LAUNCH(K_VE3, ve3w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.veset, E,
+               c.type, c.rslot, c.rlit, c.winv, c.eligible_b, &c.dc->nbig_ve3);
+    PFG_LAUNCH(K_BIGVAR, ve3_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.veset, E, c.type, c.rslot, c.rlit, c.winv,
+               c.eligible_b, &c.dc->nbig_ve3);
+    // resizeCNF_k (cnf.cu:55-80): the store ends after the last slot that fit
+    pull_inst_out(c);
     if (!c.err.empty()) return false;
-    const int32_t last = c.hc->last_elim;
-    const uint32_t survivors = c.hc->survivors;
-    cudaMemcpyAsync(c.elected, c.work, survivors * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
-    if (last >= 0) {   // resizeCNF_k (cnf.cu:55-80)
-        uint32_t lt = 0;
-        unsigned long long lp = 0, lr = 0;
-        cudaMemcpyAsync(&lt, c.type + last, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-        cudaMemcpyAsync(&lp, c.rpos + last, sizeof(lp), cudaMemcpyDeviceToHost, c.s);
-        cudaMemcpyAsync(&lr, c.rref + last, sizeof(lr), cudaMemcpyDeviceToHost, c.s);
-        if (!cuda_ok(c, cudaStreamSynchronize(c.s), "ve resize")) return false;
-        const uint64_t nC = (lt & 0xFFFCu) >> 2, nL = lt >> 16;
-        c.ncls = lp + nC;
-        c.data_size = lr + nL + NBUCKETS * nC;
-        c.lits_used = c.data_size - NBUCKETS * c.ncls;
+    c.ncls = c.hc->ve_cls;
+    c.lits_used = c.hc->ve_lits;
+    for (uint32_t i = 0; i < c.ninst; i++) {
+        const unsigned long long ac = c.hout.add[2 * i], al = c.hout.add[2 * i + 1];
+        unsigned long long* acc = c.hi.acc + 4 * i;
+        acc[0] += ac;
+        acc[1] += al + (unsigned long long)NBUCKETS * ac;
+        c.ih[i].resolvents += ac;
     }
-    c.nelected = survivors;
+    push_inst_in(c);
     return cuda_ok(c, cudaGetLastError(), "ve");
 }
 
 void ere_pass(Ctx& c) {
-    if (!c.nelected) return;
-    PFG_LAUNCH(K_ERE, ere_k, grid_for((uint64_t)c.nelected * 32, 128), 128, 0, c.s, make_ek(c), c.elected, c.nelected);
+    if (!c.nere) return;
+    PFG_LAUNCH(K_ERE, ere_k, grid_for((uint64_t)c.nere * 32, 128), 128, 0, c.s, make_ek(c), c.ereset, c.nere);
 }
 
 }  // namespace pfg

@@ -288,8 +288,7 @@ PFG_D void ws_save_side(const EK& k, WS& w, const Side& s, uint32_t witlit, uint
         total += t;
     }
     if (lane == 0) {
-        sbase = atomicAdd(&k.dc->nstack, (unsigned long long)total);
-        if (sbase + total > k.stack_cap) { atomicOr(&k.dc->err, ERR_STACK_OVERFLOW); sbase = ~0ull; }
+        sbase = stack_reserve(k, ABSV(wit), (unsigned long long)total);
     }
     sbase = __shfl_sync(FULL, sbase, 0);
     if (sbase == ~0ull) return;
@@ -685,7 +684,7 @@ PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
         else if (ws_find_xor_gate(k, w, P, N, nClsBefore, nE, nC, nL, lane)) elimType = AOIX_MASK;
         else if (!nC && ws_find_xor_gate(k, w, N, P, nClsBefore, nE, nC, nL, lane)) elimType = AOIX_MASK;
     }
-    if (k.varcore_on && !elimType && nClsBefore > 2) {
+    if (vc_on(k, x) && !elimType && nClsBefore > 2) {
         ws_flush(k, w, lane);
         if (lane == 0) {
             dlist[atomicAdd(dcount, 1u)] = tid;
@@ -724,10 +723,9 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve1w_k(EK k, const uint32_t* el
 
 // ---- BVE phase 3 on the stage (bounded.cuh:69-258, 488-544) ----
 __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* elected, uint32_t nelected,
-                                                        const uint32_t* type, const unsigned long long* rpos,
-                                                        const unsigned long long* rref, unsigned long long cs_cap,
-                                                        unsigned long long data_cap, uint8_t* keep, uint32_t* big,
-                                                        uint32_t* nbig) {
+                                                        const uint32_t* type, const unsigned long long* rslot,
+                                                        const unsigned long long* rlit, const uint8_t* fits,
+                                                        uint32_t* big, uint32_t* nbig) {
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
@@ -737,26 +735,21 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
         const uint32_t x = elected[tid];
         const uint32_t xinfo = type[tid];
         const uint32_t et = xinfo & 3u;
-        if (!et) {
-            if (lane == 0) keep[tid] = k.elim[x] ? 0 : 1;
-            continue;
-        }
+        if (!et) continue;
         const uint32_t p = 2 * x, n = p | 1;
         if (!ws_stage(k, w, p, n, lane)) {
             if (lane == 0) big[atomicAdd(nbig, 1u)] = tid;
             continue;
         }
         const Side P{0, w.np, p}, N{w.np, w.nn, n};
-        const uint32_t nAddedCls = (xinfo & 0xFFFCu) >> 2, nAddedLits = xinfo >> 16;
-        const unsigned long long addedPos = rpos[tid], addedRef = rref[tid];
-        if (addedPos + nAddedCls <= cs_cap &&
-            addedRef + nAddedLits + (unsigned long long)NBUCKETS * nAddedCls <= data_cap) {
+        const uint32_t nAddedCls = (xinfo & 0xFFFCu) >> 2;
+        if (fits[tid]) {
             // saveResolved by list sizes (elimination.cuh:551-594)
             if (P.n > N.n) ws_save_side(k, w, N, N.lit, P.lit, lane);
             else ws_save_side(k, w, P, P.lit, N.lit, lane);
             const int kind = et == RES_MASK ? CNT_RES_BOUNDED : (et == CORE_MASK ? CNT_CORE : CNT_SUBS);
-            unsigned long long slot = addedPos;
-            unsigned long long woff = addedRef - (unsigned long long)NBUCKETS * addedPos;
+            unsigned long long slot = rslot[tid];
+            unsigned long long woff = rlit[tid];
             uint32_t added = 0;
             const uint32_t total = P.n * N.n;
             for (uint32_t q0 = 0; q0 < total && added < nAddedCls; q0 += 32) {
@@ -802,10 +795,7 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
             if (added != nAddedCls && lane == 0) atomicOr(&k.dc->err, ERR_SLOT_MISMATCH);
             ws_toblivion(k, w, P, N, lane);
             ws_flush(k, w, lane);
-            if (lane == 0) {
-                k.elim[x] |= MELTING_MASK | ADDING_MASK;
-                atomicMax(&k.dc->last_elim, (int)tid);
-            }
+            if (lane == 0) k.elim[x] |= MELTING_MASK | ADDING_MASK;
         } else if (et != RES_MASK) {
             __syncwarp();
             const uint32_t nc = w.np + w.nn;
@@ -813,7 +803,6 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
                 if (m_orig(w.meta[i]) && m_molten(w.meta[i])) w.meta[i] = m_set_molten(w.meta[i], 0);
             ws_flush(k, w, lane);
         }
-        if (lane == 0) keep[tid] = k.elim[x] ? 0 : 1;
         __syncwarp();
     }
 }

@@ -1,9 +1,9 @@
 // C-ABI and round driver of the GB300 CNF inprocessing engine.
 //
-// pfg_upload replaces Solver::awaken (src/gpu/simplify.cu:77-134),
+// pfg_upload / pfg_batch_upload replace Solver::awaken (src/gpu/simplify.cu:77-134),
 // pfg_simplify the round loop of Solver::simplifying (simplify.cu:159-186),
-// pfg_download the write-back (cacheCNF cnf.cu:200-236, cacheEliminated
-// transfer.cu:69, cacheResolved transfer.cu:83).
+// pfg_download / pfg_batch_download the write-back (cacheCNF cnf.cu:200-236,
+// cacheEliminated transfer.cu:69, cacheResolved transfer.cu:83).
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -89,19 +89,87 @@ void sync_counters(Ctx& c) {
     }
 }
 
+static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+template <typename T>
+static void place(char* base, size_t& off, T** p, size_t count) {
+    if (p) *p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off = align_up(off + count * sizeof(T));
+}
+
+size_t inst_in_layout(uint32_t n, char* base, InstIn* p) {
+    InstIn dummy;
+    InstIn& q = p ? *p : dummy;
+    size_t off = 0;
+    place(base, off, &q.voff, n + 1);
+    place(base, off, &q.seg, n + 1);
+    place(base, off, &q.ucap, n);
+    place(base, off, &q.tcap, n);
+    place(base, off, &q.ubase, n);
+    place(base, off, &q.tbase, n);
+    place(base, off, &q.sbase, n);
+    place(base, off, &q.scap, n);
+    place(base, off, &q.acc, 4 * (size_t)n);
+    place(base, off, &q.active, n);
+    place(base, off, &q.vc_on, n);
+    place(base, off, &q.bcp, n);
+    place(base, off, &q.mode, n);
+    return off;
+}
+
+size_t inst_out_layout(uint32_t n, char* base, InstOut* p) {
+    InstOut dummy;
+    InstOut& q = p ? *p : dummy;
+    size_t off = 0;
+    place(base, off, &q.conflict, n);
+    place(base, off, &q.ucount, n);
+    place(base, off, &q.tcount, n);
+    place(base, off, &q.nelect, n);
+    place(base, off, &q.nfrozen, n);
+    place(base, off, &q.fbase, n + 1);
+    place(base, off, &q.scount, n);
+    place(base, off, &q.cnt, 2 * (size_t)n);
+    place(base, off, &q.add, 2 * (size_t)n);
+    return off;
+}
+
+void push_inst_in(Ctx& c) {
+    // the pinned mirror may be rewritten right after this call: wait for the copy
+    cudaMemcpyAsync(c.di.voff, c.hi.voff, c.in_bytes, cudaMemcpyHostToDevice, c.s);
+    cuda_ok(c, cudaStreamSynchronize(c.s), "instance inputs");
+}
+
+void pull_inst_out(Ctx& c) {
+    cudaMemcpyAsync(c.hout.conflict, c.dout.conflict, c.out_bytes, cudaMemcpyDeviceToHost, c.s);
+    sync_counters(c);
+}
+
 namespace {
 
+// header of every uploaded clause; literals moved to their instance's variable range
 __global__ void init_hdr_k(ClsHdr* hdr, const unsigned long long* off, uint64_t ncls, const uint8_t* learnt,
-                           const uint32_t* lbd, const uint8_t* usage) {
+                           const uint32_t* lbd, const uint8_t* usage, const unsigned long long* clsbase,
+                           const unsigned long long* litbase, const uint32_t* voff, uint32_t ninst, uint32_t* lits) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = ninst;   // largest i with clsbase[i] <= c
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (clsbase[mid] <= c) lo = mid; else hi = mid;
+        }
+        const uint32_t inst = lo;
+        const uint64_t b = off[c] + litbase[inst];
+        const uint64_t e = (c + 1 < clsbase[inst + 1]) ? off[c + 1] + litbase[inst] : litbase[inst + 1];
         ClsHdr h;
-        h.off = (uint32_t)off[c];
-        h.size = (uint32_t)(off[c + 1] - off[c]);
+        h.off = (uint32_t)b;
+        h.size = (uint32_t)(e - b);
         h.sig = 0;
         const bool l = learnt && learnt[c];
         h.meta = l ? m_make(ST_LEARNT, 0, 0, usage ? (usage[c] & 3u) : 0u, lbd ? (lbd[c] & 0x03FFFFFFu) : 0u)
                    : m_make(ST_ORIGINAL, 0, 0, 0, 0);
         hdr[c] = h;
+        const uint32_t shift = 2u * voff[inst];
+        if (shift)
+            for (uint64_t k = b; k < e; k++) lits[k] += shift;
     }
 }
 
@@ -124,11 +192,16 @@ __global__ void prep_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls) {
     }
 }
 
-__global__ void identity_k(uint32_t* v, uint32_t n) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
+// instance of every global variable, and its instance-local number (the default vorg)
+__global__ void vinst_k(const uint32_t* voff, uint32_t ninst, uint32_t V, uint32_t* vinst, uint32_t* vorg) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
+        const uint32_t i = v ? inst_search(voff, ninst, v) : 0u;
+        vinst[v] = i;
+        vorg[v] = v ? v - voff[i] : 0u;
+    }
 }
 
-// sum of list sizes and literal counts over elected variables (C_E, L_E of the byte model)
+// sum of list sizes and literal counts over a variable set (C_E, L_E of the byte model)
 __global__ void elected_volume_k(const uint32_t* elected, uint32_t n, const ClsHdr* hdr, const uint32_t* ot_off,
                                  const uint32_t* ot_size, const uint32_t* ot_ids, unsigned long long* out) {
     unsigned long long cc = 0, ll = 0;
@@ -148,7 +221,14 @@ __global__ void elected_volume_k(const uint32_t* elected, uint32_t n, const ClsH
     if ((threadIdx.x & 31u) == 0 && (cc || ll)) { atomicAdd(&out[0], cc); atomicAdd(&out[1], ll); }
 }
 
-// live clauses -> packed host layout
+// elected variables of the instances in `want` mode
+__global__ void mode_flags_k(const uint32_t* elected, uint32_t n, const uint32_t* vinst, const uint8_t* mode,
+                             uint8_t want, uint8_t* flag) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        flag[i] = mode[vinst[elected[i]]] == want;
+}
+
+// live clauses -> packed host layout (one instance)
 __global__ void out_flags_k(const ClsHdr* hdr, uint64_t ncls, uint32_t* flag, unsigned long long* sz) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         const ClsHdr h = hdr[c];
@@ -172,10 +252,45 @@ __global__ void out_pack_k(const ClsHdr* hdr, const uint32_t* lits, uint64_t ncl
         if (lane == 0) {
             const uint32_t q = pos[c];
             ooff[q] = o;
-            const bool l = m_learnt(h.meta);
-            olearnt[q] = l;
+            olearnt[q] = m_learnt(h.meta);
             olbd[q] = m_lbd(h.meta);
             ousage[q] = (uint8_t)m_usage(h.meta);
+        }
+    }
+}
+
+// batch write-back: live clauses keyed by instance (deleted ones after all instances)
+__global__ void cls_inst_keys_k(const ClsHdr* hdr, const uint32_t* lits, uint64_t ncls, const uint32_t* vinst,
+                                uint32_t ninst, uint32_t* keys, uint32_t* ids) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        const ClsHdr h = hdr[c];
+        keys[c] = (m_deleted(h.meta) || !h.size) ? ninst : vinst[ABSV(lits[h.off])];
+        ids[c] = (uint32_t)c;
+    }
+}
+
+__global__ void gathered_sizes_k(const ClsHdr* hdr, const uint32_t* ids, uint64_t n, unsigned long long* sz) {
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x)
+        sz[j] = hdr[ids[j]].size;
+}
+
+// warp per clause; literals back to the instance's own numbering
+__global__ void gathered_pack_k(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ids, uint64_t n,
+                                const unsigned long long* loff, const uint32_t* vinst, const uint32_t* voff,
+                                uint32_t* olits, uint8_t* olearnt, uint32_t* olbd, uint8_t* ousage) {
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint64_t j = warp; j < n; j += nwarps) {
+        const ClsHdr h = hdr[ids[j]];
+        const uint32_t* l = lits + h.off;
+        const uint32_t shift = 2u * voff[vinst[ABSV(l[0])]];
+        const unsigned long long o = loff[j];
+        for (uint32_t k = lane; k < h.size; k += 32) olits[o + k] = l[k] - shift;
+        if (lane == 0) {
+            olearnt[j] = m_learnt(h.meta);
+            olbd[j] = m_lbd(h.meta);
+            ousage[j] = (uint8_t)m_usage(h.meta);
         }
     }
 }
@@ -188,6 +303,8 @@ void free_all(pfg_ctx* o) {
     o->sizes.clear();
     o->allocated = 0;
     if (c.s) cudaStreamSynchronize(c.s);
+    if (c.in_blob_h) cudaFreeHost(c.in_blob_h);
+    if (c.out_blob_h) cudaFreeHost(c.out_blob_h);
     Ctx fresh;
     fresh.o = c.o;
     fresh.device = c.device;
@@ -211,6 +328,266 @@ struct PassTimer {
         c.pass_ms[slot] += ms;
     }
 };
+
+bool valid_instance(Ctx& c, uint32_t idx, const pfg_instance& q, std::vector<uint64_t>& seen) {
+    const std::string who = "instance " + std::to_string(idx) + ": ";
+    if (q.max_var == 0 || q.max_var > 0x7FFFFFF0u || (q.num_clauses && (!q.lits || !q.cls_off))) {
+        c.err = who + "invalid arguments";
+        return false;
+    }
+    if (q.num_clauses && q.cls_off[0] != 0) { c.err = who + "cls_off[0] must be 0"; return false; }
+    // literal range, clause size >= 2, no duplicate or complementary literals
+    const uint64_t nlits = q.num_clauses ? q.cls_off[q.num_clauses] : 0;
+    seen.assign((size_t)q.max_var + 1, ~0ull);
+    for (uint64_t i = 0; i < q.num_clauses; i++) {
+        const uint64_t b = q.cls_off[i], e = q.cls_off[i + 1];
+        if (e < b + 2 || e > nlits) { c.err = who + "clause " + std::to_string(i) + " has fewer than 2 literals"; return false; }
+        for (uint64_t k = b; k < e; k++) {
+            const uint32_t l = q.lits[k], v = l >> 1;
+            if (v == 0 || v > q.max_var) { c.err = who + "literal out of range in clause " + std::to_string(i); return false; }
+            if (seen[v] == i) { c.err = who + "repeated variable in clause " + std::to_string(i); return false; }
+            seen[v] = i;
+        }
+    }
+    return true;
+}
+
+// Solver::awaken (simplify.cu:77-134) for n instances side by side
+int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
+    Ctx& c = o->c;
+    c.err.clear();
+    if (n == 0 || !in) { c.err = "no instances"; return PFG_INVALID; }
+    // Instance i owns global variables voff[i]+1 .. voff[i+1]. Every voff is a
+    // multiple of 16, so a literal keeps its low 5 bits when it is moved into
+    // the global range: clause signatures (1 << (lit & 31)) and with them the
+    // occurrence-list order are the ones of the instance alone.
+    uint64_t Vtot = 0, Ctot = 0, Ltot = 0;
+    std::vector<uint64_t> voffs(n + 1, 0);
+    {
+        std::vector<uint64_t> seen;
+        for (uint32_t i = 0; i < n; i++) {
+            if (!valid_instance(c, i, in[i], seen)) return PFG_INVALID;
+            Vtot = voffs[i] + in[i].max_var;
+            voffs[i + 1] = (i + 1 < n) ? ((Vtot + 15) & ~15ull) : Vtot;
+            Ctot += in[i].num_clauses;
+            Ltot += in[i].num_clauses ? in[i].cls_off[in[i].num_clauses] : 0;
+        }
+    }
+    if (Vtot > 0x7FFFFFF0ull) { c.err = "total variables exceed 2^31"; return PFG_INVALID; }
+    const uint64_t base_launches = g_launches;
+    free_all(o);
+    g_prof = &c.prof;
+    c.ninst = n;
+    c.ih.assign(n, InstHost{});
+    c.V = (uint32_t)Vtot;
+    c.nlist = 2ull * Vtot + 2;
+    c.numClauses = Ctot;
+    c.numLiterals = Ltot;
+    c.ncls = Ctot;
+    c.lits_used = Ltot;
+    // per-instance capacities of awaken (simplify.cu:83-98)
+    std::vector<unsigned long long> clsbase(n + 1), litbase(n + 1);
+    std::vector<uint64_t> acc(4 * (size_t)n);
+    std::vector<uint32_t> ucap(n), tcap(n);
+    std::vector<unsigned long long> ubase(n), tbase(n), sbase(n), scap(n);
+    uint64_t hdr_cap = 1, lits_cap = 64;
+    bool any_learnt = false, any_lbd = false, any_usage = false, any_assumed = false;
+    for (uint32_t i = 0; i < n; i++) {
+        const pfg_instance& q = in[i];
+        InstHost& h = c.ih[i];
+        const uint64_t L = q.num_clauses ? q.cls_off[q.num_clauses] : 0;
+        h.V = q.max_var;
+        h.voff = (uint32_t)voffs[i];
+        for (uint64_t k = 0; k < q.num_clauses; k++)
+            if (!(q.cls_learnt && q.cls_learnt[k])) { h.orig_cls++; h.orig_lits += q.cls_off[k + 1] - q.cls_off[k]; }
+        h.cls_in = h.numClauses = q.num_clauses;
+        h.lits_in = h.numLiterals = L;
+        clsbase[i + 1] = clsbase[i] + q.num_clauses;
+        litbase[i + 1] = litbase[i] + L;
+        uint64_t numCls = q.num_clauses, numLits = L;
+        if (c.o.phases) {
+            numCls += c.o.ve_en ? h.orig_cls : 0;
+            numLits += c.o.ve_en ? (uint64_t)((double)h.orig_lits * c.o.lits_mul) : 0;
+        }
+        acc[4 * i + 0] = q.num_clauses;
+        acc[4 * i + 1] = q.num_clauses * NBUCKETS + L;
+        acc[4 * i + 2] = numCls;
+        acc[4 * i + 3] = numCls * NBUCKETS + numLits;
+        hdr_cap += numCls;
+        lits_cap += acc[4 * i + 3] - NBUCKETS * q.num_clauses;
+        const uint64_t V1 = (uint64_t)q.max_var + 1;
+        ucap[i] = (uint32_t)std::min<uint64_t>(2 * V1 + 1024, 0xFFFFFFF0ull);
+        ubase[i] = c.units_total; c.units_total += ucap[i];
+        tcap[i] = (uint32_t)V1;
+        tbase[i] = c.trail_total; c.trail_total += tcap[i];
+        scap[i] = 2 * (numCls + numLits) + 1024;
+        sbase[i] = c.stack_total; c.stack_total += scap[i];
+        any_learnt |= q.cls_learnt != nullptr;
+        any_lbd |= q.cls_lbd != nullptr;
+        any_usage |= q.cls_usage != nullptr;
+        any_assumed |= q.assumed != nullptr;
+    }
+    c.hdr_cap = hdr_cap;
+    c.lits_cap = lits_cap;
+    if (c.lits_cap > 0xFFFFFFF0ull || c.hdr_cap > 0xFFFFFFF0ull || c.nlist > 0xFFFFFFF0ull) {
+        c.err = "instances exceed 2^32 literals";
+        return PFG_CNFALLOC_FAIL;
+    }
+    // per-instance blobs (device + pinned mirror)
+    c.in_bytes = inst_in_layout(n, nullptr, nullptr);
+    c.out_bytes = inst_out_layout(n, nullptr, nullptr);
+    if (cudaMallocHost(&c.in_blob_h, c.in_bytes) != cudaSuccess || cudaMallocHost(&c.out_blob_h, c.out_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        c.err = "pinned host allocation failed";
+        free_all(o);
+        return PFG_CNFALLOC_FAIL;
+    }
+    std::memset(c.in_blob_h, 0, c.in_bytes);
+    std::memset(c.out_blob_h, 0, c.out_bytes);
+    inst_in_layout(n, (char*)c.in_blob_h, &c.hi);
+    inst_out_layout(n, (char*)c.out_blob_h, &c.hout);
+    const uint64_t V1 = Vtot + 1;
+    void* din = nullptr;
+    void* dout = nullptr;
+    bool ok = cudaMallocAsync((void**)&c.dc, sizeof(DevCounters), c.s) == cudaSuccess;
+    if (ok) { o->sizes[c.dc] = sizeof(DevCounters); o->allocated += sizeof(DevCounters); }
+    ok = ok && dalloc(c, &din, c.in_bytes) && dalloc(c, &dout, c.out_bytes);
+    if (ok) {
+        inst_in_layout(n, (char*)din, &c.di);
+        inst_out_layout(n, (char*)dout, &c.dout);
+    }
+    ok = ok && dalloc_t(c, &c.hdr, c.hdr_cap) && dalloc_t(c, &c.lits, c.lits_cap) &&
+         dalloc_t(c, &c.hist, c.nlist) && dalloc_t(c, &c.ot_off, c.nlist + 1) &&
+         dalloc_t(c, &c.ot_size, c.nlist) && dalloc_t(c, &c.ot_fill, c.nlist) &&
+         dalloc_t(c, &c.big_lists, c.nlist) &&
+         dalloc_t(c, &c.elim, V1 + 8) && dalloc_t(c, &c.vstate, V1 + 8) && dalloc_t(c, &c.frozen, V1 + 8) &&
+         dalloc_t(c, &c.mstate, V1 + 8) && dalloc_t(c, &c.flag8, V1 + 8) && dalloc_t(c, &c.bstate, V1 + 8) &&
+         dalloc_t(c, &c.vorg, V1) && dalloc_t(c, &c.vinst, V1) && dalloc_t(c, &c.scores, V1) &&
+         dalloc_t(c, &c.keys_a, V1) && dalloc_t(c, &c.keys_b, V1) && dalloc_t(c, &c.eligible, V1) &&
+         dalloc_t(c, &c.eligible_b, V1) && dalloc_t(c, &c.rank, V1) && dalloc_t(c, &c.varcore, V1) &&
+         dalloc_t(c, &c.elected, V1) && dalloc_t(c, &c.veset, V1) && dalloc_t(c, &c.ereset, V1) &&
+         dalloc_t(c, &c.work, V1) && dalloc_t(c, &c.work_b, V1) && dalloc_t(c, &c.vscan, V1 + 1) &&
+         dalloc_t(c, &c.winv, V1 + 8) && dalloc_t(c, &c.type, V1) && dalloc_t(c, &c.ucnt, V1) &&
+         dalloc_t(c, &c.rpos, V1) && dalloc_t(c, &c.rref, V1) && dalloc_t(c, &c.rslot, V1 + 1) &&
+         dalloc_t(c, &c.rlit, V1 + 1) && dalloc_t(c, &c.units, c.units_total) &&
+         dalloc_t(c, &c.trail, c.trail_total) && dalloc_t(c, &c.stack, c.stack_total) &&
+         dalloc_t(c, &c.front_a, V1) && dalloc_t(c, &c.front_b, V1);
+    if (any_assumed) ok = ok && dalloc_t(c, &c.assumed, V1 + 8);
+    if (!ok) {
+        if (c.err.empty()) c.err = "device allocation failed";
+        free_all(o);
+        return PFG_CNFALLOC_FAIL;
+    }
+    // host-written instance inputs
+    for (uint32_t i = 0; i < n; i++) {
+        c.hi.voff[i] = c.ih[i].voff;
+        c.hi.ucap[i] = ucap[i]; c.hi.tcap[i] = tcap[i];
+        c.hi.ubase[i] = ubase[i]; c.hi.tbase[i] = tbase[i];
+        c.hi.sbase[i] = sbase[i]; c.hi.scap[i] = scap[i];
+        for (int k = 0; k < 4; k++) c.hi.acc[4 * i + k] = acc[4 * i + k];
+    }
+    c.hi.voff[n] = (uint32_t)Vtot;
+    push_inst_in(c);
+    cudaMemsetAsync(c.dout.conflict, 0, c.out_bytes, c.s);
+    // H2D: each instance's literals and offsets into its slice of the store
+    unsigned long long* d_off = nullptr;
+    unsigned long long* d_base = nullptr;   // clsbase (n+1) then litbase (n+1)
+    uint8_t* d_learnt = nullptr;
+    uint32_t* d_lbd = nullptr;
+    uint8_t* d_usage = nullptr;
+    ok = dalloc_t(c, &d_off, Ctot + 1) && dalloc_t(c, &d_base, 2 * ((size_t)n + 1));
+    if (ok && any_learnt) ok = dalloc_t(c, &d_learnt, Ctot + 1);
+    if (ok && any_lbd) ok = dalloc_t(c, &d_lbd, Ctot + 1);
+    if (ok && any_usage) ok = dalloc_t(c, &d_usage, Ctot + 1);
+    if (!ok) { free_all(o); return PFG_CNFALLOC_FAIL; }
+    if (any_learnt) cudaMemsetAsync(d_learnt, 0, Ctot + 1, c.s);
+    if (any_lbd) cudaMemsetAsync(d_lbd, 0, (Ctot + 1) * sizeof(uint32_t), c.s);
+    if (any_usage) cudaMemsetAsync(d_usage, 0, Ctot + 1, c.s);
+    {
+        std::vector<unsigned long long> bases(2 * ((size_t)n + 1));
+        for (uint32_t i = 0; i <= n; i++) { bases[i] = clsbase[i]; bases[n + 1 + i] = litbase[i]; }
+        cudaMemcpy(d_base, bases.data(), bases.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice);
+    }
+    cudaMemsetAsync(c.vstate, 0, V1, c.s);
+    if (any_assumed) cudaMemsetAsync(c.assumed, 0, V1, c.s);
+    PFG_LAUNCH(K_UPLOAD, vinst_k, grid_for(V1, 256), 256, 0, c.s, c.di.voff, n, c.V, c.vinst, c.vorg);
+    for (uint32_t i = 0; i < n; i++) {
+        const pfg_instance& q = in[i];
+        const uint64_t Ci = q.num_clauses, Li = litbase[i + 1] - litbase[i];
+        const uint32_t vo = c.ih[i].voff;
+        if (Li) cudaMemcpyAsync(c.lits + litbase[i], q.lits, Li * sizeof(uint32_t), cudaMemcpyHostToDevice, c.s);
+        if (Ci) cudaMemcpyAsync(d_off + clsbase[i], q.cls_off, Ci * sizeof(uint64_t), cudaMemcpyHostToDevice, c.s);
+        if (Ci && q.cls_learnt) cudaMemcpyAsync(d_learnt + clsbase[i], q.cls_learnt, Ci, cudaMemcpyHostToDevice, c.s);
+        if (Ci && q.cls_lbd) cudaMemcpyAsync(d_lbd + clsbase[i], q.cls_lbd, Ci * sizeof(uint32_t), cudaMemcpyHostToDevice, c.s);
+        if (Ci && q.cls_usage) cudaMemcpyAsync(d_usage + clsbase[i], q.cls_usage, Ci, cudaMemcpyHostToDevice, c.s);
+        if (q.var_state) cudaMemcpyAsync(c.vstate + vo + 1, q.var_state + 1, q.max_var, cudaMemcpyHostToDevice, c.s);
+        if (q.assumed) cudaMemcpyAsync(c.assumed + vo + 1, q.assumed + 1, q.max_var, cudaMemcpyHostToDevice, c.s);
+        if (q.vorg) cudaMemcpyAsync(c.vorg + vo + 1, q.vorg + 1, q.max_var * sizeof(uint32_t), cudaMemcpyHostToDevice, c.s);
+    }
+    if (Ctot) {
+        PFG_LAUNCH(K_UPLOAD, init_hdr_k, grid_for(Ctot, 256), 256, 0, c.s, c.hdr, d_off, Ctot, d_learnt, d_lbd, d_usage,
+                   d_base, d_base + n + 1, c.di.voff, n, c.lits);
+        PFG_LAUNCH(K_UPLOAD, prep_k, grid_for(Ctot, 128), 128, 0, c.s, c.hdr, c.lits, Ctot);
+    }
+    cudaMemsetAsync(c.elim, 0, V1, c.s);
+    cudaMemsetAsync(c.varcore, 0, V1 * sizeof(uint32_t), c.s);
+    cudaMemsetAsync(c.dc, 0, sizeof(DevCounters), c.s);
+    dfree(c, d_off); dfree(c, d_base); dfree(c, d_learnt); dfree(c, d_lbd); dfree(c, d_usage);
+    sync_counters(c);
+    c.launches += g_launches - base_launches;
+    g_prof = nullptr;
+    if (!c.err.empty()) return PFG_CUDA_ERROR;
+    c.uploaded = true;
+    c.simplified = false;
+    c.cache_ready = false;
+    c.stats = pfg_stats{};
+    c.stats.clauses_in = Ctot;
+    c.stats.literals_in = Ltot;
+    return PFG_OK;
+}
+
+// instances leaving the round loop keep the units of their last round unpropagated
+void retire(Ctx& c, const std::vector<uint32_t>& ids) {
+    bool need = false;
+    for (uint32_t i : ids) need |= c.ih[i].nUnits > 0;
+    if (need) pull_inst_out(c);
+    for (uint32_t i : ids) {
+        InstHost& h = c.ih[i];
+        h.active = false;
+        if (!h.nUnits) continue;
+        const uint64_t nu = std::min<uint64_t>(c.hout.ucount[i], c.hi.ucap[i]);
+        h.pending.resize(nu);
+        if (nu) cudaMemcpy(h.pending.data(), c.units + c.hi.ubase[i], nu * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        h.nUnits = 0;
+    }
+}
+
+std::vector<uint32_t> active_ids(const Ctx& c) {
+    std::vector<uint32_t> a;
+    for (uint32_t i = 0; i < c.ninst; i++) if (c.ih[i].active) a.push_back(i);
+    return a;
+}
+
+// elected variables of the instances in `want` mode, in order, into `out`
+uint32_t select_mode(Ctx& c, uint8_t want, uint32_t*& out) {
+    uint64_t total = 0;
+    bool exact = true;   // every elected variable belongs to an instance in `want` mode
+    for (uint32_t i = 0; i < c.ninst; i++) {
+        const InstHost& h = c.ih[i];
+        if (h.mode == want) total += h.nelected;
+        else if (h.nelected && h.mode != want) exact = false;
+    }
+    if (!total) return 0;
+    if (exact) {                        // the elected list is the set: swap buffers
+        std::swap(out, c.elected);
+        return c.nelected;
+    }
+    PFG_LAUNCH(K_MISC, mode_flags_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected, c.vinst, c.di.mode,
+               want, c.flag8);
+    if (!ensure_tmp(c, scan_temp_bytes(c.nelected + 1))) return 0;
+    select_flagged(c.elected, c.flag8, out, c.nelected, &c.dc->nwork, c.vscan, c.tmp, c.s);
+    return (uint32_t)total;
+}
 
 }  // namespace
 }  // namespace pfg
@@ -266,7 +643,7 @@ extern "C" int pfg_create(pfg_ctx** out, const pfg_options* opts, size_t arena_b
     Ctx& c = o->c;
     if (opts) c.o = *opts; else pfg_default_options(&c.o);
     pfg_resolve_options(&c.o);
-    if (c.o.bce_en || c.o.proof_en) { c.err = "BCE and proof emission are not supported"; }
+    if (c.o.bce_en || c.o.proof_en) { delete o; return PFG_INVALID; }   // BCE and proof emission are not built
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); delete o; return PFG_CUDA_ERROR; }
     c.device = dev;
@@ -278,19 +655,18 @@ extern "C" int pfg_create(pfg_ctx** out, const pfg_options* opts, size_t arena_b
         uint64_t thr = UINT64_MAX;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
-    if (cudaMallocHost((void**)&c.hc, sizeof(DevCounters)) != cudaSuccess) { cudaGetLastError(); delete o; return PFG_CUDA_ERROR; }
+    if (cudaMallocHost((void**)&c.hc, sizeof(DevCounters)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamDestroy(c.s);
+        delete o;
+        return PFG_CUDA_ERROR;
+    }
     std::memset(c.hc, 0, sizeof(DevCounters));
     if (arena_bytes == 0) {
         size_t fr = 0, tot = 0;
         if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > (256ull << 20)) o->budget = fr - (256ull << 20);
     } else {
         o->budget = arena_bytes;
-    }
-    if (c.o.bce_en || c.o.proof_en) {
-        cudaFreeHost(c.hc);
-        cudaStreamDestroy(c.s);
-        delete o;
-        return PFG_INVALID;
     }
     *out = o;
     return PFG_OK;
@@ -308,119 +684,29 @@ extern "C" int pfg_upload(pfg_ctx* o, uint32_t max_var, uint64_t num_clauses, co
                           const uint8_t* cls_usage, const uint8_t* var_state, const uint8_t* assumed,
                           const uint32_t* vorg) {
     if (!o) return PFG_INVALID;
-    Ctx& c = o->c;
-    c.err.clear();
-    if (max_var == 0 || max_var > 0x7FFFFFF0u || (num_clauses && (!lits || !cls_off))) { c.err = "invalid arguments"; return PFG_INVALID; }
-    // validate on the host: literal range, clause size >= 2, no duplicate or complementary literals
-    const uint64_t nlits = num_clauses ? cls_off[num_clauses] : 0;
-    if (num_clauses && cls_off[0] != 0) { c.err = "cls_off[0] must be 0"; return PFG_INVALID; }
-    {
-        std::vector<uint64_t> seen(max_var + 1, ~0ull);
-        for (uint64_t i = 0; i < num_clauses; i++) {
-            const uint64_t b = cls_off[i], e = cls_off[i + 1];
-            if (e < b + 2 || e > nlits) { c.err = "clause " + std::to_string(i) + " has fewer than 2 literals"; return PFG_INVALID; }
-            for (uint64_t k = b; k < e; k++) {
-                const uint32_t l = lits[k], v = l >> 1;
-                if (v == 0 || v > max_var) { c.err = "literal out of range in clause " + std::to_string(i); return PFG_INVALID; }
-                if (seen[v] == i) { c.err = "repeated variable in clause " + std::to_string(i); return PFG_INVALID; }
-                seen[v] = i;
-            }
-        }
-    }
-    const uint64_t base_launches = g_launches;
-    free_all(o);
-    g_prof = &c.prof;
-    c.V = max_var;
-    c.nlist = 2ull * max_var + 2;
-    uint64_t orgCls = 0, orgLits = 0;
-    for (uint64_t i = 0; i < num_clauses; i++) {
-        if (!(cls_learnt && cls_learnt[i])) { orgCls++; orgLits += cls_off[i + 1] - cls_off[i]; }
-    }
-    c.orig_cls = orgCls;
-    c.orig_lits = orgLits;
-    c.numClauses = num_clauses;
-    c.numLiterals = nlits;
-    c.ncls = num_clauses;
-    c.lits_used = nlits;
-    // capacities of awaken (simplify.cu:83-98)
-    uint64_t numCls = num_clauses, numLits = nlits;
-    if (c.o.phases) {
-        numCls += c.o.ve_en ? orgCls : 0;
-        numLits += c.o.ve_en ? (uint64_t)((double)orgLits * c.o.lits_mul) : 0;
-    }
-    c.cs_cap = numCls;
-    c.data_cap = numCls * NBUCKETS + numLits;
-    c.data_size = num_clauses * NBUCKETS + nlits;
-    c.hdr_cap = numCls + 1;
-    c.lits_cap = c.data_cap - NBUCKETS * num_clauses + 64;
-    if (c.lits_cap > 0xFFFFFFF0ull || c.nlist > 0xFFFFFFF0ull) { c.err = "instance exceeds 2^32 literals"; return PFG_CNFALLOC_FAIL; }
-    const uint64_t V1 = (uint64_t)max_var + 1;
-    c.units_cap = (uint32_t)std::min<uint64_t>(2 * V1 + 1024, 0xFFFFFFF0ull);
-    c.trail_cap = (uint32_t)V1;
-    c.stack_cap = 2 * (numCls + numLits) + 1024;
-    bool ok = cudaMallocAsync((void**)&c.dc, sizeof(DevCounters), c.s) == cudaSuccess;
-    if (ok) { o->sizes[c.dc] = sizeof(DevCounters); o->allocated += sizeof(DevCounters); }
-    ok = ok && dalloc_t(c, &c.hdr, c.hdr_cap) && dalloc_t(c, &c.lits, c.lits_cap) &&
-         dalloc_t(c, &c.hist, c.nlist) && dalloc_t(c, &c.ot_off, c.nlist + 1) &&
-         dalloc_t(c, &c.ot_size, c.nlist) && dalloc_t(c, &c.ot_fill, c.nlist) &&
-         dalloc_t(c, &c.big_lists, c.nlist) &&
-         dalloc_t(c, &c.elim, V1 + 8) && dalloc_t(c, &c.vstate, V1 + 8) && dalloc_t(c, &c.frozen, V1 + 8) &&
-         dalloc_t(c, &c.mstate, V1 + 8) && dalloc_t(c, &c.flag8, V1 + 8) && dalloc_t(c, &c.bstate, V1 + 8) &&
-         dalloc_t(c, &c.vorg, V1) && dalloc_t(c, &c.scores, V1) && dalloc_t(c, &c.keys_a, V1) &&
-         dalloc_t(c, &c.keys_b, V1) && dalloc_t(c, &c.eligible, V1) && dalloc_t(c, &c.eligible_b, V1) &&
-         dalloc_t(c, &c.rank, V1) && dalloc_t(c, &c.varcore, V1) && dalloc_t(c, &c.elected, V1) &&
-         dalloc_t(c, &c.work, V1) && dalloc_t(c, &c.work_b, V1) && dalloc_t(c, &c.vscan, V1 + 1) &&
-         dalloc_t(c, &c.winv, V1 + 8) &&
-         dalloc_t(c, &c.type, V1) && dalloc_t(c, &c.ucnt, V1) && dalloc_t(c, &c.rpos, V1) &&
-         dalloc_t(c, &c.rref, V1) && dalloc_t(c, &c.units, c.units_cap) && dalloc_t(c, &c.trail, c.trail_cap) &&
-         dalloc_t(c, &c.stack, c.stack_cap) && dalloc_t(c, &c.front_a, V1) && dalloc_t(c, &c.front_b, V1);
-    if (assumed) ok = ok && dalloc_t(c, &c.assumed, V1 + 8);
-    if (!ok) {
-        if (c.err.empty()) c.err = "device allocation failed";
-        free_all(o);
-        return PFG_CNFALLOC_FAIL;
-    }
-    // H2D: literals are already packed by cls_off
-    unsigned long long* d_off = nullptr;
-    uint8_t* d_learnt = nullptr;
-    uint32_t* d_lbd = nullptr;
-    uint8_t* d_usage = nullptr;
-    ok = dalloc_t(c, &d_off, num_clauses + 1);
-    if (ok && cls_learnt) ok = dalloc_t(c, &d_learnt, num_clauses + 1);
-    if (ok && cls_lbd) ok = dalloc_t(c, &d_lbd, num_clauses + 1);
-    if (ok && cls_usage) ok = dalloc_t(c, &d_usage, num_clauses + 1);
-    if (!ok) { free_all(o); return PFG_CNFALLOC_FAIL; }
-    cudaMemcpyAsync(c.lits, lits, nlits * sizeof(uint32_t), cudaMemcpyHostToDevice, c.s);
-    cudaMemcpyAsync(d_off, cls_off, (num_clauses + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, c.s);
-    if (cls_learnt) cudaMemcpyAsync(d_learnt, cls_learnt, num_clauses, cudaMemcpyHostToDevice, c.s);
-    if (cls_lbd) cudaMemcpyAsync(d_lbd, cls_lbd, num_clauses * sizeof(uint32_t), cudaMemcpyHostToDevice, c.s);
-    if (cls_usage) cudaMemcpyAsync(d_usage, cls_usage, num_clauses, cudaMemcpyHostToDevice, c.s);
-    if (num_clauses) {
-        PFG_LAUNCH(K_UPLOAD, init_hdr_k, grid_for(num_clauses, 256), 256, 0, c.s, c.hdr, d_off, num_clauses, d_learnt, d_lbd, d_usage);
-        PFG_LAUNCH(K_UPLOAD, prep_k, grid_for(num_clauses, 128), 128, 0, c.s, c.hdr, c.lits, num_clauses);
-    }
-    if (var_state) cudaMemcpyAsync(c.vstate, var_state, V1, cudaMemcpyHostToDevice, c.s);
-    else cudaMemsetAsync(c.vstate, 0, V1, c.s);
-    if (assumed) cudaMemcpyAsync(c.assumed, assumed, V1, cudaMemcpyHostToDevice, c.s);
-    if (vorg) cudaMemcpyAsync(c.vorg, vorg, V1 * sizeof(uint32_t), cudaMemcpyHostToDevice, c.s);
-    else { PFG_LAUNCH(K_UPLOAD, identity_k, grid_for(V1, 256), 256, 0, c.s, c.vorg, (uint32_t)V1); }
-    cudaMemsetAsync(c.elim, 0, V1, c.s);
-    cudaMemsetAsync(c.varcore, 0, V1 * sizeof(uint32_t), c.s);
-    cudaMemsetAsync(c.dc, 0, sizeof(DevCounters), c.s);
-    dfree(c, d_off); dfree(c, d_learnt); dfree(c, d_lbd); dfree(c, d_usage);
-    sync_counters(c);
-    c.launches += g_launches - base_launches;
-    g_prof = nullptr;
-    if (!c.err.empty()) return PFG_CUDA_ERROR;
-    c.uploaded = true;
-    c.simplified = false;
-    c.round_ends.clear();
-    c.nUnits = 0;
-    c.stats = pfg_stats{};
-    c.stats.clauses_in = num_clauses;
-    c.stats.literals_in = nlits;
-    return PFG_OK;
+    pfg_instance q;
+    std::memset(&q, 0, sizeof(q));
+    q.max_var = max_var;
+    q.num_clauses = num_clauses;
+    q.lits = lits;
+    q.cls_off = cls_off;
+    q.cls_learnt = cls_learnt;
+    q.cls_lbd = cls_lbd;
+    q.cls_usage = cls_usage;
+    q.var_state = var_state;
+    q.assumed = assumed;
+    q.vorg = vorg;
+    const int rc = upload_impl(o, 1, &q);
+    if (rc != PFG_OK && o->c.err.rfind("instance 0: ", 0) == 0) o->c.err = o->c.err.substr(12);
+    return rc;
 }
+
+extern "C" int pfg_batch_upload(pfg_ctx* o, uint32_t n, const pfg_instance* instances) {
+    if (!o) return PFG_INVALID;
+    return upload_impl(o, n, instances);
+}
+
+extern "C" uint32_t pfg_batch_size(pfg_ctx* o) { return (o && o->c.uploaded) ? o->c.ninst : 0; }
 
 static int finish(Ctx& c, pfg_stats* st, uint64_t base_launches, int rc) {
     if (c.prof.on) c.prof.resolve();
@@ -430,6 +716,11 @@ static int finish(Ctx& c, pfg_stats* st, uint64_t base_launches, int rc) {
     return rc;
 }
 
+// The round loop of Solver::simplifying (simplify.cu:159-186), run for every
+// instance at once. All instances still in the loop share the round counter
+// and the multiplier; everything else (stop rule, counts, units, accounting)
+// is per instance, and an instance leaves the loop exactly where a run of it
+// alone would break.
 extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
     if (!o) return PFG_INVALID;
     Ctx& c = o->c;
@@ -440,142 +731,262 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
     c.err.clear();
     for (double& x : c.pass_ms) x = 0;
     c.phase = c.multiplier = c.simpstate = 0;
-    c.status = PFG_UNKNOWN;
-    c.varcore_on = c.o.ve_fun_en != 0;
+    const uint32_t n = c.ninst;
     cudaEventRecord(c.ev_begin, c.s);
     uint64_t alg = 0;
     const bool disabled = !c.o.phases && !(c.o.all_en | c.o.ere_en);   // alldisabled (solver.hpp:722)
-    if (!disabled && c.orig_cls) {
-        int64_t cdiff = INT64_MAX, ldiff = INT64_MAX;
-        int64_t clsbefore = (int64_t)c.numClauses, litsbefore = (int64_t)c.numLiterals;
-        while (c.numClauses && c.numLiterals && !c.simpstate) {
-            const int times = c.phase + 1;
-            if (times > 1 && times != c.o.phases && c.o.shrink_rate > 0 && (times % c.o.shrink_rate) == 0) {
-                PassTimer t(c, 6);
-                if (!compact_cnf(c)) break;
+    std::vector<uint8_t> entered(n, 0);
+    for (uint32_t i = 0; i < n; i++) {
+        InstHost& h = c.ih[i];
+        h.status = PFG_UNKNOWN;
+        h.varcore_on = c.o.ve_fun_en != 0;
+        h.active = !disabled && h.orig_cls > 0;
+        entered[i] = h.active;
+        h.cdiff = h.ldiff = INT64_MAX;
+        h.clsbefore = (int64_t)h.numClauses;
+        h.litsbefore = (int64_t)h.numLiterals;
+    }
+    bool any_entered = false;
+    for (uint32_t i = 0; i < n; i++) any_entered |= entered[i] != 0;
+    while (true) {
+        // while (numClauses && numLiterals && !simpstate)
+        {
+            std::vector<uint32_t> out;
+            for (uint32_t i = 0; i < n; i++) {
+                const InstHost& h = c.ih[i];
+                if (h.active && (!h.numClauses || !h.numLiterals || c.simpstate)) out.push_back(i);
             }
-            {
-                PassTimer t(c, 0);
-                if (!ot_build(c)) break;
-            }
-            if (c.nUnits) {
-                PassTimer t(c, 1);
-                bool ok = true;
-                if (!bcp_prop(c, ok)) break;
-                if (!ok) { c.status = PFG_UNSAT; break; }
-                count_live(c);
-                sync_counters(c);
-                c.numClauses = c.hc->live_cls;
-                c.numLiterals = c.hc->live_lits;
-                if (!ot_build(c)) break;
-                cudaMemsetAsync(&c.dc->nunits, 0, sizeof(uint32_t), c.s);
-                c.nUnits = 0;
-            }
-            if (!c.numClauses) break;
-            {
-                PassTimer t(c, 2);
-                if (!c.o.lcve_fast && !ot_sort(c, true)) break;
-                if (!lcve(c)) break;
-            }
-            if (c.nelected < c.o.lcve_min_vars) break;
-            {
-                PassTimer t(c, 0);
-                if (!ot_sort(c, false)) break;
-            }
-            // stop() (solver.hpp:748-753)
-            if (c.phase == c.o.phases || (cdiff == 0 && ldiff == 0) ||
-                (c.phase > 2 && ldiff <= (int64_t)c.o.phase_lits_min)) {
-                if (c.o.ere_en && c.nelected) {
-                    cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
-                    PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected,
-                               c.hdr, c.ot_off, c.ot_size, c.ot_ids, &c.dc->live_cls);
-                    sync_counters(c);
-                    c.prof.bytes[K_ERE] += 4 * (c.hc->live_cls + c.hc->live_lits);
-                    PassTimer t(c, 5);
-                    ere_pass(c);
-                    c.stats.ere_ran = 1;
-                }
-                break;
-            }
-            // byte model: C_E, L_E of this round
-            cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
-            PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected, c.hdr, c.ot_off,
-                                                                         c.ot_size, c.ot_ids, &c.dc->live_cls);
-            sync_counters(c);
-            const uint64_t CE = c.hc->live_cls, LE = c.hc->live_lits;
-            const uint64_t Cin = c.numClauses, Lin = c.numLiterals;
-            c.prof.bytes[K_SUB] += 4 * (LE + CE);
-            c.prof.bytes[K_VE1] += 4 * (LE + CE);
-            const uint64_t ncls0 = c.ncls, lits0 = c.lits_used;
-            c.stats.clauses_processed += Cin;
-            c.stats.literals_processed += Lin;
-            if (c.o.sub_en || c.o.ve_plus_en) {
-                PassTimer t(c, 3);
-                sub_pass(c);
-            }
-            if (c.o.ve_en) {
-                PassTimer t(c, 4);
-                if (!ve_pass(c)) break;
-            }
-            {
-                PassTimer t(c, 6);
-                count_live(c);
-                sync_counters(c);
-            }
-            c.round_ends.push_back(c.hc->nstack);
-            c.numClauses = c.hc->live_cls;
-            c.numLiterals = c.hc->live_lits;
-            c.nUnits = c.hc->nunits;
-            const uint64_t Cres = c.ncls - ncls0, Lres = c.lits_used - lits0;
-            c.stats.resolvents += Cres;
-            c.prof.bytes[K_VE3] += 4 * (LE + CE) + 4 * (Lres + Cres);
-            alg += 4 * (Lin + Cin) + 8 * Lin + 8 * (LE + CE) + 4 * (Lres + Cres) + 4 * (c.numLiterals + c.numClauses);
-            cdiff = clsbefore - (int64_t)c.numClauses; clsbefore = (int64_t)c.numClauses;
-            ldiff = litsbefore - (int64_t)c.numLiterals; litsbefore = (int64_t)c.numLiterals;
-            c.phase++; c.multiplier++;
-            c.multiplier += (c.phase == c.o.phases);
-            if (!c.err.empty()) break;
+            retire(c, out);
         }
-        if (c.err.empty()) {   // ERE deletes after the last count (the write-back recounts, cnf.cu:211-224)
+        std::vector<uint32_t> act = active_ids(c);
+        if (act.empty() || !c.err.empty()) break;
+        const int times = c.phase + 1;
+        if (times > 1 && times != c.o.phases && c.o.shrink_rate > 0 && (times % c.o.shrink_rate) == 0) {
+            PassTimer t(c, 6);
+            if (!compact_cnf(c)) break;
+        }
+        {
+            PassTimer t(c, 0);
+            if (!ot_build(c)) break;
+        }
+        bool any_units = false;
+        for (uint32_t i = 0; i < n; i++) {
+            c.hi.bcp[i] = c.ih[i].active && c.ih[i].nUnits > 0;
+            any_units |= c.hi.bcp[i] != 0;
+        }
+        if (any_units) {
+            PassTimer t(c, 1);
+            push_inst_in(c);
+            if (!bcp_prop(c)) break;
             count_live(c);
-            sync_counters(c);
+            pull_inst_out(c);
+            if (!c.err.empty()) break;
             c.numClauses = c.hc->live_cls;
             c.numLiterals = c.hc->live_lits;
+            for (uint32_t i = 0; i < n; i++) {
+                InstHost& h = c.ih[i];
+                h.numClauses = c.hout.cnt[2 * i];
+                h.numLiterals = c.hout.cnt[2 * i + 1];
+                if (c.hi.bcp[i]) {
+                    h.nUnits = 0;
+                    if (c.hout.conflict[i]) { h.status = PFG_UNSAT; h.active = false; }
+                }
+            }
+            if (!ot_build(c)) break;
+            cudaMemsetAsync(c.dout.ucount, 0, n * sizeof(uint32_t), c.s);
         }
-        if (c.status != PFG_UNSAT && c.err.empty() && !c.numClauses) c.status = PFG_SAT;
+        for (uint32_t i = 0; i < n; i++)
+            if (c.ih[i].active && !c.ih[i].numClauses) c.ih[i].active = false;
+        act = active_ids(c);
+        if (act.empty()) break;
+        for (uint32_t i = 0; i < n; i++) {
+            c.hi.active[i] = c.ih[i].active;
+            c.hi.vc_on[i] = c.ih[i].active && c.ih[i].varcore_on;
+            c.ih[i].nelected = 0;
+            c.ih[i].mode = 0;
+        }
+        push_inst_in(c);
+        {
+            PassTimer t(c, 2);
+            if (!c.o.lcve_fast && !ot_sort(c, true)) break;
+            if (!lcve(c)) break;
+        }
+        for (uint32_t i : act)
+            if (c.ih[i].nelected < c.o.lcve_min_vars) c.ih[i].active = false;
+        act = active_ids(c);
+        if (act.empty()) break;
+        {
+            PassTimer t(c, 0);
+            if (!ot_sort(c, false)) break;
+        }
+        // stop() (solver.hpp:748-753) per instance: the last round runs ERE instead of SUB+BVE
+        uint32_t nmode1 = 0, nmode2 = 0;
+        for (uint32_t i : act) {
+            InstHost& h = c.ih[i];
+            const bool stop = c.phase == c.o.phases || (h.cdiff == 0 && h.ldiff == 0) ||
+                              (c.phase > 2 && h.ldiff <= (int64_t)c.o.phase_lits_min);
+            if (stop) {
+                h.active = false;
+                if (c.o.ere_en && h.nelected) { h.mode = 2; h.ere_ran = true; nmode2++; }
+            } else {
+                h.mode = 1;
+                nmode1++;
+            }
+        }
+        uint32_t acc_seg = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            c.hi.mode[i] = (uint8_t)c.ih[i].mode;
+            c.hi.vc_on[i] = c.ih[i].mode == 1 && c.ih[i].varcore_on;
+            c.hi.seg[i] = acc_seg;
+            if (c.ih[i].mode == 1) acc_seg += c.ih[i].nelected;
+        }
+        c.hi.seg[n] = acc_seg;
+        push_inst_in(c);
+        c.nere = nmode2 ? select_mode(c, 2, c.ereset) : 0;
+        if (c.nere) {
+            cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
+            PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nere, 256), 256, 0, c.s, c.ereset, c.nere, c.hdr,
+                       c.ot_off, c.ot_size, c.ot_ids, &c.dc->live_cls);
+            sync_counters(c);
+            c.prof.bytes[K_ERE] += 4 * (c.hc->live_cls + c.hc->live_lits);
+            PassTimer t(c, 5);
+            ere_pass(c);
+        }
+        if (!nmode1) break;
+        c.nve = select_mode(c, 1, c.veset);
+        // byte model: C_E, L_E of this round
+        cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
+        PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nve, 256), 256, 0, c.s, c.veset, c.nve, c.hdr, c.ot_off,
+                   c.ot_size, c.ot_ids, &c.dc->live_cls);
+        sync_counters(c);
+        const uint64_t CE = c.hc->live_cls, LE = c.hc->live_lits;
+        uint64_t Cin = 0, Lin = 0;
+        for (uint32_t i = 0; i < n; i++)
+            if (c.ih[i].mode == 1) {
+                Cin += c.ih[i].numClauses;
+                Lin += c.ih[i].numLiterals;
+                c.ih[i].processed_cls += c.ih[i].numClauses;
+                c.ih[i].processed_lits += c.ih[i].numLiterals;
+            }
+        c.prof.bytes[K_SUB] += 4 * (LE + CE);
+        c.prof.bytes[K_VE1] += 4 * (LE + CE);
+        const uint64_t ncls0 = c.ncls, lits0 = c.lits_used;
+        c.stats.clauses_processed += Cin;
+        c.stats.literals_processed += Lin;
+        if (c.o.sub_en || c.o.ve_plus_en) {
+            PassTimer t(c, 3);
+            sub_pass(c);
+        }
+        if (c.o.ve_en) {
+            PassTimer t(c, 4);
+            if (!ve_pass(c)) break;
+        }
+        {
+            PassTimer t(c, 6);
+            count_live(c);
+            pull_inst_out(c);
+        }
+        if (!c.err.empty()) break;
+        c.numClauses = c.hc->live_cls;
+        c.numLiterals = c.hc->live_lits;
+        for (uint32_t i = 0; i < n; i++) {
+            InstHost& h = c.ih[i];
+            h.numClauses = c.hout.cnt[2 * i];
+            h.numLiterals = c.hout.cnt[2 * i + 1];
+            if (h.mode != 1) continue;
+            h.round_ends.push_back(c.hout.scount[i]);
+            h.nUnits = c.hout.ucount[i];
+            h.cdiff = h.clsbefore - (int64_t)h.numClauses; h.clsbefore = (int64_t)h.numClauses;
+            h.ldiff = h.litsbefore - (int64_t)h.numLiterals; h.litsbefore = (int64_t)h.numLiterals;
+            h.rounds++;
+        }
+        const uint64_t Cres = c.ncls - ncls0, Lres = c.lits_used - lits0;
+        c.stats.resolvents += Cres;
+        c.prof.bytes[K_VE3] += 4 * (LE + CE) + 4 * (Lres + Cres);
+        alg += 4 * (Lin + Cin) + 8 * Lin + 8 * (LE + CE) + 4 * (Lres + Cres) + 4 * (c.numLiterals + c.numClauses);
+        c.phase++; c.multiplier++;
+        c.multiplier += (c.phase == c.o.phases);
+    }
+    retire(c, active_ids(c));
+    if (c.err.empty() && any_entered) {   // ERE deletes after the last count (the write-back recounts, cnf.cu:211-224)
+        count_live(c);
+        pull_inst_out(c);
+        c.numClauses = c.hc->live_cls;
+        c.numLiterals = c.hc->live_lits;
+        for (uint32_t i = 0; i < n; i++) {
+            InstHost& h = c.ih[i];
+            h.numClauses = c.hout.cnt[2 * i];
+            h.numLiterals = c.hout.cnt[2 * i + 1];
+            if (entered[i] && h.status != PFG_UNSAT && !h.numClauses) h.status = PFG_SAT;
+        }
     }
     cudaEventRecord(c.ev_end, c.s);
-    sync_counters(c);
+    pull_inst_out(c);
     float ms = 0;
     cudaEventElapsedTime(&ms, c.ev_begin, c.ev_end);
     c.simplified = true;
-    c.stats.status = c.status;
-    c.stats.rounds = c.phase;
+    // eliminated / forced counts per instance
+    std::vector<uint8_t> el(c.V + 1);
+    cudaMemcpy(el.data(), c.elim, c.V + 1, cudaMemcpyDeviceToHost);
+    uint64_t tot_e = 0, tot_f = 0, tot_stack = 0;
+    uint32_t max_rounds = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        InstHost& h = c.ih[i];
+        uint64_t ne = 0, nf = 0;
+        for (uint32_t v = h.voff + 1; v <= h.voff + h.V; v++) {
+            if (el[v] & FORCED_MASK) nf++;
+            else if (el[v]) ne++;
+        }
+        tot_e += ne; tot_f += nf;
+        tot_stack += c.hout.scount[i];
+        max_rounds = std::max(max_rounds, h.rounds);
+    }
+    c.stats.status = n == 1 ? c.ih[0].status : PFG_UNKNOWN;
+    c.stats.rounds = max_rounds;
+    c.stats.ere_ran = 0;
+    for (uint32_t i = 0; i < n; i++) c.stats.ere_ran |= c.ih[i].ere_ran ? 1 : 0;
     c.stats.simpstate = c.simpstate;
     c.stats.clauses_out = c.numClauses;
     c.stats.literals_out = c.numLiterals;
-    c.stats.stack_words = c.hc->nstack;
+    c.stats.stack_words = tot_stack;
     c.stats.device_ms = ms;
     for (int i = 0; i < 8; i++) c.stats.pass_ms[i] = c.pass_ms[i];
     c.stats.alg_bytes = alg;
     c.stats.kernel_launches = g_launches - base_launches;
-    // eliminated / forced counts are filled in by pfg_download's host copy; compute here cheaply
-    {
-        std::vector<uint8_t> el(c.V + 1);
-        cudaMemcpyAsync(el.data(), c.elim, c.V + 1, cudaMemcpyDeviceToHost, c.s);
-        cudaStreamSynchronize(c.s);
-        uint64_t ne = 0, nf = 0;
-        for (uint32_t v = 1; v <= c.V; v++) {
-            if (el[v] & FORCED_MASK) nf++;
-            else if (el[v]) ne++;
-        }
-        c.stats.eliminated = ne;
-        c.stats.forced = nf;
-    }
+    c.stats.eliminated = tot_e;
+    c.stats.forced = tot_f;
     int rc = PFG_OK;
     if (!c.err.empty()) rc = (c.simpstate == PFG_TIMEOUT) ? PFG_TIMEOUT : (c.simpstate ? c.simpstate : PFG_CUDA_ERROR);
     else if (c.simpstate) rc = c.simpstate;
     return finish(c, st, base_launches, rc);
+}
+
+extern "C" int pfg_batch_stats(pfg_ctx* o, uint32_t i, pfg_stats* st) {
+    if (!o || !st) return PFG_INVALID;
+    Ctx& c = o->c;
+    if (!c.simplified || i >= c.ninst) return PFG_INVALID;
+    const InstHost& h = c.ih[i];
+    pfg_stats s = c.stats;
+    s.status = h.status;
+    s.rounds = h.rounds;
+    s.ere_ran = h.ere_ran ? 1 : 0;
+    s.clauses_in = h.cls_in;
+    s.literals_in = h.lits_in;
+    s.clauses_out = h.numClauses;
+    s.literals_out = h.numLiterals;
+    s.clauses_processed = h.processed_cls;
+    s.literals_processed = h.processed_lits;
+    s.resolvents = h.resolvents;
+    s.stack_words = c.hout.scount[i];
+    std::vector<uint8_t> el(h.V);
+    cudaMemcpy(el.data(), c.elim + h.voff + 1, h.V, cudaMemcpyDeviceToHost);
+    s.eliminated = s.forced = 0;
+    for (uint8_t b : el) {
+        if (b & FORCED_MASK) s.forced++;
+        else if (b) s.eliminated++;
+    }
+    *st = s;
+    return PFG_OK;
 }
 
 extern "C" int pfg_result_sizes_get(pfg_ctx* o, pfg_result_sizes* r) {
@@ -583,26 +994,35 @@ extern "C" int pfg_result_sizes_get(pfg_ctx* o, pfg_result_sizes* r) {
     Ctx& c = o->c;
     if (!c.uploaded) return PFG_INVALID;
     std::memset(r, 0, sizeof(*r));
-    sync_counters(c);
+    pull_inst_out(c);
     r->clauses = c.numClauses;
     r->literals = c.numLiterals;
-    r->units = c.hc->ntrail;
-    r->pending_units = c.nUnits ? std::min<uint64_t>(c.hc->nunits, c.units_cap) : 0;
-    r->stack_words = c.hc->nstack;
-    r->rounds = c.round_ends.size();
+    uint64_t units = 0, pend = 0, words = 0, rounds = 0;
+    for (uint32_t i = 0; i < c.ninst; i++) {
+        units += c.hout.tcount[i];
+        pend += c.ih[i].pending.size();
+        words += c.hout.scount[i];
+        rounds = std::max<uint64_t>(rounds, c.ih[i].round_ends.size());
+    }
+    r->units = units;
+    r->pending_units = pend;
+    r->stack_words = words;
+    r->rounds = rounds;
     r->max_var = c.V;
     return PFG_OK;
 }
 
+// one-instance write-back straight into the caller's buffers
 extern "C" int pfg_download(pfg_ctx* o, uint32_t* lits, uint64_t* cls_off, uint8_t* cls_learnt, uint32_t* cls_lbd,
                             uint8_t* cls_usage, uint8_t* eliminated, uint32_t* units, uint32_t* pending_units,
                             uint32_t* stack, uint64_t* round_ends) {
     if (!o) return PFG_INVALID;
     Ctx& c = o->c;
     if (!c.uploaded) return PFG_INVALID;
+    if (c.ninst != 1) { c.err = "several instances uploaded: use pfg_batch_download"; return PFG_INVALID; }
     const uint64_t base_launches = g_launches;
     g_prof = &c.prof;
-    sync_counters(c);
+    pull_inst_out(c);
     const uint64_t n = c.ncls;
     if (lits || cls_off || cls_learnt || cls_lbd || cls_usage) {
         uint32_t* flag = nullptr;
@@ -632,16 +1052,169 @@ extern "C" int pfg_download(pfg_ctx* o, uint32_t* lits, uint64_t* cls_off, uint8
         if (cls_usage) cudaMemcpyAsync(cls_usage, ousage, C, cudaMemcpyDeviceToHost, c.s);
         dfree(c, flag); dfree(c, sz); dfree(c, olits); dfree(c, ooff); dfree(c, olearnt); dfree(c, olbd); dfree(c, ousage);
     }
+    const InstHost& h = c.ih[0];
+    const uint32_t ntrail = c.hout.tcount[0];
+    const uint64_t nstack = c.hout.scount[0];
     if (eliminated) cudaMemcpyAsync(eliminated, c.elim, c.V + 1, cudaMemcpyDeviceToHost, c.s);
-    if (units && c.hc->ntrail) cudaMemcpyAsync(units, c.trail, c.hc->ntrail * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    const uint64_t npend = c.nUnits ? std::min<uint64_t>(c.hc->nunits, c.units_cap) : 0;
-    if (pending_units && npend) cudaMemcpyAsync(pending_units, c.units, npend * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    if (stack && c.hc->nstack) cudaMemcpyAsync(stack, c.stack, c.hc->nstack * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (units && ntrail) cudaMemcpyAsync(units, c.trail, ntrail * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (stack && nstack) cudaMemcpyAsync(stack, c.stack, nstack * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     if (!cuda_ok(c, cudaStreamSynchronize(c.s), "download")) return finish(c, nullptr, base_launches, PFG_CUDA_ERROR);
-    if (units && c.hc->ntrail) std::sort(units, units + c.hc->ntrail);
-    if (pending_units && npend) std::sort(pending_units, pending_units + npend);
-    if (round_ends) for (size_t i = 0; i < c.round_ends.size(); i++) round_ends[i] = c.round_ends[i];
+    if (units && ntrail) std::sort(units, units + ntrail);
+    if (pending_units && !h.pending.empty()) {
+        std::copy(h.pending.begin(), h.pending.end(), pending_units);
+        std::sort(pending_units, pending_units + h.pending.size());
+    }
+    if (round_ends) std::copy(h.round_ends.begin(), h.round_ends.end(), round_ends);
     return finish(c, nullptr, base_launches, PFG_OK);
+}
+
+namespace pfg {
+namespace {
+
+// Gathers every instance's results to the host once: live clauses grouped by
+// instance (clause order kept) with literals back in the instance's numbering,
+// the eliminated bytes, the trail and the model-stack regions.
+int build_cache(Ctx& c) {
+    if (c.cache_ready) return PFG_OK;
+    const uint32_t n = c.ninst;
+    pull_inst_out(c);
+    const uint64_t N = c.ncls;
+    uint64_t C = 0;
+    for (uint32_t i = 0; i < n; i++) C += c.ih[i].numClauses;
+    uint32_t *k0 = nullptr, *v0 = nullptr, *k1 = nullptr, *v1 = nullptr, *olits = nullptr, *olbd = nullptr;
+    unsigned long long* loff = nullptr;
+    uint8_t *olearnt = nullptr, *ousage = nullptr;
+    bool ok = dalloc_t(c, &k0, N + 1) && dalloc_t(c, &v0, N + 1) && dalloc_t(c, &k1, N + 1) &&
+              dalloc_t(c, &v1, N + 1) && dalloc_t(c, &loff, C + 1) && dalloc_t(c, &olits, c.numLiterals + 1) &&
+              dalloc_t(c, &olbd, C + 1) && dalloc_t(c, &olearnt, C + 1) && dalloc_t(c, &ousage, C + 1) &&
+              ensure_tmp(c, std::max(radix_temp_bytes(N + 1), scan_temp_bytes(C + 1)));
+    auto release = [&]() {
+        dfree(c, k0); dfree(c, v0); dfree(c, k1); dfree(c, v1); dfree(c, loff); dfree(c, olits);
+        dfree(c, olbd); dfree(c, olearnt); dfree(c, ousage);
+    };
+    if (!ok) { release(); return PFG_CNFALLOC_FAIL; }
+    uint32_t* ids = v0;
+    if (N) {
+        int bits = 0;
+        while (bits < 32 && (n >> bits)) bits += 8;
+        PFG_LAUNCH(K_DOWNLOAD, cls_inst_keys_k, grid_for(N, 256), 256, 0, c.s, c.hdr, c.lits, N, c.vinst, n, k0, v0);
+        const int which = radix_sort_pairs(k0, v0, k1, v1, N, 0, bits, c.tmp, c.s);
+        ids = which ? v1 : v0;
+    }
+    if (C) {
+        PFG_LAUNCH(K_DOWNLOAD, gathered_sizes_k, grid_for(C, 256), 256, 0, c.s, c.hdr, ids, C, loff);
+        exclusive_scan_u64(loff, loff, C, 0ull, loff + C, c.tmp, c.s);
+        PFG_LAUNCH(K_DOWNLOAD, gathered_pack_k, grid_for(C * 32, 256), 256, 0, c.s, c.hdr, c.lits, ids, C, loff,
+                   c.vinst, c.di.voff, olits, olearnt, olbd, ousage);
+    } else {
+        cudaMemsetAsync(loff, 0, sizeof(unsigned long long), c.s);
+    }
+    c.cache_off.resize(C + 1);
+    c.cache_lits.resize(c.numLiterals);
+    c.cache_learnt.resize(C);
+    c.cache_lbd.resize(C);
+    c.cache_usage.resize(C);
+    c.cache_elim.resize((size_t)c.V + 1);
+    c.cache_trail.resize(c.trail_total);
+    cudaMemcpyAsync(c.cache_off.data(), loff, (C + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, c.s);
+    if (c.numLiterals) cudaMemcpyAsync(c.cache_lits.data(), olits, c.numLiterals * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (C) {
+        cudaMemcpyAsync(c.cache_learnt.data(), olearnt, C, cudaMemcpyDeviceToHost, c.s);
+        cudaMemcpyAsync(c.cache_lbd.data(), olbd, C * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+        cudaMemcpyAsync(c.cache_usage.data(), ousage, C, cudaMemcpyDeviceToHost, c.s);
+    }
+    cudaMemcpyAsync(c.cache_elim.data(), c.elim, (size_t)c.V + 1, cudaMemcpyDeviceToHost, c.s);
+    cudaMemcpyAsync(c.cache_trail.data(), c.trail, c.trail_total * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    // stack regions, packed back to back on the host
+    uint64_t words = 0;
+    for (uint32_t i = 0; i < n; i++) words += c.hout.scount[i];
+    c.cache_stack.resize(words);
+    uint64_t at = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const uint64_t w = c.hout.scount[i];
+        if (w) cudaMemcpyAsync(c.cache_stack.data() + at, c.stack + c.hi.sbase[i], w * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+        at += w;
+    }
+    const bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "batch download");
+    release();
+    if (!synced) return PFG_CUDA_ERROR;
+    c.cache_cls_base.assign((size_t)n + 1, 0);
+    for (uint32_t i = 0; i < n; i++) c.cache_cls_base[i + 1] = c.cache_cls_base[i] + c.ih[i].numClauses;
+    c.cache_ready = true;
+    return PFG_OK;
+}
+
+uint64_t stack_offset(const Ctx& c, uint32_t i) {
+    uint64_t at = 0;
+    for (uint32_t j = 0; j < i; j++) at += c.hout.scount[j];
+    return at;
+}
+
+}  // namespace
+}  // namespace pfg
+
+extern "C" int pfg_batch_result_sizes(pfg_ctx* o, uint32_t i, pfg_result_sizes* r) {
+    if (!o || !r) return PFG_INVALID;
+    Ctx& c = o->c;
+    if (!c.uploaded || i >= c.ninst) return PFG_INVALID;
+    const uint64_t base_launches = g_launches;
+    g_prof = &c.prof;
+    const int rc = build_cache(c);
+    finish(c, nullptr, base_launches, rc);
+    if (rc != PFG_OK) return rc;
+    const InstHost& h = c.ih[i];
+    std::memset(r, 0, sizeof(*r));
+    const uint64_t b = c.cache_cls_base[i], e = c.cache_cls_base[i + 1];
+    r->clauses = e - b;
+    r->literals = c.cache_off[e] - c.cache_off[b];
+    r->units = std::min<uint64_t>(c.hout.tcount[i], c.hi.tcap[i]);
+    r->pending_units = h.pending.size();
+    r->stack_words = c.hout.scount[i];
+    r->rounds = h.round_ends.size();
+    r->max_var = h.V;
+    return PFG_OK;
+}
+
+extern "C" int pfg_batch_download(pfg_ctx* o, uint32_t i, uint32_t* lits, uint64_t* cls_off, uint8_t* cls_learnt,
+                                  uint32_t* cls_lbd, uint8_t* cls_usage, uint8_t* eliminated, uint32_t* units,
+                                  uint32_t* pending_units, uint32_t* stack, uint64_t* round_ends) {
+    if (!o) return PFG_INVALID;
+    Ctx& c = o->c;
+    if (!c.uploaded || i >= c.ninst) return PFG_INVALID;
+    const uint64_t base_launches = g_launches;
+    g_prof = &c.prof;
+    const int rc = build_cache(c);
+    finish(c, nullptr, base_launches, rc);
+    if (rc != PFG_OK) return rc;
+    const InstHost& h = c.ih[i];
+    const uint64_t b = c.cache_cls_base[i], e = c.cache_cls_base[i + 1];
+    const uint64_t lb = c.cache_off[b], le = c.cache_off[e];
+    if (lits) std::copy(c.cache_lits.begin() + lb, c.cache_lits.begin() + le, lits);
+    if (cls_off) for (uint64_t k = b; k <= e; k++) cls_off[k - b] = c.cache_off[k] - lb;
+    if (cls_learnt) std::copy(c.cache_learnt.begin() + b, c.cache_learnt.begin() + e, cls_learnt);
+    if (cls_lbd) std::copy(c.cache_lbd.begin() + b, c.cache_lbd.begin() + e, cls_lbd);
+    if (cls_usage) std::copy(c.cache_usage.begin() + b, c.cache_usage.begin() + e, cls_usage);
+    if (eliminated) {
+        eliminated[0] = 0;
+        std::copy(c.cache_elim.begin() + h.voff + 1, c.cache_elim.begin() + h.voff + 1 + h.V, eliminated + 1);
+    }
+    const uint64_t nt = std::min<uint64_t>(c.hout.tcount[i], c.hi.tcap[i]);
+    if (units && nt) {
+        // trail literals back to the instance's numbering
+        const uint32_t* t = c.cache_trail.data() + c.hi.tbase[i];
+        for (uint64_t k = 0; k < nt; k++) units[k] = t[k] - 2u * h.voff;
+        std::sort(units, units + nt);
+    }
+    if (pending_units && !h.pending.empty()) {
+        for (size_t k = 0; k < h.pending.size(); k++) pending_units[k] = h.pending[k] - 2u * h.voff;
+        std::sort(pending_units, pending_units + h.pending.size());
+    }
+    if (stack && c.hout.scount[i]) {
+        const uint64_t at = stack_offset(c, i);
+        std::copy(c.cache_stack.begin() + at, c.cache_stack.begin() + at + c.hout.scount[i], stack);
+    }
+    if (round_ends) std::copy(h.round_ends.begin(), h.round_ends.end(), round_ends);
+    return PFG_OK;
 }
 
 extern "C" int pfg_profile_enable(pfg_ctx* o, int on) {
@@ -678,6 +1251,8 @@ extern "C" void pfg_destroy(pfg_ctx* o) {
     if (c.ev_a) cudaEventDestroy(c.ev_a);
     if (c.ev_b) cudaEventDestroy(c.ev_b);
     if (c.hc) cudaFreeHost(c.hc);
+    if (c.in_blob_h) cudaFreeHost(c.in_blob_h);
+    if (c.out_blob_h) cudaFreeHost(c.out_blob_h);
     c.prof.destroy();
     cudaGetLastError();
     delete o;

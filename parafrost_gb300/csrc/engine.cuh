@@ -1,10 +1,17 @@
 // Engine context and pass launchers (host side).
 //
-// One context = one device-resident CNF instance on one GPU stream. The
-// round driver in engine.cu mirrors Solver::simplifying
-// (src/gpu/simplify.cu:136-241); each pass lives in its own translation unit.
+// One context holds n >= 1 independent CNF instances in one device clause
+// store on one GPU stream. Instance i owns the global variables
+// voff[i]+1 .. voff[i+1] (its local variable v is global voff[i] + v), so the
+// instances share no clause and every pass runs once over all of them. All
+// state the reference keeps per Solver (round counter, stop-rule differences,
+// arena accounting, units, trail, model stack) is kept per instance, so each
+// instance's result is the one a run of that instance alone gives. The round
+// driver in engine.cu mirrors Solver::simplifying (src/gpu/simplify.cu:136-241);
+// each pass lives in its own translation unit.
 #pragma once
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -13,6 +20,61 @@
 #include "prims.cuh"
 
 namespace pfg {
+
+// Host-side state of one instance (the reference's per-Solver simplifier state).
+struct InstHost {
+    uint32_t V = 0;                 // variables of the instance
+    uint32_t voff = 0;              // global variable = local variable + voff
+    uint64_t orig_cls = 0, orig_lits = 0;       // original (non-learnt) clauses at upload
+    uint64_t cls_in = 0, lits_in = 0;
+    uint64_t numClauses = 0, numLiterals = 0;   // live clauses / literals
+    int status = PFG_UNKNOWN;
+    bool active = false;            // still in the round loop
+    bool varcore_on = false;        // function-table gates enabled (vars->varcore != NULL)
+    bool ere_ran = false;
+    int mode = 0;                   // this round: 0 idle, 1 SUB+BVE, 2 ERE
+    int64_t cdiff = 0, ldiff = 0, clsbefore = 0, litsbefore = 0;
+    uint64_t nUnits = 0;            // units produced by its last round, not yet propagated
+    uint32_t rounds = 0;
+    uint32_t nelected = 0;
+    uint64_t processed_cls = 0, processed_lits = 0, resolvents = 0;
+    std::vector<uint32_t> pending;  // units left unpropagated when it stopped
+    std::vector<uint64_t> round_ends;
+};
+
+// Per-instance kernel inputs, written by the host (one allocation, mirrored in
+// pinned host memory with the same layout).
+struct InstIn {
+    uint32_t* voff = nullptr;              // n+1
+    uint32_t* seg = nullptr;               // n+1: first index of each instance in the BVE set
+    uint32_t* ucap = nullptr;              // n: unit region capacity
+    uint32_t* tcap = nullptr;              // n: trail region capacity
+    unsigned long long* ubase = nullptr;   // n
+    unsigned long long* tbase = nullptr;   // n
+    unsigned long long* sbase = nullptr;   // n: model-stack region
+    unsigned long long* scap = nullptr;    // n
+    unsigned long long* acc = nullptr;     // 4n: reference accounting vncls, vdata, cs_cap, data_cap
+    uint8_t* active = nullptr;             // n: its variables may be elected this round
+    uint8_t* vc_on = nullptr;              // n: function-table gates on
+    uint8_t* bcp = nullptr;                // n: propagates its units this round
+    uint8_t* mode = nullptr;               // n: 1 SUB+BVE, 2 ERE this round
+};
+
+// Per-instance kernel outputs, written by the device.
+struct InstOut {
+    uint32_t* conflict = nullptr;          // n
+    uint32_t* ucount = nullptr;            // n: units in its region
+    uint32_t* tcount = nullptr;            // n: trail length
+    uint32_t* nelect = nullptr;            // n: elected variables
+    uint32_t* nfrozen = nullptr;           // n
+    uint32_t* fbase = nullptr;             // n+1: frozen-scan value at the instance's first variable
+    unsigned long long* scount = nullptr;  // n: model-stack words
+    unsigned long long* cnt = nullptr;     // 2n: live clauses, live literals
+    unsigned long long* add = nullptr;     // 2n: clauses, literals added by the last BVE
+};
+
+size_t inst_in_layout(uint32_t n, char* base, InstIn* p);    // returns bytes; base may be null
+size_t inst_out_layout(uint32_t n, char* base, InstOut* p);
 
 struct Ctx {
     pfg_options o{};
@@ -24,7 +86,17 @@ struct Ctx {
     bool uploaded = false;
     bool simplified = false;
 
-    // instance
+    // instances (the single-instance API is n = 1)
+    uint32_t ninst = 0;
+    std::vector<InstHost> ih;
+    InstIn di, hi;                  // device / pinned host mirror
+    InstOut dout, hout;
+    void* in_blob_h = nullptr; void* out_blob_h = nullptr;
+    size_t in_bytes = 0, out_bytes = 0;
+    uint32_t* vinst = nullptr;      // V+1: instance of a global variable
+    int phase = 0, multiplier = 0;  // shared by every instance still in the loop
+
+    // union of all instances
     uint32_t V = 0;
     uint64_t nlist = 0;  // 2V + 2 literal lists
 
@@ -32,11 +104,9 @@ struct Ctx {
     ClsHdr* hdr = nullptr;
     uint32_t* lits = nullptr;
     uint64_t hdr_cap = 0, lits_cap = 0;
-    uint64_t ncls = 0;                 // clauses in the array (cnf->size())
+    uint64_t ncls = 0;                 // clauses in the array (deleted ones included)
     uint64_t lits_used = 0;            // packed literal words in use
-    uint64_t data_size = 0, data_cap = 0, cs_cap = 0;  // reference bucket accounting
-    uint64_t orig_cls = 0, orig_lits = 0;
-    uint64_t numClauses = 0, numLiterals = 0;
+    uint64_t numClauses = 0, numLiterals = 0;   // live totals over all instances
 
     // occurrence table (CSR)
     uint32_t* hist = nullptr;    // nlist
@@ -60,7 +130,7 @@ struct Ctx {
     uint8_t* frozen = nullptr;   // V+1
     uint8_t* mstate = nullptr;   // V+1
     uint8_t* flag8 = nullptr;    // V+1 scratch flags
-    uint32_t* vorg = nullptr;    // V+1
+    uint32_t* vorg = nullptr;    // V+1: original (instance-local) variable
     uint32_t* scores = nullptr;  // V+1
     uint32_t* keys_a = nullptr;  // V+1 sort keys
     uint32_t* keys_b = nullptr;
@@ -72,24 +142,26 @@ struct Ctx {
     uint32_t* work = nullptr;    // V+1 MIS worklist
     uint32_t* work_b = nullptr;  // V+1
     uint32_t* vscan = nullptr;   // V+2 scan scratch
-    uint8_t* winv = nullptr;     // V+1 MIS round winners
+    uint8_t* winv = nullptr;     // V+1 MIS round winners / BVE slot-fits flags
     uint4* ckeys = nullptr;      // per-clause sort key (size, first, last, sig)
     uint64_t ckeys_cap = 0;
     uint32_t nelected = 0;
-    bool varcore_on = false;
 
-    // BVE per elected index
+    // BVE per index of the SUB+BVE set
     uint32_t* type = nullptr;
     uint32_t* ucnt = nullptr;
-    unsigned long long* rpos = nullptr;
-    unsigned long long* rref = nullptr;
+    unsigned long long* rpos = nullptr;   // clauses added (scan)
+    unsigned long long* rref = nullptr;   // buckets added (scan)
+    unsigned long long* rslot = nullptr;  // physical first clause slot
+    unsigned long long* rlit = nullptr;   // physical first literal word
+    uint32_t* veset = nullptr;            // SUB+BVE set (elected of instances in mode 1)
+    uint32_t* ereset = nullptr;           // ERE set (elected of instances in mode 2)
+    uint32_t nve = 0, nere = 0;
 
-    // units, trail and model stack
-    uint32_t* units = nullptr; uint32_t units_cap = 0;
-    uint32_t* trail = nullptr; uint32_t trail_cap = 0;
-    uint32_t* stack = nullptr; uint64_t stack_cap = 0;
-    std::vector<uint64_t> round_ends;
-    uint64_t nUnits = 0;
+    // units, trail and model stack (one region per instance)
+    uint32_t* units = nullptr; uint64_t units_total = 0;
+    uint32_t* trail = nullptr; uint64_t trail_total = 0;
+    uint32_t* stack = nullptr; uint64_t stack_total = 0;
 
     // BCP
     uint8_t* bstate = nullptr;
@@ -108,10 +180,20 @@ struct Ctx {
     Profiler prof;
 
     // round state
-    int phase = 0, multiplier = 0, simpstate = 0, status = PFG_UNKNOWN;
+    int simpstate = 0;
     uint32_t mis_rounds = 0;
     pfg_stats stats{};
     double pass_ms[8] = {0};
+
+    // batch download cache (built on the first per-instance download)
+    bool cache_ready = false;
+    std::vector<uint32_t> cache_lits;
+    std::vector<uint64_t> cache_off;            // global offsets into cache_lits
+    std::vector<uint8_t> cache_learnt, cache_usage;
+    std::vector<uint32_t> cache_lbd;
+    std::vector<uint64_t> cache_cls_base;       // n+1: first clause of each instance
+    std::vector<uint8_t> cache_elim;
+    std::vector<uint32_t> cache_trail, cache_stack;
 };
 
 // ---- memory helpers (engine.cu) ----
@@ -122,6 +204,8 @@ inline bool dalloc_t(Ctx& c, T** p, size_t count) { return dalloc(c, (void**)p, 
 bool ensure_tmp(Ctx& c, size_t bytes);
 bool ensure_tmp_u32(Ctx& c, uint64_t count);
 void sync_counters(Ctx& c);     // D2H copy of counters + stream sync
+void push_inst_in(Ctx& c);      // H2D copy of the per-instance inputs
+void pull_inst_out(Ctx& c);     // D2H copy of the per-instance outputs and counters + sync
 bool cuda_ok(Ctx& c, cudaError_t e, const char* what);
 
 // ---- passes ----
@@ -129,15 +213,25 @@ bool cuda_ok(Ctx& c, cudaError_t e, const char* what);
 bool ot_build(Ctx& c);          // histogram + CSR offsets + unsorted fill (clause order irrelevant)
 bool ot_sort(Ctx& c, bool by_id);  // sort every list by OLIST_CMP (key.cuh:67-85) or by clause id
 // counting + compaction (gc.cu)
-void count_live(Ctx& c);        // counters live_cls/live_lits (needs sync to read)
+void count_live(Ctx& c);        // totals into counters, per instance into dout.cnt (read after a sync)
 bool compact_cnf(Ctx& c);       // Solver::reallocCNF(true) (cnf.cu:129-144, recycle.cu:60)
-// device BCP (bcp.cu): returns false on conflict
-bool bcp_prop(Ctx& c, bool& ok);
-// LCVE (lcve.cu): returns number elected
+// device BCP (bcp.cu) of the instances flagged in di.bcp; conflicts land in dout.conflict
+bool bcp_prop(Ctx& c);
+// LCVE (lcve.cu) over the active instances; per-instance counts in dout.nelect
 bool lcve(Ctx& c);
-// SUB, BVE, ERE (elim.cu)
+// SUB, BVE, ERE (elim.cu) over c.veset / c.ereset
 void sub_pass(Ctx& c);
 bool ve_pass(Ctx& c);
 void ere_pass(Ctx& c);
+
+// device helper: instance of a global variable (binary search over voff[0..n])
+PFG_D uint32_t inst_search(const uint32_t* voff, uint32_t n, uint32_t v) {
+    uint32_t lo = 0, hi = n;   // largest i < n with voff[i] < v
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (voff[mid] < v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
 
 }  // namespace pfg

@@ -2,18 +2,33 @@
 //
 // Replaces cnt_cls_lits + the host block reduction (count.cu:83-131,171) and
 // cuMM::compactCNF (recycle.cu:34-103): live clauses are kept in order,
-// packed into freshly sized arrays, and the reference's bucket accounting is
-// reset to 3 * clauses + literals (recycle.cu:71).
+// packed into freshly sized arrays, and the reference's bucket accounting of
+// every instance still in the round loop is reset to 3 * clauses + literals
+// (recycle.cu:71) with the capacities of reallocCNF (cnf.cu:129-139).
 #include "engine.cuh"
 
 namespace pfg {
 namespace {
 
-__global__ void count_k(const ClsHdr* __restrict__ hdr, uint64_t ncls, DevCounters* dc) {
+// totals; with several instances also per instance (the instance of a clause
+// is the instance of its literals), summed per warp over equal instances
+__global__ void count_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
+                        const uint32_t* __restrict__ vinst, int multi, unsigned long long* icnt, DevCounters* dc) {
     unsigned long long nc = 0, nl = 0;
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         const ClsHdr h = hdr[c];
-        if (!m_deleted(h.meta)) { nc++; nl += h.size; }
+        const bool live = !m_deleted(h.meta);
+        if (live) { nc++; nl += h.size; }
+        if (multi) {
+            const uint32_t inst = live ? vinst[ABSV(lits[h.off])] : 0xFFFFFFFFu;
+            const unsigned peers = __match_any_sync(__activemask(), inst);
+            const unsigned a = __reduce_add_sync(peers, live ? 1u : 0u);
+            const unsigned b = __reduce_add_sync(peers, live ? h.size : 0u);
+            if (inst != 0xFFFFFFFFu && (int)(threadIdx.x & 31u) == __ffs(peers) - 1) {
+                atomicAdd(&icnt[2 * inst], (unsigned long long)a);
+                atomicAdd(&icnt[2 * inst + 1], (unsigned long long)b);
+            }
+        }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -54,21 +69,40 @@ __global__ void compact_k(const ClsHdr* __restrict__ hdr, const uint32_t* __rest
 
 void count_live(Ctx& c) {
     cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
+    const int multi = c.ninst > 1;
+    if (multi) cudaMemsetAsync(c.dout.cnt, 0, 2 * c.ninst * sizeof(unsigned long long), c.s);
     c.prof.bytes[K_COUNT] += 8 * c.ncls;
-    if (c.ncls) {
-        PFG_LAUNCH(K_COUNT, count_k, grid_for(c.ncls, 256, 8), 256, 0, c.s, c.hdr, c.ncls, c.dc);
-    }
+    if (c.ncls)
+        PFG_LAUNCH(K_COUNT, count_k, grid_for(c.ncls, 256, 8), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.vinst, multi,
+                   c.dout.cnt, c.dc);
+    if (!multi)
+        cudaMemcpyAsync(c.dout.cnt, &c.dc->live_cls, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c.s);
 }
 
 bool compact_cnf(Ctx& c) {
-    // capacities of the new store (cnf.cu:129-139)
-    const uint64_t addCls = c.o.ve_en ? c.numClauses : 0;
-    const uint64_t addLits = c.o.ve_en ? (uint64_t)((double)c.orig_lits * c.o.lits_mul) : 0;
-    const uint64_t clsCap = c.numClauses + addCls, litsCap = c.numLiterals + addLits;
-    const uint64_t data_cap = clsCap * NBUCKETS + litsCap;
-    // physical literal words: data_cap minus the header buckets of the clauses kept
-    const uint64_t phys_lits = data_cap - NBUCKETS * c.numClauses + 64;
-    if (phys_lits > 0xFFFFFFF0ull) { c.simpstate = PFG_CNFALLOC_FAIL; c.err = "clause store exceeds 2^32 literals"; return false; }
+    // capacities of reallocCNF (cnf.cu:129-139) for every instance still in the
+    // loop; stopped instances only keep their live clauses
+    uint64_t clsCap = 0, litsCap = 0;
+    for (uint32_t i = 0; i < c.ninst; i++) {
+        InstHost& h = c.ih[i];
+        const uint64_t addCls = (h.active && c.o.ve_en) ? h.numClauses : 0;
+        const uint64_t addLits = (h.active && c.o.ve_en) ? (uint64_t)((double)h.orig_lits * c.o.lits_mul) : 0;
+        clsCap += h.numClauses + addCls;
+        litsCap += h.numLiterals + NBUCKETS * addCls + addLits;   // data_cap - 3 * live clauses
+        if (h.active) {
+            unsigned long long* acc = c.hi.acc + 4 * i;
+            acc[0] = h.numClauses;
+            acc[1] = h.numClauses * NBUCKETS + h.numLiterals;
+            acc[2] = h.numClauses + addCls;
+            acc[3] = acc[2] * NBUCKETS + h.numLiterals + addLits;
+        }
+    }
+    const uint64_t phys_lits = litsCap + 64;
+    if (phys_lits > 0xFFFFFFF0ull || clsCap > 0xFFFFFFF0ull) {
+        c.simpstate = PFG_CNFALLOC_FAIL;
+        c.err = "clause store exceeds 2^32 entries";
+        return false;
+    }
     ClsHdr* nhdr = nullptr;
     uint32_t* nlits = nullptr;
     if (!dalloc_t(c, &nhdr, clsCap + 1) || !dalloc_t(c, &nlits, phys_lits)) {
@@ -96,9 +130,7 @@ bool compact_cnf(Ctx& c) {
     c.hdr_cap = clsCap + 1; c.lits_cap = phys_lits;
     c.ncls = c.numClauses;
     c.lits_used = c.numLiterals;
-    c.cs_cap = clsCap;
-    c.data_cap = data_cap;
-    c.data_size = c.numClauses * NBUCKETS + c.numLiterals;
+    push_inst_in(c);
     return cuda_ok(c, cudaGetLastError(), "compact_cnf");
 }
 

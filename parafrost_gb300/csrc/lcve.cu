@@ -8,8 +8,12 @@
 //     (round, rank) order -- one legal order of the reference's atomic appends;
 //   - frozen variables get their function-table index from a scan in
 //     ascending variable order (mis_collect_k + mapfrozen_k :211-260).
-// The sequential lcve_k (:63-98, option lcvefast=0) runs on one thread, as in
-// the reference, over occurrence lists sorted by clause id.
+// The sequential lcve_k (:63-98, option lcvefast=0) runs on one thread per
+// instance, as in the reference, over occurrence lists sorted by clause id.
+// With several instances the global (score, var) order restricted to one
+// instance is that instance's own order, neighbours never cross instances, and
+// the elected list is grouped by instance, so every instance elects exactly
+// what it elects alone.
 #include "engine.cuh"
 
 namespace pfg {
@@ -44,12 +48,13 @@ PFG_D bool oversize(const ClsHdr* hdr, const uint32_t* ot_off, const uint32_t* o
 __global__ void mis_init_k(const uint32_t* eligible, uint32_t V, uint32_t* rank, uint8_t* mstate,
                            const uint8_t* vstate, const uint8_t* assumed, const uint32_t* hist,
                            const ClsHdr* hdr, const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids,
-                           uint32_t pmax, uint32_t nmax, uint32_t maxoccurs, int maxcsize, uint8_t* cand) {
+                           uint32_t pmax, uint32_t nmax, uint32_t maxoccurs, int maxcsize, uint8_t* cand,
+                           const uint32_t* vinst, const uint8_t* active) {
     for (uint32_t ei = blockIdx.x * blockDim.x + threadIdx.x; ei < V; ei += gridDim.x * blockDim.x) {
         const uint32_t v = eligible[ei];
         rank[v] = ei;
         uint8_t st = MIS_NONE;
-        if (!vstate[v] && !(assumed && assumed[v])) {
+        if (active[vinst[v]] && !vstate[v] && !(assumed && assumed[v])) {
             const uint32_t p = 2 * v, n = p | 1;
             const uint32_t ps = hist[p], ns = hist[n];
             if ((ps || ns) && ps <= maxoccurs && ns <= maxoccurs && !(ps >= pmax && ns >= nmax) &&
@@ -136,63 +141,101 @@ __global__ void frozen_u32_k(const uint8_t* frozen, uint32_t V, uint32_t* out) {
         out[v] = (v >= 1 && frozen[v]) ? 1u : 0u;
 }
 
-__global__ void varcore_k(const uint8_t* frozen, uint32_t V, const uint32_t* pos, uint32_t* varcore) {
-    for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x)
-        if (frozen[v]) varcore[v] = pos[v];
+// fbase[i] = frozen variables before instance i (fbase[n] = all of them)
+__global__ void frozen_base_k(const uint32_t* pos, const uint32_t* voff, uint32_t ninst, uint32_t* fbase) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= ninst; i += gridDim.x * blockDim.x)
+        fbase[i] = pos[voff[i] + 1];
 }
 
-// sequential lcve_k (lcve.cu:63-98) on one thread
-__global__ void lcve_seq_k(const uint32_t* eligible, uint32_t V, uint32_t* elected, uint32_t* flist,
-                           uint8_t* frozen, const uint8_t* vstate, const uint8_t* assumed, const uint32_t* hist,
-                           const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
-                           const uint32_t* ot_ids, uint32_t pmax, uint32_t nmax, uint32_t maxoccurs, int maxcsize,
-                           DevCounters* dc) {
-    uint32_t tail = 0, ne = 0;
-    for (uint32_t ei = 0; ei < V; ei++) {
-        const uint32_t cand = eligible[ei];
-        if (frozen[cand]) continue;
-        if (vstate[cand]) continue;
-        if (assumed && assumed[cand]) continue;
-        const uint32_t p = 2 * cand, n = p | 1;
-        const uint32_t ps = hist[p], ns = hist[n];
-        if (!ps && !ns) continue;
-        if (ps > maxoccurs || ns > maxoccurs) break;
-        if (ps >= pmax && ns >= nmax) break;
-        bool okp = true;
-        for (int side = 0; side < 2 && okp; side++) {
-            const uint32_t lit = side ? n : p;
-            const uint32_t saved = tail;
-            const uint32_t o = ot_off[lit], sz = ot_size[lit];
-            for (uint32_t i = 0; i < sz; i++) {
-                const ClsHdr h = hdr[ot_ids[o + i]];
-                if (m_deleted(h.meta)) continue;
-                if ((int)h.size > maxcsize) {
-                    for (uint32_t q = saved; q < tail; q++) frozen[flist[q]] = 0;
-                    tail = saved;
-                    okp = false;
-                    break;
+// function-table index of a frozen variable: its rank among its instance's frozen variables
+__global__ void varcore_k(const uint8_t* frozen, uint32_t V, const uint32_t* pos, const uint32_t* vinst,
+                          const uint32_t* fbase, uint32_t* varcore) {
+    for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x)
+        if (frozen[v]) varcore[v] = pos[v] - fbase[vinst[v]];
+}
+
+// per-instance counts of a variable list (warp-aggregated over equal instances)
+__global__ void inst_count_k(const uint32_t* list, uint32_t n, const uint32_t* vinst, uint32_t* cnt) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t inst = vinst[list[i]];
+        const unsigned peers = __match_any_sync(__activemask(), inst);
+        if ((int)(threadIdx.x & 31u) == __ffs(peers) - 1) atomicAdd(&cnt[inst], (uint32_t)__popc(peers));
+    }
+}
+
+__global__ void inst_keys_k(const uint32_t* list, uint32_t n, const uint32_t* vinst, const uint32_t* mround,
+                            int rbits, uint32_t* keys) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t v = list[i];
+        keys[i] = (vinst[v] << rbits) | (mround ? mround[v] : 0u);
+    }
+}
+
+// sequential lcve_k (lcve.cu:63-98): one thread per instance walks the
+// instance's segment [voff[i], voff[i+1]) of the eligible order
+__global__ void lcve_seq_k(const uint32_t* eligible, const uint32_t* voff, const uint8_t* active, uint32_t ninst,
+                           uint8_t* eflag, uint32_t* flist, uint8_t* frozen, const uint8_t* vstate,
+                           const uint8_t* assumed, const uint32_t* hist, const ClsHdr* hdr, const uint32_t* lits,
+                           const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids, uint32_t pmax,
+                           uint32_t nmax, uint32_t maxoccurs, int maxcsize, uint32_t* nelect, uint32_t* nfrozen) {
+    for (uint32_t inst = blockIdx.x * blockDim.x + threadIdx.x; inst < ninst; inst += gridDim.x * blockDim.x) {
+        const uint32_t b = voff[inst], e = voff[inst + 1];
+        uint32_t tail = b, ne = 0;
+        if (active[inst]) {
+            for (uint32_t ei = b; ei < e; ei++) {
+                const uint32_t cand = eligible[ei];
+                if (frozen[cand]) continue;
+                if (vstate[cand]) continue;
+                if (assumed && assumed[cand]) continue;
+                const uint32_t p = 2 * cand, n = p | 1;
+                const uint32_t ps = hist[p], ns = hist[n];
+                if (!ps && !ns) continue;
+                if (ps > maxoccurs || ns > maxoccurs) break;
+                if (ps >= pmax && ns >= nmax) break;
+                bool okp = true;
+                for (int side = 0; side < 2 && okp; side++) {
+                    const uint32_t lit = side ? n : p;
+                    const uint32_t saved = tail;
+                    const uint32_t o = ot_off[lit], sz = ot_size[lit];
+                    for (uint32_t i = 0; i < sz; i++) {
+                        const ClsHdr h = hdr[ot_ids[o + i]];
+                        if (m_deleted(h.meta)) continue;
+                        if ((int)h.size > maxcsize) {
+                            for (uint32_t q = saved; q < tail; q++) frozen[flist[q]] = 0;
+                            tail = saved;
+                            okp = false;
+                            break;
+                        }
+                        for (uint32_t k = 0; k < h.size; k++) {
+                            const uint32_t u = ABSV(lits[h.off + k]);
+                            if (!frozen[u] && u != cand) { frozen[u] = 1; flist[tail++] = u; }
+                        }
+                    }
                 }
-                for (uint32_t k = 0; k < h.size; k++) {
-                    const uint32_t u = ABSV(lits[h.off + k]);
-                    if (!frozen[u] && u != cand) { frozen[u] = 1; flist[tail++] = u; }
-                }
+                if (okp) { eflag[ei] = 1; ne++; }
             }
         }
-        if (okp) elected[ne++] = cand;
+        nelect[inst] = ne;
+        nfrozen[inst] = tail - b;
     }
-    dc->nelected = ne;
-    dc->nfrozen = tail;
 }
 
-__global__ void mapfrozen_k(const uint32_t* flist, uint32_t n, uint32_t* varcore) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        varcore[flist[i]] = i;
+// varcore[flist[j]] = j within each instance's frozen list (mapfrozen_k, lcve.cu:253)
+__global__ void mapfrozen_k(const uint32_t* flist, uint32_t V, const uint32_t* voff, const uint32_t* vinst,
+                            const uint32_t* nfrozen, uint32_t* varcore) {
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < V; idx += gridDim.x * blockDim.x) {
+        const uint32_t inst = vinst[idx + 1];
+        const uint32_t j = idx - voff[inst];
+        if (j < nfrozen[inst]) varcore[flist[idx]] = j;
+    }
 }
 
 }  // namespace
 
+
 bool lcve(Ctx& c) {
     const uint32_t V = c.V;
+    const uint32_t ninst = c.ninst;
     // scores and the (score, var) order
     cudaMemsetAsync(&c.dc->nfrozen, 0, sizeof(uint32_t), c.s);
     PFG_LAUNCH(K_LCVE, scores_k, grid_for(V, 256), 256, 0, c.s, c.hist, V, c.scores, c.keys_a, c.eligible, c.dc);
@@ -200,24 +243,28 @@ bool lcve(Ctx& c) {
     const uint32_t maxscore = c.hc->nfrozen;
     int bits = 0;
     while (bits < 32 && (maxscore >> bits)) bits += 8;
-    if (!ensure_tmp(c, radix_temp_bytes(V))) return false;
+    if (!ensure_tmp(c, std::max(radix_temp_bytes(V), scan_temp_bytes(V + 1)))) return false;
     if (bits) {
         const int which = radix_sort_pairs(c.keys_a, c.eligible, c.keys_b, c.eligible_b, V, 0, bits, c.tmp, c.s);
         if (which) cudaMemcpyAsync(c.eligible, c.eligible_b, V * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
     }
+    int ibits = 0;
+    while (ibits < 32 && ((ninst - 1) >> ibits)) ibits += 8;
     const uint32_t maxoccurs = c.o.lcve_max_occurs;
     const uint32_t pmax = c.o.mu_pos << c.multiplier;
     const uint32_t nmax = c.o.mu_neg << c.multiplier;
     const int maxcsize = c.o.lcve_clause_max;
+    bool any_vc = false;
+    for (uint32_t i = 0; i < ninst; i++) any_vc |= c.ih[i].active && c.ih[i].varcore_on;
     cudaMemsetAsync(c.frozen, 0, V + 1, c.s);
+    cudaMemsetAsync(c.dout.nelect, 0, ninst * sizeof(uint32_t), c.s);
+    cudaMemsetAsync(c.dout.nfrozen, 0, ninst * sizeof(uint32_t), c.s);
     c.nelected = 0;
     c.mis_rounds = 0;
-    uint32_t nfrozen = 0;
     if (c.o.lcve_fast) {
-        PFG_LAUNCH(K_LCVE, mis_init_k, grid_for(V, 256), 256, 0, c.s, c.eligible, V, c.rank, c.mstate, c.vstate, c.assumed, c.hist,
-                                                      c.hdr, c.ot_off, c.ot_size, c.ot_ids, pmax, nmax, maxoccurs,
-                                                      maxcsize, c.flag8);
-        if (!ensure_tmp(c, scan_temp_bytes(V + 1))) return false;
+        PFG_LAUNCH(K_LCVE, mis_init_k, grid_for(V, 256), 256, 0, c.s, c.eligible, V, c.rank, c.mstate, c.vstate,
+                   c.assumed, c.hist, c.hdr, c.ot_off, c.ot_size, c.ot_ids, pmax, nmax, maxoccurs, maxcsize, c.flag8,
+                   c.vinst, c.di.active);
         select_flagged(c.eligible, c.flag8, c.work, V, &c.dc->nwork, c.vscan, c.tmp, c.s);
         sync_counters(c);
         const uint32_t nwork = c.hc->nwork;
@@ -240,7 +287,8 @@ bool lcve(Ctx& c) {
             else if (r > nwork + 2) { c.err = "MIS did not converge"; c.simpstate = PFG_TIMEOUT; return false; }
         }
         c.mis_rounds = r;
-        // elected in (round, rank) order: select in rank order, then stable sort by round
+        // elected in (instance, round, rank) order: select in rank order, then a
+        // stable sort by (instance, round)
         PFG_LAUNCH(K_LCVE, elected_flags_k, grid_for(nwork, 256), 256, 0, c.s, c.work, nwork, c.mstate, c.flag8);
         select_flagged(c.work, c.flag8, c.elected, nwork, &c.dc->nelected, c.vscan, c.tmp, c.s);
         sync_counters(c);
@@ -248,35 +296,68 @@ bool lcve(Ctx& c) {
         if (c.nelected > 1) {
             int rbits = 0;
             while (rbits < 32 && (r >> rbits)) rbits += 8;
-            PFG_LAUNCH(K_LCVE, round_keys_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected, mround,
-                       c.keys_a);
             if (!ensure_tmp(c, radix_temp_bytes(c.nelected))) return false;
-            const int which = radix_sort_pairs(c.keys_a, c.elected, c.keys_b, c.work_b, c.nelected, 0, rbits, c.tmp, c.s);
+            const bool fused = ninst > 1 && rbits + ibits <= 32;
+            if (fused)
+                PFG_LAUNCH(K_LCVE, inst_keys_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected, c.vinst,
+                           mround, rbits, c.keys_a);
+            else
+                PFG_LAUNCH(K_LCVE, round_keys_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected, mround,
+                           c.keys_a);
+            int which = radix_sort_pairs(c.keys_a, c.elected, c.keys_b, c.work_b, c.nelected, 0,
+                                         fused ? rbits + ibits : rbits, c.tmp, c.s);
             if (which) cudaMemcpyAsync(c.elected, c.work_b, c.nelected * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+            if (ninst > 1 && !fused) {
+                PFG_LAUNCH(K_LCVE, inst_keys_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected, c.vinst,
+                           (const uint32_t*)nullptr, 0, c.keys_a);
+                which = radix_sort_pairs(c.keys_a, c.elected, c.keys_b, c.work_b, c.nelected, 0, ibits, c.tmp, c.s);
+                if (which) cudaMemcpyAsync(c.elected, c.work_b, c.nelected * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+            }
         }
-
-        if (c.varcore_on) {
+        if (ninst > 1) {
+            if (c.nelected)
+                PFG_LAUNCH(K_LCVE, inst_count_k, grid_for(c.nelected, 256), 256, 0, c.s, c.elected, c.nelected, c.vinst,
+                           c.dout.nelect);
+        } else {
+            cudaMemcpyAsync(c.dout.nelect, &c.dc->nelected, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+        }
+        if (any_vc) {
             PFG_LAUNCH(K_LCVE, frozen_u32_k, grid_for(V + 1, 256), 256, 0, c.s, c.frozen, V, c.vscan);
-            exclusive_scan_u32(c.vscan, c.vscan, V + 1, 0u, &c.dc->nfrozen, c.tmp, c.s);
-            PFG_LAUNCH(K_LCVE, varcore_k, grid_for(V, 256), 256, 0, c.s, c.frozen, V, c.vscan, c.varcore);
-            sync_counters(c);
-            nfrozen = c.hc->nfrozen;
+            exclusive_scan_u32(c.vscan, c.vscan, V + 1, 0u, c.vscan + V + 1, c.tmp, c.s);
+            PFG_LAUNCH(K_LCVE, frozen_base_k, grid_for(ninst + 1, 256), 256, 0, c.s, c.vscan, c.di.voff, ninst,
+                       c.dout.fbase);
+            PFG_LAUNCH(K_LCVE, varcore_k, grid_for(V, 256), 256, 0, c.s, c.frozen, V, c.vscan, c.vinst, c.dout.fbase,
+                       c.varcore);
         }
     } else {
-        // flist in keys_b
-        PFG_LAUNCH(K_LCVE, lcve_seq_k, 1, 1, 0, c.s, c.eligible, V, c.elected, c.keys_b, c.frozen, c.vstate, c.assumed, c.hist,
-                                     c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids, pmax, nmax, maxoccurs, maxcsize,
-                                     c.dc);
-        sync_counters(c);
-        c.nelected = c.hc->nelected;
-        nfrozen = c.hc->nfrozen;
-        if (c.varcore_on && nfrozen) {
-            PFG_LAUNCH(K_LCVE, mapfrozen_k, grid_for(nfrozen, 256), 256, 0, c.s, c.keys_b, nfrozen, c.varcore);
+        // eligible grouped by instance (stable), so instance i owns positions [voff[i], voff[i+1])
+        if (ninst > 1) {
+            PFG_LAUNCH(K_LCVE, inst_keys_k, grid_for(V, 256), 256, 0, c.s, c.eligible, V, c.vinst,
+                       (const uint32_t*)nullptr, 0, c.keys_a);
+            const int which = radix_sort_pairs(c.keys_a, c.eligible, c.keys_b, c.eligible_b, V, 0, ibits, c.tmp, c.s);
+            if (which) cudaMemcpyAsync(c.eligible, c.eligible_b, V * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
         }
+        // per-instance frozen lists in keys_b at the instance's offset
+        cudaMemsetAsync(c.flag8, 0, V + 1, c.s);
+        PFG_LAUNCH(K_LCVE, lcve_seq_k, grid_for(ninst, 32), 32, 0, c.s, c.eligible, c.di.voff, c.di.active, ninst,
+                   c.flag8, c.keys_b, c.frozen, c.vstate, c.assumed, c.hist, c.hdr, c.lits, c.ot_off, c.ot_size,
+                   c.ot_ids, pmax, nmax, maxoccurs, maxcsize, c.dout.nelect, c.dout.nfrozen);
+        select_flagged(c.eligible, c.flag8, c.elected, V, &c.dc->nelected, c.vscan, c.tmp, c.s);
+        if (any_vc)
+            PFG_LAUNCH(K_LCVE, mapfrozen_k, grid_for(V, 256), 256, 0, c.s, c.keys_b, V, c.di.voff, c.vinst,
+                       c.dout.nfrozen, c.varcore);
     }
-    if (c.varcore_on && !nfrozen) c.varcore_on = false;   // vars->varcore = NULL (lcve.cu:403)
-    if (!cuda_ok(c, cudaGetLastError(), "lcve")) return false;
-    return true;
+    pull_inst_out(c);
+    if (!c.err.empty()) return false;
+    c.nelected = c.hc->nelected;
+    for (uint32_t i = 0; i < ninst; i++) {
+        InstHost& h = c.ih[i];
+        if (!h.active) continue;
+        h.nelected = c.hout.nelect[i];
+        const uint32_t nf = c.o.lcve_fast ? (any_vc ? c.hout.fbase[i + 1] - c.hout.fbase[i] : 0u) : c.hout.nfrozen[i];
+        if (h.varcore_on && !nf) h.varcore_on = false;   // vars->varcore = NULL (lcve.cu:403)
+    }
+    return cuda_ok(c, cudaGetLastError(), "lcve");
 }
 
 }  // namespace pfg

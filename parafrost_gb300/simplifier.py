@@ -48,7 +48,8 @@ class SimplifyResult:
 
 
 class Simplifier:
-    """One device-resident instance at a time (a `pfg_ctx`)."""
+    """One device context (a `pfg_ctx`): one instance, or a batch of instances
+    simplified together with per-instance results."""
 
     def __init__(self, arena_bytes: int = 0, **options):
         self.lib = _lib.lib()
@@ -113,6 +114,67 @@ class Simplifier:
         self.run()
         return self.download()
 
+    # ---- batches: n instances simplified together, results per instance ----
+
+    def upload_batch(self, cnfs, var_states=None, assumeds=None, vorgs=None) -> None:
+        n = len(cnfs)
+        arr = (_abi.PfgInstance * max(n, 1))()
+        keep = []   # the arrays must outlive the call
+
+        def opt(seq, i, dtype):
+            if seq is None or seq[i] is None:
+                return None
+            a = np.ascontiguousarray(seq[i], dtype=dtype)
+            keep.append(a)
+            return a
+
+        for i, cnf in enumerate(cnfs):
+            q = arr[i]
+            q.max_var = cnf.max_var
+            q.num_clauses = cnf.num_clauses
+            q.lits = _ptr(cnf.lits, C.c_uint32)
+            q.cls_off = _ptr(cnf.off, C.c_uint64)
+            q.cls_learnt = _ptr(cnf.learnt, C.c_uint8)
+            q.cls_lbd = _ptr(cnf.lbd, C.c_uint32)
+            q.cls_usage = _ptr(cnf.usage, C.c_uint8)
+            q.var_state = _ptr(opt(var_states, i, np.uint8), C.c_uint8)
+            q.assumed = _ptr(opt(assumeds, i, np.uint8), C.c_uint8)
+            q.vorg = _ptr(opt(vorgs, i, np.uint32), C.c_uint32)
+        self._check(self.lib.pfg_batch_upload(self._ctx, n, arr), "pfg_batch_upload")
+
+    def batch_size(self) -> int:
+        return int(self.lib.pfg_batch_size(self._ctx))
+
+    def download_instance(self, i: int) -> SimplifyResult:
+        sz = _abi.PfgResultSizes()
+        self._check(self.lib.pfg_batch_result_sizes(self._ctx, i, C.byref(sz)), "pfg_batch_result_sizes")
+        lits = np.empty(sz.literals, dtype=np.uint32)
+        off = np.empty(sz.clauses + 1, dtype=np.uint64)
+        learnt = np.empty(sz.clauses, dtype=np.uint8)
+        lbd = np.empty(sz.clauses, dtype=np.uint32)
+        usage = np.empty(sz.clauses, dtype=np.uint8)
+        elim = np.empty(sz.max_var + 1, dtype=np.uint8)
+        units = np.empty(sz.units, dtype=np.uint32)
+        pend = np.empty(sz.pending_units, dtype=np.uint32)
+        stack = np.empty(sz.stack_words, dtype=np.uint32)
+        rends = np.empty(sz.rounds, dtype=np.uint64)
+        rc = self.lib.pfg_batch_download(self._ctx, i, _ptr(lits, C.c_uint32), _ptr(off, C.c_uint64),
+                                         _ptr(learnt, C.c_uint8), _ptr(lbd, C.c_uint32), _ptr(usage, C.c_uint8),
+                                         _ptr(elim, C.c_uint8), _ptr(units, C.c_uint32), _ptr(pend, C.c_uint32),
+                                         _ptr(stack, C.c_uint32), _ptr(rends, C.c_uint64))
+        self._check(rc, "pfg_batch_download")
+        st = _abi.PfgStats()
+        self._check(self.lib.pfg_batch_stats(self._ctx, i, C.byref(st)), "pfg_batch_stats")
+        stats = {f[0]: getattr(st, f[0]) for f in _abi.PfgStats._fields_ if f[0] != "pass_ms"}
+        return SimplifyResult(int(st.status), Cnf(sz.max_var, lits, off, learnt, lbd, usage), elim, units, pend,
+                              stack, rends, stats)
+
+    def simplify_batch(self, cnfs, var_states=None, assumeds=None, vorgs=None) -> list:
+        """Simplify every CNF of `cnfs` in one device store; one result per instance."""
+        self.upload_batch(cnfs, var_states, assumeds, vorgs)
+        self.run()
+        return [self.download_instance(i) for i in range(len(cnfs))]
+
     def profile(self, on: bool = True) -> None:
         """Per-kernel CUDA-event timing of the following simplify calls."""
         self.lib.pfg_profile_enable(self._ctx, 1 if on else 0)
@@ -155,3 +217,8 @@ class Simplifier:
 def simplify(cnf: Cnf, **options) -> SimplifyResult:
     with Simplifier(**options) as s:
         return s.simplify(cnf)
+
+
+def simplify_batch(cnfs, **options) -> list:
+    with Simplifier(**options) as s:
+        return s.simplify_batch(cnfs)
