@@ -2,17 +2,22 @@
 """Benchmark of the GPU simplify path: inprocessing clauses/s (SUB + BVE rounds).
 
 One step = one full `Solver::simplify`-equivalent call (all rounds until the
-reference's stop rule) on one seeded synthetic instance. The metric counts,
-per step, the live clauses entering every SUB+BVE round (sum of C_in).
+reference's stop rule). The metric counts, per step, the live clauses entering
+every SUB+BVE round (sum of C_in over rounds and instances).
 
-  value : clauses/s with the instance resident in HBM when timing starts
+Workloads: `batched` (the default) simplifies 512 seeded instances of uneven
+size (log-uniform 1k..200k variables; random 3-SAT, Tseitin and scale-free
+generators) in one batch per step, and times the plain path -- the same
+instances one per simplify call -- beside it. `tseitin`, `ksat` and
+`scalefree` run one instance per step.
+
+  value : clauses/s with the input resident in HBM when timing starts
           (CUDA events around the engine's rounds on its own stream);
   e2e   : the same metric through the C ABI with host buffers: upload (H2D),
           simplify and download (D2H) inside the timed region.
 
 `--impl reference` times the CPU restatement of the same passes (the oracle
-port; the reference's GPU simplifier cannot run here) on all host cores, one
-independent replica per core.
+port; the reference's GPU simplifier cannot run here) on all host cores.
 """
 import argparse
 import json
@@ -41,6 +46,13 @@ WORKLOADS = {
                            "geometric lengths on [2,50] mean 4, planted model"),
 }
 
+# configs[3]: 512 instances per batch, sizes log-uniform on [1e3, 2e5] variables,
+# generator per instance uniform over {3-SAT (ratio 4.26), Tseitin, scale-free
+# (ratio 4.0, planted)}, per-instance seeds
+BATCH = dict(n=512, vmin=1_000, vmax=200_000, seed=7,
+             desc="512 instances per batch, log-uniform 1k..200k vars each, generator per instance uniform over "
+                  "random 3-SAT (4.26 clauses/var), Tseitin (5% inputs) and scale-free (4 clauses/var, planted)")
+
 METRIC = "inprocessing clauses/s (BVE+SUB)"
 UNIT = "clauses/s"
 
@@ -57,6 +69,31 @@ def load_peaks():
 def make_cnf(w):
     import parafrost_gb300 as pg
     return pg.generate(w["family"], w["a"], w["b"], w["c"], w["seed"])
+
+
+def batch_specs(rank=0):
+    """(family, a, b, c, seed) of every instance of the batched workload."""
+    import numpy as np
+    rng = np.random.default_rng(BATCH["seed"] + 1000 * rank)
+    specs = []
+    for i in range(BATCH["n"]):
+        v = int(np.exp(rng.uniform(np.log(BATCH["vmin"]), np.log(BATCH["vmax"]))))
+        fam = int(rng.integers(0, 3))
+        seed = int(rng.integers(1, 2**31))
+        if fam == 0:
+            specs.append((0, v, int(round(v * 4.26)), 3, seed))
+        elif fam == 1:
+            inputs = max(8, v // 20)
+            gates = v - inputs
+            specs.append((1, gates, inputs, max(1, gates // 1000), seed))
+        else:
+            specs.append((2, v, 4 * v, 1, seed))
+    return specs
+
+
+def make_batch(rank=0):
+    import parafrost_gb300 as pg
+    return [pg.generate(*sp) for sp in batch_specs(rank)]
 
 
 class Clocks:
@@ -141,9 +178,58 @@ def cpu_baseline(wname, opts, cores):
     return processed, wall, res
 
 
+def oracle_run_spec(args):
+    """The CPU restatement on one generated instance (run in a spawned worker)."""
+    spec, opts = args
+    sys.path.insert(0, ROOT)
+    import parafrost_gb300 as pg
+    from oracle import pyoracle as po
+    cnf = pg.generate(*spec)
+    t0 = time.perf_counter()
+    r = po.simplify(cnf, pg.options_from(**opts))
+    dt = time.perf_counter() - t0
+    return sum(s["clauses_before"] for s in r.round_stats), dt
+
+
+def batch_sample(specs, every):
+    """Bounded sample of the batched workload: every `every`-th instance."""
+    return [sp for i, sp in enumerate(specs) if i % every == 0]
+
+
+def run_reference_batch(a, world, rank):
+    cores = os.cpu_count() or 1
+    specs = batch_sample(batch_specs(0), 4)
+    ctx = mp.get_context("spawn")
+    times, proc = [], 0
+    with ctx.Pool(cores) as pool:
+        for step in range(a.warmup + a.steps):
+            t0 = time.perf_counter()
+            res = pool.map(oracle_run_spec, [(sp, {}) for sp in specs], chunksize=1)
+            wall = time.perf_counter() - t0
+            if step >= a.warmup:
+                times.append(wall)
+                proc += sum(r[0] for r in res)
+    total = sum(times)
+    value = proc / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1000.0 * total / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generators)",
+        "config": {"workload": "batched", "desc": BATCH["desc"], "options": "reference defaults"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"every 4th instance of the batch ({len(specs)} instances) per step, one "
+                                   f"instance per worker process on {cores} cores (oracle/pfo.c)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(a, world, rank):
     if rank != 0:
         return 0
+    if a.workload == "batched":
+        return run_reference_batch(a, world, rank)
     cores = os.cpu_count() or 1
     opts = {}
     for _ in range(a.warmup):
@@ -288,6 +374,151 @@ def run_gpu(a, world, rank, local):
     return 0
 
 
+def result_bytes(res):
+    return (res.cnf.lits.nbytes + res.cnf.off.nbytes + res.cnf.learnt.nbytes + res.cnf.lbd.nbytes +
+            res.cnf.usage.nbytes + res.eliminated.nbytes + res.units.nbytes + res.pending_units.nbytes +
+            res.stack.nbytes)
+
+
+def run_gpu_batch(a, world, rank, local):
+    import torch
+    import parafrost_gb300 as pg
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    from parafrost_gb300.dist import allreduce_max, allreduce_sum
+    cnfs = make_batch(rank)               # every rank its own batch (weak scaling)
+    n = len(cnfs)
+    cls_in = sum(int(c.num_clauses) for c in cnfs)
+    sim = pg.Simplifier()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    for _ in range(a.warmup):
+        sim.upload_batch(cnfs)
+        sim.run()
+    # ---- batched, device-timed: the batch resident in HBM, rounds timed with CUDA events ----
+    sim.profile(True)
+    sim.profile_reset()
+    clocks = Clocks(local)
+    barrier()
+    clocks.start()
+    dev_ms, processed, launches, alg = 0.0, 0, 0, 0
+    last = None
+    for _ in range(a.steps):
+        sim.upload_batch(cnfs)
+        flush.fill_(1.0)
+        st = sim.run()
+        dev_ms += st.device_ms
+        processed += st.clauses_processed
+        launches += st.kernel_launches
+        alg += st.alg_bytes
+        last = st
+    barrier()
+    clk = clocks.stop()
+    prof = sim.profile_report()
+    sim.profile(False)
+    # ---- plain path on the same instances: one simplify call per instance ----
+    for cnf in cnfs[:8]:
+        sim.upload(cnf)
+        sim.run()
+    barrier()
+    plain_ms, plain_proc, plain_launches = 0.0, 0, 0
+    for cnf in cnfs:
+        sim.upload(cnf)
+        flush.fill_(1.0)
+        st = sim.run()
+        plain_ms += st.device_ms
+        plain_proc += st.clauses_processed
+        plain_launches += st.kernel_launches
+    barrier()
+    # ---- end to end through the C ABI with host buffers ----
+    e2e_s, e2e_proc, h2d, d2h = 0.0, 0, 0, 0
+    for _ in range(a.steps):
+        t1 = time.perf_counter()
+        outs = sim.simplify_batch(cnfs)
+        e2e_s += time.perf_counter() - t1
+        e2e_proc += sum(int(o.stats["clauses_processed"]) for o in outs)
+        h2d = sum(c.lits.nbytes + c.off.nbytes for c in cnfs)
+        d2h = sum(result_bytes(o) for o in outs)
+    barrier()
+    pe2e_s, pe2e_proc = 0.0, 0
+    t1 = time.perf_counter()
+    for cnf in cnfs:
+        res = sim.simplify(cnf)
+        pe2e_proc += int(res.stats["clauses_processed"])
+    pe2e_s = time.perf_counter() - t1
+    barrier()
+    dev_ms_max = allreduce_max(dev_ms, device="cuda")
+    total_proc = allreduce_sum(processed, device="cuda")
+    e2e_max = allreduce_max(e2e_s, device="cuda")
+    e2e_total = allreduce_sum(e2e_proc, device="cuda")
+    plain_max = allreduce_max(plain_ms, device="cuda")
+    plain_total = allreduce_sum(plain_proc, device="cuda")
+    pe2e_max = allreduce_max(pe2e_s, device="cuda")
+    pe2e_total = allreduce_sum(pe2e_proc, device="cuda")
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    value = total_proc / (dev_ms_max / 1000.0)
+    plain_value = plain_total / (plain_max / 1000.0)
+    peak, peak_kind = load_peaks()
+    dom_name, dom = max(((k, v) for k, v in prof.items() if v["ms"] > 0), key=lambda kv: kv[1]["ms"])
+    achieved = (dom["alg_bytes"] / 1e9) / (dom["ms"] / 1e3) if dom["ms"] > 0 else 0.0
+    roofline = {
+        "bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_kind, "traffic": TRAFFIC.get(("batched", dom_name)),
+        "launches": dom["launches"], "ms_per_launch": dom["ms"] / max(1, dom["launches"]),
+        "alg_bytes_per_launch": dom["alg_bytes"] / max(1, dom["launches"]),
+        "share": dom["ms"] / sum(v["ms"] for v in prof.values()),
+        "all_alg_bytes_gbs": (alg / 1e9) / (dev_ms / 1e3),
+    }
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": dev_ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic (seeded generators)",
+        "config": {"workload": "batched", "desc": BATCH["desc"], "instances": n, "clauses_in": cls_in,
+                   "literals_in": int(sum(int(c.num_literals) for c in cnfs)),
+                   "clauses_out": int(last.clauses_out), "max_rounds": int(last.rounds),
+                   "options": "reference defaults (phases=5, ERE on)",
+                   "l2": "256 MB buffer written before every timed simplify call (batched and plain)",
+                   "parallelism": "replicas only" if world > 1 else "single GPU"},
+        "plain": {"value": plain_value, "unit": UNIT, "ms_per_pass": plain_max,
+                  "gpu_launches": int(plain_launches),
+                  "e2e": {"value": pe2e_total / pe2e_max, "unit": UNIT, "ms_per_pass": 1000 * pe2e_max},
+                  "what": "the same instances, one pfg_upload + pfg_simplify call each"},
+        "batched_vs_plain": value / plain_value,
+        "e2e": {"value": e2e_total / e2e_max, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_max / a.steps},
+        "roofline": roofline,
+        "gpu_launches": int(launches),
+        "kernel_ms": {k: round(v["ms"] / a.steps, 4) for k, v in prof.items() if v["launches"]},
+        "clocks": clk,
+    }
+    if not a.no_cpu_baseline:
+        specs = batch_sample(batch_specs(0), 16)
+        t0 = time.perf_counter()
+        p = 0
+        for sp in specs:
+            p += oracle_run_spec((sp, {}))[0]
+        wall = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": p / wall, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"every 16th instance of the batch ({len(specs)} instances), oracle/pfo.c "
+                                          f"on one thread"}
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 # DRAM traffic per launch of the dominant kernel group from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (workload, group).
 TRAFFIC = {}
@@ -299,12 +530,19 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="tseitin", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="batched", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--single-step", action="store_true",
                     help="one simplify call of the workload, nothing timed (the command profiled by ncu)")
     a = ap.parse_args()
     world, rank, local = dist_setup()
+    if a.single_step and a.workload == "batched":
+        import parafrost_gb300 as pg
+        with pg.Simplifier() as sim:
+            outs = sim.simplify_batch(make_batch(0))
+        print(json.dumps({"workload": "batched", "instances": len(outs),
+                          "clauses_out": int(sum(o.cnf.num_clauses for o in outs))}))
+        return 0
     if a.single_step:
         import parafrost_gb300 as pg
         cnf = make_cnf(WORKLOADS[a.workload])
@@ -315,6 +553,8 @@ def main():
         return 0
     if a.impl == "reference":
         return run_reference(a, world, rank)
+    if a.workload == "batched":
+        return run_gpu_batch(a, world, rank, local)
     return run_gpu(a, world, rank, local)
 
 
