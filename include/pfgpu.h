@@ -217,6 +217,35 @@ int  pfg_batch_download(pfg_ctx* ctx, uint32_t i, uint32_t* lits, uint64_t* cls_
                         uint8_t* eliminated, uint32_t* units, uint32_t* pending_units,
                         uint32_t* stack, uint64_t* round_ends);
 
+/*
+ * The simplified CNF of a one-instance context written straight into
+ * caller-owned DEVICE buffers (sizes from pfg_result_sizes_get; any pointer
+ * may be NULL), allocating no device or host memory. No counterpart in the
+ * reference, whose write-back always goes through host buffers (cacheCNF,
+ * src/gpu/cnf.cu:200-236).
+ *
+ * For callers that pass the clauses on to another GPU stage and cannot
+ * allocate while doing so: a serving loop that has reserved the device's
+ * memory for its own arena (an allocation would fail or eat into another
+ * job's share), or code that must not stall on the device-wide
+ * synchronisation cudaMalloc/cudaFree bring while other streams are busy.
+ * pfg_download allocates packing buffers on every call.
+ *
+ * Scratch is one static 16 MiB device array per device, enough for a clause
+ * store of about 1.3 million slots (live or deleted); a larger store is
+ * rejected with PFG_INVALID and pfg_last_error says the limit. The first call
+ * on a device looks the array up with cudaGetSymbolAddress, which may load
+ * the module: make that first call before any stream capture. No scratch word
+ * has to start at zero (each call writes every word before reading it). Calls
+ * that overlap in time on one device -- from two threads, or on two contexts
+ * whose streams run at once -- share the array and corrupt each other's
+ * output: run them one after another. Returns once its work on the context's
+ * stream has finished.
+ */
+int  pfg_download_device_noalloc(pfg_ctx* ctx, uint32_t* d_lits, uint64_t* d_cls_off,
+                                 uint8_t* d_cls_learnt, uint32_t* d_cls_lbd,
+                                 uint8_t* d_cls_usage);
+
 /* Release all device memory of the context. Replaces Solver::freeSimp (simplify.cu:254). */
 void pfg_destroy(pfg_ctx* ctx);
 

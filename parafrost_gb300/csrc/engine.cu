@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <unordered_map>
 #include <vector>
 
@@ -1256,4 +1257,112 @@ extern "C" void pfg_destroy(pfg_ctx* o) {
     c.prof.destroy();
     cudaGetLastError();
     delete o;
+}
+
+// ---- allocation-free write-back into caller-owned device buffers ----
+namespace pfg {
+namespace {
+
+// Scratch of pfg_download_device_noalloc: per clause slot a u32 flag and a u64
+// size (each region 256-byte aligned), then the tile sums of the scans.
+constexpr size_t NOALLOC_SCRATCH_BYTES = 16ull << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+size_t noalloc_bytes(uint64_t n) {
+    return align_up(4 * (n + 1)) + align_up(8 * (n + 1)) + scan_temp_bytes(n + 1);
+}
+
+// the largest clause store (slots, live or deleted) the scratch covers
+uint64_t noalloc_max_slots() {
+    uint64_t lo = 0, hi = NOALLOC_SCRATCH_BYTES / 12;
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi + 1) / 2;
+        if (noalloc_bytes(mid) <= NOALLOC_SCRATCH_BYTES) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// device address of the scratch array; looked up once per device
+bool noalloc_scratch(Ctx& c, char** out) {
+    int dev = -1;
+    if (!cuda_ok(c, cudaGetDevice(&dev), "cudaGetDevice")) return false;
+    if (dev != c.device) { c.err = "the context's device is not the current device"; return false; }
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) { c.err = "device index out of range"; return false; }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            c.err = std::string("cudaGetSymbolAddress of the download scratch failed: ") + cudaGetErrorString(e);
+            return false;
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = (char*)g_noalloc_ptr[dev];
+    return true;
+}
+
+// out_pack_k that skips the outputs the caller did not ask for
+__global__ void out_pack_opt_k(const ClsHdr* hdr, const uint32_t* lits, uint64_t ncls, const uint32_t* pos,
+                               const unsigned long long* loff, uint32_t* olits, unsigned long long* ooff,
+                               uint8_t* olearnt, uint32_t* olbd, uint8_t* ousage) {
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint64_t c = warp; c < ncls; c += nwarps) {
+        const ClsHdr h = hdr[c];
+        if (m_deleted(h.meta)) continue;
+        const unsigned long long o = loff[c];
+        if (olits)
+            for (uint32_t k = lane; k < h.size; k += 32) olits[o + k] = lits[h.off + k];
+        if (lane == 0) {
+            const uint32_t q = pos[c];
+            if (ooff) ooff[q] = o;
+            if (olearnt) olearnt[q] = m_learnt(h.meta);
+            if (olbd) olbd[q] = m_lbd(h.meta);
+            if (ousage) ousage[q] = (uint8_t)m_usage(h.meta);
+        }
+    }
+}
+
+}  // namespace
+}  // namespace pfg
+
+extern "C" int pfg_download_device_noalloc(pfg_ctx* o, uint32_t* d_lits, uint64_t* d_cls_off, uint8_t* d_cls_learnt,
+                                           uint32_t* d_cls_lbd, uint8_t* d_cls_usage) {
+    if (!o) return PFG_INVALID;
+    Ctx& c = o->c;
+    c.err.clear();
+    if (!c.uploaded) { c.err = "no instance uploaded"; return PFG_INVALID; }
+    if (c.ninst != 1) { c.err = "several instances uploaded: the allocation-free download takes one"; return PFG_INVALID; }
+    const uint64_t n = c.ncls, C = c.numClauses;
+    if (noalloc_bytes(n) > NOALLOC_SCRATCH_BYTES) {
+        c.err = "the clause store has " + std::to_string(n) + " clause slots; the allocation-free download handles at most " +
+                std::to_string(noalloc_max_slots()) + " (its scratch is a fixed 16 MiB device array)";
+        return PFG_INVALID;
+    }
+    char* scratch = nullptr;
+    if (!noalloc_scratch(c, &scratch)) return PFG_CUDA_ERROR;
+    uint32_t* flag = (uint32_t*)scratch;
+    unsigned long long* sz = (unsigned long long*)(scratch + align_up(4 * (n + 1)));
+    void* tmp = scratch + align_up(4 * (n + 1)) + align_up(8 * (n + 1));
+    unsigned long long* ooff = reinterpret_cast<unsigned long long*>(d_cls_off);
+    const uint64_t base_launches = g_launches;
+    if (n) {
+        PFG_LAUNCH(K_DOWNLOAD, out_flags_k, grid_for(n, 256), 256, 0, c.s, c.hdr, n, flag, sz);
+        exclusive_scan_u32(flag, flag, n, 0u, nullptr, tmp, c.s);
+        exclusive_scan_u64(sz, sz, n, 0ull, ooff ? ooff + C : nullptr, tmp, c.s);
+        PFG_LAUNCH(K_DOWNLOAD, out_pack_opt_k, grid_for(n * 32, 256), 256, 0, c.s, c.hdr, c.lits, n, flag, sz, d_lits,
+                   ooff, d_cls_learnt, d_cls_lbd, d_cls_usage);
+    } else if (ooff) {
+        cudaMemsetAsync(ooff, 0, sizeof(unsigned long long), c.s);
+    }
+    const bool ok = cuda_ok(c, cudaStreamSynchronize(c.s), "allocation-free download");
+    c.launches += g_launches - base_launches;
+    return ok ? PFG_OK : PFG_CUDA_ERROR;
 }
