@@ -8,7 +8,9 @@ every SUB+BVE round (sum of C_in over rounds and instances).
 Workloads: `batched` (the default) simplifies 512 seeded instances of uneven
 size (log-uniform 1k..200k variables; random 3-SAT, Tseitin and scale-free
 generators) in one batch per step, and times the plain path -- the same
-instances one per simplify call -- beside it. `tseitin`, `ksat` and
+instances one per simplify call -- beside it. The same line carries the
+serving stream: 10,000 jobs with Poisson arrivals submitted to the native
+request loop (throughput, p50/p99 latency). `tseitin`, `ksat` and
 `scalefree` run one instance per step.
 
   value : clauses/s with the input resident in HBM when timing starts
@@ -53,6 +55,15 @@ BATCH = dict(n=512, vmin=1_000, vmax=200_000, seed=7,
              desc="512 instances per batch, log-uniform 1k..200k vars each, generator per instance uniform over "
                   "random 3-SAT (4.26 clauses/var), Tseitin (5% inputs) and scale-free (4 clauses/var, planted)")
 
+# configs[4]: Poisson stream of 10,000 jobs, clause counts log-uniform on [1e3, 1e6]
+# from the three generators, admitted by a 120 GB device-arena budget, 3 rounds each.
+# Jobs are drawn from a pool of seeded instances (with replacement).
+SERVE = dict(jobs=10_000, cmin=1_000, cmax=1_000_000, pool=256, rate=800.0, budget=120_000_000_000, phases=3,
+             slots=4, max_batch=512, seed=11,
+             desc="Poisson arrivals of 10,000 jobs at a fixed rate; clause counts log-uniform 1e3..1e6 from random "
+                  "3-SAT / Tseitin / scale-free generators (pool of 256 seeded instances drawn with replacement); "
+                  "admission by a 120 GB device-arena budget; 3 rounds per job")
+
 METRIC = "inprocessing clauses/s (BVE+SUB)"
 UNIT = "clauses/s"
 
@@ -89,6 +100,79 @@ def batch_specs(rank=0):
         else:
             specs.append((2, v, 4 * v, 1, seed))
     return specs
+
+
+def serve_pool(rank=0):
+    """Pool of instances with clause counts log-uniform on [cmin, cmax]."""
+    import numpy as np
+    import parafrost_gb300 as pg
+    rng = np.random.default_rng(SERVE["seed"] + 1000 * rank)
+    pool = []
+    for _ in range(SERVE["pool"]):
+        c = float(np.exp(rng.uniform(np.log(SERVE["cmin"]), np.log(SERVE["cmax"]))))
+        fam = int(rng.integers(0, 3))
+        seed = int(rng.integers(1, 2**31))
+        if fam == 0:
+            pool.append(pg.generate(0, max(10, int(c / 4.26)), int(c), 3, seed))
+        elif fam == 1:
+            gates = max(16, int(c / 3.3))
+            pool.append(pg.generate(1, gates, max(8, gates // 20), max(1, gates // 1000), seed))
+        else:
+            pool.append(pg.generate(2, max(10, int(c / 4)), int(c), 1, seed))
+    return pool
+
+
+def serve_stream(pool, jobs, rate, rank=0):
+    """Submit `jobs` jobs drawn from `pool` with Poisson arrivals at `rate` jobs/s;
+    returns throughput, latency percentiles and the server's counters."""
+    import threading
+    import numpy as np
+    import parafrost_gb300 as pg
+    rng = np.random.default_rng(SERVE["seed"] + 7 + 1000 * rank)
+    picks = rng.integers(0, len(pool), jobs)
+    gaps = rng.exponential(1.0 / rate, jobs)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    infos = [None] * jobs
+    tickets = [None] * jobs
+    have = threading.Semaphore(0)
+    with pg.Server(arena_bytes=SERVE["budget"], slots=SERVE["slots"], max_batch=SERVE["max_batch"],
+                   phases=SERVE["phases"]) as srv:
+        def collect():
+            for k in range(jobs):
+                have.acquire()
+                infos[k] = srv.wait(tickets[k])
+                srv.fetch(tickets[k])
+        th = threading.Thread(target=collect)
+        th.start()
+        t0 = time.perf_counter()
+        late = 0.0
+        for k in range(jobs):
+            dt = t0 + arrivals[k] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            else:
+                late = max(late, -dt)
+            tickets[k] = srv.submit(pool[picks[k]])
+            have.release()
+        th.join()
+        st = srv.stats()
+    lat = np.array([i.latency_s for i in infos]) * 1e3
+    qlat = np.array([i.queue_s for i in infos]) * 1e3
+    span = (max(i.t_done_ns for i in infos) - min(i.t_submit_ns for i in infos)) * 1e-9
+    proc = sum(int(i.clauses_processed) for i in infos)
+    return {
+        "value": proc / span, "unit": UNIT, "jobs": jobs, "offered_rate_jobs_s": rate,
+        "achieved_rate_jobs_s": jobs / span, "span_s": span,
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "p50_queue_ms": float(np.percentile(qlat, 50)), "p99_queue_ms": float(np.percentile(qlat, 99)),
+        "clauses_in": int(sum(int(pool[p].num_clauses) for p in picks)), "clauses_processed": proc,
+        "errors": int(sum(1 for i in infos if i.rc != 0)),
+        "mean_batch": float(np.mean([i.batch_size for i in infos])),
+        "max_in_flight_batches": st["max_in_flight_batches"], "max_jobs_in_flight": st["max_jobs_in_flight"],
+        "peak_admitted_gb": st["peak_est_bytes"] / 1e9, "budget_gb": st["budget_bytes"] / 1e9,
+        "slots": SERVE["slots"], "max_batch": SERVE["max_batch"], "producer_max_lateness_s": late,
+        "latency": "submit to result on the host (admission wait, upload, rounds, download)",
+    }
 
 
 def make_batch(rank=0):
@@ -456,6 +540,11 @@ def run_gpu_batch(a, world, rank, local):
         pe2e_proc += int(res.stats["clauses_processed"])
     pe2e_s = time.perf_counter() - t1
     barrier()
+    serving = None
+    if not a.no_serving:
+        serving = serve_stream(serve_pool(rank), a.serve_jobs, SERVE["rate"], rank)
+        serving["desc"] = SERVE["desc"]
+    barrier()
     dev_ms_max = allreduce_max(dev_ms, device="cuda")
     total_proc = allreduce_sum(processed, device="cuda")
     e2e_max = allreduce_max(e2e_s, device="cuda")
@@ -496,6 +585,7 @@ def run_gpu_batch(a, world, rank, local):
                   "e2e": {"value": pe2e_total / pe2e_max, "unit": UNIT, "ms_per_pass": 1000 * pe2e_max},
                   "what": "the same instances, one pfg_upload + pfg_simplify call each"},
         "batched_vs_plain": value / plain_value,
+        "serving": serving,
         "e2e": {"value": e2e_total / e2e_max, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_max / a.steps},
         "roofline": roofline,
@@ -532,6 +622,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving stream of the batched line")
+    ap.add_argument("--serve-jobs", type=int, default=SERVE["jobs"])
     ap.add_argument("--single-step", action="store_true",
                     help="one simplify call of the workload, nothing timed (the command profiled by ncu)")
     a = ap.parse_args()

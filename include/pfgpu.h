@@ -39,6 +39,7 @@ extern "C" {
 #define PFG_TIMEOUT        4  /* a bounded device-side loop gave up           */
 #define PFG_INVALID        5  /* invalid argument or input                    */
 #define PFG_CUDA_ERROR     6  /* a CUDA runtime call failed                   */
+#define PFG_PENDING        7  /* serving: the job has not finished yet        */
 
 /* solver status after pfg_simplify (same values as the reference CLI/IPASIR) */
 #define PFG_UNKNOWN        0
@@ -245,6 +246,58 @@ int  pfg_batch_download(pfg_ctx* ctx, uint32_t i, uint32_t* lits, uint64_t* cls_
 int  pfg_download_device_noalloc(pfg_ctx* ctx, uint32_t* d_lits, uint64_t* d_cls_off,
                                  uint8_t* d_cls_learnt, uint32_t* d_cls_lbd,
                                  uint8_t* d_cls_usage);
+
+/*
+ * Serving: a request loop for simplification jobs that arrive over time (no
+ * counterpart in the reference). Jobs are queued by pfg_server_submit (the
+ * server copies the instance) and admitted in arrival order while their
+ * estimated device footprint fits the server's arena budget. `slots` worker
+ * threads each own a context and stream; a free worker takes every admitted
+ * job that is waiting (up to `max_batch`) and simplifies them as one batch
+ * (pfg_batch_upload), so jobs that arrive while other batches are on the GPU
+ * start as soon as a slot and memory free up, and the batches of different
+ * slots overlap on the device. Each job's result is the one it gives alone.
+ */
+typedef struct pfg_server pfg_server;
+
+typedef struct pfg_job_info {
+    int32_t  rc;              /* PFG_OK or the error of the job's batch      */
+    int32_t  status;          /* PFG_UNKNOWN / PFG_SAT / PFG_UNSAT           */
+    uint32_t batch_size;      /* jobs in the batch that ran it               */
+    uint32_t slot;            /* worker that ran it                          */
+    uint64_t est_bytes;       /* device footprint charged at admission       */
+    uint64_t t_submit_ns;     /* steady-clock times                          */
+    uint64_t t_admit_ns;
+    uint64_t t_done_ns;
+    uint64_t clauses_processed;
+    pfg_result_sizes sizes;   /* buffer sizes for pfg_server_fetch           */
+} pfg_job_info;
+
+typedef struct pfg_server_stats {
+    uint64_t submitted, admitted, done, batches;
+    uint64_t max_in_flight_batches;   /* most batches on the device at once   */
+    uint64_t max_jobs_in_flight;
+    uint64_t peak_est_bytes;          /* most device bytes charged at once    */
+    uint64_t budget_bytes;
+} pfg_server_stats;
+
+int  pfg_server_create(pfg_server** server, const pfg_options* opts, size_t arena_bytes,
+                       uint32_t slots, uint32_t max_batch);
+/* queue one job; the instance is copied, the caller's buffers may be reused at once */
+int  pfg_server_submit(pfg_server* server, const pfg_instance* job, uint64_t* ticket);
+/* PFG_OK and `info` once the job is done, PFG_PENDING while it is queued or
+   running (waits up to wait_ms first), PFG_INVALID for an unknown ticket */
+int  pfg_server_poll(pfg_server* server, uint64_t ticket, int32_t wait_ms, pfg_job_info* info);
+/* copy the result of a finished job (buffers sized by info.sizes, any may be
+   NULL) and forget the job; outputs as pfg_download */
+int  pfg_server_fetch(pfg_server* server, uint64_t ticket, uint32_t* lits, uint64_t* cls_off,
+                      uint8_t* cls_learnt, uint32_t* cls_lbd, uint8_t* cls_usage,
+                      uint8_t* eliminated, uint32_t* units, uint32_t* pending_units,
+                      uint32_t* stack, uint64_t* round_ends);
+int  pfg_server_stats_get(pfg_server* server, pfg_server_stats* stats);
+/* finish every queued job, stop the workers and free everything */
+void pfg_server_destroy(pfg_server* server);
+const char* pfg_server_last_error(pfg_server* server);
 
 /* Release all device memory of the context. Replaces Solver::freeSimp (simplify.cu:254). */
 void pfg_destroy(pfg_ctx* ctx);

@@ -8,10 +8,11 @@ from ._abi import (PFG_SAT, PFG_UNKNOWN, PFG_UNSAT, PfgOptions, PfgStats, defaul
                    options_from)
 from .cnf import Cnf, generate, lit_to_int, int_to_lit, random_ksat, read_dimacs, scale_free, tseitin, write_dimacs
 from .simplifier import SimplifyError, SimplifyResult, Simplifier, simplify, simplify_batch
+from .server import JobInfo, Server
 
 __all__ = [
     "Cnf", "Simplifier", "SimplifyResult", "SimplifyError", "simplify", "generate", "random_ksat", "tseitin",
     "scale_free", "read_dimacs", "write_dimacs", "lit_to_int", "int_to_lit", "default_options", "options_from",
-    "simplify_batch",
+    "simplify_batch", "Server", "JobInfo",
     "options_dict", "PfgOptions", "PfgStats", "PFG_SAT", "PFG_UNSAT", "PFG_UNKNOWN",
 ]

@@ -21,6 +21,7 @@ RETURN_NAMES = {
     PFG_TIMEOUT: "device-side loop timed out",
     PFG_INVALID: "invalid input",
     PFG_CUDA_ERROR: "CUDA error",
+    7: "job pending",
 }
 
 
@@ -108,6 +109,37 @@ class PfgInstance(C.Structure):
         ("vorg", C.POINTER(C.c_uint32)),
     ]
 
+
+class PfgJobInfo(C.Structure):
+    """Serving: state of one finished job (pfg_job_info)."""
+    _fields_ = [
+        ("rc", C.c_int32),
+        ("status", C.c_int32),
+        ("batch_size", C.c_uint32),
+        ("slot", C.c_uint32),
+        ("est_bytes", C.c_uint64),
+        ("t_submit_ns", C.c_uint64),
+        ("t_admit_ns", C.c_uint64),
+        ("t_done_ns", C.c_uint64),
+        ("clauses_processed", C.c_uint64),
+        ("sizes", PfgResultSizes),
+    ]
+
+
+class PfgServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_uint64),
+        ("admitted", C.c_uint64),
+        ("done", C.c_uint64),
+        ("batches", C.c_uint64),
+        ("max_in_flight_batches", C.c_uint64),
+        ("max_jobs_in_flight", C.c_uint64),
+        ("peak_est_bytes", C.c_uint64),
+        ("budget_bytes", C.c_uint64),
+    ]
+
+
+PFG_PENDING = 7
 
 PASS_NAMES = ("ot", "bcp", "lcve", "sub", "ve", "ere", "gc", "other")
 

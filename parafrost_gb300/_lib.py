@@ -6,7 +6,7 @@ implementation to fall back to, so a missing or broken library raises.
 import ctypes as C
 import os
 
-from ._abi import PfgInstance, PfgOptions, PfgResultSizes, PfgStats
+from ._abi import PfgInstance, PfgJobInfo, PfgOptions, PfgResultSizes, PfgServerStats, PfgStats
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libpfgpu.so")
@@ -54,6 +54,20 @@ def lib():
     L.pfg_batch_download.restype = C.c_int
     L.pfg_download_device_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.pfg_download_device_noalloc.restype = C.c_int
+    L.pfg_server_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(PfgOptions), C.c_size_t, C.c_uint32, C.c_uint32]
+    L.pfg_server_create.restype = C.c_int
+    L.pfg_server_submit.argtypes = [C.c_void_p, C.POINTER(PfgInstance), C.POINTER(C.c_uint64)]
+    L.pfg_server_submit.restype = C.c_int
+    L.pfg_server_poll.argtypes = [C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(PfgJobInfo)]
+    L.pfg_server_poll.restype = C.c_int
+    L.pfg_server_fetch.argtypes = [C.c_void_p, C.c_uint64, u32p, u64p, u8p, u32p, u8p, u8p, u32p, u32p, u32p, u64p]
+    L.pfg_server_fetch.restype = C.c_int
+    L.pfg_server_stats_get.argtypes = [C.c_void_p, C.POINTER(PfgServerStats)]
+    L.pfg_server_stats_get.restype = C.c_int
+    L.pfg_server_destroy.argtypes = [C.c_void_p]
+    L.pfg_server_destroy.restype = None
+    L.pfg_server_last_error.argtypes = [C.c_void_p]
+    L.pfg_server_last_error.restype = C.c_char_p
     L.pfg_destroy.argtypes = [C.c_void_p]
     L.pfg_destroy.restype = None
     L.pfg_last_error.argtypes = [C.c_void_p]
@@ -83,5 +97,6 @@ EXPORTED = (
     "pfg_result_sizes_get", "pfg_download", "pfg_destroy", "pfg_last_error", "pfg_kernel_launches",
     "pfg_generate", "pfg_profile_enable", "pfg_profile_reset", "pfg_profile_count", "pfg_profile_name",
     "pfg_profile_get", "pfg_batch_upload", "pfg_batch_size", "pfg_batch_stats", "pfg_batch_result_sizes",
-    "pfg_batch_download", "pfg_download_device_noalloc",
+    "pfg_batch_download", "pfg_download_device_noalloc", "pfg_server_create", "pfg_server_submit",
+    "pfg_server_poll", "pfg_server_fetch", "pfg_server_stats_get", "pfg_server_destroy", "pfg_server_last_error",
 )
