@@ -175,9 +175,9 @@ def serve_stream(pool, jobs, rate, rank=0):
     }
 
 
-def make_batch(rank=0):
+def make_batch(rank=0, n=None):
     import parafrost_gb300 as pg
-    return [pg.generate(*sp) for sp in batch_specs(rank)]
+    return [pg.generate(*sp) for sp in batch_specs(rank)[:n]]
 
 
 class Clocks:
@@ -624,6 +624,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving stream of the batched line")
     ap.add_argument("--serve-jobs", type=int, default=SERVE["jobs"])
+    ap.add_argument("--batch-n", type=int, default=None,
+                    help="with --single-step: only the first N instances of the batch (small profiling case)")
     ap.add_argument("--single-step", action="store_true",
                     help="one simplify call of the workload, nothing timed (the command profiled by ncu)")
     a = ap.parse_args()
@@ -631,7 +633,7 @@ def main():
     if a.single_step and a.workload == "batched":
         import parafrost_gb300 as pg
         with pg.Simplifier() as sim:
-            outs = sim.simplify_batch(make_batch(0))
+            outs = sim.simplify_batch(make_batch(0, a.batch_n))
         print(json.dumps({"workload": "batched", "instances": len(outs),
                           "clauses_out": int(sum(o.cnf.num_clauses for o in outs))}))
         return 0

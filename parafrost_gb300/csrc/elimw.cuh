@@ -674,15 +674,28 @@ PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
     }
     const uint32_t nClsBefore = pOrgs + nOrgs;
     elimType = 0; nE = 0; nC = 0; nL = 0;
+    // each detector is tried for both definitions (the second only while no
+    // substitution was counted) from one call site, so its code exists once
     if (nClsBefore > 2) {
-        if (nOrgs < SH_MAX_BVE_OUT1 && ws_find_ao_gate(k, w, N, P, nClsBefore, nE, nC, nL, lane)) elimType = AOIX_MASK;
-        else if (!nC && pOrgs < SH_MAX_BVE_OUT1 && ws_find_ao_gate(k, w, P, N, nClsBefore, nE, nC, nL, lane)) elimType = AOIX_MASK;
+#pragma unroll 1
+        for (int o = 0; o < 2 && !elimType && !(o && nC); o++) {
+            const Side& D = o ? P : N;
+            const Side& F = o ? N : P;
+            if ((o ? pOrgs : nOrgs) < SH_MAX_BVE_OUT1 && ws_find_ao_gate(k, w, D, F, nClsBefore, nE, nC, nL, lane))
+                elimType = AOIX_MASK;
+        }
     }
     if (!elimType && nClsBefore > 3) {
-        if (ws_find_ite_gate(k, w, P, N, nClsBefore, nE, nC, nL, lane)) elimType = AOIX_MASK;
-        else if (!nC && ws_find_ite_gate(k, w, N, P, nClsBefore, nE, nC, nL, lane)) elimType = AOIX_MASK;
-        else if (ws_find_xor_gate(k, w, P, N, nClsBefore, nE, nC, nL, lane)) elimType = AOIX_MASK;
-        else if (!nC && ws_find_xor_gate(k, w, N, P, nClsBefore, nE, nC, nL, lane)) elimType = AOIX_MASK;
+#pragma unroll 1
+        for (int g = 0; g < 4 && !elimType; g++) {
+            const int o = g & 1;
+            if (o && nC) continue;
+            const Side& D = o ? N : P;
+            const Side& F = o ? P : N;
+            const bool found = g < 2 ? ws_find_ite_gate(k, w, D, F, nClsBefore, nE, nC, nL, lane)
+                                     : ws_find_xor_gate(k, w, D, F, nClsBefore, nE, nC, nL, lane);
+            if (found) elimType = AOIX_MASK;
+        }
     }
     if (vc_on(k, x) && !elimType && nClsBefore > 2) {
         ws_flush(k, w, lane);

@@ -793,7 +793,7 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
                     if (c.hout.conflict[i]) { h.status = PFG_UNSAT; h.active = false; }
                 }
             }
-            if (!ot_build(c)) break;
+            if (!ot_filter(c, c.bstate)) break;
             cudaMemsetAsync(c.dout.ucount, 0, n * sizeof(uint32_t), c.s);
         }
         for (uint32_t i = 0; i < n; i++)

@@ -212,6 +212,7 @@ bool cuda_ok(Ctx& c, cudaError_t e, const char* what);
 // occurrence table (ot.cu)
 bool ot_build(Ctx& c);          // histogram + CSR offsets + unsorted fill (clause order irrelevant)
 bool ot_sort(Ctx& c, bool by_id);  // sort every list by OLIST_CMP (key.cuh:67-85) or by clause id
+bool ot_filter(Ctx& c, const uint8_t* assigned);   // drop what unit propagation removed from the lists
 // counting + compaction (gc.cu)
 void count_live(Ctx& c);        // totals into counters, per instance into dout.cnt (read after a sync)
 bool compact_cnf(Ctx& c);       // Solver::reallocCNF(true) (cnf.cu:129-144, recycle.cu:60)

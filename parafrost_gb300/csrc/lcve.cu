@@ -35,20 +35,20 @@ __global__ void scores_k(const uint32_t* hist, uint32_t V, uint32_t* scores, uin
     if ((threadIdx.x & 31u) == 0 && mx) atomicMax(&dc->nfrozen, mx);   // nfrozen reused as max score here
 }
 
-PFG_D bool oversize(const ClsHdr* hdr, const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids,
-                    uint32_t lit, int maxcsize) {
-    const uint32_t o = ot_off[lit], n = ot_size[lit];
-    for (uint32_t i = 0; i < n; i++) {
-        const ClsHdr h = hdr[ot_ids[o + i]];
-        if (!m_deleted(h.meta) && (int)h.size > maxcsize) return true;
+// A variable that occurs in a live clause longer than lcveclausemax is never a
+// candidate (mis_init_k, lcve.cu:150-173); one pass over the clauses marks them.
+__global__ void oversize_mark_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
+                                int maxcsize, uint8_t* mark) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        const ClsHdr h = hdr[c];
+        if (m_deleted(h.meta) || (int)h.size <= maxcsize) continue;
+        for (uint32_t k = 0; k < h.size; k++) mark[ABSV(lits[h.off + k])] = 1;
     }
-    return false;
 }
 
 __global__ void mis_init_k(const uint32_t* eligible, uint32_t V, uint32_t* rank, uint8_t* mstate,
                            const uint8_t* vstate, const uint8_t* assumed, const uint32_t* hist,
-                           const ClsHdr* hdr, const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids,
-                           uint32_t pmax, uint32_t nmax, uint32_t maxoccurs, int maxcsize, uint8_t* cand,
+                           const uint8_t* oversized, uint32_t pmax, uint32_t nmax, uint32_t maxoccurs, uint8_t* cand,
                            const uint32_t* vinst, const uint8_t* active) {
     for (uint32_t ei = blockIdx.x * blockDim.x + threadIdx.x; ei < V; ei += gridDim.x * blockDim.x) {
         const uint32_t v = eligible[ei];
@@ -57,9 +57,7 @@ __global__ void mis_init_k(const uint32_t* eligible, uint32_t V, uint32_t* rank,
         if (active[vinst[v]] && !vstate[v] && !(assumed && assumed[v])) {
             const uint32_t p = 2 * v, n = p | 1;
             const uint32_t ps = hist[p], ns = hist[n];
-            if ((ps || ns) && ps <= maxoccurs && ns <= maxoccurs && !(ps >= pmax && ns >= nmax) &&
-                !oversize(hdr, ot_off, ot_size, ot_ids, p, maxcsize) &&
-                !oversize(hdr, ot_off, ot_size, ot_ids, n, maxcsize))
+            if ((ps || ns) && ps <= maxoccurs && ns <= maxoccurs && !(ps >= pmax && ns >= nmax) && !oversized[v])
                 st = MIS_UNDECIDED;
         }
         mstate[v] = st;
@@ -262,9 +260,12 @@ bool lcve(Ctx& c) {
     c.nelected = 0;
     c.mis_rounds = 0;
     if (c.o.lcve_fast) {
+        // winv is free until the rounds start: it holds the oversize marks here
+        cudaMemsetAsync(c.winv, 0, V + 1, c.s);
+        PFG_LAUNCH(K_LCVE, oversize_mark_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, maxcsize,
+                   c.winv);
         PFG_LAUNCH(K_LCVE, mis_init_k, grid_for(V, 256), 256, 0, c.s, c.eligible, V, c.rank, c.mstate, c.vstate,
-                   c.assumed, c.hist, c.hdr, c.ot_off, c.ot_size, c.ot_ids, pmax, nmax, maxoccurs, maxcsize, c.flag8,
-                   c.vinst, c.di.active);
+                   c.assumed, c.hist, c.winv, pmax, nmax, maxoccurs, c.flag8, c.vinst, c.di.active);
         select_flagged(c.eligible, c.flag8, c.work, V, &c.dc->nwork, c.vscan, c.tmp, c.s);
         sync_counters(c);
         const uint32_t nwork = c.hc->nwork;

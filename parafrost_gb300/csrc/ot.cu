@@ -43,6 +43,53 @@ __global__ void fill_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restric
     }
 }
 
+// After unit propagation (bcp_apply_k) a list of an assigned variable is empty:
+// a true literal's clauses are satisfied and deleted, a false literal was
+// stripped from its clauses. Other lists only lose deleted clauses. Thread per
+// list, order kept; lists longer than FILTER_THREAD_MAX go to a warp each.
+constexpr uint32_t FILTER_THREAD_MAX = 64;
+
+__global__ void ot_filter_k(const ClsHdr* __restrict__ hdr, uint64_t nlist, const uint32_t* __restrict__ off,
+                            uint32_t* size, uint32_t* hist, uint32_t* ids, const uint8_t* __restrict__ assigned,
+                            uint32_t* long_lists, uint32_t* nlong) {
+    for (uint64_t l = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlist; l += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t n = size[l];
+        if (!n) continue;
+        if (assigned[l >> 1]) { size[l] = 0; hist[l] = 0; continue; }
+        if (n > FILTER_THREAD_MAX) { long_lists[atomicAdd(nlong, 1u)] = (uint32_t)l; continue; }
+        uint32_t* L = ids + off[l];
+        uint32_t kept = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            const uint32_t c = L[i];
+            if (!m_deleted(hdr[c].meta)) L[kept++] = c;
+        }
+        size[l] = kept;
+        hist[l] = kept;
+    }
+}
+
+__global__ void ot_filter_long_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ off, uint32_t* size,
+                                 uint32_t* hist, uint32_t* ids, const uint32_t* long_lists, const uint32_t* nlong) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t nl = *nlong;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nl; q += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t l = long_lists[q];
+        const uint32_t n = size[l];
+        uint32_t* L = ids + off[l];
+        uint32_t kept = 0;
+        for (uint32_t b = 0; b < n; b += 32) {
+            const uint32_t i = b + lane;
+            const uint32_t c = i < n ? L[i] : 0u;
+            const bool keep = i < n && !m_deleted(hdr[c].meta);
+            const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
+            __syncwarp();
+            if (keep) L[kept + __popc(bal & ((1u << lane) - 1u))] = c;
+            kept += __popc(bal);
+        }
+        if (lane == 0) { size[l] = kept; hist[l] = kept; }
+    }
+}
+
 // OLIST_CMP key of every live clause, computed once per sort in clause order
 __global__ void ckeys_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
                         uint4* keys, bool by_id) {
@@ -231,6 +278,15 @@ bool ot_build(Ctx& c) {
     cudaMemcpyAsync(c.ot_size, c.hist, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
     PFG_LAUNCH(K_FILL, fill_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.ot_fill, c.ot_ids);
     return cuda_ok(c, cudaGetLastError(), "ot_build");
+}
+
+bool ot_filter(Ctx& c, const uint8_t* assigned) {
+    cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
+    PFG_LAUNCH(K_FILL, ot_filter_k, grid_for(c.nlist, 256), 256, 0, c.s, c.hdr, c.nlist, c.ot_off, c.ot_size, c.hist,
+               c.ot_ids, assigned, c.big_lists, &c.dc->big_lists);
+    PFG_LAUNCH(K_FILL, ot_filter_long_k, grid_for((uint64_t)c.nlist * 32 / FILTER_THREAD_MAX, 256, 8), 256, 0, c.s,
+               c.hdr, c.ot_off, c.ot_size, c.hist, c.ot_ids, c.big_lists, &c.dc->big_lists);
+    return cuda_ok(c, cudaGetLastError(), "ot_filter");
 }
 
 bool ot_sort(Ctx& c, bool by_id) {
