@@ -353,8 +353,14 @@ PFG_D bool ws_is_equal(WS& w, uint32_t c, const uint32_t* d, uint32_t n) {
 }
 
 // find_ao_gate (and.cuh:27-113)
-PFG_D bool ws_find_ao_gate(const EK& k, WS& w, const Side& D, const Side& F, uint32_t nOrgCls, uint32_t& nE,
-                           uint32_t& nC, uint32_t& nL, unsigned lane) {
+// Clauses a found gate melted, for the undo when its substitution is too large.
+struct GateUndo {
+    uint32_t a, b, c, d;
+};
+
+// find_ao_gate (and.cuh:46-105) up to the substitution count: the gate's
+// clauses are left molten and the count is made by the caller
+PFG_D bool ws_find_ao_gate(const EK& k, WS& w, const Side& D, const Side& F, GateUndo& undo, unsigned lane) {
     if (w.size[D.b] > 2 || w.size[F.b + F.n - 1] < 3) return false;
     const uint32_t dx = D.lit, fx = F.lit;
     uint32_t sig = 0;
@@ -372,7 +378,6 @@ PFG_D bool ws_find_ao_gate(const EK& k, WS& w, const Side& D, const Side& F, uin
     }
     __syncwarp();
     if (nImps > 1) {
-        const uint32_t x = ABSV(dx);
         if (lane == 0) { w.outs[nImps] = fx; sort_small(w.outs, (uint32_t)nImps + 1); }
         nImps++;
         sig |= MAPHASH(fx);
@@ -382,11 +387,7 @@ PFG_D bool ws_find_ao_gate(const EK& k, WS& w, const Side& D, const Side& F, uin
             if (m_orig(w.meta[c]) && w.size[c] == (uint32_t)nImps && SUBSIG(w.sig[c], sig) &&
                 ws_is_equal(w, c, w.outs, (uint32_t)nImps)) {
                 ws_melt(w, c, 1, lane);
-                nE = 0; nC = 0; nL = 0;
-                if (ws_count_subst(k, w, CNT_SUBS, x, nOrgCls, D, F, nE, nC, nL, lane)) {
-                    ws_melt(w, c, 0, lane);
-                    break;
-                }
+                undo.a = c;
                 return true;
             }
         }
@@ -428,11 +429,10 @@ PFG_D uint32_t ws_fast_eq(const EK& k, const WS& w, uint32_t x, uint32_t y, uint
     return NOREF;
 }
 
-// find_ite_gate (ifthenelse.cuh:50-123)
-PFG_D bool ws_find_ite_gate(const EK& k, WS& w, const Side& D, const Side& F, uint32_t nOrgCls, uint32_t& nE,
-                            uint32_t& nC, uint32_t& nL, unsigned lane) {
+// find_ite_gate (ifthenelse.cuh:50-123) up to the substitution count
+PFG_D bool ws_find_ite_gate(const EK& k, WS& w, const Side& D, const Side& F, GateUndo& undo, unsigned lane) {
     if (w.size[D.b + D.n - 1] == 2) return false;
-    const uint32_t dx = D.lit, fx = F.lit, v = ABSV(dx);
+    const uint32_t dx = D.lit, fx = F.lit;
     for (uint32_t i = 0; i < D.n; i++) {
         const uint32_t ci = D.b + i;
         if (!(m_orig(w.meta[ci]) && w.size[ci] == 3)) continue;
@@ -459,14 +459,7 @@ PFG_D bool ws_find_ite_gate(const EK& k, WS& w, const Side& D, const Side& F, ui
             ws_melt(w, cj, 1, lane);
             if (s1 != NOREF) ws_melt(w, s1, 1, lane);
             if (s2 != NOREF) ws_melt(w, s2, 1, lane);
-            nE = 0; nC = 0; nL = 0;
-            if (ws_count_subst(k, w, CNT_SUBS, v, nOrgCls, D, F, nE, nC, nL, lane)) {
-                ws_melt(w, ci, 0, lane);
-                ws_melt(w, cj, 0, lane);
-                if (s1 != NOREF) ws_melt(w, s1, 0, lane);
-                if (s2 != NOREF) ws_melt(w, s2, 0, lane);
-                return false;
-            }
+            undo = GateUndo{ci, cj, s1, s2};
             return true;
         }
     }
@@ -521,13 +514,11 @@ PFG_D bool ws_make_arity(const EK& k, WS& w, uint32_t& parity, uint32_t* lits, u
     return false;
 }
 
-// find_xor_gate (xor.cuh:102-178)
-PFG_D bool ws_find_xor_gate(const EK& k, WS& w, const Side& D, const Side& F, uint32_t nOrgCls, uint32_t& nE,
-                            uint32_t& nC, uint32_t& nL, unsigned lane) {
+// find_xor_gate (xor.cuh:102-178) up to the substitution count
+PFG_D bool ws_find_xor_gate(const EK& k, WS& w, const Side& D, const Side& F, unsigned lane) {
     if (w.size[D.b + D.n - 1] == 2 || w.size[F.b + F.n - 1] == 2) return false;
     const int maxarity = (int)k.xor_max_arity;
     if ((int)w.size[D.b] - 1 > maxarity) return false;
-    const uint32_t v = ABSV(D.lit);
     uint32_t* out = w.outs;
     for (uint32_t i = 0; i < D.n; i++) {
         const uint32_t ci = D.b + i;
@@ -543,11 +534,6 @@ PFG_D bool ws_find_xor_gate(const EK& k, WS& w, const Side& D, const Side& F, ui
         if (itargets) ws_freeze_arities(w, lane);
         else {
             ws_melt(w, ci, 1, lane);
-            nE = 0; nC = 0; nL = 0;
-            if (ws_count_subst(k, w, CNT_SUBS, v, nOrgCls, D, F, nE, nC, nL, lane)) {
-                ws_freeze_arities(w, lane);
-                break;
-            }
             return true;
         }
     }
@@ -674,27 +660,41 @@ PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
     }
     const uint32_t nClsBefore = pOrgs + nOrgs;
     elimType = 0; nE = 0; nC = 0; nL = 0;
-    // each detector is tried for both definitions (the second only while no
-    // substitution was counted) from one call site, so its code exists once
-    if (nClsBefore > 2) {
+    // AND/OR gates for both definitions, then ITE and XOR gates for both
+    // (bounded.cuh:336-356); a second definition is tried only while no
+    // substitution was counted. The substitution of a found gate is counted
+    // here, at one call site for all detectors.
 #pragma unroll 1
-        for (int o = 0; o < 2 && !elimType && !(o && nC); o++) {
-            const Side& D = o ? P : N;
-            const Side& F = o ? N : P;
-            if ((o ? pOrgs : nOrgs) < SH_MAX_BVE_OUT1 && ws_find_ao_gate(k, w, D, F, nClsBefore, nE, nC, nL, lane))
-                elimType = AOIX_MASK;
+    for (int g = 0; g < 6 && !elimType; g++) {
+        const int o = g & 1;
+        if (g < 2 ? nClsBefore <= 2 : nClsBefore <= 3) continue;
+        if (o && nC) continue;
+        // AND/OR: (N, P) then (P, N); ITE and XOR: (P, N) then (N, P)
+        const bool pfirst = g < 2 ? o != 0 : o == 0;
+        const Side& D = pfirst ? P : N;
+        const Side& F = pfirst ? N : P;
+        GateUndo undo{NOREF, NOREF, NOREF, NOREF};
+        bool found;
+        if (g < 2) found = (pfirst ? pOrgs : nOrgs) < SH_MAX_BVE_OUT1 && ws_find_ao_gate(k, w, D, F, undo, lane);
+        else if (g < 4) found = ws_find_ite_gate(k, w, D, F, undo, lane);
+        else found = ws_find_xor_gate(k, w, D, F, lane);
+        if (!found) continue;
+        nE = 0; nC = 0; nL = 0;
+        if (!ws_count_subst(k, w, CNT_SUBS, x, nClsBefore, D, F, nE, nC, nL, lane)) {
+            elimType = AOIX_MASK;
+            break;
         }
-    }
-    if (!elimType && nClsBefore > 3) {
-#pragma unroll 1
-        for (int g = 0; g < 4 && !elimType; g++) {
-            const int o = g & 1;
-            if (o && nC) continue;
-            const Side& D = o ? N : P;
-            const Side& F = o ? P : N;
-            const bool found = g < 2 ? ws_find_ite_gate(k, w, D, F, nClsBefore, nE, nC, nL, lane)
-                                     : ws_find_xor_gate(k, w, D, F, nClsBefore, nE, nC, nL, lane);
-            if (found) elimType = AOIX_MASK;
+        // too many resolvents: undo what the detector melted
+        if (g < 2) {
+            ws_melt(w, undo.a, 0, lane);
+            ws_freeze_binaries(w, D, lane);
+        } else if (g < 4) {
+            ws_melt(w, undo.a, 0, lane);
+            ws_melt(w, undo.b, 0, lane);
+            if (undo.c != NOREF) ws_melt(w, undo.c, 0, lane);
+            if (undo.d != NOREF) ws_melt(w, undo.d, 0, lane);
+        } else {
+            ws_freeze_arities(w, lane);
         }
     }
     if (vc_on(k, x) && !elimType && nClsBefore > 2) {
