@@ -396,37 +396,42 @@ PFG_D bool ws_find_ao_gate(const EK& k, WS& w, const Side& D, const Side& F, Gat
     return false;
 }
 
-// fast_equality_check (ifthenelse.cuh:27-48): first clause (x, y, z) of the
-// shortest of the three lists that is not molten; global id or NOREF
-PFG_D uint32_t ws_fast_eq(const EK& k, const WS& w, uint32_t x, uint32_t y, uint32_t z, unsigned lane) {
-    uint32_t t;
-    if (OLs(k, y) > OLs(k, z)) { t = y; y = z; z = t; }
-    if (OLs(k, x) > OLs(k, y)) { t = x; x = y; y = t; }
-    const uint32_t lst = x;
-    if (z < y) { t = y; y = z; z = t; }
-    if (z < x) { t = x; x = z; z = t; }
-    if (y < x) { t = x; x = y; y = t; }
-    const uint32_t* ol = OLp(k, lst);
-    const uint32_t n = OLs(k, lst);
-    for (uint32_t i0 = 0; i0 < n; i0 += 32) {
+// First staged clause of side S equal to the sorted literals t[0..n) that is
+// original (and not molten when `unmelted`), or NOREF. The reference searches
+// the shortest occurrence list of t's literals (fast_equality_check,
+// ifthenelse.cuh:27-48; makeArity, xor.cuh:69-100). Every clause equal to t
+// holds the eliminated variable's literal, so it is in S as well; equal
+// clauses share their sort key, so the first one in any of those sorted lists
+// is the one with the smallest id -- the first one in S.
+PFG_D uint32_t ws_match(const WS& w, const Side& S, const uint32_t* t, uint32_t n, bool unmelted, unsigned lane) {
+    for (uint32_t i0 = 0; i0 < S.n; i0 += 32) {
         const uint32_t i = i0 + lane;
         bool hit = false;
-        uint32_t id = 0;
-        if (i < n) {
-            id = ol[i];
-            const ClsHdr h = k.hdr[id];
-            if (h.size == 3) {
-                const uint32_t* l = k.lits + h.off;
-                if (l[0] == x && l[1] == y && l[2] == z) {
-                    const uint32_t m = ws_meta_of(k, w, id, lane);
-                    hit = !m_molten(m) && m_orig(m);
-                }
+        if (i < S.n) {
+            const uint32_t c = S.b + i;
+            const uint32_t m = w.meta[c];
+            if (w.size[c] == n && m_orig(m) && !(unmelted && m_molten(m))) {
+                const uint32_t* l = w.lits + w.off[c];
+                hit = true;
+                for (uint32_t q = 0; q < n; q++)
+                    if (l[q] != t[q]) { hit = false; break; }
             }
         }
         const unsigned b = __ballot_sync(FULL, hit);
-        if (b) return __shfl_sync(FULL, id, __ffs(b) - 1);
+        if (b) return S.b + i0 + __ffs(b) - 1;
     }
     return NOREF;
+}
+
+// fast_equality_check (ifthenelse.cuh:27-48) for the clause (fx, y, z):
+// staged index in F, or NOREF
+PFG_D uint32_t ws_fast_eq(const WS& w, const Side& F, uint32_t y, uint32_t z, unsigned lane) {
+    uint32_t x = F.lit, t;
+    if (z < y) { t = y; y = z; z = t; }
+    if (z < x) { t = x; x = z; z = t; }
+    if (y < x) { t = x; x = y; y = t; }
+    const uint32_t c[3] = {x, y, z};
+    return ws_match(w, F, c, 3, true, lane);
 }
 
 // find_ite_gate (ifthenelse.cuh:50-123) up to the substitution count
@@ -450,11 +455,10 @@ PFG_D bool ws_find_ite_gate(const EK& k, WS& w, const Side& D, const Side& F, Ga
             if (ABSV(yi) == ABSV(zj)) { t = yj; yj = zj; zj = t; }
             if (ABSV(zi) == ABSV(zj)) continue;
             if (yi != FLIPL(yj)) continue;
-            const uint32_t r1 = ws_fast_eq(k, w, fx, yi, FLIPL(zi), lane);
-            if (r1 == NOREF) continue;
-            const uint32_t r2 = ws_fast_eq(k, w, fx, yj, FLIPL(zj), lane);
-            if (r2 == NOREF) continue;
-            const uint32_t s1 = ws_find(w, r1, lane), s2 = ws_find(w, r2, lane);
+            const uint32_t s1 = ws_fast_eq(w, F, yi, FLIPL(zi), lane);
+            if (s1 == NOREF) continue;
+            const uint32_t s2 = ws_fast_eq(w, F, yj, FLIPL(zj), lane);
+            if (s2 == NOREF) continue;
             ws_melt(w, ci, 1, lane);
             ws_melt(w, cj, 1, lane);
             if (s1 != NOREF) ws_melt(w, s1, 1, lane);
@@ -474,8 +478,10 @@ PFG_D void ws_freeze_arities(WS& w, unsigned lane) {
     __syncwarp();
 }
 
-// makeArity (xor.cuh:69-100); `lits` is warp-shared
-PFG_D bool ws_make_arity(const EK& k, WS& w, uint32_t& parity, uint32_t* lits, uint32_t size, unsigned lane) {
+// makeArity (xor.cuh:69-100); `lits` is warp-shared. The flipped clause
+// holds the literal of D or of F, and is looked up on that side of the stage.
+PFG_D bool ws_make_arity(WS& w, const Side& D, const Side& F, uint32_t& parity, uint32_t* lits, uint32_t size,
+                         unsigned lane) {
     const uint32_t old = parity;
     do { parity++; } while (__popc(parity) & 1);
     __syncwarp();
@@ -485,33 +491,12 @@ PFG_D bool ws_make_arity(const EK& k, WS& w, uint32_t& parity, uint32_t* lits, u
             if ((parity & bit) != (old & bit)) lits[q] = FLIPL(lits[q]);
         }
     __syncwarp();
-    uint32_t best = lits[0];
-    uint32_t minsize = OLs(k, best);
-    for (uint32_t q = 1; q < size; q++) {
-        const uint32_t ls = OLs(k, lits[q]);
-        if (ls < minsize) { minsize = ls; best = lits[q]; }
-    }
-    const uint32_t* ol = OLp(k, best);
-    const uint32_t n = OLs(k, best);
-    for (uint32_t i0 = 0; i0 < n; i0 += 32) {
-        const uint32_t i = i0 + lane;
-        bool hit = false;
-        uint32_t id = 0;
-        if (i < n) {
-            id = ol[i];
-            const ClsHdr h = k.hdr[id];
-            if (h.size == size && check_arity(k, h, lits, size)) hit = m_orig(ws_meta_of(k, w, id, lane));
-        }
-        const unsigned b = __ballot_sync(FULL, hit);
-        if (b) {
-            id = __shfl_sync(FULL, id, __ffs(b) - 1);
-            const uint32_t s = ws_find(w, id, lane);
-            if (s != NOREF) ws_melt(w, s, 1, lane);
-            else { if (lane == 0) SET_MOLTEN(k, id, 1); __syncwarp(); }
-            return true;
-        }
-    }
-    return false;
+    bool has_d = false;
+    for (uint32_t q = 0; q < size; q++) has_d |= lits[q] == D.lit;
+    const uint32_t s = ws_match(w, has_d ? D : F, lits, size, false, lane);
+    if (s == NOREF) return false;
+    ws_melt(w, s, 1, lane);
+    return true;
 }
 
 // find_xor_gate (xor.cuh:102-178) up to the substitution count
@@ -530,7 +515,7 @@ PFG_D bool ws_find_xor_gate(const EK& k, WS& w, const Side& D, const Side& F, un
         __syncwarp();
         uint32_t parity = 0;
         int itargets = 1 << arity;
-        while (--itargets && ws_make_arity(k, w, parity, out, (uint32_t)size, lane)) {}
+        while (--itargets && ws_make_arity(w, D, F, parity, out, (uint32_t)size, lane)) {}
         if (itargets) ws_freeze_arities(w, lane);
         else {
             ws_melt(w, ci, 1, lane);
