@@ -85,6 +85,7 @@ struct DevCounters {
     uint32_t big_lists;
     uint32_t nbig_sub, nbig_ve1, nbig_ve3;   // variables too large for the warp stage
     unsigned long long ve_cls, ve_lits;      // store size after the last BVE emission
+    uint32_t sort_warp;                      // lists sorted by one warp each
 };
 
 constexpr uint32_t ERR_UNITS_OVERFLOW = 1u;

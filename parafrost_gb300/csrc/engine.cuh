@@ -118,6 +118,7 @@ struct Ctx {
     // big-list sort scratch
     uint32_t* big_lists = nullptr;   // nlist (worst case)
     uint32_t* mid_desc = nullptr;    // descriptors (offset, size) pairs
+    uint32_t* warp_desc = nullptr;   // descriptors of the lists sorted by one warp
     uint64_t mid_desc_cap = 0;
     uint4* big_keys = nullptr; uint4* big_keys_alt = nullptr;
     uint32_t* big_ids = nullptr; uint32_t* big_ids_alt = nullptr;

@@ -8,8 +8,9 @@
 //   2. an exclusive scan into CSR offsets,
 //   3. an atomic scatter of clause ids,
 //   4. a size-tiered segmented sort by the OLIST_CMP key (key.cuh:67-85):
-//      thread-per-list insertion sort (<= 16), block bitonic sort in shared
-//      memory (<= 2048), chunk sort + merge-path passes for longer lists.
+//      insertion sort, a thread per list (<= 16 entries); shuffle bitonic
+//      network, a warp per list (<= 64); block bitonic sort in shared
+//      memory (<= 2048); chunk sort + merge-path passes for longer lists.
 #include <algorithm>
 #include <vector>
 
@@ -19,6 +20,7 @@ namespace pfg {
 namespace {
 
 constexpr uint32_t SMALL_MAX = 16;
+constexpr uint32_t WARP_MAX = 64;
 constexpr uint32_t MID_MAX = 2048;
 constexpr int MID_THREADS = 256;
 
@@ -113,12 +115,17 @@ PFG_D bool kless(const uint4& a, uint32_t ia, const uint4& b, uint32_t ib) {
 
 __global__ void sort_small_k(const uint4* keys, uint64_t nlist,
                              const uint32_t* off, const uint32_t* size, uint32_t* ids,
-                             uint32_t* mid_desc, uint32_t* mid_cnt, uint32_t* big_lists, uint32_t* big_cnt) {
+                             uint32_t* mid_desc, uint32_t* mid_cnt, uint32_t* big_lists, uint32_t* big_cnt,
+                             uint32_t* warp_desc, uint32_t* warp_cnt) {
     for (uint64_t l = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlist; l += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t n = size[l];
         if (n < 2) continue;
         if (n > SMALL_MAX) {
-            if (n <= MID_MAX) {
+            if (n <= WARP_MAX) {
+                const uint32_t q = atomicAdd(warp_cnt, 1u);
+                warp_desc[2 * q] = off[l];
+                warp_desc[2 * q + 1] = n;
+            } else if (n <= MID_MAX) {
                 const uint32_t q = atomicAdd(mid_cnt, 1u);
                 mid_desc[2 * q] = off[l];
                 mid_desc[2 * q + 1] = n;
@@ -139,6 +146,55 @@ __global__ void sort_small_k(const uint4* keys, uint64_t nlist,
             k[j] = tk; id[j] = ti;
         }
         for (uint32_t i = 0; i < n; i++) L[i] = id[i];
+    }
+}
+
+// One list of 17..64 entries per warp: lane holds positions lane and lane+32;
+// a bitonic network with shuffles for partners in the same half.
+PFG_D void warp_cx(uint4& k, uint32_t& id, int j, bool keep_min) {
+    uint4 o;
+    o.x = __shfl_xor_sync(0xFFFFFFFFu, k.x, j);
+    o.y = __shfl_xor_sync(0xFFFFFFFFu, k.y, j);
+    o.z = __shfl_xor_sync(0xFFFFFFFFu, k.z, j);
+    o.w = __shfl_xor_sync(0xFFFFFFFFu, k.w, j);
+    const uint32_t oid = __shfl_xor_sync(0xFFFFFFFFu, id, j);
+    const bool other_less = kless(o, oid, k, id);
+    if (other_less == keep_min) { k = o; id = oid; }
+}
+
+__global__ void sort_warp_k(const uint4* keys, const uint32_t* desc, const uint32_t* count, uint32_t* ids) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t nd = *count;
+    const uint4 pad = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nd; q += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t o = desc[2 * q], n = desc[2 * q + 1];
+        uint32_t* L = ids + o;
+        uint32_t ia = lane < n ? L[lane] : 0xFFFFFFFFu;
+        uint32_t ib = lane + 32 < n ? L[lane + 32] : 0xFFFFFFFFu;
+        uint4 ka = lane < n ? keys[ia] : pad;
+        uint4 kb = lane + 32 < n ? keys[ib] : pad;
+#pragma unroll
+        for (int sz = 2; sz <= 64; sz <<= 1) {
+#pragma unroll
+            for (int j = sz >> 1; j > 0; j >>= 1) {
+                const bool asc_a = (lane & sz) == 0;          // position lane
+                const bool asc_b = ((lane + 32) & sz) == 0;   // position lane + 32
+                if (j == 32) {
+                    // partners in the same lane: a (lower position) keeps the min when ascending
+                    const bool sw = asc_a ? kless(kb, ib, ka, ia) : kless(ka, ia, kb, ib);
+                    if (sw) {
+                        const uint4 tk = ka; ka = kb; kb = tk;
+                        const uint32_t ti = ia; ia = ib; ib = ti;
+                    }
+                } else {
+                    const bool lower = (lane & j) == 0;
+                    warp_cx(ka, ia, j, lower == asc_a);
+                    warp_cx(kb, ib, j, lower == asc_b);
+                }
+            }
+        }
+        if (lane < n) L[lane] = ia;
+        if (lane + 32 < n) L[lane + 32] = ib;
     }
 }
 
@@ -295,8 +351,13 @@ bool ot_sort(Ctx& c, bool by_id) {
     const uint64_t want_desc = std::max<uint64_t>(1024, c.numLiterals / (SMALL_MAX + 1) + 1);
     if (c.mid_desc_cap < want_desc) {
         dfree(c, c.mid_desc);
-        c.mid_desc = nullptr;
-        if (!dalloc_t(c, &c.mid_desc, 2 * want_desc)) { c.simpstate = PFG_OTALLOC_FAIL; return false; }
+        dfree(c, c.warp_desc);
+        c.mid_desc = c.warp_desc = nullptr;
+        if (!dalloc_t(c, &c.mid_desc, 2 * want_desc) || !dalloc_t(c, &c.warp_desc, 2 * want_desc)) {
+            c.simpstate = PFG_OTALLOC_FAIL;
+            c.mid_desc_cap = 0;
+            return false;
+        }
         c.mid_desc_cap = want_desc;
     }
     if (c.ckeys_cap < c.ncls) {
@@ -309,8 +370,12 @@ bool ot_sort(Ctx& c, bool by_id) {
     PFG_LAUNCH(K_SORT_SMALL, ckeys_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.ckeys, by_id);
     cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
+    cudaMemsetAsync(&c.dc->sort_warp, 0, sizeof(uint32_t), c.s);
     PFG_LAUNCH(K_SORT_SMALL, sort_small_k, grid_for(nl, 256), 256, 0, c.s, c.ckeys, nl, c.ot_off, c.ot_size, c.ot_ids,
-               c.mid_desc, &c.dc->nwin, c.big_lists, &c.dc->big_lists);
+               c.mid_desc, &c.dc->nwin, c.big_lists, &c.dc->big_lists, c.warp_desc, &c.dc->sort_warp);
+    // lists of 17..64 entries: a warp each; the grid walks the device-side count
+    PFG_LAUNCH(K_SORT_MID, sort_warp_k, grid_for(c.numLiterals * 32 / (SMALL_MAX + 1) + 32, 256, 16), 256, 0, c.s,
+               c.ckeys, c.warp_desc, &c.dc->sort_warp, c.ot_ids);
     sync_counters(c);
     const uint32_t nmid = c.hc->nwin, nbig = c.hc->big_lists;
     if (nmid) {
