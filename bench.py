@@ -611,7 +611,10 @@ def run_gpu_batch(a, world, rank, local):
 
 # DRAM traffic per launch of the dominant kernel group from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (workload, group).
-TRAFFIC = {}
+TRAFFIC = {
+    # profiles/ve1w_k_batched.md: 12.186 GB read + 2.175 GB written over the 5 launches of one step
+    ("batched", "ve_phase1"): (12.186e9 + 2.175e9) / 5,
+}
 
 
 def main():
