@@ -377,11 +377,12 @@ PFG_D bool find_ao_gate(const EK& k, uint32_t dx, uint32_t fx, uint32_t nOrgCls,
     return false;
 }
 
-// fast_equality_check (ifthenelse.cuh:27-48)
+// fast_equality_check (ifthenelse.cuh:27-48). The reference searches the
+// shortest of the three lists; every clause (x, y, z) holds x, the eliminated
+// variable's literal, and equal clauses share their sort key, so the first
+// match in x's own list is the same clause.
 PFG_D uint32_t fast_equality_check(const EK& k, uint32_t x, uint32_t y, uint32_t z) {
     uint32_t t;
-    if (OLs(k, y) > OLs(k, z)) { t = y; y = z; z = t; }
-    if (OLs(k, x) > OLs(k, y)) { t = x; x = y; y = t; }
     const uint32_t lst = x;
     if (z < y) { t = y; y = z; z = t; }
     if (z < x) { t = x; x = z; z = t; }
@@ -465,8 +466,10 @@ PFG_D bool check_arity(const EK& k, const ClsHdr& h, const uint32_t* lits, uint3
     return true;
 }
 
-// makeArity (xor.cuh:69-100)
-PFG_D bool make_arity(const EK& k, uint32_t& parity, uint32_t* lits, uint32_t size) {
+// makeArity (xor.cuh:69-100). The flipped clause holds a literal of the
+// eliminated variable v; it is looked up in that literal's own list (the
+// reference takes the shortest list of the clause; the first match is the same).
+PFG_D bool make_arity(const EK& k, uint32_t v, uint32_t& parity, uint32_t* lits, uint32_t size) {
     const uint32_t old = parity;
     do { parity++; } while (__popc(parity) & 1);
     for (uint32_t q = 0; q < size; q++) {
@@ -474,11 +477,8 @@ PFG_D bool make_arity(const EK& k, uint32_t& parity, uint32_t* lits, uint32_t si
         if ((parity & bit) != (old & bit)) lits[q] = FLIPL(lits[q]);
     }
     uint32_t best = lits[0];
-    uint32_t minsize = OLs(k, best);
-    for (uint32_t q = 1; q < size; q++) {
-        const uint32_t ls = OLs(k, lits[q]);
-        if (ls < minsize) { minsize = ls; best = lits[q]; }
-    }
+    for (uint32_t q = 0; q < size; q++)
+        if (ABSV(lits[q]) == v) best = lits[q];
     const uint32_t* ol = OLp(k, best);
     const uint32_t n = OLs(k, best);
     for (uint32_t i = 0; i < n; i++) {
@@ -509,7 +509,7 @@ PFG_D bool find_xor_gate(const EK& k, uint32_t dx, uint32_t fx, uint32_t nOrgCls
         for (int q = 0; q < size; q++) out[q] = l[q];
         uint32_t parity = 0;
         int itargets = 1 << arity;
-        while (--itargets && make_arity(k, parity, out, (uint32_t)size)) {}
+        while (--itargets && make_arity(k, v, parity, out, (uint32_t)size)) {}
         if (itargets) freeze_arities(k, dx, fx);
         else {
             SET_MOLTEN(k, ci, 1);

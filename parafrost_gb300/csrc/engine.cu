@@ -816,10 +816,6 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
             if (c.ih[i].nelected < c.o.lcve_min_vars) c.ih[i].active = false;
         act = active_ids(c);
         if (act.empty()) break;
-        {
-            PassTimer t(c, 0);
-            if (!ot_sort(c, false)) break;
-        }
         // stop() (solver.hpp:748-753) per instance: the last round runs ERE instead of SUB+BVE
         uint32_t nmode1 = 0, nmode2 = 0;
         for (uint32_t i : act) {
@@ -844,6 +840,15 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         c.hi.seg[n] = acc_seg;
         push_inst_in(c);
         c.nere = nmode2 ? select_mode(c, 2, c.ereset) : 0;
+        c.nve = nmode1 ? select_mode(c, 1, c.veset) : 0;
+        // sortOT (segsort.cu:37). A SUB+BVE round reads in list order only the
+        // lists of its elected variables (staging, subsumption order, witness and
+        // resolvent order; gate lookups search those lists too), so only they are
+        // sorted; ERE searches the lists of every literal of a resolvent.
+        if (c.nere || c.nve) {
+            PassTimer t(c, 0);
+            if (!(c.nere ? ot_sort(c, false) : ot_sort(c, false, c.veset, c.nve))) break;
+        }
         if (c.nere) {
             cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
             PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nere, 256), 256, 0, c.s, c.ereset, c.nere, c.hdr,
@@ -854,7 +859,6 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
             ere_pass(c);
         }
         if (!nmode1) break;
-        c.nve = select_mode(c, 1, c.veset);
         // byte model: C_E, L_E of this round
         cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
         PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nve, 256), 256, 0, c.s, c.veset, c.nve, c.hdr, c.ot_off,

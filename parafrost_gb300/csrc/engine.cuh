@@ -212,7 +212,9 @@ bool cuda_ok(Ctx& c, cudaError_t e, const char* what);
 // ---- passes ----
 // occurrence table (ot.cu)
 bool ot_build(Ctx& c);          // histogram + CSR offsets + unsorted fill (clause order irrelevant)
-bool ot_sort(Ctx& c, bool by_id);  // sort every list by OLIST_CMP (key.cuh:67-85) or by clause id
+// sort lists by OLIST_CMP (key.cuh:67-85) or by clause id: all of them, or the two
+// lists of every variable in vlist[0..nv)
+bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist = nullptr, uint32_t nv = 0);
 bool ot_filter(Ctx& c, const uint8_t* assigned);   // drop what unit propagation removed from the lists
 // counting + compaction (gc.cu)
 void count_live(Ctx& c);        // totals into counters, per instance into dout.cnt (read after a sync)

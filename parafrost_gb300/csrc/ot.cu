@@ -113,11 +113,14 @@ PFG_D bool kless(const uint4& a, uint32_t ia, const uint4& b, uint32_t ib) {
     return ia < ib;
 }
 
-__global__ void sort_small_k(const uint4* keys, uint64_t nlist,
+// All lists (vlist null, count = number of lists) or the two lists of each
+// variable of vlist[0..count/2).
+__global__ void sort_small_k(const uint4* keys, const uint32_t* vlist, uint64_t count,
                              const uint32_t* off, const uint32_t* size, uint32_t* ids,
                              uint32_t* mid_desc, uint32_t* mid_cnt, uint32_t* big_lists, uint32_t* big_cnt,
                              uint32_t* warp_desc, uint32_t* warp_cnt) {
-    for (uint64_t l = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlist; l += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t l = vlist ? 2ull * vlist[t >> 1] + (t & 1) : t;
         const uint32_t n = size[l];
         if (n < 2) continue;
         if (n > SMALL_MAX) {
@@ -345,8 +348,9 @@ bool ot_filter(Ctx& c, const uint8_t* assigned) {
     return cuda_ok(c, cudaGetLastError(), "ot_filter");
 }
 
-bool ot_sort(Ctx& c, bool by_id) {
+bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist, uint32_t nv) {
     const uint64_t nl = c.nlist;
+    const uint64_t count = vlist ? 2ull * nv : nl;
     // worst case: every list is mid-sized
     const uint64_t want_desc = std::max<uint64_t>(1024, c.numLiterals / (SMALL_MAX + 1) + 1);
     if (c.mid_desc_cap < want_desc) {
@@ -371,8 +375,9 @@ bool ot_sort(Ctx& c, bool by_id) {
     cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->sort_warp, 0, sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_SORT_SMALL, sort_small_k, grid_for(nl, 256), 256, 0, c.s, c.ckeys, nl, c.ot_off, c.ot_size, c.ot_ids,
-               c.mid_desc, &c.dc->nwin, c.big_lists, &c.dc->big_lists, c.warp_desc, &c.dc->sort_warp);
+    PFG_LAUNCH(K_SORT_SMALL, sort_small_k, grid_for(count, 256), 256, 0, c.s, c.ckeys, vlist, count, c.ot_off,
+               c.ot_size, c.ot_ids, c.mid_desc, &c.dc->nwin, c.big_lists, &c.dc->big_lists, c.warp_desc,
+               &c.dc->sort_warp);
     // lists of 17..64 entries: a warp each; the grid walks the device-side count
     PFG_LAUNCH(K_SORT_MID, sort_warp_k, grid_for(c.numLiterals * 32 / (SMALL_MAX + 1) + 32, 256, 16), 256, 0, c.s,
                c.ckeys, c.warp_desc, &c.dc->sort_warp, c.ot_ids);
