@@ -88,6 +88,8 @@ __global__ void bcp_advance_k(DevCounters* dc) {
 }
 
 // warp per frontier literal, lanes stride its occurrence list
+constexpr uint32_t BCP_GROUP = 32;
+
 __global__ void bcp_propagate_k(BK k, const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off,
                                 const uint32_t* ot_size, const uint32_t* ot_ids, const uint32_t* front_a,
                                 uint32_t* front_b) {
@@ -96,15 +98,15 @@ __global__ void bcp_propagate_k(BK k, const ClsHdr* hdr, const uint32_t* lits, c
     const uint32_t* cur = (level & 1u) ? front_b : (uint32_t*)front_a;
     uint32_t* nxt = (level & 1u) ? (uint32_t*)front_a : front_b;
     const uint32_t n = dc->bcp_curr;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const unsigned lane = threadIdx.x & 31u;
-    for (uint32_t fi = warp; fi < n; fi += nwarps) {
+    const uint32_t group = (blockIdx.x * blockDim.x + threadIdx.x) / BCP_GROUP;
+    const uint32_t ngroups = (gridDim.x * blockDim.x) / BCP_GROUP;
+    const uint32_t lane = threadIdx.x % BCP_GROUP;
+    for (uint32_t fi = group; fi < n; fi += ngroups) {
         const uint32_t f = cur[fi];
         const uint32_t inst = k.vinst[ABSV(f)];
         if (k.conflict[inst]) continue;       // this instance is UNSAT: stop propagating it
         const uint32_t o = ot_off[f], sz = ot_size[f];
-        for (uint32_t j = lane; j < sz; j += 32) {
+        for (uint32_t j = lane; j < sz; j += BCP_GROUP) {
             const ClsHdr h = hdr[ot_ids[o + j]];
             if (m_deleted(h.meta)) continue;
             uint32_t unit = 0;

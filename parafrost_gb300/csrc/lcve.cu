@@ -65,6 +65,11 @@ __global__ void mis_init_k(const uint32_t* eligible, uint32_t V, uint32_t* rank,
     }
 }
 
+// The first MIS_HEAD literals of a clause are loaded together, then their
+// states, then the ranks of the undecided ones: independent loads in flight
+// instead of one dependent chain per literal (most clauses are that short).
+constexpr uint32_t MIS_HEAD = 4;
+
 PFG_D bool blocked(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
                    const uint32_t* ot_ids, uint32_t lit, uint32_t cand, uint32_t r, const uint32_t* rank,
                    const uint8_t* mstate) {
@@ -72,9 +77,19 @@ PFG_D bool blocked(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_o
     for (uint32_t i = 0; i < n; i++) {
         const ClsHdr h = hdr[ot_ids[o + i]];
         if (m_deleted(h.meta)) continue;
-        for (uint32_t k = 0; k < h.size; k++) {
-            const uint32_t u = ABSV(lits[h.off + k]);
-            if (u != cand && mstate[u] == MIS_UNDECIDED && rank[u] < r) return true;
+        const uint32_t* l = lits + h.off;
+        uint32_t u[MIS_HEAD];
+        uint8_t st[MIS_HEAD];
+#pragma unroll
+        for (uint32_t q = 0; q < MIS_HEAD; q++) u[q] = q < h.size ? ABSV(l[q]) : cand;
+#pragma unroll
+        for (uint32_t q = 0; q < MIS_HEAD; q++) st[q] = u[q] != cand ? mstate[u[q]] : MIS_NONE;
+#pragma unroll
+        for (uint32_t q = 0; q < MIS_HEAD; q++)
+            if (st[q] == MIS_UNDECIDED && rank[u[q]] < r) return true;
+        for (uint32_t k = MIS_HEAD; k < h.size; k++) {
+            const uint32_t v = ABSV(l[k]);
+            if (v != cand && mstate[v] == MIS_UNDECIDED && rank[v] < r) return true;
         }
     }
     return false;
@@ -86,11 +101,24 @@ PFG_D void freeze_list(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* 
     for (uint32_t i = 0; i < n; i++) {
         const ClsHdr h = hdr[ot_ids[o + i]];
         if (m_deleted(h.meta)) continue;
-        for (uint32_t k = 0; k < h.size; k++) {
-            const uint32_t u = ABSV(lits[h.off + k]);
-            if (u != cand) {
-                frozen[u] = 1;
-                if (mstate[u] == MIS_UNDECIDED) mstate[u] = MIS_FROZEN;
+        const uint32_t* l = lits + h.off;
+        uint32_t u[MIS_HEAD];
+        uint8_t st[MIS_HEAD];
+#pragma unroll
+        for (uint32_t q = 0; q < MIS_HEAD; q++) u[q] = q < h.size ? ABSV(l[q]) : cand;
+#pragma unroll
+        for (uint32_t q = 0; q < MIS_HEAD; q++) st[q] = u[q] != cand ? mstate[u[q]] : MIS_NONE;
+#pragma unroll
+        for (uint32_t q = 0; q < MIS_HEAD; q++) {
+            if (u[q] == cand) continue;
+            frozen[u[q]] = 1;
+            if (st[q] == MIS_UNDECIDED) mstate[u[q]] = MIS_FROZEN;
+        }
+        for (uint32_t k = MIS_HEAD; k < h.size; k++) {
+            const uint32_t v = ABSV(l[k]);
+            if (v != cand) {
+                frozen[v] = 1;
+                if (mstate[v] == MIS_UNDECIDED) mstate[v] = MIS_FROZEN;
             }
         }
     }
