@@ -217,6 +217,16 @@ int  pfg_batch_download(pfg_ctx* ctx, uint32_t i, uint32_t* lits, uint64_t* cls_
                         uint8_t* cls_learnt, uint32_t* cls_lbd, uint8_t* cls_usage,
                         uint8_t* eliminated, uint32_t* units, uint32_t* pending_units,
                         uint32_t* stack, uint64_t* round_ends);
+/* The same for all instances at once: sizes[0..n), then every output holds the
+   instances back to back in instance order, each part laid out as
+   pfg_batch_download writes it (cls_off: clauses + 1 entries from 0,
+   eliminated: max_var + 1 entries). One copy per output instead of one per
+   instance and output. */
+int  pfg_batch_result_sizes_all(pfg_ctx* ctx, pfg_result_sizes* sizes);
+int  pfg_batch_download_all(pfg_ctx* ctx, uint32_t* lits, uint64_t* cls_off,
+                            uint8_t* cls_learnt, uint32_t* cls_lbd, uint8_t* cls_usage,
+                            uint8_t* eliminated, uint32_t* units, uint32_t* pending_units,
+                            uint32_t* stack, uint64_t* round_ends);
 
 /*
  * The simplified CNF of a one-instance context written straight into

@@ -52,6 +52,10 @@ def lib():
     L.pfg_batch_result_sizes.restype = C.c_int
     L.pfg_batch_download.argtypes = [C.c_void_p, C.c_uint32, u32p, u64p, u8p, u32p, u8p, u8p, u32p, u32p, u32p, u64p]
     L.pfg_batch_download.restype = C.c_int
+    L.pfg_batch_result_sizes_all.argtypes = [C.c_void_p, C.POINTER(PfgResultSizes)]
+    L.pfg_batch_result_sizes_all.restype = C.c_int
+    L.pfg_batch_download_all.argtypes = [C.c_void_p, u32p, u64p, u8p, u32p, u8p, u8p, u32p, u32p, u32p, u64p]
+    L.pfg_batch_download_all.restype = C.c_int
     L.pfg_download_device_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.pfg_download_device_noalloc.restype = C.c_int
     L.pfg_server_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(PfgOptions), C.c_size_t, C.c_uint32, C.c_uint32]
@@ -97,6 +101,6 @@ EXPORTED = (
     "pfg_result_sizes_get", "pfg_download", "pfg_destroy", "pfg_last_error", "pfg_kernel_launches",
     "pfg_generate", "pfg_profile_enable", "pfg_profile_reset", "pfg_profile_count", "pfg_profile_name",
     "pfg_profile_get", "pfg_batch_upload", "pfg_batch_size", "pfg_batch_stats", "pfg_batch_result_sizes",
-    "pfg_batch_download", "pfg_download_device_noalloc", "pfg_server_create", "pfg_server_submit",
+    "pfg_batch_download", "pfg_batch_result_sizes_all", "pfg_batch_download_all", "pfg_download_device_noalloc", "pfg_server_create", "pfg_server_submit",
     "pfg_server_poll", "pfg_server_fetch", "pfg_server_stats_get", "pfg_server_destroy", "pfg_server_last_error",
 )

@@ -5,9 +5,11 @@
 // pfg_download / pfg_batch_download the write-back (cacheCNF cnf.cu:200-236,
 // cacheEliminated transfer.cu:69, cacheResolved transfer.cu:83).
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -296,6 +298,13 @@ __global__ void gathered_pack_k(const ClsHdr* hdr, const uint32_t* lits, const u
     }
 }
 
+// offsets relative to the instance: minus the instance's first packed literal
+__global__ void relative_off_k(const uint32_t* inst_of, uint64_t n, const unsigned long long* lit_base,
+                               unsigned long long* off) {
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x)
+        off[j] -= lit_base[inst_of[j]];
+}
+
 void free_all(pfg_ctx* o) {
     Ctx& c = o->c;
     std::vector<void*> ptrs;
@@ -330,26 +339,58 @@ struct PassTimer {
     }
 };
 
-bool valid_instance(Ctx& c, uint32_t idx, const pfg_instance& q, std::vector<uint64_t>& seen) {
+// Host checks of one instance (literal range, clause size >= 2, no duplicate or
+// complementary literals); also counts its original clauses and literals.
+bool valid_instance(uint32_t idx, const pfg_instance& q, std::vector<uint64_t>& seen, std::string& err,
+                    uint64_t& orig_cls, uint64_t& orig_lits) {
     const std::string who = "instance " + std::to_string(idx) + ": ";
+    orig_cls = orig_lits = 0;
     if (q.max_var == 0 || q.max_var > 0x7FFFFFF0u || (q.num_clauses && (!q.lits || !q.cls_off))) {
-        c.err = who + "invalid arguments";
+        err = who + "invalid arguments";
         return false;
     }
-    if (q.num_clauses && q.cls_off[0] != 0) { c.err = who + "cls_off[0] must be 0"; return false; }
-    // literal range, clause size >= 2, no duplicate or complementary literals
+    if (q.num_clauses && q.cls_off[0] != 0) { err = who + "cls_off[0] must be 0"; return false; }
     const uint64_t nlits = q.num_clauses ? q.cls_off[q.num_clauses] : 0;
     seen.assign((size_t)q.max_var + 1, ~0ull);
     for (uint64_t i = 0; i < q.num_clauses; i++) {
         const uint64_t b = q.cls_off[i], e = q.cls_off[i + 1];
-        if (e < b + 2 || e > nlits) { c.err = who + "clause " + std::to_string(i) + " has fewer than 2 literals"; return false; }
+        if (e < b + 2 || e > nlits) { err = who + "clause " + std::to_string(i) + " has fewer than 2 literals"; return false; }
         for (uint64_t k = b; k < e; k++) {
             const uint32_t l = q.lits[k], v = l >> 1;
-            if (v == 0 || v > q.max_var) { c.err = who + "literal out of range in clause " + std::to_string(i); return false; }
-            if (seen[v] == i) { c.err = who + "repeated variable in clause " + std::to_string(i); return false; }
+            if (v == 0 || v > q.max_var) { err = who + "literal out of range in clause " + std::to_string(i); return false; }
+            if (seen[v] == i) { err = who + "repeated variable in clause " + std::to_string(i); return false; }
             seen[v] = i;
         }
+        if (!(q.cls_learnt && q.cls_learnt[i])) { orig_cls++; orig_lits += e - b; }
     }
+    return true;
+}
+
+// valid_instance over all instances on the host's cores; the first failing
+// instance (lowest index) is reported
+bool valid_instances(Ctx& c, uint32_t n, const pfg_instance* in, std::vector<uint64_t>& orig_cls,
+                     std::vector<uint64_t>& orig_lits) {
+    orig_cls.assign(n, 0);
+    orig_lits.assign(n, 0);
+    std::vector<std::string> errs(n);
+    std::vector<uint8_t> ok(n, 1);
+    std::atomic<uint32_t> next{0};
+    auto work = [&]() {
+        std::vector<uint64_t> seen;
+        for (uint32_t i = next.fetch_add(1); i < n; i = next.fetch_add(1))
+            ok[i] = valid_instance(i, in[i], seen, errs[i], orig_cls[i], orig_lits[i]) ? 1 : 0;
+    };
+    const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const uint32_t nt = std::min<uint32_t>(n, std::min<uint32_t>(hw, 64));
+    if (nt <= 1) {
+        work();
+    } else {
+        std::vector<std::thread> th;
+        for (uint32_t t = 0; t < nt; t++) th.emplace_back(work);
+        for (std::thread& t : th) t.join();
+    }
+    for (uint32_t i = 0; i < n; i++)
+        if (!ok[i]) { c.err = errs[i]; return false; }
     return true;
 }
 
@@ -363,16 +404,13 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
     // the global range: clause signatures (1 << (lit & 31)) and with them the
     // occurrence-list order are the ones of the instance alone.
     uint64_t Vtot = 0, Ctot = 0, Ltot = 0;
-    std::vector<uint64_t> voffs(n + 1, 0);
-    {
-        std::vector<uint64_t> seen;
-        for (uint32_t i = 0; i < n; i++) {
-            if (!valid_instance(c, i, in[i], seen)) return PFG_INVALID;
-            Vtot = voffs[i] + in[i].max_var;
-            voffs[i + 1] = (i + 1 < n) ? ((Vtot + 15) & ~15ull) : Vtot;
-            Ctot += in[i].num_clauses;
-            Ltot += in[i].num_clauses ? in[i].cls_off[in[i].num_clauses] : 0;
-        }
+    std::vector<uint64_t> voffs(n + 1, 0), orig_cls, orig_lits;
+    if (!valid_instances(c, n, in, orig_cls, orig_lits)) return PFG_INVALID;
+    for (uint32_t i = 0; i < n; i++) {
+        Vtot = voffs[i] + in[i].max_var;
+        voffs[i + 1] = (i + 1 < n) ? ((Vtot + 15) & ~15ull) : Vtot;
+        Ctot += in[i].num_clauses;
+        Ltot += in[i].num_clauses ? in[i].cls_off[in[i].num_clauses] : 0;
     }
     if (Vtot > 0x7FFFFFF0ull) { c.err = "total variables exceed 2^31"; return PFG_INVALID; }
     const uint64_t base_launches = g_launches;
@@ -399,8 +437,8 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
         const uint64_t L = q.num_clauses ? q.cls_off[q.num_clauses] : 0;
         h.V = q.max_var;
         h.voff = (uint32_t)voffs[i];
-        for (uint64_t k = 0; k < q.num_clauses; k++)
-            if (!(q.cls_learnt && q.cls_learnt[k])) { h.orig_cls++; h.orig_lits += q.cls_off[k + 1] - q.cls_off[k]; }
+        h.orig_cls = orig_cls[i];
+        h.orig_lits = orig_lits[i];
         h.cls_in = h.numClauses = q.num_clauses;
         h.lits_in = h.numLiterals = L;
         clsbase[i + 1] = clsbase[i] + q.num_clauses;
@@ -966,6 +1004,12 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
     return finish(c, st, base_launches, rc);
 }
 
+namespace pfg {
+namespace {
+int build_cache(Ctx& c);
+}  // namespace
+}  // namespace pfg
+
 extern "C" int pfg_batch_stats(pfg_ctx* o, uint32_t i, pfg_stats* st) {
     if (!o || !st) return PFG_INVALID;
     Ctx& c = o->c;
@@ -983,13 +1027,10 @@ extern "C" int pfg_batch_stats(pfg_ctx* o, uint32_t i, pfg_stats* st) {
     s.literals_processed = h.processed_lits;
     s.resolvents = h.resolvents;
     s.stack_words = c.hout.scount[i];
-    std::vector<uint8_t> el(h.V);
-    cudaMemcpy(el.data(), c.elim + h.voff + 1, h.V, cudaMemcpyDeviceToHost);
-    s.eliminated = s.forced = 0;
-    for (uint8_t b : el) {
-        if (b & FORCED_MASK) s.forced++;
-        else if (b) s.eliminated++;
-    }
+    const int rc = build_cache(c);
+    if (rc != PFG_OK) return rc;
+    s.eliminated = c.cache_elim_cnt[i];
+    s.forced = c.cache_forced_cnt[i];
     *st = s;
     return PFG_OK;
 }
@@ -1076,83 +1117,70 @@ extern "C" int pfg_download(pfg_ctx* o, uint32_t* lits, uint64_t* cls_off, uint8
 namespace pfg {
 namespace {
 
-// Gathers every instance's results to the host once: live clauses grouped by
-// instance (clause order kept) with literals back in the instance's numbering,
-// the eliminated bytes, the trail and the model-stack regions.
+// Packs every instance's live clauses once: grouped by instance (clause order
+// kept), literals back in the instance's numbering, offsets relative to the
+// instance. Per-instance eliminated / forced counts come from one copy of the
+// eliminated bytes.
 int build_cache(Ctx& c) {
     if (c.cache_ready) return PFG_OK;
     const uint32_t n = c.ninst;
     pull_inst_out(c);
     const uint64_t N = c.ncls;
-    uint64_t C = 0;
-    for (uint32_t i = 0; i < n; i++) C += c.ih[i].numClauses;
-    uint32_t *k0 = nullptr, *v0 = nullptr, *k1 = nullptr, *v1 = nullptr, *olits = nullptr, *olbd = nullptr;
-    unsigned long long* loff = nullptr;
-    uint8_t *olearnt = nullptr, *ousage = nullptr;
+    c.cache_cls_base.assign((size_t)n + 1, 0);
+    c.cache_lit_base.assign((size_t)n + 1, 0);
+    for (uint32_t i = 0; i < n; i++) {
+        c.cache_cls_base[i + 1] = c.cache_cls_base[i] + c.ih[i].numClauses;
+        c.cache_lit_base[i + 1] = c.cache_lit_base[i] + c.ih[i].numLiterals;
+    }
+    const uint64_t C = c.cache_cls_base[n];
+    dfree(c, c.pk_lits); dfree(c, c.pk_roff); dfree(c, c.pk_learnt); dfree(c, c.pk_lbd); dfree(c, c.pk_usage);
+    c.pk_lits = nullptr; c.pk_roff = nullptr; c.pk_learnt = nullptr; c.pk_lbd = nullptr; c.pk_usage = nullptr;
+    uint32_t *k0 = nullptr, *v0 = nullptr, *k1 = nullptr, *v1 = nullptr;
+    unsigned long long* bases = nullptr;
     bool ok = dalloc_t(c, &k0, N + 1) && dalloc_t(c, &v0, N + 1) && dalloc_t(c, &k1, N + 1) &&
-              dalloc_t(c, &v1, N + 1) && dalloc_t(c, &loff, C + 1) && dalloc_t(c, &olits, c.numLiterals + 1) &&
-              dalloc_t(c, &olbd, C + 1) && dalloc_t(c, &olearnt, C + 1) && dalloc_t(c, &ousage, C + 1) &&
+              dalloc_t(c, &v1, N + 1) && dalloc_t(c, &bases, (size_t)n + 1) &&
+              dalloc_t(c, &c.pk_roff, C + 1) && dalloc_t(c, &c.pk_lits, c.numLiterals + 1) &&
+              dalloc_t(c, &c.pk_lbd, C + 1) && dalloc_t(c, &c.pk_learnt, C + 1) && dalloc_t(c, &c.pk_usage, C + 1) &&
               ensure_tmp(c, std::max(radix_temp_bytes(N + 1), scan_temp_bytes(C + 1)));
-    auto release = [&]() {
-        dfree(c, k0); dfree(c, v0); dfree(c, k1); dfree(c, v1); dfree(c, loff); dfree(c, olits);
-        dfree(c, olbd); dfree(c, olearnt); dfree(c, ousage);
-    };
+    auto release = [&]() { dfree(c, k0); dfree(c, v0); dfree(c, k1); dfree(c, v1); dfree(c, bases); };
     if (!ok) { release(); return PFG_CNFALLOC_FAIL; }
     uint32_t* ids = v0;
+    uint32_t* keys = k0;
     if (N) {
         int bits = 0;
         while (bits < 32 && (n >> bits)) bits += 8;
         PFG_LAUNCH(K_DOWNLOAD, cls_inst_keys_k, grid_for(N, 256), 256, 0, c.s, c.hdr, c.lits, N, c.vinst, n, k0, v0);
         const int which = radix_sort_pairs(k0, v0, k1, v1, N, 0, bits, c.tmp, c.s);
         ids = which ? v1 : v0;
+        keys = which ? k1 : k0;
     }
     if (C) {
-        PFG_LAUNCH(K_DOWNLOAD, gathered_sizes_k, grid_for(C, 256), 256, 0, c.s, c.hdr, ids, C, loff);
-        exclusive_scan_u64(loff, loff, C, 0ull, loff + C, c.tmp, c.s);
-        PFG_LAUNCH(K_DOWNLOAD, gathered_pack_k, grid_for(C * 32, 256), 256, 0, c.s, c.hdr, c.lits, ids, C, loff,
-                   c.vinst, c.di.voff, olits, olearnt, olbd, ousage);
-    } else {
-        cudaMemsetAsync(loff, 0, sizeof(unsigned long long), c.s);
+        PFG_LAUNCH(K_DOWNLOAD, gathered_sizes_k, grid_for(C, 256), 256, 0, c.s, c.hdr, ids, C, c.pk_roff);
+        exclusive_scan_u64(c.pk_roff, c.pk_roff, C, 0ull, c.pk_roff + C, c.tmp, c.s);
+        PFG_LAUNCH(K_DOWNLOAD, gathered_pack_k, grid_for(C * 32, 256), 256, 0, c.s, c.hdr, c.lits, ids, C,
+                   c.pk_roff, c.vinst, c.di.voff, c.pk_lits, c.pk_learnt, c.pk_lbd, c.pk_usage);
+        cudaMemcpyAsync(bases, c.cache_lit_base.data(), ((size_t)n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, c.s);
+        PFG_LAUNCH(K_DOWNLOAD, relative_off_k, grid_for(C, 256), 256, 0, c.s, keys, C, bases, c.pk_roff);
     }
-    c.cache_off.resize(C + 1);
-    c.cache_lits.resize(c.numLiterals);
-    c.cache_learnt.resize(C);
-    c.cache_lbd.resize(C);
-    c.cache_usage.resize(C);
-    c.cache_elim.resize((size_t)c.V + 1);
-    c.cache_trail.resize(c.trail_total);
-    cudaMemcpyAsync(c.cache_off.data(), loff, (C + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, c.s);
-    if (c.numLiterals) cudaMemcpyAsync(c.cache_lits.data(), olits, c.numLiterals * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    if (C) {
-        cudaMemcpyAsync(c.cache_learnt.data(), olearnt, C, cudaMemcpyDeviceToHost, c.s);
-        cudaMemcpyAsync(c.cache_lbd.data(), olbd, C * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-        cudaMemcpyAsync(c.cache_usage.data(), ousage, C, cudaMemcpyDeviceToHost, c.s);
-    }
-    cudaMemcpyAsync(c.cache_elim.data(), c.elim, (size_t)c.V + 1, cudaMemcpyDeviceToHost, c.s);
-    cudaMemcpyAsync(c.cache_trail.data(), c.trail, c.trail_total * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    // stack regions, packed back to back on the host
-    uint64_t words = 0;
-    for (uint32_t i = 0; i < n; i++) words += c.hout.scount[i];
-    c.cache_stack.resize(words);
-    uint64_t at = 0;
-    for (uint32_t i = 0; i < n; i++) {
-        const uint64_t w = c.hout.scount[i];
-        if (w) cudaMemcpyAsync(c.cache_stack.data() + at, c.stack + c.hi.sbase[i], w * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-        at += w;
-    }
-    const bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "batch download");
+    std::vector<uint8_t> el((size_t)c.V + 1);
+    cudaMemcpyAsync(el.data(), c.elim, (size_t)c.V + 1, cudaMemcpyDeviceToHost, c.s);
+    const bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "batch write-back");
     release();
     if (!synced) return PFG_CUDA_ERROR;
-    c.cache_cls_base.assign((size_t)n + 1, 0);
-    for (uint32_t i = 0; i < n; i++) c.cache_cls_base[i + 1] = c.cache_cls_base[i] + c.ih[i].numClauses;
+    c.cache_elim_cnt.assign(n, 0);
+    c.cache_forced_cnt.assign(n, 0);
+    for (uint32_t i = 0; i < n; i++) {
+        const InstHost& h = c.ih[i];
+        uint64_t ne = 0, nf = 0;
+        for (uint32_t v = h.voff + 1; v <= h.voff + h.V; v++) {
+            if (el[v] & FORCED_MASK) nf++;
+            else if (el[v]) ne++;
+        }
+        c.cache_elim_cnt[i] = ne;
+        c.cache_forced_cnt[i] = nf;
+    }
     c.cache_ready = true;
     return PFG_OK;
-}
-
-uint64_t stack_offset(const Ctx& c, uint32_t i) {
-    uint64_t at = 0;
-    for (uint32_t j = 0; j < i; j++) at += c.hout.scount[j];
-    return at;
 }
 
 }  // namespace
@@ -1169,9 +1197,8 @@ extern "C" int pfg_batch_result_sizes(pfg_ctx* o, uint32_t i, pfg_result_sizes* 
     if (rc != PFG_OK) return rc;
     const InstHost& h = c.ih[i];
     std::memset(r, 0, sizeof(*r));
-    const uint64_t b = c.cache_cls_base[i], e = c.cache_cls_base[i + 1];
-    r->clauses = e - b;
-    r->literals = c.cache_off[e] - c.cache_off[b];
+    r->clauses = c.cache_cls_base[i + 1] - c.cache_cls_base[i];
+    r->literals = c.cache_lit_base[i + 1] - c.cache_lit_base[i];
     r->units = std::min<uint64_t>(c.hout.tcount[i], c.hi.tcap[i]);
     r->pending_units = h.pending.size();
     r->stack_words = c.hout.scount[i];
@@ -1188,38 +1215,185 @@ extern "C" int pfg_batch_download(pfg_ctx* o, uint32_t i, uint32_t* lits, uint64
     if (!c.uploaded || i >= c.ninst) return PFG_INVALID;
     const uint64_t base_launches = g_launches;
     g_prof = &c.prof;
-    const int rc = build_cache(c);
-    finish(c, nullptr, base_launches, rc);
-    if (rc != PFG_OK) return rc;
+    int rc = build_cache(c);
+    if (rc != PFG_OK) return finish(c, nullptr, base_launches, rc);
     const InstHost& h = c.ih[i];
-    const uint64_t b = c.cache_cls_base[i], e = c.cache_cls_base[i + 1];
-    const uint64_t lb = c.cache_off[b], le = c.cache_off[e];
-    if (lits) std::copy(c.cache_lits.begin() + lb, c.cache_lits.begin() + le, lits);
-    if (cls_off) for (uint64_t k = b; k <= e; k++) cls_off[k - b] = c.cache_off[k] - lb;
-    if (cls_learnt) std::copy(c.cache_learnt.begin() + b, c.cache_learnt.begin() + e, cls_learnt);
-    if (cls_lbd) std::copy(c.cache_lbd.begin() + b, c.cache_lbd.begin() + e, cls_lbd);
-    if (cls_usage) std::copy(c.cache_usage.begin() + b, c.cache_usage.begin() + e, cls_usage);
-    if (eliminated) {
-        eliminated[0] = 0;
-        std::copy(c.cache_elim.begin() + h.voff + 1, c.cache_elim.begin() + h.voff + 1 + h.V, eliminated + 1);
-    }
+    const uint64_t b = c.cache_cls_base[i], nc = c.cache_cls_base[i + 1] - b;
+    const uint64_t lb = c.cache_lit_base[i], nl = c.cache_lit_base[i + 1] - lb;
     const uint64_t nt = std::min<uint64_t>(c.hout.tcount[i], c.hi.tcap[i]);
+    const uint64_t ns = c.hout.scount[i];
+    // straight from the packed device arrays into the caller's buffers
+    if (lits && nl) cudaMemcpyAsync(lits, c.pk_lits + lb, nl * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (cls_off && nc) cudaMemcpyAsync(cls_off, c.pk_roff + b, nc * sizeof(uint64_t), cudaMemcpyDeviceToHost, c.s);
+    if (cls_learnt && nc) cudaMemcpyAsync(cls_learnt, c.pk_learnt + b, nc, cudaMemcpyDeviceToHost, c.s);
+    if (cls_lbd && nc) cudaMemcpyAsync(cls_lbd, c.pk_lbd + b, nc * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (cls_usage && nc) cudaMemcpyAsync(cls_usage, c.pk_usage + b, nc, cudaMemcpyDeviceToHost, c.s);
+    if (eliminated) cudaMemcpyAsync(eliminated + 1, c.elim + h.voff + 1, h.V, cudaMemcpyDeviceToHost, c.s);
+    if (units && nt) cudaMemcpyAsync(units, c.trail + c.hi.tbase[i], nt * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (stack && ns) cudaMemcpyAsync(stack, c.stack + c.hi.sbase[i], ns * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (!cuda_ok(c, cudaStreamSynchronize(c.s), "batch download")) return finish(c, nullptr, base_launches, PFG_CUDA_ERROR);
+    if (cls_off) cls_off[nc] = nl;
+    if (eliminated) eliminated[0] = 0;
     if (units && nt) {
         // trail literals back to the instance's numbering
-        const uint32_t* t = c.cache_trail.data() + c.hi.tbase[i];
-        for (uint64_t k = 0; k < nt; k++) units[k] = t[k] - 2u * h.voff;
+        for (uint64_t k = 0; k < nt; k++) units[k] -= 2u * h.voff;
         std::sort(units, units + nt);
     }
     if (pending_units && !h.pending.empty()) {
         for (size_t k = 0; k < h.pending.size(); k++) pending_units[k] = h.pending[k] - 2u * h.voff;
         std::sort(pending_units, pending_units + h.pending.size());
     }
-    if (stack && c.hout.scount[i]) {
-        const uint64_t at = stack_offset(c, i);
-        std::copy(c.cache_stack.begin() + at, c.cache_stack.begin() + at + c.hout.scount[i], stack);
-    }
     if (round_ends) std::copy(h.round_ends.begin(), h.round_ends.end(), round_ends);
+    return finish(c, nullptr, base_launches, PFG_OK);
+}
+
+namespace pfg {
+namespace {
+
+// instance of output position q, given the instances' output starts base[0..n]
+PFG_D uint32_t region_of(const unsigned long long* base, uint32_t n, uint64_t q) {
+    uint32_t lo = 0, hi = n;   // largest i < n with base[i] <= q
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (base[mid] <= q) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// cls_off of all instances back to back, each with its final entry (its literal count)
+__global__ void offsets_all_k(const unsigned long long* roff, uint64_t C, const unsigned long long* cls_base,
+                              const unsigned long long* lit_base, uint32_t n, unsigned long long* out) {
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < C + n; j += (uint64_t)gridDim.x * blockDim.x) {
+        if (j < C) {
+            const uint32_t i = region_of(cls_base, n, j);
+            out[j + i] = roff[j];
+        } else {
+            const uint32_t i = (uint32_t)(j - C);
+            out[cls_base[i + 1] + i] = lit_base[i + 1] - lit_base[i];
+        }
+    }
+}
+
+// eliminated bytes of all instances back to back, max_var + 1 each, entry 0 zero
+__global__ void elim_all_k(const uint8_t* elim, const unsigned long long* ebase, const uint32_t* voff, uint32_t n,
+                           uint64_t total, uint8_t* out) {
+    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = region_of(ebase, n, q);
+        const uint64_t v = q - ebase[i];
+        out[q] = v ? elim[voff[i] + v] : 0;
+    }
+}
+
+// per-instance regions [src_base[i], +count) back to back; literals moved down by 2 * shift[i]
+__global__ void regions_all_k(const uint32_t* src, const unsigned long long* src_base,
+                              const unsigned long long* dst_base, const uint32_t* shift, uint32_t n, uint64_t total,
+                              uint32_t* out) {
+    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = region_of(dst_base, n, q);
+        const uint32_t w = src[src_base[i] + (q - dst_base[i])];
+        out[q] = shift ? w - 2u * shift[i] : w;
+    }
+}
+
+}  // namespace
+}  // namespace pfg
+
+extern "C" int pfg_batch_result_sizes_all(pfg_ctx* o, pfg_result_sizes* sizes) {
+    if (!o || !sizes) return PFG_INVALID;
+    Ctx& c = o->c;
+    if (!c.uploaded) return PFG_INVALID;
+    for (uint32_t i = 0; i < c.ninst; i++) {
+        const int rc = pfg_batch_result_sizes(o, i, sizes + i);
+        if (rc != PFG_OK) return rc;
+    }
     return PFG_OK;
+}
+
+extern "C" int pfg_batch_download_all(pfg_ctx* o, uint32_t* lits, uint64_t* cls_off, uint8_t* cls_learnt,
+                                      uint32_t* cls_lbd, uint8_t* cls_usage, uint8_t* eliminated, uint32_t* units,
+                                      uint32_t* pending_units, uint32_t* stack, uint64_t* round_ends) {
+    if (!o) return PFG_INVALID;
+    Ctx& c = o->c;
+    if (!c.uploaded) return PFG_INVALID;
+    const uint64_t base_launches = g_launches;
+    g_prof = &c.prof;
+    int rc = build_cache(c);
+    if (rc != PFG_OK) return finish(c, nullptr, base_launches, rc);
+    const uint32_t n = c.ninst;
+    const uint64_t C = c.cache_cls_base[n], L = c.cache_lit_base[n];
+    // output starts of every instance: eliminated, units, stack
+    std::vector<unsigned long long> hb(6 * ((size_t)n + 1), 0);
+    unsigned long long* eb = hb.data();
+    unsigned long long* ub = eb + (n + 1);
+    unsigned long long* sb = ub + (n + 1);
+    unsigned long long* tsrc = sb + (n + 1);
+    unsigned long long* ssrc = tsrc + (n + 1);
+    unsigned long long* cb = ssrc + (n + 1);
+    for (uint32_t i = 0; i < n; i++) {
+        eb[i + 1] = eb[i] + c.ih[i].V + 1;
+        ub[i + 1] = ub[i] + std::min<uint64_t>(c.hout.tcount[i], c.hi.tcap[i]);
+        sb[i + 1] = sb[i] + c.hout.scount[i];
+        tsrc[i] = c.hi.tbase[i];
+        ssrc[i] = c.hi.sbase[i];
+    }
+    for (uint32_t i = 0; i <= n; i++) cb[i] = c.cache_cls_base[i];
+    std::vector<uint32_t> shift(n);
+    for (uint32_t i = 0; i < n; i++) shift[i] = c.ih[i].voff;
+    unsigned long long* dbases = nullptr;
+    uint32_t* dshift = nullptr;
+    unsigned long long* doff = nullptr;
+    uint8_t* delim = nullptr;
+    uint32_t *dunits = nullptr, *dstack = nullptr;
+    bool ok = dalloc_t(c, &dbases, hb.size() + (size_t)n + 1) && dalloc_t(c, &dshift, (size_t)n + 1) &&
+              dalloc_t(c, &doff, C + n + 1) && dalloc_t(c, &delim, eb[n] + 1) && dalloc_t(c, &dunits, ub[n] + 1) &&
+              dalloc_t(c, &dstack, sb[n] + 1);
+    auto release = [&]() { dfree(c, dbases); dfree(c, dshift); dfree(c, doff); dfree(c, delim); dfree(c, dunits); dfree(c, dstack); };
+    if (!ok) { release(); return finish(c, nullptr, base_launches, PFG_CNFALLOC_FAIL); }
+    cudaMemcpyAsync(dbases, hb.data(), hb.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, c.s);
+    cudaMemcpyAsync(dbases + hb.size(), c.cache_lit_base.data(), ((size_t)n + 1) * sizeof(unsigned long long),
+                    cudaMemcpyHostToDevice, c.s);
+    cudaMemcpyAsync(dshift, shift.data(), (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, c.s);
+    const unsigned long long* d_eb = dbases;
+    const unsigned long long* d_ub = d_eb + (n + 1);
+    const unsigned long long* d_sb = d_ub + (n + 1);
+    const unsigned long long* d_tsrc = d_sb + (n + 1);
+    const unsigned long long* d_ssrc = d_tsrc + (n + 1);
+    const unsigned long long* d_cb = d_ssrc + (n + 1);
+    const unsigned long long* d_lb = dbases + hb.size();
+    if (cls_off)
+        PFG_LAUNCH(K_DOWNLOAD, offsets_all_k, grid_for(C + n, 256), 256, 0, c.s, c.pk_roff, C, d_cb, d_lb, n, doff);
+    if (eliminated)
+        PFG_LAUNCH(K_DOWNLOAD, elim_all_k, grid_for(eb[n], 256), 256, 0, c.s, c.elim, d_eb, c.di.voff, n, eb[n], delim);
+    if (units && ub[n])
+        PFG_LAUNCH(K_DOWNLOAD, regions_all_k, grid_for(ub[n], 256), 256, 0, c.s, c.trail, d_tsrc, d_ub, dshift, n,
+                   ub[n], dunits);
+    if (stack && sb[n])
+        PFG_LAUNCH(K_DOWNLOAD, regions_all_k, grid_for(sb[n], 256), 256, 0, c.s, c.stack, d_ssrc, d_sb,
+                   (const uint32_t*)nullptr, n, sb[n], dstack);
+    if (lits && L) cudaMemcpyAsync(lits, c.pk_lits, L * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (cls_off) cudaMemcpyAsync(cls_off, doff, (C + n) * sizeof(uint64_t), cudaMemcpyDeviceToHost, c.s);
+    if (cls_learnt && C) cudaMemcpyAsync(cls_learnt, c.pk_learnt, C, cudaMemcpyDeviceToHost, c.s);
+    if (cls_lbd && C) cudaMemcpyAsync(cls_lbd, c.pk_lbd, C * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (cls_usage && C) cudaMemcpyAsync(cls_usage, c.pk_usage, C, cudaMemcpyDeviceToHost, c.s);
+    if (eliminated) cudaMemcpyAsync(eliminated, delim, eb[n], cudaMemcpyDeviceToHost, c.s);
+    if (units && ub[n]) cudaMemcpyAsync(units, dunits, ub[n] * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (stack && sb[n]) cudaMemcpyAsync(stack, dstack, sb[n] * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    const bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "batch download");
+    release();
+    if (!synced) return finish(c, nullptr, base_launches, PFG_CUDA_ERROR);
+    uint64_t pend = 0, rends = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const InstHost& h = c.ih[i];
+        if (units) std::sort(units + ub[i], units + ub[i + 1]);
+        if (pending_units && !h.pending.empty()) {
+            for (size_t k = 0; k < h.pending.size(); k++) pending_units[pend + k] = h.pending[k] - 2u * h.voff;
+            std::sort(pending_units + pend, pending_units + pend + h.pending.size());
+        }
+        pend += h.pending.size();
+        if (round_ends) std::copy(h.round_ends.begin(), h.round_ends.end(), round_ends + rends);
+        rends += h.round_ends.size();
+    }
+    return finish(c, nullptr, base_launches, PFG_OK);
 }
 
 extern "C" int pfg_profile_enable(pfg_ctx* o, int on) {

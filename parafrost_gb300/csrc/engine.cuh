@@ -186,15 +186,19 @@ struct Ctx {
     pfg_stats stats{};
     double pass_ms[8] = {0};
 
-    // batch download cache (built on the first per-instance download)
+    // batch write-back (built on the first per-instance call): live clauses packed
+    // on the device, grouped by instance, literals back in instance numbering and
+    // offsets relative to the instance; each instance is copied from there
+    // straight into the caller's buffers
     bool cache_ready = false;
-    std::vector<uint32_t> cache_lits;
-    std::vector<uint64_t> cache_off;            // global offsets into cache_lits
-    std::vector<uint8_t> cache_learnt, cache_usage;
-    std::vector<uint32_t> cache_lbd;
-    std::vector<uint64_t> cache_cls_base;       // n+1: first clause of each instance
-    std::vector<uint8_t> cache_elim;
-    std::vector<uint32_t> cache_trail, cache_stack;
+    uint32_t* pk_lits = nullptr;
+    unsigned long long* pk_roff = nullptr;
+    uint8_t* pk_learnt = nullptr;
+    uint8_t* pk_usage = nullptr;
+    uint32_t* pk_lbd = nullptr;
+    std::vector<uint64_t> cache_cls_base;       // n+1: first packed clause of each instance
+    std::vector<uint64_t> cache_lit_base;       // n+1: first packed literal of each instance
+    std::vector<uint64_t> cache_elim_cnt, cache_forced_cnt;
 };
 
 // ---- memory helpers (engine.cu) ----

@@ -169,11 +169,52 @@ class Simplifier:
         return SimplifyResult(int(st.status), Cnf(sz.max_var, lits, off, learnt, lbd, usage), elim, units, pend,
                               stack, rends, stats)
 
+    def download_all(self) -> list:
+        """Results of every instance of the batch, one copy per output array
+        (each instance's arrays are views into them)."""
+        n = self.batch_size()
+        sizes = (_abi.PfgResultSizes * max(n, 1))()
+        self._check(self.lib.pfg_batch_result_sizes_all(self._ctx, sizes), "pfg_batch_result_sizes_all")
+        f = lambda name: np.array([getattr(sizes[i], name) for i in range(n)], dtype=np.int64)
+        ncls, nlit, nvar = f("clauses"), f("literals"), f("max_var")
+        nun, npend, nstk, nrnd = f("units"), f("pending_units"), f("stack_words"), f("rounds")
+        lits = np.empty(int(nlit.sum()), dtype=np.uint32)
+        off = np.empty(int((ncls + 1).sum()), dtype=np.uint64)
+        learnt = np.empty(int(ncls.sum()), dtype=np.uint8)
+        lbd = np.empty(int(ncls.sum()), dtype=np.uint32)
+        usage = np.empty(int(ncls.sum()), dtype=np.uint8)
+        elim = np.empty(int((nvar + 1).sum()), dtype=np.uint8)
+        units = np.empty(int(nun.sum()), dtype=np.uint32)
+        pend = np.empty(int(npend.sum()), dtype=np.uint32)
+        stack = np.empty(int(nstk.sum()), dtype=np.uint32)
+        rends = np.empty(int(nrnd.sum()), dtype=np.uint64)
+        rc = self.lib.pfg_batch_download_all(self._ctx, _ptr(lits, C.c_uint32), _ptr(off, C.c_uint64),
+                                             _ptr(learnt, C.c_uint8), _ptr(lbd, C.c_uint32), _ptr(usage, C.c_uint8),
+                                             _ptr(elim, C.c_uint8), _ptr(units, C.c_uint32), _ptr(pend, C.c_uint32),
+                                             _ptr(stack, C.c_uint32), _ptr(rends, C.c_uint64))
+        self._check(rc, "pfg_batch_download_all")
+
+        def starts(counts):
+            return np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+
+        sl, so, sc, se = starts(nlit), starts(ncls + 1), starts(ncls), starts(nvar + 1)
+        su, sp, ss, sr = starts(nun), starts(npend), starts(nstk), starts(nrnd)
+        out = []
+        for i in range(n):
+            st = _abi.PfgStats()
+            self._check(self.lib.pfg_batch_stats(self._ctx, i, C.byref(st)), "pfg_batch_stats")
+            stats = {k[0]: getattr(st, k[0]) for k in _abi.PfgStats._fields_ if k[0] != "pass_ms"}
+            cnf = Cnf(int(nvar[i]), lits[sl[i]:sl[i + 1]], off[so[i]:so[i + 1]], learnt[sc[i]:sc[i + 1]],
+                      lbd[sc[i]:sc[i + 1]], usage[sc[i]:sc[i + 1]])
+            out.append(SimplifyResult(int(st.status), cnf, elim[se[i]:se[i + 1]], units[su[i]:su[i + 1]],
+                                      pend[sp[i]:sp[i + 1]], stack[ss[i]:ss[i + 1]], rends[sr[i]:sr[i + 1]], stats))
+        return out
+
     def simplify_batch(self, cnfs, var_states=None, assumeds=None, vorgs=None) -> list:
         """Simplify every CNF of `cnfs` in one device store; one result per instance."""
         self.upload_batch(cnfs, var_states, assumeds, vorgs)
         self.run()
-        return [self.download_instance(i) for i in range(len(cnfs))]
+        return self.download_all()
 
     def profile(self, on: bool = True) -> None:
         """Per-kernel CUDA-event timing of the following simplify calls."""

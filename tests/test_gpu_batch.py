@@ -140,3 +140,19 @@ def test_invalid_instance_is_named():
         with pytest.raises(pg.SimplifyError) as e:
             s.upload_batch([inst(1), bad])
     assert e.value.code == 5 and "instance 1" in str(e.value)
+
+
+def test_bulk_and_per_instance_downloads_agree():
+    cnfs = [inst(60 + j, scale=1 + j % 2) for j in range(6)] + [with_learnts(inst(70), 70)]
+    with pg.Simplifier() as s:
+        s.upload_batch(cnfs)
+        s.run()
+        bulk = s.download_all()
+        single = [s.download_instance(i) for i in range(len(cnfs))]
+    for a, b in zip(bulk, single):
+        for x, y in ((a.cnf.lits, b.cnf.lits), (a.cnf.off, b.cnf.off), (a.cnf.learnt, b.cnf.learnt),
+                     (a.cnf.lbd, b.cnf.lbd), (a.cnf.usage, b.cnf.usage), (a.eliminated, b.eliminated),
+                     (a.units, b.units), (a.pending_units, b.pending_units), (a.stack, b.stack),
+                     (a.round_ends, b.round_ends)):
+            assert np.array_equal(x, y)
+        assert a.status == b.status and a.stats["clauses_out"] == b.stats["clauses_out"]
