@@ -89,6 +89,7 @@ __global__ void bcp_advance_k(DevCounters* dc) {
 
 // warp per frontier literal, lanes stride its occurrence list
 constexpr uint32_t BCP_GROUP = 32;
+constexpr uint32_t BCP_HEAD = 4;
 
 __global__ void bcp_propagate_k(BK k, const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off,
                                 const uint32_t* ot_size, const uint32_t* ot_ids, const uint32_t* front_a,
@@ -112,11 +113,24 @@ __global__ void bcp_propagate_k(BK k, const ClsHdr* hdr, const uint32_t* lits, c
             uint32_t unit = 0;
             int nunset = 0;
             bool sat = false;
-            for (uint32_t q = 0; q < h.size; q++) {
-                const uint32_t l = lits[h.off + q];
+            // the first BCP_HEAD literals and their values are loaded together
+            const uint32_t* cl = lits + h.off;
+            uint32_t hl[BCP_HEAD];
+            uint32_t hv[BCP_HEAD];
+#pragma unroll
+            for (uint32_t q = 0; q < BCP_HEAD; q++) hl[q] = q < h.size ? cl[q] : 0u;
+#pragma unroll
+            for (uint32_t q = 0; q < BCP_HEAD; q++) hv[q] = q < h.size ? litval(k.st, hl[q]) : BCP_FALSE;
+#pragma unroll
+            for (uint32_t q = 0; q < BCP_HEAD; q++) {
+                if (hv[q] == BCP_TRUE) sat = true;
+                else if (hv[q] == BCP_UNSET) { unit = hl[q]; nunset++; }
+            }
+            for (uint32_t q = BCP_HEAD; q < h.size && !sat && nunset < 2; q++) {
+                const uint32_t l = cl[q];
                 const uint32_t ve = litval(k.st, l);
                 if (ve == BCP_TRUE) { sat = true; break; }
-                if (ve == BCP_UNSET) { unit = l; if (++nunset > 1) break; }
+                if (ve == BCP_UNSET) { unit = l; nunset++; }
             }
             if (sat) continue;
             if (!nunset) set_conflict(k, inst);

@@ -891,25 +891,37 @@ PFG_D bool wf_build(const EK& k, uint32_t lit, WFun& f, unsigned lane) {
     return true;
 }
 
-PFG_D void wf_build_core(const EK& k, uint32_t lit, uint32_t tail, WFun& fun, bool& core, unsigned lane) {
+// The core test of find_fun_gate for every original clause i of lit's list:
+// `base` AND the functions of the non-learnt clauses before i; when that is
+// all-false, clause i is not part of the gate and is melted. The reference
+// rebuilds the prefix for every i; one running AND in list order gives the
+// same prefixes (melting changes no clause's status).
+PFG_D void wf_cores(const EK& k, uint32_t lit, const WFun& base, bool& core, unsigned lane) {
     const uint32_t* ol = OLp(k, lit);
-    for (uint32_t j = 0; j < tail; j++) {
-        const ClsHdr h = k.hdr[ol[j]];
-        if (m_learnt(h.meta)) continue;
-        WFun cls{0, 0};
-        const uint32_t* l = k.lits + h.off;
-        for (uint32_t t = 0; t < h.size; t++) {
-            const uint32_t other = l[t];
-            if (other == lit) continue;
-            wf_clause2fun(k.varcore[ABSV(other)], SIGNL(other), cls, lane);
+    const uint32_t n = OLs(k, lit);
+    WFun run;
+    wf_set(run, ~0ULL);
+    for (uint32_t i = 0; i < n; i++) {
+        const ClsHdr h = k.hdr[ol[i]];
+        if (m_orig(h.meta)) {
+            const uint64_t w0 = base.w0 & run.w0, w1 = base.w1 & run.w1;
+            const bool isfalse = __all_sync(0xFFFFFFFFu, (w0 | w1) == 0);
+            if (isfalse) {
+                if (lane == 0) SET_MOLTEN(k, ol[i], 1);   // non-gate clause
+                core = true;
+            }
         }
-        fun.w0 &= cls.w0;
-        fun.w1 &= cls.w1;
-    }
-    const bool isfalse = __all_sync(0xFFFFFFFFu, (fun.w0 | fun.w1) == 0);
-    if (isfalse) {
-        if (lane == 0) SET_MOLTEN(k, ol[tail], 1);   // non-gate clause
-        core = true;
+        if (!m_learnt(h.meta)) {
+            WFun cls{0, 0};
+            const uint32_t* l = k.lits + h.off;
+            for (uint32_t t = 0; t < h.size; t++) {
+                const uint32_t other = l[t];
+                if (other == lit) continue;
+                wf_clause2fun(k.varcore[ABSV(other)], SIGNL(other), cls, lane);
+            }
+            run.w0 &= cls.w0;
+            run.w1 &= cls.w1;
+        }
     }
     __syncwarp();
 }
@@ -922,17 +934,10 @@ PFG_D bool wf_find_fun_gate(const EK& k, uint32_t p, uint32_t n, uint32_t nOrgCl
     const bool nonzero = __any_sync(0xFFFFFFFFu, ((pos.w0 & neg.w0) | (pos.w1 & neg.w1)) != 0);
     if (nonzero) return false;
     bool core = false;
-    const uint32_t* pl = OLp(k, p);
-    for (int i = (int)OLs(k, p) - 1; i >= 0; i--) {
-        WFun fun = neg;
-        if (m_orig(META(k, pl[i]))) wf_build_core(k, p, (uint32_t)i, fun, core, lane);
-    }
-    const uint32_t* nl = OLp(k, n);
-    for (int i = (int)OLs(k, n) - 1; i >= 0; i--) {
-        WFun fun;
-        wf_set(fun, ~0ULL);
-        if (m_orig(META(k, nl[i]))) wf_build_core(k, n, (uint32_t)i, fun, core, lane);
-    }
+    wf_cores(k, p, neg, core, lane);
+    WFun ones;
+    wf_set(ones, ~0ULL);
+    wf_cores(k, n, ones, core, lane);
     nE = 0; nC = 0; nL = 0;
     if (count_subst(k, PAIR_CORE, ABSV(p), nOrgCls, p, n, nE, nC, nL)) {
         __syncwarp();
