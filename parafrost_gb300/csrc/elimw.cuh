@@ -26,6 +26,7 @@ struct WS {
     uint32_t np, nn, nlit, pad;
     uint32_t id[WS_MAXC];
     uint32_t meta[WS_MAXC];
+    uint32_t meta0[WS_MAXC];    // meta as staged (only changed words are written back)
     uint32_t size[WS_MAXC];
     uint32_t sig[WS_MAXC];
     uint32_t off[WS_MAXC];
@@ -52,6 +53,7 @@ PFG_D bool ws_stage(const EK& k, WS& w, uint32_t p, uint32_t n, unsigned lane) {
         const ClsHdr h = k.hdr[id];
         w.id[i] = id;
         w.meta[i] = h.meta;
+        w.meta0[i] = h.meta;
         w.size[i] = h.size;
         w.sig[i] = h.sig;
         w.goff[i] = h.off;
@@ -93,7 +95,10 @@ PFG_D void ws_flush(const EK& k, WS& w, unsigned lane) {
     const uint32_t nc = w.np + w.nn;
     for (uint32_t i = lane; i < nc; i += 32) {
         const uint32_t id = w.id[i];
-        k.hdr[id].meta = w.meta[i];
+        if (w.meta[i] != w.meta0[i]) {
+            k.hdr[id].meta = w.meta[i];
+            w.meta0[i] = w.meta[i];
+        }
         if (w.dirty[i]) {
             k.hdr[id].size = w.size[i];
             k.hdr[id].sig = w.sig[i];

@@ -74,8 +74,10 @@ PFG_D bool blocked(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_o
                    const uint32_t* ot_ids, uint32_t lit, uint32_t cand, uint32_t r, const uint32_t* rank,
                    const uint8_t* mstate) {
     const uint32_t o = ot_off[lit], n = ot_size[lit];
+    ClsHdr next = n ? hdr[ot_ids[o]] : ClsHdr{0, 0, 0, 0};
     for (uint32_t i = 0; i < n; i++) {
-        const ClsHdr h = hdr[ot_ids[o + i]];
+        const ClsHdr h = next;
+        if (i + 1 < n) next = hdr[ot_ids[o + i + 1]];   // in flight while h is checked
         if (m_deleted(h.meta)) continue;
         const uint32_t* l = lits + h.off;
         uint32_t u[MIS_HEAD];
@@ -98,8 +100,10 @@ PFG_D bool blocked(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_o
 PFG_D void freeze_list(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
                        const uint32_t* ot_ids, uint32_t lit, uint32_t cand, uint8_t* frozen, uint8_t* mstate) {
     const uint32_t o = ot_off[lit], n = ot_size[lit];
+    ClsHdr next = n ? hdr[ot_ids[o]] : ClsHdr{0, 0, 0, 0};
     for (uint32_t i = 0; i < n; i++) {
-        const ClsHdr h = hdr[ot_ids[o + i]];
+        const ClsHdr h = next;
+        if (i + 1 < n) next = hdr[ot_ids[o + i + 1]];
         if (m_deleted(h.meta)) continue;
         const uint32_t* l = lits + h.off;
         uint32_t u[MIS_HEAD];
