@@ -1037,64 +1037,184 @@ __global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint
     }
 }
 
-// ---- ERE: one warp per elected variable ----
-__global__ void __launch_bounds__(128) ere_k(EK k, const uint32_t* elected, uint32_t nelected) {
+// ---- ERE (redundancy.cuh:27-175) ----
+// The reference searches, for every resolvent r, the sorted occurrence list of
+// r's rarest literal with 32 strided lanes, and every lane deletes the first
+// clause on its positions that equals r and has a matching type. The clauses
+// equal to r form one block of that list, ordered by id (they share the sort
+// key), so lane j's first hit is the first matching clause at a block offset
+// congruent to j modulo 32, wherever the block starts. The block is found
+// through a hash table of the live clauses (by literal set) instead of a list
+// scan, so the lists of other variables need no sorting.
+constexpr uint32_t ERE_EMPTY = 0xFFFFFFFFu;
+
+// A running combination of the literals, then the length, then MurmurHash3's
+// 32-bit finalizer; computable while a resolvent is being merged.
+PFG_D uint32_t hash_step(uint32_t h, uint32_t lit) { return h ^ (lit + 0x9E3779B9u + (h << 6) + (h >> 2)); }
+
+PFG_D uint32_t hash_final(uint32_t h, uint32_t n) {
+    h ^= n * 0x9E3779B9u;
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return h;
+}
+
+PFG_D uint32_t cls_hash(const uint32_t* l, uint32_t n) {
+    uint32_t h = 0;
+    for (uint32_t i = 0; i < n; i++) h = hash_step(h, l[i]);
+    return hash_final(h, n);
+}
+
+// length and hash of the resolvent of two clauses on x without writing it;
+// 0 for a tautology (the merge order of merge_out, elimination.cuh:216-240)
+PFG_D int merge_hash(const EK& k, uint32_t x, const ClsHdr& h1, const ClsHdr& h2, uint32_t& hash) {
+    const uint32_t* a = k.lits + h1.off;
+    const uint32_t* b = k.lits + h2.off;
+    const int n1 = (int)h1.size, n2 = (int)h2.size;
+    int i = 0, j = 0, len = 0;
+    uint32_t h = 0;
+    while (i < n1 && j < n2) {
+        const uint32_t l1 = a[i], l2 = b[j], v1 = ABSV(l1), v2 = ABSV(l2);
+        if (v1 == x) i++;
+        else if (v2 == x) j++;
+        else if ((l1 ^ l2) == 1u) return 0;
+        else if (v1 < v2) { i++; h = hash_step(h, l1); len++; }
+        else if (v2 < v1) { j++; h = hash_step(h, l2); len++; }
+        else { i++; j++; h = hash_step(h, l1); len++; }
+    }
+    for (; i < n1; i++) if (ABSV(a[i]) != x) { h = hash_step(h, a[i]); len++; }
+    for (; j < n2; j++) if (ABSV(b[j]) != x) { h = hash_step(h, b[j]); len++; }
+    hash = hash_final(h, (uint32_t)len);
+    return len;
+}
+
+// does clause c equal the resolvent of h1 and h2 on x (of length len)?
+PFG_D bool merge_equals(const EK& k, uint32_t x, const ClsHdr& h1, const ClsHdr& h2, uint32_t c) {
+    const uint32_t* a = k.lits + h1.off;
+    const uint32_t* b = k.lits + h2.off;
+    const uint32_t* d = CLp(k, c);
+    const int n1 = (int)h1.size, n2 = (int)h2.size;
+    int i = 0, j = 0, q = 0;
+    while (i < n1 || j < n2) {
+        uint32_t lit;
+        if (i < n1 && ABSV(a[i]) == x) { i++; continue; }
+        if (j < n2 && ABSV(b[j]) == x) { j++; continue; }
+        if (i < n1 && j < n2) {
+            const uint32_t l1 = a[i], l2 = b[j];
+            if (ABSV(l1) < ABSV(l2)) { lit = l1; i++; }
+            else if (ABSV(l2) < ABSV(l1)) { lit = l2; j++; }
+            else { lit = l1; i++; j++; }
+        } else if (i < n1) {
+            lit = a[i++];
+        } else {
+            lit = b[j++];
+        }
+        if (d[q++] != lit) return false;
+    }
+    return true;
+}
+
+__global__ void ere_table_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
+                            uint32_t* table, uint32_t mask) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        const ClsHdr h = hdr[c];
+        if (m_deleted(h.meta) || h.size < 2) continue;
+        uint32_t s = cls_hash(lits + h.off, h.size) & mask;
+        for (uint32_t q = 0; q <= mask; q++) {   // the table has room for every clause twice over
+            if (atomicCAS(&table[s], ERE_EMPTY, (uint32_t)c) == ERE_EMPTY) break;
+            s = (s + 1) & mask;
+        }
+    }
+}
+
+// smallest id above `after` (or any id when after < 0) of a clause equal to d[0..n)
+PFG_D uint32_t ere_next_equal(const EK& k, const uint32_t* table, uint32_t mask, uint32_t s0, const uint32_t* d,
+                              uint32_t n, int64_t after) {
+    uint32_t best = ERE_EMPTY;
+    uint32_t s = s0;
+    for (uint32_t q = 0; q <= mask; q++) {
+        const uint32_t id = table[s];
+        if (id == ERE_EMPTY) break;
+        if ((int64_t)id > after && id < best && SIZE(k, id) == n && is_equal(k, id, d, n)) best = id;
+        s = (s + 1) & mask;
+    }
+    return best;
+}
+
+// one warp per elected variable. The lanes test 32 resolvents at a time for an
+// equal clause in the table; lane 0 then walks, in pair order, the resolvents
+// that have one, and for each the block of equal clauses in id order. (No
+// clause of the variable equals one of its resolvents, and another elected
+// variable's resolvents never contain it, so the pair tests cannot be changed
+// by the deletions.)
+__global__ void __launch_bounds__(128) ere_k(EK k, const uint32_t* elected, uint32_t nelected, const uint32_t* table,
+                                             uint32_t mask) {
     __shared__ uint32_t bufs[4][SH_MAX_ERE_OUT + 8];
     const uint32_t wib = threadIdx.x >> 5;
     const unsigned lane = threadIdx.x & 31u;
     uint32_t* buf = bufs[wib];
     const uint32_t cmax = k.ere_clause_max;
     for (uint32_t q = blockIdx.x * 4 + wib; q < nelected; q += gridDim.x * 4) {
-        const uint32_t e = q;
-        const uint32_t v = elected[e], p = 2 * v, n = p | 1;
+        const uint32_t v = elected[q], p = 2 * v, n = p | 1;
         const uint32_t ds = OLs(k, p), fs = OLs(k, n);
         if (!(ds && fs && ds <= k.ere_max_occurs && fs <= k.ere_max_occurs)) continue;
         const uint32_t* pl = OLp(k, p);
         const uint32_t* nl = OLp(k, n);
         if (!(SIZE(k, pl[0]) <= cmax && SIZE(k, nl[0]) <= cmax)) continue;
-        for (uint32_t i = 0; i < ds; i++) {
-            const uint32_t pc = pl[i];
-            const ClsHdr ph = k.hdr[pc];
-            if (m_deleted(ph.meta)) continue;
-            for (uint32_t j = 0; j < fs; j++) {
-                const uint32_t nc = nl[j];
-                const ClsHdr nh = k.hdr[nc];
-                if (m_deleted(nh.meta) || ph.size + nh.size - 2 > cmax) continue;
-                int mlen = 0;
-                if (lane == 0) mlen = merge_out(k, v, pc, nc, buf);
-                mlen = __shfl_sync(0xFFFFFFFFu, mlen, 0);
-                __syncwarp();
-                if (mlen > 1) {
-                    const uint32_t type = (m_learnt(ph.meta) || m_learnt(nh.meta)) ? ST_LEARNT : ST_ORIGINAL;
-                    uint32_t best = buf[0], msig = MAPHASH(best);
-                    uint32_t minsize = OLs(k, best);
-                    for (int q = 1; q < mlen; q++) {
-                        const uint32_t ls = OLs(k, buf[q]);
-                        if (ls < minsize) { minsize = ls; best = buf[q]; }
-                        msig |= MAPHASH(buf[q]);
-                    }
-                    const uint32_t* ml = OLp(k, best);
-                    for (uint32_t ii = lane; ii < minsize; ii += 32) {
-                        const uint32_t c = ml[ii];
-                        const ClsHdr h = k.hdr[c];
-                        if ((uint32_t)mlen == h.size && (m_learnt(h.meta) || m_st(h.meta) == type) &&
-                            SUBSIG(msig, h.sig) && !m_deleted(h.meta) && is_equal(k, c, buf, (uint32_t)mlen)) {
-                            // claim: the first non-deleted match of this lane's stride is deleted
-                            unsigned int* mp = (unsigned int*)&k.hdr[c].meta;
-                            unsigned int old = h.meta;
-                            bool won = false;
-                            for (int it = 0; it < 8; it++) {
-                                if (m_deleted(old)) break;
-                                const unsigned int prev = atomicCAS(mp, old, m_set_st(old, ST_DELETED));
-                                if (prev == old) { won = true; break; }
-                                old = prev;
-                            }
-                            if (won) break;
+        const uint32_t total = ds * fs;
+        for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+            const uint32_t pr = b0 + lane;
+            bool hit = false;
+            if (pr < total) {
+                const uint32_t pc = pl[pr / fs], nc = nl[pr % fs];
+                const ClsHdr ph = k.hdr[pc], nh = k.hdr[nc];
+                if (!m_deleted(ph.meta) && !m_deleted(nh.meta) && ph.size + nh.size - 2 <= cmax) {
+                    uint32_t hs;
+                    const int mlen = merge_hash(k, v, ph, nh, hs);
+                    if (mlen > 1) {
+                        uint32_t s = hs & mask;
+                        for (uint32_t t = 0; t <= mask && !hit; t++) {
+                            const uint32_t id = table[s];
+                            if (id == ERE_EMPTY) break;
+                            hit = SIZE(k, id) == (uint32_t)mlen && merge_equals(k, v, ph, nh, id);
+                            s = (s + 1) & mask;
                         }
                     }
                 }
-                __syncwarp();
             }
+            unsigned todo = __ballot_sync(0xFFFFFFFFu, hit);
+            if (lane == 0) {
+                for (; todo; todo &= todo - 1) {
+                    const uint32_t r = b0 + (uint32_t)(__ffs(todo) - 1);
+                    const uint32_t pc = pl[r / fs], nc = nl[r % fs];
+                    const ClsHdr ph = k.hdr[pc], nh = k.hdr[nc];
+                    const int mlen = merge_out(k, v, pc, nc, buf);
+                    const uint32_t type = (m_learnt(ph.meta) || m_learnt(nh.meta)) ? ST_LEARNT : ST_ORIGINAL;
+                    const uint32_t s0 = cls_hash(buf, (uint32_t)mlen) & mask;
+                    uint32_t done = 0;        // strided lanes that already deleted a clause
+                    int64_t after = -1;
+                    for (uint32_t t = 0; done != 0xFFFFFFFFu; t++) {
+                        const uint32_t c = ere_next_equal(k, table, mask, s0, buf, (uint32_t)mlen, after);
+                        if (c == ERE_EMPTY) break;
+                        after = c;
+                        const uint32_t bit = 1u << (t & 31u);
+                        if (done & bit) continue;
+                        unsigned int* mp = (unsigned int*)&k.hdr[c].meta;
+                        unsigned int old = *((volatile unsigned int*)mp);
+                        if (!(m_learnt(old) || m_st(old) == type)) continue;
+                        for (int it = 0; it < 8; it++) {
+                            if (m_deleted(old)) break;
+                            const unsigned int prev = atomicCAS(mp, old, m_set_st(old, ST_DELETED));
+                            if (prev == old) { done |= bit; break; }
+                            old = prev;
+                        }
+                    }
+                }
+            }
+            __syncwarp();
         }
     }
 }
@@ -1230,9 +1350,21 @@ bool ve_pass(Ctx& c) {
     return cuda_ok(c, cudaGetLastError(), "ve");
 }
 
-void ere_pass(Ctx& c) {
-    if (!c.nere) return;
-    PFG_LAUNCH(K_ERE, ere_k, grid_for((uint64_t)c.nere * 32, 128), 128, 0, c.s, make_ek(c), c.ereset, c.nere);
+bool ere_pass(Ctx& c) {
+    if (!c.nere) return true;
+    // hash table of the live clauses, at least twice their number of slots
+    uint64_t cap = 1024;
+    while (cap < 2 * c.numClauses + 2) cap <<= 1;
+    if (cap > (1ull << 32)) { c.err = "ERE table exceeds 2^32 slots"; c.simpstate = PFG_OTALLOC_FAIL; return false; }
+    uint32_t* table = nullptr;
+    if (!dalloc_t(c, &table, cap)) { c.simpstate = PFG_OTALLOC_FAIL; return false; }
+    const uint32_t mask = (uint32_t)(cap - 1);
+    cudaMemsetAsync(table, 0xFF, cap * sizeof(uint32_t), c.s);
+    PFG_LAUNCH(K_ERE, ere_table_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, table, mask);
+    PFG_LAUNCH(K_ERE, ere_k, grid_for((uint64_t)c.nere * 32, 128), 128, 0, c.s, make_ek(c), c.ereset, c.nere, table,
+               mask);
+    dfree(c, table);
+    return cuda_ok(c, cudaGetLastError(), "ere");
 }
 
 }  // namespace pfg

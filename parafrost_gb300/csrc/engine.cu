@@ -879,13 +879,14 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         push_inst_in(c);
         c.nere = nmode2 ? select_mode(c, 2, c.ereset) : 0;
         c.nve = nmode1 ? select_mode(c, 1, c.veset) : 0;
-        // sortOT (segsort.cu:37). A SUB+BVE round reads in list order only the
-        // lists of its elected variables (staging, subsumption order, witness and
-        // resolvent order; gate lookups search those lists too), so only they are
-        // sorted; ERE searches the lists of every literal of a resolvent.
+        // sortOT (segsort.cu:37). Only the elected variables' lists are read in
+        // list order (staging, subsumption order, witness and resolvent order;
+        // gate lookups search those lists too; ERE finds equal clauses through a
+        // hash table), so only they are sorted.
         if (c.nere || c.nve) {
             PassTimer t(c, 0);
-            if (!(c.nere ? ot_sort(c, false) : ot_sort(c, false, c.veset, c.nve))) break;
+            if (c.nere && !ot_sort(c, false, c.ereset, c.nere)) break;
+            if (c.nve && !ot_sort(c, false, c.veset, c.nve)) break;
         }
         if (c.nere) {
             cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
@@ -894,7 +895,7 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
             sync_counters(c);
             c.prof.bytes[K_ERE] += 4 * (c.hc->live_cls + c.hc->live_lits);
             PassTimer t(c, 5);
-            ere_pass(c);
+            if (!ere_pass(c)) break;
         }
         if (!nmode1) break;
         // byte model: C_E, L_E of this round
