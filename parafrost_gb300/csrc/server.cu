@@ -33,6 +33,18 @@ uint64_t now_ns() {
                std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Results of one batch, every instance back to back (pfg_batch_download_all);
+// each job of the batch keeps a reference and its offsets.
+struct BatchResult {
+    std::vector<uint32_t> lits, lbd, units, pending, stack;
+    std::vector<uint64_t> off, rends;
+    std::vector<uint8_t> learnt, usage, elim;
+};
+
+struct Slice {
+    uint64_t lits = 0, cls = 0, off = 0, elim = 0, units = 0, pending = 0, stack = 0, rends = 0;
+};
+
 struct Job {
     uint64_t ticket = 0;
     // the instance (owned copy, released once uploaded)
@@ -44,10 +56,8 @@ struct Job {
     uint64_t est = 0;
     bool done = false;
     pfg_job_info info{};
-    // results
-    std::vector<uint32_t> r_lits, r_lbd, r_units, r_pending, r_stack;
-    std::vector<uint64_t> r_off, r_rends;
-    std::vector<uint8_t> r_learnt, r_usage, r_elim;
+    std::shared_ptr<BatchResult> res;   // results, from `at`
+    Slice at;
 };
 
 template <typename T>
@@ -57,12 +67,6 @@ void copy_in(std::vector<T>& dst, const T* src, uint64_t n) {
 
 template <typename T>
 const T* ptr_or_null(const std::vector<T>& v) { return v.empty() ? nullptr : v.data(); }
-
-template <typename T>
-T* out_ptr(std::vector<T>& v, uint64_t n) {
-    v.resize(n);
-    return v.data();
-}
 
 // Device bytes an instance needs inside one batch: the clause store at the
 // capacities of awaken (originals may double the clauses and literals), the
@@ -154,6 +158,30 @@ void run_batch(pfg_server* s, pfg_ctx* ctx, uint32_t slot, std::vector<Job*>& ba
     }
     pfg_stats total;
     if (rc == PFG_OK) rc = pfg_simplify(ctx, &total);
+    std::vector<pfg_result_sizes> z(n);
+    auto res = std::make_shared<BatchResult>();
+    if (rc == PFG_OK) rc = pfg_batch_result_sizes_all(ctx, z.data());
+    if (rc == PFG_OK) {
+        Slice tot;
+        for (uint32_t i = 0; i < n; i++) {
+            batch[i]->at = tot;
+            tot.lits += z[i].literals;
+            tot.cls += z[i].clauses;
+            tot.off += z[i].clauses + 1;
+            tot.elim += (uint64_t)z[i].max_var + 1;
+            tot.units += z[i].units;
+            tot.pending += z[i].pending_units;
+            tot.stack += z[i].stack_words;
+            tot.rends += z[i].rounds;
+        }
+        res->lits.resize(tot.lits); res->off.resize(tot.off); res->learnt.resize(tot.cls);
+        res->lbd.resize(tot.cls); res->usage.resize(tot.cls); res->elim.resize(tot.elim);
+        res->units.resize(tot.units); res->pending.resize(tot.pending); res->stack.resize(tot.stack);
+        res->rends.resize(tot.rends);
+        rc = pfg_batch_download_all(ctx, res->lits.data(), res->off.data(), res->learnt.data(), res->lbd.data(),
+                                    res->usage.data(), res->elim.data(), res->units.data(), res->pending.data(),
+                                    res->stack.data(), res->rends.data());
+    }
     for (uint32_t i = 0; i < n; i++) {
         Job* j = batch[i];
         pfg_job_info& in = j->info;
@@ -161,16 +189,10 @@ void run_batch(pfg_server* s, pfg_ctx* ctx, uint32_t slot, std::vector<Job*>& ba
         in.batch_size = n;
         in.slot = slot;
         if (rc != PFG_OK) continue;
-        pfg_result_sizes& z = in.sizes;
-        int r = pfg_batch_result_sizes(ctx, i, &z);
-        if (r == PFG_OK)
-            r = pfg_batch_download(ctx, i, out_ptr(j->r_lits, z.literals), out_ptr(j->r_off, z.clauses + 1),
-                                   out_ptr(j->r_learnt, z.clauses), out_ptr(j->r_lbd, z.clauses),
-                                   out_ptr(j->r_usage, z.clauses), out_ptr(j->r_elim, (uint64_t)z.max_var + 1),
-                                   out_ptr(j->r_units, z.units), out_ptr(j->r_pending, z.pending_units),
-                                   out_ptr(j->r_stack, z.stack_words), out_ptr(j->r_rends, z.rounds));
+        in.sizes = z[i];
+        j->res = res;
         pfg_stats st;
-        if (r == PFG_OK) r = pfg_batch_stats(ctx, i, &st);
+        const int r = pfg_batch_stats(ctx, i, &st);
         in.rc = r;
         if (r == PFG_OK) {
             in.status = st.status;
@@ -333,19 +355,22 @@ extern "C" int pfg_server_fetch(pfg_server* s, uint64_t ticket, uint32_t* lits, 
         s->jobs.erase(it);
     }
     if (j->info.rc != PFG_OK) return j->info.rc;
-    auto put = [](auto* dst, const auto& v) {
-        if (dst && !v.empty()) std::copy(v.begin(), v.end(), dst);
+    const pfg_result_sizes& z = j->info.sizes;
+    const BatchResult& r = *j->res;
+    const Slice& a = j->at;
+    auto put = [](auto* dst, const auto& v, uint64_t from, uint64_t count) {
+        if (dst && count) std::copy(v.begin() + from, v.begin() + from + count, dst);
     };
-    put(lits, j->r_lits);
-    put(cls_off, j->r_off);
-    put(cls_learnt, j->r_learnt);
-    put(cls_lbd, j->r_lbd);
-    put(cls_usage, j->r_usage);
-    put(eliminated, j->r_elim);
-    put(units, j->r_units);
-    put(pending_units, j->r_pending);
-    put(stack, j->r_stack);
-    put(round_ends, j->r_rends);
+    put(lits, r.lits, a.lits, z.literals);
+    put(cls_off, r.off, a.off, z.clauses + 1);
+    put(cls_learnt, r.learnt, a.cls, z.clauses);
+    put(cls_lbd, r.lbd, a.cls, z.clauses);
+    put(cls_usage, r.usage, a.cls, z.clauses);
+    put(eliminated, r.elim, a.elim, (uint64_t)z.max_var + 1);
+    put(units, r.units, a.units, z.units);
+    put(pending_units, r.pending, a.pending, z.pending_units);
+    put(stack, r.stack, a.stack, z.stack_words);
+    put(round_ends, r.rends, a.rends, z.rounds);
     return PFG_OK;
 }
 

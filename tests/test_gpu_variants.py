@@ -146,3 +146,30 @@ def test_profiler_counts_match_launches():
 def test_config3_scalefree_full_size():
     cnf = pg.scale_free(4_000_000, 16_000_000, seed=1, planted=True)
     assert_parity(cnf)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_ere_duplicate_blocks(seed):
+    # x_i's only resolvent is (a_i | b_i); the CNF holds blocks of copies of it
+    # (originals and learnts with distinct lbd/usage, so the canonical form
+    # shows which copies ERE deleted). With SUB and BVE off the first round is
+    # the ERE round; blocks longer than 32 exercise the strided-lane rule.
+    rng = np.random.default_rng(seed)
+    clauses, learnt, lbd, usage = [], [], [], []
+    nv = 0
+    for k in (1, 2, 33, 40, 70, 5):
+        x, a, b = nv + 1, nv + 2, nv + 3
+        nv += 3
+        for c in ([x, a], [-x, b]):
+            clauses.append(c); learnt.append(0); lbd.append(0); usage.append(0)
+        for _ in range(k):
+            sa = a if rng.random() < 0.8 else -a
+            clauses.append([sa, b]); learnt.append(int(rng.random() < 0.5))
+            lbd.append(int(rng.integers(1, 1000))); usage.append(int(rng.integers(0, 4)))
+    order = np.argsort(np.array(learnt), kind="stable")        # originals first, then learnts
+    cl = [clauses[i] for i in order]
+    base = pg.Cnf.from_ints(nv, cl)
+    cnf = pg.Cnf(base.max_var, base.lits, base.off, np.array(learnt, dtype=np.uint8)[order],
+                 np.array(lbd, dtype=np.uint32)[order], np.array(usage, dtype=np.uint8)[order])
+    res, ref = assert_parity(cnf, sub=False, ve=False, veextend=False, electionsmin=1)
+    assert res.stats["ere_ran"] == 1
