@@ -22,6 +22,7 @@ request loop (throughput, p50/p99 latency). `tseitin`, `ksat` and
 port; the reference's GPU simplifier cannot run here) on all host cores.
 """
 import argparse
+import concurrent.futures as cf
 import json
 import multiprocessing as mp
 import os
@@ -254,9 +255,9 @@ def oracle_run(args):
 def cpu_baseline(wname, opts, cores):
     """Oracle port timed on host cores: `cores` independent replicas at once."""
     ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
+    with cf.ProcessPoolExecutor(cores, mp_context=ctx) as pool:
         t0 = time.perf_counter()
-        res = pool.map(oracle_run, [(wname, opts)] * cores)
+        res = list(pool.map(oracle_run, [(wname, opts)] * cores))
         wall = time.perf_counter() - t0
     processed = sum(r[0] for r in res)
     return processed, wall, res
@@ -285,10 +286,11 @@ def run_reference_batch(a, world, rank):
     specs = batch_sample(batch_specs(0), 4)
     ctx = mp.get_context("spawn")
     times, proc = [], 0
-    with ctx.Pool(cores) as pool:
+    # a worker that dies raises BrokenProcessPool here instead of hanging the run
+    with cf.ProcessPoolExecutor(cores, mp_context=ctx) as pool:
         for step in range(a.warmup + a.steps):
             t0 = time.perf_counter()
-            res = pool.map(oracle_run_spec, [(sp, {}) for sp in specs], chunksize=1)
+            res = list(pool.map(oracle_run_spec, [(sp, {}) for sp in specs], chunksize=1))
             wall = time.perf_counter() - t0
             if step >= a.warmup:
                 times.append(wall)

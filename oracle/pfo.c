@@ -116,6 +116,7 @@ typedef struct {
     pfo_round* rstats; uint64_t nrstats, rstats_cap;
     uint32_t mis_rounds;
     int phase, multiplier, simpstate, status, ere_ran;
+    uint32_t* mbuf; uint64_t mcap;   /* resolvent scratch, grown to the longest merge */
 } Ctx;
 
 static inline uint32_t* CL(Ctx* c, const Cls* k) { return c->lits + k->off; }
@@ -1273,7 +1274,19 @@ static void ve_phase1_var(Ctx* c, uint32_t tid, uint32_t x, uint32_t* outs) {
 }
 
 /* ---- BVE phase 3 emission (bounded.cuh:69-258, 488-544) ---- */
-static void emit_resolvents(Ctx* c, int kind, uint32_t x, uint32_t nAddedCls, uint32_t* buf) {
+/* scratch for a merge of clauses of sizes a and b (resolvents can be longer
+   than any uploaded clause, so the buffer grows with them) */
+static uint32_t* merge_buf(Ctx* c, uint64_t a, uint64_t b) {
+    const uint64_t need = a + b + 8;
+    if (need > c->mcap) {
+        c->mcap = 2 * need;
+        c->mbuf = (uint32_t*)realloc(c->mbuf, c->mcap * sizeof(uint32_t));
+        if (!c->mbuf) { fprintf(stderr, "pfo: out of memory\n"); abort(); }
+    }
+    return c->mbuf;
+}
+
+static void emit_resolvents(Ctx* c, int kind, uint32_t x, uint32_t nAddedCls) {
     const uint32_t p = 2 * x, n = p | 1;
     uint32_t added = 0;
     const uint32_t* ml = OL(c, p); const uint32_t* ot = OL(c, n);
@@ -1285,6 +1298,7 @@ static void emit_resolvents(Ctx* c, int kind, uint32_t x, uint32_t nAddedCls, ui
             if (is_learnt(cj)) continue;
             if (kind == PAIR_SUBS && ci->molten == cj->molten) continue;
             if (kind == PAIR_CORE && ci->molten && cj->molten) continue;
+            uint32_t* buf = merge_buf(c, ci->size, cj->size);
             const int rsize = merge_out(c, x, ci, cj, buf);
             if (!rsize) continue;
             if (rsize == 1) { vpush(&c->units, buf[0]); continue; }
@@ -1300,7 +1314,7 @@ static void emit_resolvents(Ctx* c, int kind, uint32_t x, uint32_t nAddedCls, ui
     toblivion(c, p, n);
 }
 
-static void VE(Ctx* c, uint32_t* outs, uint32_t* buf) {
+static void VE(Ctx* c, uint32_t* outs) {
     const uint32_t E = c->nelected;
     for (uint32_t tid = 0; tid < E; tid++) ve_phase1_var(c, tid, c->elected[tid], outs);
     /* vePhase2: exclusive scans with the current CNF size as init (elimination.cu:74-100) */
@@ -1326,7 +1340,7 @@ static void VE(Ctx* c, uint32_t* outs, uint32_t* buf) {
                 if (c->ncls != addedPos) { fprintf(stderr, "pfo: slot mismatch\n"); abort(); }
                 saveResolvedLists(c, p, n);
                 emit_resolvents(c, et == RES_MASK ? PAIR_RES : (et == CORE_MASK ? PAIR_CORE : PAIR_SUBS),
-                                x, nAddedCls, buf);
+                                x, nAddedCls);
                 c->eliminated[x] |= MELTING_MASK | ADDING_MASK;
                 last = tid;
             } else if (et != RES_MASK) {
@@ -1369,7 +1383,7 @@ static void forward_equ(Ctx* c, const uint32_t* m, uint32_t mlen, uint32_t type)
     }
 }
 
-static void ERE(Ctx* c, uint32_t* buf) {
+static void ERE(Ctx* c) {
     const uint32_t cmax = c->o.ere_clause_max;
     for (uint32_t e = 0; e < c->nelected; e++) {
         const uint32_t v = c->elected[e], p = 2 * v, n = p | 1;
@@ -1383,6 +1397,7 @@ static void ERE(Ctx* c, uint32_t* buf) {
             for (uint32_t j = 0; j < fs; j++) {
                 Cls* neg = &c->cls[nl[j]];
                 if (is_deleted(neg) || pos->size + neg->size - 2 > cmax) continue;
+                uint32_t* buf = merge_buf(c, pos->size, neg->size);
                 const int mlen = merge_ere(c, v, pos, neg, buf);
                 if (mlen > 1) {
                     const uint32_t type = (is_learnt(pos) || is_learnt(neg)) ? ST_LEARNT : ST_ORIGINAL;
@@ -1401,6 +1416,9 @@ static void resolve_opts(pfg_options* o) {
     if (o->phases && !(o->ve_en || o->sub_en || o->bce_en)) o->phases = 0;
     if (o->phases > 1 && !o->ve_en) o->phases = 1;
     if (o->ere_clause_max > SH_MAX_ERE_OUT) o->ere_clause_max = SH_MAX_ERE_OUT;
+    /* "xormaxarity" accepts 2..20 (options.cu:60) */
+    if (o->xor_max_arity < 2) o->xor_max_arity = 2;
+    if (o->xor_max_arity > 20) o->xor_max_arity = 20;
 }
 
 static int cmp_u32(const void* a, const void* b) {
@@ -1492,7 +1510,7 @@ int pfo_simplify(const pfg_options* opts, uint32_t max_var, uint64_t ncls,
         sort_u32(CL(c, k), sz);
         calcSig(c, k);
     }
-    uint32_t* buf = (uint32_t*)xcalloc(2 * (uint64_t)maxsz + 8, sizeof(uint32_t));
+    merge_buf(c, maxsz, maxsz);
     c->numClauses = orgCls + lrnCls;
     c->numLiterals = orgLits + lrnLits;
     c->orig_lits_stat = orgLits;
@@ -1526,7 +1544,7 @@ int pfo_simplify(const pfg_options* opts, uint32_t max_var, uint64_t ncls,
             /* stop() (solver.hpp:748-753) */
             if (c->phase == c->o.phases || (cdiff == 0 && ldiff == 0) ||
                 (c->phase > 2 && ldiff <= (int64_t)c->o.phase_lits_min)) {
-                if (c->o.ere_en && c->nelected) { ERE(c, buf); c->ere_ran = 1; }
+                if (c->o.ere_en && c->nelected) { ERE(c); c->ere_ran = 1; }
                 break;
             }
             pfo_round* rs = new_rstat(c);
@@ -1538,7 +1556,7 @@ int pfo_simplify(const pfg_options* opts, uint32_t max_var, uint64_t ncls,
             const uint32_t nel0 = c->nelected;
             if (c->o.sub_en || c->o.ve_plus_en)
                 for (uint32_t e = 0; e < c->nelected; e++) sub_var(c, c->elected[e]);
-            if (c->o.ve_en) VE(c, outs, buf);
+            if (c->o.ve_en) VE(c, outs);
             push_round_end(c);
             countAll(c, &c->numClauses, &c->numLiterals);
             c->nUnits = c->units.n;
@@ -1601,7 +1619,7 @@ int pfo_simplify(const pfg_options* opts, uint32_t max_var, uint64_t ncls,
     free(c->elected); free(c->varcore); free(c->eligible); free(c->scores); free(c->rank);
     free(c->mstate); free(c->mround); free(c->frozen); free(c->win); free(c->type); free(c->ucnt);
     free(c->rpos); free(c->rref); free(c->units.d); free(c->trail.d); free(c->resolved.d);
-    free(c->round_ends_v.d); free(outs); free(buf);
+    free(c->round_ends_v.d); free(outs); free(c->mbuf);
     *out = r;
     return PFG_OK;
 }

@@ -673,6 +673,9 @@ extern "C" void pfg_resolve_options(pfg_options* o) {
     if (o->phases > 1 && !o->ve_en) o->phases = 1;
     // GOPTION::init (options.cu:84): ERE resolvents are staged in SH_MAX_ERE_OUT words
     if (o->ere_clause_max > SH_MAX_ERE_OUT) o->ere_clause_max = SH_MAX_ERE_OUT;
+    // "xormaxarity" accepts 2..20 (options.cu:60)
+    if (o->xor_max_arity < 2) o->xor_max_arity = 2;
+    if (o->xor_max_arity > 20) o->xor_max_arity = 20;
 }
 
 extern "C" int pfg_create(pfg_ctx** out, const pfg_options* opts, size_t arena_bytes) {
