@@ -173,3 +173,10 @@ def test_ere_duplicate_blocks(seed):
                  np.array(lbd, dtype=np.uint32)[order], np.array(usage, dtype=np.uint8)[order])
     res, ref = assert_parity(cnf, sub=False, ve=False, veextend=False, electionsmin=1)
     assert res.stats["ere_ran"] == 1
+
+
+def test_resolvents_longer_than_any_uploaded_clause():
+    # scale-free instance whose ERE round merges resolvents longer than every
+    # uploaded clause (it once overran the oracle's merge buffer)
+    cnf = pg.generate(2, 72030, 288120, 1, 1163604499)
+    assert_parity(cnf)
