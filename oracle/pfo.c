@@ -1357,6 +1357,49 @@ static void VE(Ctx* c, uint32_t* outs) {
     c->nelected = survivors;
 }
 
+/* ---- BCE (blocked.cuh:26-100, elimination.cu:178-291) ---- */
+/* isTautology (elimination.cuh:119-138): do c1 and c2 clash on a variable other than x? */
+static int is_tautology(Ctx* c, uint32_t x, Cls* c1, Cls* c2) {
+    const uint32_t* a = CL(c, c1); const uint32_t* b = CL(c, c2);
+    const int n1 = (int)c1->size, n2 = (int)c2->size;
+    int i = 0, j = 0;
+    while (i < n1 && j < n2) {
+        const uint32_t l1 = a[i], l2 = b[j], v1 = ABSV(l1), v2 = ABSV(l2);
+        if (v1 == x) i++;
+        else if (v2 == x) j++;
+        else if ((l1 ^ l2) == 1u) return 1;
+        else if (v1 < v2) i++;
+        else if (v2 < v1) j++;
+        else { i++; j++; }
+    }
+    return 0;
+}
+
+/* blocked_x over the (surviving) elected variables: a non-learnt clause of -x
+   whose resolvents with every non-learnt clause of x are tautologies is saved
+   with witness -x and deleted */
+static void BCE(Ctx* c) {
+    for (uint32_t e = 0; e < c->nelected; e++) {
+        const uint32_t x = c->elected[e], p = 2 * x, n = p | 1;
+        if (OLSZ(c, p) > c->o.bce_max_occurs || OLSZ(c, n) > c->o.bce_max_occurs) continue;
+        const uint32_t* pl = OL(c, p); const uint32_t* nl = OL(c, n);
+        for (uint32_t i = 0; i < OLSZ(c, n); i++) {
+            Cls* ci = &c->cls[nl[i]];
+            if (is_deleted(ci) || is_learnt(ci)) continue;
+            int all = 1;
+            for (uint32_t j = 0; j < OLSZ(c, p) && all; j++) {
+                Cls* cj = &c->cls[pl[j]];
+                if (is_deleted(cj) || is_learnt(cj)) continue;
+                if (!is_tautology(c, x, ci, cj)) all = 0;
+            }
+            if (all) {
+                saveClause(c, ci, n);
+                ci->st = ST_DELETED;
+            }
+        }
+    }
+}
+
 /* ---- ERE (redundancy.cuh:27-175) ---- */
 static int merge_ere(Ctx* c, uint32_t x, Cls* c1, Cls* c2, uint32_t* out) {
     return merge_out(c, x, c1, c2, out);
@@ -1459,7 +1502,7 @@ int pfo_simplify(const pfg_options* opts, uint32_t max_var, uint64_t ncls,
                  const uint8_t* assumed, const uint32_t* vorg,
                  pfo_result** out) {
     if (!opts || !out || !max_var || (ncls && (!lits || !cls_off))) return PFG_INVALID;
-    if (opts->bce_en || opts->proof_en) return PFG_INVALID;
+    if (opts->proof_en) return PFG_INVALID;
     Ctx C; memset(&C, 0, sizeof(C));
     Ctx* c = &C;
     c->o = *opts;
@@ -1557,6 +1600,7 @@ int pfo_simplify(const pfg_options* opts, uint32_t max_var, uint64_t ncls,
             if (c->o.sub_en || c->o.ve_plus_en)
                 for (uint32_t e = 0; e < c->nelected; e++) sub_var(c, c->elected[e]);
             if (c->o.ve_en) VE(c, outs);
+            if (c->o.bce_en && c->nelected) BCE(c);
             push_round_end(c);
             countAll(c, &c->numClauses, &c->numLiterals);
             c->nUnits = c->units.n;
@@ -1673,14 +1717,19 @@ int pfo_canon_cnf(uint64_t ncls, const uint32_t* lits, const uint64_t* off,
     return 0;
 }
 
-typedef struct { uint64_t b, e; uint32_t w; } Block;
+typedef struct { uint64_t b, e; uint32_t w, tail; } Block;
 static int block_cmp(const void* pa, const void* pb) {
     const Block* a = (const Block*)pa; const Block* b = (const Block*)pb;
+    if (a->tail != b->tail) return a->tail < b->tail ? -1 : 1;
     if ((a->w >> 1) != (b->w >> 1)) return (a->w >> 1) < (b->w >> 1) ? -1 : 1;
     return a->b < b->b ? -1 : (a->b > b->b ? 1 : 0);
 }
 
-/* A block is [clause*] [witness, 1]; stack words k > 1 are clause lengths. */
+/* A BVE block is [clause*] [witness, 1]; stack words k > 1 are clause lengths.
+   BCE saves blocked clauses one by one after the round's BVE blocks, with the
+   witness literal first and no [witness, 1] entry (blocked.cuh:64-67): those
+   trailing entries are ordered by witness variable, keeping each variable's
+   own order. */
 int pfo_canon_stack(uint64_t nstack, const uint32_t* stack, uint64_t nrounds,
                     const uint64_t* round_ends, uint32_t* out_stack) {
     Block* blocks = (Block*)xcalloc(nstack / 2 + 2, sizeof(Block));
@@ -1699,12 +1748,15 @@ int pfo_canon_stack(uint64_t nstack, const uint32_t* stack, uint64_t nrounds,
             if (k == 0 || x - 1 < rb + k) { free(blocks); return -2; }
             const uint64_t start = x - 1 - k;
             if (k == 1) {
-                if (have) { blocks[nb].b = x; blocks[nb].e = bend; blocks[nb].w = w; nb++; }
+                if (have) { blocks[nb].b = x; blocks[nb].e = bend; blocks[nb].w = w; blocks[nb].tail = 0; nb++; }
                 have = 1; w = stack[start]; bend = x;
+            } else if (!have) {   /* a BCE entry after the last BVE block */
+                blocks[nb].b = start; blocks[nb].e = x; blocks[nb].w = stack[start]; blocks[nb].tail = 1; nb++;
+                bend = start;
             }
             x = start;
         }
-        if (have) { blocks[nb].b = rb; blocks[nb].e = bend; blocks[nb].w = w; nb++; }
+        if (have) { blocks[nb].b = rb; blocks[nb].e = bend; blocks[nb].w = w; blocks[nb].tail = 0; nb++; }
         qsort(blocks, nb, sizeof(Block), block_cmp);
         for (uint64_t q = 0; q < nb; q++) {
             memcpy(out_stack + wo, stack + blocks[q].b, (blocks[q].e - blocks[q].b) * sizeof(uint32_t));

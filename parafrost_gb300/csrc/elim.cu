@@ -1221,6 +1221,79 @@ __global__ void __launch_bounds__(128) ere_k(EK k, const uint32_t* elected, uint
 
 #include "elimw.cuh"
 
+// ---- BCE (blocked.cuh:26-100): warp per surviving elected variable ----
+// isTautology (elimination.cuh:119-138)
+PFG_D bool clash_except(const EK& k, uint32_t x, const ClsHdr& h1, const ClsHdr& h2) {
+    const uint32_t* a = k.lits + h1.off;
+    const uint32_t* b = k.lits + h2.off;
+    const int n1 = (int)h1.size, n2 = (int)h2.size;
+    int i = 0, j = 0;
+    while (i < n1 && j < n2) {
+        const uint32_t l1 = a[i], l2 = b[j], v1 = ABSV(l1), v2 = ABSV(l2);
+        if (v1 == x) i++;
+        else if (v2 == x) j++;
+        else if ((l1 ^ l2) == 1u) return true;
+        else if (v1 < v2) i++;
+        else if (v2 < v1) j++;
+        else { i++; j++; }
+    }
+    return false;
+}
+
+// A lane per clause of -x (32 at a time): blocked when every non-learnt clause
+// of x clashes with it on another variable. Blocked clauses are saved with
+// witness -x in list order (one stack reservation per chunk) and deleted.
+__global__ void __launch_bounds__(128) bce_k(EK k, const uint32_t* elected, uint32_t nelected, uint32_t maxoccurs) {
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected; q += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t x = elected[q];
+        if (k.elim[x]) continue;                          // eliminated by BVE this round
+        const uint32_t p = 2 * x, n = p | 1;
+        const uint32_t ps = OLs(k, p), ns = OLs(k, n);
+        if (ps > maxoccurs || ns > maxoccurs) continue;
+        const uint32_t* pl = OLp(k, p);
+        const uint32_t* nl = OLp(k, n);
+        for (uint32_t b = 0; b < ns; b += 32) {
+            const uint32_t i = b + lane;
+            bool blocked = false;
+            uint32_t ci = 0;
+            ClsHdr hi{0, 0, 0, 0};
+            if (i < ns) {
+                ci = nl[i];
+                hi = k.hdr[ci];
+                if (!m_deleted(hi.meta) && !m_learnt(hi.meta)) {
+                    blocked = true;
+                    for (uint32_t j = 0; j < ps && blocked; j++) {
+                        const ClsHdr hj = k.hdr[pl[j]];
+                        if (m_deleted(hj.meta) || m_learnt(hj.meta)) continue;
+                        if (!clash_except(k, x, hi, hj)) blocked = false;
+                    }
+                }
+            }
+            const uint32_t words = blocked ? hi.size + 1 : 0u;
+            uint32_t total;
+            const uint32_t ex = warp_excl_scan(words, lane, total);
+            if (!total) continue;
+            unsigned long long base = 0;
+            if (lane == 0) base = stack_reserve(k, x, total);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (blocked && base != ~0ull) {
+                uint32_t* s = k.stack + base + ex;
+                const uint32_t* l = k.lits + hi.off;
+                uint32_t wpos = 0;
+                for (uint32_t t = 0; t < hi.size; t++) {
+                    if (l[t] == n) wpos = t;
+                    s[t] = org_lit(k, l[t]);
+                }
+                if (wpos) { const uint32_t tmp = s[0]; s[0] = s[wpos]; s[wpos] = tmp; }
+                s[hi.size] = hi.size;
+                k.hdr[ci].meta = m_set_st(hi.meta, ST_DELETED);
+            }
+        }
+    }
+}
+
+
 EK make_ek(Ctx& c) {
     EK k;
     k.hdr = c.hdr;
@@ -1348,6 +1421,12 @@ bool ve_pass(Ctx& c) {
     }
     push_inst_in(c);
     return cuda_ok(c, cudaGetLastError(), "ve");
+}
+
+void bce_pass(Ctx& c) {
+    if (!c.nve) return;
+    PFG_LAUNCH(K_BCE, bce_k, grid_for((uint64_t)c.nve * 32, 128), 128, 0, c.s, make_ek(c), c.veset, c.nve,
+               c.o.bce_max_occurs);
 }
 
 bool ere_pass(Ctx& c) {

@@ -685,7 +685,7 @@ extern "C" int pfg_create(pfg_ctx** out, const pfg_options* opts, size_t arena_b
     Ctx& c = o->c;
     if (opts) c.o = *opts; else pfg_default_options(&c.o);
     pfg_resolve_options(&c.o);
-    if (c.o.bce_en || c.o.proof_en) { delete o; return PFG_INVALID; }   // BCE and proof emission are not built
+    if (c.o.proof_en) { delete o; return PFG_INVALID; }   // proof emission is not built
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); delete o; return PFG_CUDA_ERROR; }
     c.device = dev;
@@ -927,6 +927,10 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         if (c.o.ve_en) {
             PassTimer t(c, 4);
             if (!ve_pass(c)) break;
+        }
+        if (c.o.bce_en) {   // SUB(), VE(), BCE() (simplify.cu:173)
+            PassTimer t(c, 7);
+            bce_pass(c);
         }
         {
             PassTimer t(c, 6);

@@ -231,6 +231,7 @@ bool lcve(Ctx& c);
 void sub_pass(Ctx& c);
 bool ve_pass(Ctx& c);
 bool ere_pass(Ctx& c);
+void bce_pass(Ctx& c);   // blocked clause elimination over the surviving elected variables
 
 // device helper: instance of a global variable (binary search over voff[0..n])
 PFG_D uint32_t inst_search(const uint32_t* voff, uint32_t n, uint32_t v) {

@@ -9,7 +9,7 @@ thread_local Profiler* g_prof = nullptr;
 const char* const kKernelNames[K_NUM] = {
     "ot_hist", "ot_fill", "ot_sort_small", "ot_sort_mid", "ot_sort_big", "scan", "radix_sort", "select",
     "lcve", "mis_win", "mis_apply", "sub", "ve_phase1", "ve_phase1_fun", "ve_phase3", "thread_fallback", "ere", "bcp", "count", "compact",
-    "upload", "download", "misc",
+    "upload", "download", "misc", "bce",
 };
 
 cudaEvent_t Profiler::next_event() {

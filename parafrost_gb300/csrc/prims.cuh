@@ -16,7 +16,7 @@ namespace pfg {
 enum KernelId : int {
     K_HIST = 0, K_FILL, K_SORT_SMALL, K_SORT_MID, K_SORT_BIG, K_SCAN, K_RADIX, K_SELECT,
     K_LCVE, K_MIS_WIN, K_MIS_APPLY, K_SUB, K_VE1, K_VE1B, K_VE3, K_BIGVAR, K_ERE, K_BCP, K_COUNT, K_COMPACT,
-    K_UPLOAD, K_DOWNLOAD, K_MISC, K_NUM
+    K_UPLOAD, K_DOWNLOAD, K_MISC, K_BCE, K_NUM
 };
 extern const char* const kKernelNames[K_NUM];
 

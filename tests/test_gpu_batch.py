@@ -64,6 +64,7 @@ VARIANTS = [
     dict(lcvefast=False), dict(vefunction=False), dict(ere=False), dict(phases=1), dict(phases=8),
     dict(collectfreq=1), dict(mupos=10, muneg=10), dict(electionsmax=6), dict(literalsmul=0.0),
     dict(velitsbound=True), dict(sub=False, veextend=False), dict(eliminatedlitsmin=1),
+    dict(all=True), dict(bce=True, ve=False, veextend=False),
 ]
 
 

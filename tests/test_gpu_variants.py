@@ -29,15 +29,14 @@ VARIANTS = [
     dict(collectfreq=0), dict(literalsmul=0.0), dict(electionsmax=6), dict(lcveclausemax=3), dict(phases=1),
     dict(phases=2, ere=False), dict(phases=8), dict(mupos=10, muneg=10), dict(eliminatedlitsmin=1),
     dict(ereclausemax=3), dict(eremaxoccurs=100), dict(submaxoccurs=100), dict(electionsmin=1000000),
-    dict(ve=False, veextend=False), dict(all=True, bce=False),
+    dict(ve=False, veextend=False), dict(all=True), dict(bce=True), dict(bce=True, ve=False, veextend=False),
+    dict(bce=True, bcemaxoccurs=100),
 ]
 
 
 @pytest.mark.parametrize("vi", range(len(VARIANTS)))
 def test_option_variants(vi):
     opts = dict(VARIANTS[vi])
-    if opts.get("all"):
-        pytest.skip("all=True enables BCE, which is not implemented")
     for seed in (vi * 3 + 1, vi * 3 + 2, vi * 3 + 3):
         assert_parity(inst(seed), **opts)
 
@@ -180,3 +179,20 @@ def test_resolvents_longer_than_any_uploaded_clause():
     # uploaded clause (it once overran the oracle's merge buffer)
     cnf = pg.generate(2, 72030, 288120, 1, 1163604499)
     assert_parity(cnf)
+
+
+
+def test_blocked_clause_elimination_fires():
+    # with BVE off BCE sees every elected variable: it must remove clauses on
+    # these instances and stay equal to the oracle
+    changed = 0
+    for seed in range(1, 9):
+        cnf = inst(seed)
+        on, _ = assert_parity(cnf, bce=True, ve=False, veextend=False, mupos=10, muneg=10)
+        off, _ = run_both(cnf, bce=False, ve=False, veextend=False, mupos=10, muneg=10)
+        changed += on.cnf.num_clauses < off.cnf.num_clauses
+    assert changed > 0
+    # variable 1 is elected and (-1 | 2) is blocked by (1 | -2)
+    cnf = pg.Cnf.from_ints(6, [[-1, 2], [1, -2], [3, 4], [-3, 5], [4, -5, 6], [-4, -6]])
+    res, _ = assert_parity(cnf, sub=False, ve=False, veextend=False, bce=True, ere=False, electionsmin=1)
+    assert res.cnf.num_clauses < cnf.num_clauses and len(res.stack) > 0

@@ -53,6 +53,7 @@ def test_oracle_preserves_satisfiability(seed):
     dict(ere=False), dict(sub=False, veextend=False), dict(vefunction=False), dict(velitsbound=True),
     dict(lcvefast=False), dict(resolventmax=0), dict(xormaxarity=2), dict(phases=1, ere=False),
     dict(collectfreq=1), dict(literalsmul=0.0), dict(electionsmax=4), dict(lcveclausemax=2),
+    dict(bce=True), dict(all=True), dict(bce=True, ve=False, veextend=False),
 ])
 def test_oracle_option_variants(variant):
     for seed in range(1, 16):
@@ -128,3 +129,27 @@ def test_known_answer_and_gate_substitution():
         for want in ([2, 4], [3, 4], [2, 5], [3, 5]):
             assert sorted(want) in cl
         assert all(1 not in c and -1 not in c for c in cl)
+
+
+def test_canon_stack_orders_trailing_blocked_clauses():
+    # round: a BVE block for var 5, then BCE entries (witness first, no [w, 1])
+    # for vars 4, 2, 4 in append order
+    b5 = [10, 4, 2, 11, 1]
+    e4a = [9, 12, 2]                 # witness 9 = -4
+    e2 = [5, 14, 2]                  # witness 5 = -2
+    e4b = [9, 16, 2]
+    stack = np.array(b5 + e4a + e2 + e4b, dtype=np.uint32)
+    ends = np.array([len(stack)], dtype=np.uint64)
+    out = po.canon_stack(stack, ends)
+    assert out.tolist() == b5 + e2 + e4a + e4b
+
+
+def test_blocked_clause_is_removed_and_model_rebuilt():
+    # variable 1 ranks first (score 1, lowest index) and is elected; (-1 | 2) is
+    # blocked on -1 by (1 | -2), the only clause of 1 (the resolvent is a
+    # tautology). SUB and BVE are off so the clause is left to BCE.
+    cnf = pg.Cnf.from_ints(6, [[-1, 2], [1, -2], [3, 4], [-3, 5], [4, -5, 6], [-4, -6]])
+    opts = pg.options_from(sub=False, ve=False, veextend=False, bce=True, ere=False, electionsmin=1)
+    res = po.simplify(cnf, opts)
+    assert res.cnf.num_clauses < cnf.num_clauses and len(res.stack) > 0
+    check_equisat(cnf, opts)
