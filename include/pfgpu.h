@@ -309,6 +309,32 @@ int  pfg_server_stats_get(pfg_server* server, pfg_server_stats* stats);
 void pfg_server_destroy(pfg_server* server);
 const char* pfg_server_last_error(pfg_server* server);
 
+/*
+ * DIMACS ingest (Solver::parse / toClause, src/gpu/dimacs.cpp:41-290): the file
+ * is memory-mapped and normalised as the reference does while parsing --
+ * repeated literals dropped, tautologies dropped, literals of unit clauses read
+ * earlier applied, one-literal clauses returned as units, an empty clause
+ * reported as PFG_UNSAT. The clauses come out in the layout pfg_upload takes.
+ */
+typedef struct pfg_dimacs pfg_dimacs;
+typedef struct pfg_dimacs_info {
+    uint32_t max_var;          /* from the header                                  */
+    int32_t  status;           /* PFG_UNKNOWN, or PFG_UNSAT (empty clause, conflict) */
+    uint64_t header_clauses;
+    uint64_t num_clauses;      /* clauses of two or more literals                  */
+    uint64_t num_literals;
+    uint64_t num_units;
+} pfg_dimacs_info;
+
+/* *out is always set (free it with pfg_dimacs_free); on PFG_INVALID
+   pfg_dimacs_error says why */
+int  pfg_dimacs_read(const char* path, pfg_dimacs** out);
+int  pfg_dimacs_get_info(pfg_dimacs* d, pfg_dimacs_info* info);
+/* lits[num_literals], cls_off[num_clauses + 1], units[num_units]; any may be NULL */
+int  pfg_dimacs_copy(pfg_dimacs* d, uint32_t* lits, uint64_t* cls_off, uint32_t* units);
+const char* pfg_dimacs_error(pfg_dimacs* d);
+void pfg_dimacs_free(pfg_dimacs* d);
+
 /* Release all device memory of the context. Replaces Solver::freeSimp (simplify.cu:254). */
 void pfg_destroy(pfg_ctx* ctx);
 

@@ -6,13 +6,14 @@ include/pfgpu.h; this package loads it (ctypes) and mirrors the reference's
 """
 from ._abi import (PFG_SAT, PFG_UNKNOWN, PFG_UNSAT, PfgOptions, PfgStats, default_options, options_dict,
                    options_from)
-from .cnf import Cnf, generate, lit_to_int, int_to_lit, random_ksat, read_dimacs, scale_free, tseitin, write_dimacs
+from .cnf import (Cnf, generate, lit_to_int, int_to_lit, parse_dimacs, random_ksat, read_dimacs, scale_free, tseitin,
+                  write_dimacs)
 from .simplifier import SimplifyError, SimplifyResult, Simplifier, simplify, simplify_batch
 from .server import JobInfo, Server
 
 __all__ = [
     "Cnf", "Simplifier", "SimplifyResult", "SimplifyError", "simplify", "generate", "random_ksat", "tseitin",
     "scale_free", "read_dimacs", "write_dimacs", "lit_to_int", "int_to_lit", "default_options", "options_from",
-    "simplify_batch", "Server", "JobInfo",
+    "simplify_batch", "Server", "JobInfo", "parse_dimacs",
     "options_dict", "PfgOptions", "PfgStats", "PFG_SAT", "PFG_UNSAT", "PFG_UNKNOWN",
 ]

@@ -139,6 +139,17 @@ class PfgServerStats(C.Structure):
     ]
 
 
+class PfgDimacsInfo(C.Structure):
+    _fields_ = [
+        ("max_var", C.c_uint32),
+        ("status", C.c_int32),
+        ("header_clauses", C.c_uint64),
+        ("num_clauses", C.c_uint64),
+        ("num_literals", C.c_uint64),
+        ("num_units", C.c_uint64),
+    ]
+
+
 PFG_PENDING = 7
 
 PASS_NAMES = ("ot", "bcp", "lcve", "sub", "ve", "ere", "gc", "other")

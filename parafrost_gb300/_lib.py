@@ -6,7 +6,7 @@ implementation to fall back to, so a missing or broken library raises.
 import ctypes as C
 import os
 
-from ._abi import PfgInstance, PfgJobInfo, PfgOptions, PfgResultSizes, PfgServerStats, PfgStats
+from ._abi import PfgDimacsInfo, PfgInstance, PfgJobInfo, PfgOptions, PfgResultSizes, PfgServerStats, PfgStats
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libpfgpu.so")
@@ -72,6 +72,16 @@ def lib():
     L.pfg_server_destroy.restype = None
     L.pfg_server_last_error.argtypes = [C.c_void_p]
     L.pfg_server_last_error.restype = C.c_char_p
+    L.pfg_dimacs_read.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+    L.pfg_dimacs_read.restype = C.c_int
+    L.pfg_dimacs_get_info.argtypes = [C.c_void_p, C.POINTER(PfgDimacsInfo)]
+    L.pfg_dimacs_get_info.restype = C.c_int
+    L.pfg_dimacs_copy.argtypes = [C.c_void_p, u32p, u64p, u32p]
+    L.pfg_dimacs_copy.restype = C.c_int
+    L.pfg_dimacs_error.argtypes = [C.c_void_p]
+    L.pfg_dimacs_error.restype = C.c_char_p
+    L.pfg_dimacs_free.argtypes = [C.c_void_p]
+    L.pfg_dimacs_free.restype = None
     L.pfg_destroy.argtypes = [C.c_void_p]
     L.pfg_destroy.restype = None
     L.pfg_last_error.argtypes = [C.c_void_p]
@@ -103,4 +113,5 @@ EXPORTED = (
     "pfg_profile_get", "pfg_batch_upload", "pfg_batch_size", "pfg_batch_stats", "pfg_batch_result_sizes",
     "pfg_batch_download", "pfg_batch_result_sizes_all", "pfg_batch_download_all", "pfg_download_device_noalloc", "pfg_server_create", "pfg_server_submit",
     "pfg_server_poll", "pfg_server_fetch", "pfg_server_stats_get", "pfg_server_destroy", "pfg_server_last_error",
+    "pfg_dimacs_read", "pfg_dimacs_get_info", "pfg_dimacs_copy", "pfg_dimacs_error", "pfg_dimacs_free",
 )

@@ -9,6 +9,8 @@ import ctypes as C
 from dataclasses import dataclass, field
 from typing import Iterable, List, Optional
 
+import os
+
 import numpy as np
 
 from . import _lib
@@ -117,6 +119,34 @@ def write_dimacs(cnf: Cnf, path: str, extra_units: Iterable[int] = ()) -> None:
             f.write(" ".join(map(str, ints[int(off[i]):int(off[i + 1])].tolist())) + " 0\n")
         for u in units:
             f.write(f"{u} 0\n")
+
+
+def parse_dimacs(path: str):
+    """Native DIMACS ingest (pfg_dimacs_read): returns (cnf, units, status).
+
+    Clauses are normalised as the reference's parser does (repeated literals
+    and tautologies dropped, earlier unit clauses applied); one-literal clauses
+    come back in `units` (literals 2v|s) and `status` is 20 when the formula
+    has an empty clause."""
+    import ctypes as C
+    from . import _abi, _lib
+    L = _lib.lib()
+    h = C.c_void_p()
+    rc = L.pfg_dimacs_read(os.fsencode(path), C.byref(h))
+    try:
+        if rc != 0:
+            msg = L.pfg_dimacs_error(h)
+            raise ValueError(f"{path}: {msg.decode() if msg else 'parse error'}")
+        info = _abi.PfgDimacsInfo()
+        L.pfg_dimacs_get_info(h, C.byref(info))
+        lits = np.empty(info.num_literals, dtype=np.uint32)
+        off = np.empty(info.num_clauses + 1, dtype=np.uint64)
+        units = np.empty(info.num_units, dtype=np.uint32)
+        L.pfg_dimacs_copy(h, lits.ctypes.data_as(C.POINTER(C.c_uint32)), off.ctypes.data_as(C.POINTER(C.c_uint64)),
+                          units.ctypes.data_as(C.POINTER(C.c_uint32)))
+        return Cnf(info.max_var, lits, off), units, int(info.status)
+    finally:
+        L.pfg_dimacs_free(h)
 
 
 def read_dimacs(path: str) -> Cnf:
