@@ -335,6 +335,21 @@ int  pfg_dimacs_copy(pfg_dimacs* d, uint32_t* lits, uint64_t* cls_off, uint32_t*
 const char* pfg_dimacs_error(pfg_dimacs* d);
 void pfg_dimacs_free(pfg_dimacs* d);
 
+/*
+ * Write-back helpers for the host solver (host code, no device work).
+ * pfg_map_vars: VMAP::initiate (src/gpu/vmap.hpp:61-72) -- variables whose
+ * eliminated byte is 0 are renumbered 1..*new_max_var in increasing order
+ * (new_of_old[max_var + 1], 0 for dropped ones; old_of_new[max_var + 1] may be
+ * NULL). pfg_map_lits: mapLit (vmap.hpp:44) over n literals; PFG_INVALID if
+ * one belongs to a dropped variable. pfg_extend_model: MODEL::extend
+ * (src/gpu/model.cpp:101-160) over the model stack, value[1..max_var] in
+ * {0, 1} on entry and on return.
+ */
+int  pfg_map_vars(uint32_t max_var, const uint8_t* eliminated, uint32_t* new_of_old, uint32_t* old_of_new,
+                  uint32_t* new_max_var);
+int  pfg_map_lits(const uint32_t* new_of_old, uint32_t max_var, uint64_t n, const uint32_t* in, uint32_t* out);
+int  pfg_extend_model(uint64_t nstack, const uint32_t* stack, uint32_t max_var, uint8_t* value);
+
 /* Release all device memory of the context. Replaces Solver::freeSimp (simplify.cu:254). */
 void pfg_destroy(pfg_ctx* ctx);
 

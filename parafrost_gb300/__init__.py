@@ -10,10 +10,11 @@ from .cnf import (Cnf, generate, lit_to_int, int_to_lit, parse_dimacs, random_ks
                   write_dimacs)
 from .simplifier import SimplifyError, SimplifyResult, Simplifier, simplify, simplify_batch
 from .server import JobInfo, Server
+from .writeback import Mapped, map_result, reconstruct_model
 
 __all__ = [
     "Cnf", "Simplifier", "SimplifyResult", "SimplifyError", "simplify", "generate", "random_ksat", "tseitin",
     "scale_free", "read_dimacs", "write_dimacs", "lit_to_int", "int_to_lit", "default_options", "options_from",
-    "simplify_batch", "Server", "JobInfo", "parse_dimacs",
+    "simplify_batch", "Server", "JobInfo", "parse_dimacs", "Mapped", "map_result", "reconstruct_model",
     "options_dict", "PfgOptions", "PfgStats", "PFG_SAT", "PFG_UNSAT", "PFG_UNKNOWN",
 ]

@@ -82,6 +82,12 @@ def lib():
     L.pfg_dimacs_error.restype = C.c_char_p
     L.pfg_dimacs_free.argtypes = [C.c_void_p]
     L.pfg_dimacs_free.restype = None
+    L.pfg_map_vars.argtypes = [C.c_uint32, u8p, u32p, u32p, C.POINTER(C.c_uint32)]
+    L.pfg_map_vars.restype = C.c_int
+    L.pfg_map_lits.argtypes = [u32p, C.c_uint32, C.c_uint64, u32p, u32p]
+    L.pfg_map_lits.restype = C.c_int
+    L.pfg_extend_model.argtypes = [C.c_uint64, u32p, C.c_uint32, u8p]
+    L.pfg_extend_model.restype = C.c_int
     L.pfg_destroy.argtypes = [C.c_void_p]
     L.pfg_destroy.restype = None
     L.pfg_last_error.argtypes = [C.c_void_p]
@@ -114,4 +120,5 @@ EXPORTED = (
     "pfg_batch_download", "pfg_batch_result_sizes_all", "pfg_batch_download_all", "pfg_download_device_noalloc", "pfg_server_create", "pfg_server_submit",
     "pfg_server_poll", "pfg_server_fetch", "pfg_server_stats_get", "pfg_server_destroy", "pfg_server_last_error",
     "pfg_dimacs_read", "pfg_dimacs_get_info", "pfg_dimacs_copy", "pfg_dimacs_error", "pfg_dimacs_free",
+    "pfg_map_vars", "pfg_map_lits", "pfg_extend_model",
 )
