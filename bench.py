@@ -614,8 +614,8 @@ def run_gpu_batch(a, world, rank, local):
 # DRAM traffic per launch of the dominant kernel group from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (workload, group).
 TRAFFIC = {
-    # profiles/ve1w_k_batched.md: 12.186 GB read + 2.175 GB written over the 5 launches of one step
-    ("batched", "ve_phase1"): (12.186e9 + 2.175e9) / 5,
+    # profiles/ve1w_k_batched.md: 12.409 GB read + 0.940 GB written over the 5 launches of one step
+    ("batched", "ve_phase1"): (12.409e9 + 0.940e9) / 5,
 }
 
 
