@@ -67,11 +67,12 @@ typedef struct pfg_options {
     uint8_t  ve_plus_en;      /* "veextend"          1     */
     uint8_t  sub_en;          /* "sub"               1     */
     uint8_t  ere_en;          /* "ere"               1     */
-    uint8_t  bce_en;          /* "bce"               0 (not implemented: must be 0) */
+    uint8_t  bce_en;          /* "bce"               0     */
     uint8_t  all_en;          /* "all"               0     */
     uint8_t  ve_fun_en;       /* "vefunction"        1     */
     uint8_t  ve_lbound_en;    /* "velitsbound"       0     */
-    uint8_t  proof_en;        /* "proof"             0 (not implemented: must be 0) */
+    uint8_t  proof_en;        /* "proof"             0: emit the binary DRAT lines of
+                                 SUB, BVE, BCE and ERE (pfg_download_proof)           */
     uint8_t  ve_inprocess;    /* 1 when Solver::stats.sigma.calls > 1: BVE counts only
                                  original clauses (in_ve_k_1, bounded.cuh:397)       */
     uint8_t  _pad[6];
@@ -101,7 +102,7 @@ typedef struct pfg_stats {
     uint64_t stack_words;     /* model-reconstruction words produced                */
     double   device_ms;       /* cudaEvent time of all rounds (upload/download excluded) */
     double   pass_ms[8];      /* per pass: ot, bcp, lcve, sub, ve, ere, gc/count, other */
-    uint64_t alg_bytes;       /* algorithmic bytes of all rounds (byte model in the design doc) */
+    uint64_t alg_bytes;       /* algorithmic bytes of all rounds (4-byte literal and clause words each pass must move) */
     uint64_t kernel_launches; /* kernels launched by pfg_simplify                   */
 } pfg_stats;
 
@@ -115,6 +116,7 @@ typedef struct pfg_result_sizes {
     uint64_t rounds;          /* entries of round_ends                              */
     uint32_t max_var;
     uint32_t _pad;
+    uint64_t proof_bytes;     /* binary DRAT bytes (proof_en)                       */
 } pfg_result_sizes;
 
 typedef struct pfg_ctx pfg_ctx;
@@ -227,6 +229,30 @@ int  pfg_batch_download_all(pfg_ctx* ctx, uint32_t* lits, uint64_t* cls_off,
                             uint8_t* cls_learnt, uint32_t* cls_lbd, uint8_t* cls_usage,
                             uint8_t* eliminated, uint32_t* units, uint32_t* pending_units,
                             uint32_t* stack, uint64_t* round_ends);
+
+/*
+ * DRAT proof of the last pfg_simplify (proof_en), size in
+ * pfg_result_sizes.proof_bytes: the binary lines the reference's device passes
+ * write (src/gpu/proof.cu, proofutils.cuh) -- clauses strengthened by SUB
+ * added and clauses it subsumed deleted, clauses substituted and resolvents
+ * (units included) added by BVE, blocked clauses deleted by BCE, redundant
+ * clauses deleted by ERE -- with literals in original variable numbering
+ * (vorg). A line is 'a' (97) or 'd' (100), then every literal 2v+s in 7-bit
+ * groups, low group first, the high bit set on all groups but the last, then
+ * a zero byte. The reference appends the lines of a pass in the order its
+ * threads get to them; here the passes of a round follow each other (SUB, BVE
+ * substitutions, BVE resolvents, BCE, ERE) and inside a pass the lines of the
+ * variables come in variable order, each variable's in the reference's order.
+ * Replaces: cuPROOF::cacheProof / writeProof (src/gpu/proof.cu:184-246).
+ */
+int  pfg_download_proof(pfg_ctx* ctx, uint8_t* out);
+int  pfg_batch_download_proof(pfg_ctx* ctx, uint32_t i, uint8_t* out);
+/* Text form of a binary proof (the reference's non-binary writer,
+   cuPROOF::writeClause, src/gpu/proof.cu:130-160): "d " before deletions,
+   signed decimal literals each followed by a space, then "0\n". *len gets the
+   text length; `out` (may be NULL) receives min(cap, *len) bytes. PFG_INVALID
+   on a malformed stream. */
+int  pfg_proof_text(const uint8_t* bin, uint64_t n, char* out, uint64_t cap, uint64_t* len);
 
 /*
  * The simplified CNF of a one-instance context written straight into
@@ -363,7 +389,8 @@ uint64_t pfg_kernel_launches(pfg_ctx* ctx);
  * Per-kernel profiling of pfg_simplify. Launch counts are always kept; with
  * profiling enabled every launch is also bracketed by CUDA events on the
  * context's stream. Kernel groups are numbered 0 .. pfg_profile_count()-1;
- * alg_bytes is the algorithmic byte count of the group (byte model in the design doc).
+ * alg_bytes is the algorithmic byte count of the group (the literal and
+ * clause words its passes must read or write, 4 bytes each).
  */
 int  pfg_profile_enable(pfg_ctx* ctx, int on);
 void pfg_profile_reset(pfg_ctx* ctx);

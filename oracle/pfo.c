@@ -46,6 +46,9 @@
 #define MAX_LBD_M 0x03FFFFFFu
 #define NOREF32 0xFFFFFFFFu
 #define ERE_LANES 32u            /* blockDim.x of ere_k = warpSize (elimination.cu:201) */
+#define ADDEDPROOF_MAX 0x3FFFFu  /* proof bytes one variable may add (constants.cuh:46)  */
+#define PROOF_ADDED   97u        /* 'a' (constants.hpp:45)                              */
+#define PROOF_DELETED 100u       /* 'd' (constants.hpp:46)                              */
 
 #define ABSV(l) ((l) >> 1)
 #define SIGNL(l) ((l) & 1u)
@@ -117,6 +120,13 @@ typedef struct {
     uint32_t mis_rounds;
     int phase, multiplier, simpstate, status, ere_ran;
     uint32_t* mbuf; uint64_t mcap;   /* resolvent scratch, grown to the longest merge */
+    /* DRAT proof (proofutils.cuh): lines of the running pass, in chunks keyed by
+       (variable << 32 | sequence); the pass's chunks are appended to the stream
+       in key order */
+    uint8_t* pbuf; uint64_t pn, pcap;
+    uint64_t* pch; uint64_t npch, pchcap;   /* triples: key, start, length */
+    uint64_t pkey, pstart;
+    uint8_t* proof; uint64_t nproof, proofcap;
 } Ctx;
 
 static inline uint32_t* CL(Ctx* c, const Cls* k) { return c->lits + k->off; }
@@ -137,6 +147,75 @@ static void* xcalloc(size_t n, size_t s) {
 /* ---- primitives (src/gpu/primitives.cuh:34-190) ---- */
 static inline uint32_t orgLit(Ctx* c, uint32_t lit) {      /* ORIGINIZELIT, primitives.cuh:34 */
     return (c->vorg[ABSV(lit)] << 1) | SIGNL(lit);
+}
+
+/* ---- DRAT proof bytes (proofutils.cuh:30-200, proof.cu:30-44) ----
+   A line is the byte 'a' or 'd', then every literal of the clause in original
+   numbering as 7-bit groups (low group first, high bit = more groups follow),
+   then a zero byte. */
+static uint32_t varint_len(uint32_t x) {             /* COUNTBYTES / BLUT (proof.cu:30-44) */
+    uint32_t n = 1;
+    while (x >= 0x80u) { x >>= 7; n++; }
+    return n;
+}
+
+static void pf_grow(Ctx* c, uint64_t more) {
+    if (c->pn + more <= c->pcap) return;
+    while (c->pn + more > c->pcap) c->pcap = c->pcap ? 2 * c->pcap : 4096;
+    c->pbuf = (uint8_t*)realloc(c->pbuf, c->pcap);
+    if (!c->pbuf) { fprintf(stderr, "pfo: out of memory\n"); abort(); }
+}
+
+static void pf_open(Ctx* c, uint32_t x, uint32_t seq) {
+    c->pkey = ((uint64_t)x << 32) | seq;
+    c->pstart = c->pn;
+}
+
+static void pf_close(Ctx* c) {
+    if (c->pn == c->pstart) return;
+    if (c->npch + 3 > c->pchcap) {
+        c->pchcap = c->pchcap ? 2 * c->pchcap : 768;
+        c->pch = (uint64_t*)realloc(c->pch, c->pchcap * sizeof(uint64_t));
+        if (!c->pch) { fprintf(stderr, "pfo: out of memory\n"); abort(); }
+    }
+    c->pch[c->npch++] = c->pkey;
+    c->pch[c->npch++] = c->pstart;
+    c->pch[c->npch++] = c->pn - c->pstart;
+}
+
+/* saveProofClause / saveProofUnit (proofutils.cuh:113-170) */
+static void pf_line(Ctx* c, uint32_t state, const uint32_t* l, uint32_t n) {
+    pf_grow(c, 2 + 5ull * n);
+    c->pbuf[c->pn++] = (uint8_t)state;
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t v = (c->vorg[l[i] >> 1] << 1) | (l[i] & 1u);        /* ORIGINIZELIT */
+        while (v >= 0x80u) { c->pbuf[c->pn++] = (uint8_t)((v & 0x7Fu) | 0x80u); v >>= 7; }
+        c->pbuf[c->pn++] = (uint8_t)v;
+    }
+    c->pbuf[c->pn++] = 0;
+}
+
+static int pch_cmp(const void* pa, const void* pb) {
+    const uint64_t a = *(const uint64_t*)pa, b = *(const uint64_t*)pb;
+    return a < b ? -1 : (a > b ? 1 : 0);
+}
+
+/* end of a pass: its chunks join the stream ordered by (variable, sequence) */
+static void pf_flush(Ctx* c) {
+    if (!c->o.proof_en || !c->npch) { c->pn = 0; c->npch = 0; return; }
+    qsort(c->pch, c->npch / 3, 3 * sizeof(uint64_t), pch_cmp);
+    for (uint64_t i = 0; i < c->npch; i += 3) {
+        const uint64_t st = c->pch[i + 1], len = c->pch[i + 2];
+        if (c->nproof + len > c->proofcap) {
+            while (c->nproof + len > c->proofcap) c->proofcap = c->proofcap ? 2 * c->proofcap : 4096;
+            c->proof = (uint8_t*)realloc(c->proof, c->proofcap);
+            if (!c->proof) { fprintf(stderr, "pfo: out of memory\n"); abort(); }
+        }
+        memcpy(c->proof + c->nproof, c->pbuf + st, len);
+        c->nproof += len;
+    }
+    c->pn = 0;
+    c->npch = 0;
 }
 
 static void sort_u32(uint32_t* d, uint32_t n) {             /* devSort result: ascending */
@@ -566,6 +645,49 @@ static int merge_out(Ctx* c, uint32_t x, Cls* c1, Cls* c2, uint32_t* out) {
     return len;
 }
 
+/* mergeProof (elimination.cuh:162-213): proof bytes of the resolvent of c1 and
+   c2 on x (prefix + literals + terminator), 0 for a tautology */
+static uint32_t merge_bytes(Ctx* c, uint32_t x, Cls* c1, Cls* c2) {
+    const uint32_t* a = CL(c, c1); const uint32_t* b = CL(c, c2);
+    const int n1 = (int)c1->size, n2 = (int)c2->size;
+    int i = 0, j = 0;
+    uint32_t bytes = 2;
+    while (i < n1 && j < n2) {
+        const uint32_t l1 = a[i], l2 = b[j], v1 = ABSV(l1), v2 = ABSV(l2);
+        if (v1 == x) i++;
+        else if (v2 == x) j++;
+        else if ((l1 ^ l2) == 1u) return 0;
+        else if (v1 < v2) { i++; bytes += varint_len(orgLit(c, l1)); }
+        else if (v2 < v1) { j++; bytes += varint_len(orgLit(c, l2)); }
+        else { i++; j++; bytes += varint_len(orgLit(c, l1)); }
+    }
+    while (i < n1) { const uint32_t l1 = a[i++]; if (ABSV(l1) != x) bytes += varint_len(orgLit(c, l1)); }
+    while (j < n2) { const uint32_t l2 = b[j++]; if (ABSV(l2) != x) bytes += varint_len(orgLit(c, l2)); }
+    return bytes;
+}
+
+static inline int pair_ok(int kind, Cls* ci, Cls* cj);
+
+/* the guard the counting loops add when proofs are on (resolve.cuh:66-70,
+   elimination.cuh:445-447, function.cuh:233): more than ADDEDCLS_MAX unit
+   resolvents or more than ADDEDPROOF_MAX proof bytes rule the variable out;
+   true = ruled out */
+static int proof_guard(Ctx* c, int kind, uint32_t x, uint32_t me, uint32_t other, uint32_t nUnits) {
+    if (nUnits > ADDEDCLS_MAX) return 1;
+    uint64_t bytes = 0;
+    const uint32_t* ml = OL(c, me); const uint32_t* ot = OL(c, other);
+    for (uint32_t i = 0; i < OLSZ(c, me); i++) {
+        Cls* ci = &c->cls[ml[i]];
+        if (is_learnt(ci)) continue;
+        for (uint32_t j = 0; j < OLSZ(c, other); j++) {
+            Cls* cj = &c->cls[ot[j]];
+            if (!pair_ok(kind, ci, cj)) continue;
+            bytes += merge_bytes(c, x, ci, cj);
+        }
+    }
+    return bytes > ADDEDPROOF_MAX;
+}
+
 static uint32_t countLitsBefore(Ctx* c, uint32_t lit) {           /* elimination.cuh:365 */
     uint32_t s = 0; const uint32_t* ol = OL(c, lit);
     for (uint32_t i = 0; i < OLSZ(c, lit); i++) {
@@ -611,6 +733,7 @@ static int countSubst(Ctx* c, int kind, uint32_t x, uint32_t nClsBefore, uint32_
         const uint32_t before = countLitsBefore(c, me) + countLitsBefore(c, other);
         if (*nL > before) return 1;
     }
+    if (c->o.proof_en && proof_guard(c, kind, x, me, other, *nE)) return 1;
     return 0;
 }
 
@@ -635,6 +758,7 @@ static int countResolventsU(Ctx* c, uint32_t x, uint32_t me, uint32_t other,
         }
     }
     if (*nC > ADDEDCLS_MAX || *nL > ADDEDLITS_MAX) return 0;
+    if (c->o.proof_en && proof_guard(c, PAIR_RES, x, me, other, *nE)) return 0;
     return 1;
 }
 
@@ -663,6 +787,7 @@ static int countResolventsB(Ctx* c, uint32_t x, uint32_t nClsBefore, uint32_t me
         const uint32_t before = countLitsBefore(c, me) + countLitsBefore(c, other);
         if (*nL > before) return 0;
     }
+    if (c->o.proof_en && proof_guard(c, PAIR_RES, x, me, other, *nE)) return 0;
     return 1;
 }
 
@@ -1048,6 +1173,18 @@ static void substitute_single(Ctx* c, uint32_t p, uint32_t n, uint32_t def) {
         if (nNeg) appendUnits(c, n);
         if (nPos) appendUnits(c, p);
     }
+    if (c->o.proof_en) {                 /* addProof over negs, then poss (equivalence.cuh:100-111) */
+        pf_open(c, ABSV(p), 0);
+        for (int side = 0; side < 2; side++) {
+            const uint32_t lit = side ? p : n;
+            const uint32_t* ol = OL(c, lit);
+            for (uint32_t i = 0; i < OLSZ(c, lit); i++) {
+                Cls* k = &c->cls[ol[i]];
+                if (is_orig(k)) pf_line(c, PROOF_ADDED, CL(c, k), k->size);
+            }
+        }
+        pf_close(c);
+    }
 }
 
 /* find_sfanin (equivalence.cuh:106-122) */
@@ -1209,6 +1346,19 @@ static void sub_var(Ctx* c, uint32_t x) {
         if (nPos) appendUnits(c, p);
         if (nNeg) appendUnits(c, n);
     }
+    if (c->o.proof_en) {                 /* saveProof over poss, then negs (subsume.cuh:464-474, proofutils.cuh:180-200) */
+        pf_open(c, x, 0);
+        for (int side = 0; side < 2; side++) {
+            const uint32_t lit = side ? n : p;
+            const uint32_t* ol = OL(c, lit);
+            for (uint32_t i = 0; i < OLSZ(c, lit); i++) {
+                Cls* k = &c->cls[ol[i]];
+                if (k->molten) pf_line(c, PROOF_ADDED, CL(c, k), k->size);
+                if (is_deleted(k)) pf_line(c, PROOF_DELETED, CL(c, k), k->size);
+            }
+        }
+        pf_close(c);
+    }
     updateOL(c, p);
     updateOL(c, n);
 }
@@ -1290,6 +1440,7 @@ static void emit_resolvents(Ctx* c, int kind, uint32_t x, uint32_t nAddedCls) {
     const uint32_t p = 2 * x, n = p | 1;
     uint32_t added = 0;
     const uint32_t* ml = OL(c, p); const uint32_t* ot = OL(c, n);
+    if (c->o.proof_en) pf_open(c, x, 0);
     for (uint32_t i = 0; i < OLSZ(c, p) && added < nAddedCls; i++) {
         Cls* ci = &c->cls[ml[i]];
         if (is_learnt(ci)) continue;
@@ -1301,6 +1452,7 @@ static void emit_resolvents(Ctx* c, int kind, uint32_t x, uint32_t nAddedCls) {
             uint32_t* buf = merge_buf(c, ci->size, cj->size);
             const int rsize = merge_out(c, x, ci, cj, buf);
             if (!rsize) continue;
+            if (c->o.proof_en) pf_line(c, PROOF_ADDED, buf, (uint32_t)rsize);    /* ADD_RESOLVENT's proof line */
             if (rsize == 1) { vpush(&c->units, buf[0]); continue; }
             /* ADD_RESOLVENT (bounded.cuh:69-122): ORIGINAL, added, sig */
             const uint64_t off = push_lits(c, buf, (uint32_t)rsize);
@@ -1311,12 +1463,14 @@ static void emit_resolvents(Ctx* c, int kind, uint32_t x, uint32_t nAddedCls) {
             added++;
         }
     }
+    if (c->o.proof_en) pf_close(c);
     toblivion(c, p, n);
 }
 
 static void VE(Ctx* c, uint32_t* outs) {
     const uint32_t E = c->nelected;
     for (uint32_t tid = 0; tid < E; tid++) ve_phase1_var(c, tid, c->elected[tid], outs);
+    pf_flush(c);                                                   /* substitution lines (ve_k_1) */
     /* vePhase2: exclusive scans with the current CNF size as init (elimination.cu:74-100) */
     uint64_t pos = c->ncls, ref = c->data_size;
     for (uint32_t tid = 0; tid < E; tid++) {
@@ -1349,6 +1503,7 @@ static void VE(Ctx* c, uint32_t* outs) {
         }
         if (!c->eliminated[x]) c->elected[survivors++] = x;     /* postVE: DeviceSelect::If */
     }
+    pf_flush(c);                                                   /* resolvent lines (ve_k_2) */
     if (last >= 0) {                                               /* resizeCNF_k (cnf.cu:55-80) */
         const uint32_t xinfo = c->type[last];
         const uint64_t nAddedCls = (xinfo & 0xFFFCu) >> 2, nAddedLits = xinfo >> 16;
@@ -1394,10 +1549,16 @@ static void BCE(Ctx* c) {
             }
             if (all) {
                 saveClause(c, ci, n);
+                if (c->o.proof_en) {          /* blocked.cuh:67-72 */
+                    pf_open(c, x, i);
+                    pf_line(c, PROOF_DELETED, CL(c, ci), ci->size);
+                    pf_close(c);
+                }
                 ci->st = ST_DELETED;
             }
         }
     }
+    pf_flush(c);
 }
 
 /* ---- ERE (redundancy.cuh:27-175) ---- */
@@ -1405,7 +1566,7 @@ static int merge_ere(Ctx* c, uint32_t x, Cls* c1, Cls* c2, uint32_t* out) {
     return merge_out(c, x, c1, c2, out);
 }
 
-static void forward_equ(Ctx* c, const uint32_t* m, uint32_t mlen, uint32_t type) {
+static void forward_equ(Ctx* c, const uint32_t* m, uint32_t mlen, uint32_t type, uint32_t v, uint32_t* seq) {
     uint32_t best = m[0], msig = MAPHASH(best);
     uint32_t minsize = OLSZ(c, best);
     for (uint32_t k = 1; k < mlen; k++) {
@@ -1420,6 +1581,11 @@ static void forward_equ(Ctx* c, const uint32_t* m, uint32_t mlen, uint32_t type)
             if (mlen == k->size && (is_learnt(k) || k->st == type) && SUBSIG(msig, k->sig) &&
                 !is_deleted(k) && isEqual(c, k, m, mlen)) {
                 k->st = ST_DELETED;
+                if (c->o.proof_en) {          /* redundancy.cuh:122-128 */
+                    pf_open(c, v, (*seq)++);
+                    pf_line(c, PROOF_DELETED, CL(c, k), k->size);
+                    pf_close(c);
+                }
                 break;
             }
         }
@@ -1434,6 +1600,7 @@ static void ERE(Ctx* c) {
         if (!(ds && fs && ds <= c->o.ere_max_occurs && fs <= c->o.ere_max_occurs)) continue;
         const uint32_t* pl = OL(c, p); const uint32_t* nl = OL(c, n);
         if (!(c->cls[pl[0]].size <= cmax && c->cls[nl[0]].size <= cmax)) continue;
+        uint32_t seq = 0;
         for (uint32_t i = 0; i < ds; i++) {
             Cls* pos = &c->cls[pl[i]];
             if (is_deleted(pos)) continue;
@@ -1444,11 +1611,12 @@ static void ERE(Ctx* c) {
                 const int mlen = merge_ere(c, v, pos, neg, buf);
                 if (mlen > 1) {
                     const uint32_t type = (is_learnt(pos) || is_learnt(neg)) ? ST_LEARNT : ST_ORIGINAL;
-                    forward_equ(c, buf, (uint32_t)mlen, type);
+                    forward_equ(c, buf, (uint32_t)mlen, type, v, &seq);
                 }
             }
         }
     }
+    pf_flush(c);
 }
 
 /* ---- option folding (OPTION::init, options.cpp:276-297; GOPTION::init, options.cu:75-88) ---- */
@@ -1502,7 +1670,6 @@ int pfo_simplify(const pfg_options* opts, uint32_t max_var, uint64_t ncls,
                  const uint8_t* assumed, const uint32_t* vorg,
                  pfo_result** out) {
     if (!opts || !out || !max_var || (ncls && (!lits || !cls_off))) return PFG_INVALID;
-    if (opts->proof_en) return PFG_INVALID;
     Ctx C; memset(&C, 0, sizeof(C));
     Ctx* c = &C;
     c->o = *opts;
@@ -1597,8 +1764,10 @@ int pfo_simplify(const pfg_options* opts, uint32_t max_var, uint64_t ncls,
             rs->literals_before = c->numLiterals;
             const uint64_t ncls0 = c->ncls;
             const uint32_t nel0 = c->nelected;
-            if (c->o.sub_en || c->o.ve_plus_en)
+            if (c->o.sub_en || c->o.ve_plus_en) {
                 for (uint32_t e = 0; e < c->nelected; e++) sub_var(c, c->elected[e]);
+                pf_flush(c);
+            }
             if (c->o.ve_en) VE(c, outs);
             if (c->o.bce_en && c->nelected) BCE(c);
             push_round_end(c);
@@ -1657,13 +1826,16 @@ int pfo_simplify(const pfg_options* opts, uint32_t max_var, uint64_t ncls,
     r->nround_stats = c->nrstats;
     r->round_stats = c->rstats ? c->rstats : (pfo_round*)xcalloc(1, sizeof(pfo_round));
     c->rstats = NULL;
+    r->nproof = c->nproof;
+    r->proof = c->proof ? c->proof : (uint8_t*)xcalloc(1, 1);
+    c->proof = NULL;
     /* free context */
     free(c->vorg); free(c->vstate); free(c->assumed); free(c->lits); free(c->cls);
     free(c->hist); free(c->ot_off); free(c->ot_size); free(c->ot_pool); free(c->eliminated);
     free(c->elected); free(c->varcore); free(c->eligible); free(c->scores); free(c->rank);
     free(c->mstate); free(c->mround); free(c->frozen); free(c->win); free(c->type); free(c->ucnt);
     free(c->rpos); free(c->rref); free(c->units.d); free(c->trail.d); free(c->resolved.d);
-    free(c->round_ends_v.d); free(outs); free(c->mbuf);
+    free(c->round_ends_v.d); free(outs); free(c->mbuf); free(c->pbuf); free(c->pch);
     *out = r;
     return PFG_OK;
 }
@@ -1672,7 +1844,7 @@ void pfo_free(pfo_result* r) {
     if (!r) return;
     free(r->lits); free(r->cls_off); free(r->cls_learnt); free(r->cls_lbd); free(r->cls_usage);
     free(r->eliminated); free(r->units); free(r->pending); free(r->stack); free(r->round_ends);
-    free(r->round_stats);
+    free(r->round_stats); free(r->proof);
     free(r);
 }
 
@@ -1788,6 +1960,90 @@ void pfo_extend_model(uint64_t nstack, const uint32_t* stack, uint8_t* value) {
 /* ---- small DPLL solver used by the tests to check satisfiability and models ----
    Two watched literals, chronological backtracking; returns 10 (SAT, model in
    value[1..V]), 20 (UNSAT) or 0 (decision budget exhausted). */
+/* ---- DRAT RUP check of a simplifier proof (test helper) ----
+   Naive unit propagation over all active clauses; enough for the small
+   formulas the tests check. */
+typedef struct { uint32_t* l; uint32_t n; int active; } RupCls;
+
+static int rup_propagate(RupCls* db, uint64_t n, int8_t* val) {   /* 1 = conflict */
+    int changed = 1;
+    while (changed) {
+        changed = 0;
+        for (uint64_t i = 0; i < n; i++) {
+            if (!db[i].active) continue;
+            uint32_t unset = 0, last = 0; int sat = 0;
+            for (uint32_t t = 0; t < db[i].n && !sat; t++) {
+                const uint32_t l = db[i].l[t];
+                const int8_t v = val[l >> 1];
+                if (!v) { unset++; last = l; }
+                else if ((v > 0) != ((l & 1u) != 0)) sat = 1;
+            }
+            if (sat) continue;
+            if (!unset) return 1;
+            if (unset == 1) { val[last >> 1] = (last & 1u) ? -1 : 1; changed = 1; }
+        }
+    }
+    return 0;
+}
+
+static int rup_same(const RupCls* k, const uint32_t* l, uint32_t n) {
+    if (k->n != n) return 0;
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t f = 0;
+        for (uint32_t j = 0; j < n && !f; j++) f = k->l[j] == l[i];
+        if (!f) return 0;
+    }
+    return 1;
+}
+
+int64_t pfo_check_rup(uint32_t V, uint64_t ncls, const uint32_t* lits, const uint64_t* off,
+                      const uint8_t* proof, uint64_t nproof, uint64_t* missing_deletions) {
+    uint64_t cap = ncls + 64, n = 0;
+    RupCls* db = (RupCls*)xcalloc(cap, sizeof(RupCls));
+    for (uint64_t i = 0; i < ncls; i++) {
+        const uint32_t sz = (uint32_t)(off[i + 1] - off[i]);
+        db[n].l = (uint32_t*)xcalloc(sz + 1, sizeof(uint32_t));
+        memcpy(db[n].l, lits + off[i], sz * sizeof(uint32_t));
+        db[n].n = sz; db[n].active = 1; n++;
+    }
+    int8_t* val = (int8_t*)xcalloc(V + 1, 1);
+    uint32_t* line = (uint32_t*)xcalloc(V + 8, sizeof(uint32_t));
+    int64_t bad = 0, lineno = 0;
+    uint64_t p = 0, missing = 0;
+    while (p < nproof && !bad) {
+        const uint8_t st = proof[p++];
+        uint32_t len = 0;
+        lineno++;
+        if (st != PROOF_ADDED && st != PROOF_DELETED) { bad = lineno; break; }
+        while (p < nproof && proof[p]) {
+            uint32_t v = 0, sh = 0; uint8_t b;
+            do { b = proof[p++]; v |= (uint32_t)(b & 0x7Fu) << sh; sh += 7; } while ((b & 0x80u) && p < nproof);
+            if ((v >> 1) == 0 || (v >> 1) > V || len > V + 4) { bad = lineno; break; }
+            line[len++] = v;
+        }
+        if (bad) break;
+        if (p >= nproof) { bad = lineno; break; }
+        p++;                                            /* terminator */
+        if (st == PROOF_DELETED) {
+            uint64_t i = 0;
+            for (; i < n; i++) if (db[i].active && rup_same(&db[i], line, len)) break;
+            if (i < n) db[i].active = 0; else missing++;
+            continue;
+        }
+        memset(val, 0, V + 1);
+        for (uint32_t i = 0; i < len; i++) val[line[i] >> 1] = (line[i] & 1u) ? 1 : -1;   /* negation */
+        if (!rup_propagate(db, n, val)) { bad = lineno; break; }
+        if (n == cap) { cap *= 2; db = (RupCls*)realloc(db, cap * sizeof(RupCls)); }
+        db[n].l = (uint32_t*)xcalloc(len + 1, sizeof(uint32_t));
+        memcpy(db[n].l, line, len * sizeof(uint32_t));
+        db[n].n = len; db[n].active = 1; n++;
+    }
+    for (uint64_t i = 0; i < n; i++) free(db[i].l);
+    free(db); free(val); free(line);
+    if (missing_deletions) *missing_deletions = missing;
+    return bad;
+}
+
 int pfo_solve(uint32_t V, uint64_t ncls, const uint32_t* lits, const uint64_t* off,
               uint8_t* value, uint64_t max_decisions) {
     const uint64_t nl = 2ull * V + 2;

@@ -63,6 +63,8 @@ typedef struct pfo_result {
     uint64_t* round_ends;    /* stack length after each round              */
     uint64_t  nround_stats;
     pfo_round* round_stats;
+    uint64_t  nproof;
+    uint8_t*  proof;         /* binary DRAT lines of the simplifier (proof_en)  */
 } pfo_result;
 
 /* Run one Solver::simplify call on the given clause database. */
@@ -96,6 +98,16 @@ int pfo_canon_stack(uint64_t nstack, const uint32_t* stack, uint64_t nrounds,
  * 0/1 for v in [1, max_var]; updated in place.
  */
 void pfo_extend_model(uint64_t nstack, const uint32_t* stack, uint8_t* value);
+
+/*
+ * RUP check of a binary DRAT proof (test helper): every added line must follow
+ * by unit propagation from the formula plus the earlier lines, minus deleted
+ * clauses. Returns 0 when every line checks, else the 1-based number of the
+ * first line that does not (or is malformed); *missing_deletions counts
+ * deletions of clauses that were not present.
+ */
+int64_t pfo_check_rup(uint32_t V, uint64_t ncls, const uint32_t* lits, const uint64_t* off,
+                      const uint8_t* proof, uint64_t nproof, uint64_t* missing_deletions);
 
 /*
  * Small DPLL solver for the tests (two watched literals). Returns 10 (SAT,

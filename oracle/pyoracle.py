@@ -45,6 +45,7 @@ class PfoResult(C.Structure):
         ("nstack", C.c_uint64), ("stack", u32p),
         ("nround_ends", C.c_uint64), ("round_ends", u64p),
         ("nround_stats", C.c_uint64), ("round_stats", C.POINTER(PfoRound)),
+        ("nproof", C.c_uint64), ("proof", u8p),
     ]
 
 
@@ -68,6 +69,8 @@ def lib():
         L.pfo_extend_model.restype = None
         L.pfo_solve.argtypes = [C.c_uint32, C.c_uint64, u32p, u64p, u8p, C.c_uint64]
         L.pfo_solve.restype = C.c_int
+        L.pfo_check_rup.argtypes = [C.c_uint32, C.c_uint64, u32p, u64p, u8p, C.c_uint64, u64p]
+        L.pfo_check_rup.restype = C.c_int64
         _L = L
     return _L
 
@@ -99,6 +102,7 @@ class OracleResult:
         self.round_ends = _arr(r.round_ends, r.nround_ends, np.uint64)
         self.round_stats = [{f[0]: getattr(r.round_stats[i], f[0]) for f in PfoRound._fields_}
                             for i in range(r.nround_stats)]
+        self.proof = bytes(_arr(r.proof, r.nproof, np.uint8))
 
 
 def simplify(cnf: Cnf, opts: PfgOptions, var_state=None, assumed=None, vorg=None) -> OracleResult:
@@ -161,6 +165,18 @@ def solve(cnf: Cnf, max_decisions: int = 10_000_000):
     rc = L.pfo_solve(cnf.max_var, cnf.num_clauses, _p(cnf.lits, C.c_uint32), _p(cnf.off, C.c_uint64),
                      _p(model, C.c_uint8), max_decisions)
     return rc, model
+
+
+def check_rup(cnf: Cnf, proof: bytes):
+    """RUP-check a binary DRAT proof against `cnf`: returns (first failing
+    line or 0, deletions of absent clauses)."""
+    L = lib()
+    pb = np.frombuffer(proof, dtype=np.uint8) if proof else np.zeros(1, dtype=np.uint8)
+    pb = np.ascontiguousarray(pb)
+    missing = C.c_uint64(0)
+    bad = L.pfo_check_rup(cnf.max_var, cnf.num_clauses, _p(cnf.lits, C.c_uint32), _p(cnf.off, C.c_uint64),
+                          _p(pb, C.c_uint8), len(proof), C.byref(missing))
+    return int(bad), int(missing.value)
 
 
 def satisfies(cnf: Cnf, value: np.ndarray) -> bool:

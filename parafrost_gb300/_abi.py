@@ -90,6 +90,7 @@ class PfgResultSizes(C.Structure):
         ("rounds", C.c_uint64),
         ("max_var", C.c_uint32),
         ("_pad", C.c_uint32),
+        ("proof_bytes", C.c_uint64),
     ]
 
 

@@ -88,6 +88,12 @@ def lib():
     L.pfg_map_lits.restype = C.c_int
     L.pfg_extend_model.argtypes = [C.c_uint64, u32p, C.c_uint32, u8p]
     L.pfg_extend_model.restype = C.c_int
+    L.pfg_download_proof.argtypes = [C.c_void_p, u8p]
+    L.pfg_download_proof.restype = C.c_int
+    L.pfg_batch_download_proof.argtypes = [C.c_void_p, C.c_uint32, u8p]
+    L.pfg_batch_download_proof.restype = C.c_int
+    L.pfg_proof_text.argtypes = [u8p, C.c_uint64, C.c_char_p, C.c_uint64, u64p]
+    L.pfg_proof_text.restype = C.c_int
     L.pfg_destroy.argtypes = [C.c_void_p]
     L.pfg_destroy.restype = None
     L.pfg_last_error.argtypes = [C.c_void_p]
@@ -120,5 +126,6 @@ EXPORTED = (
     "pfg_batch_download", "pfg_batch_result_sizes_all", "pfg_batch_download_all", "pfg_download_device_noalloc", "pfg_server_create", "pfg_server_submit",
     "pfg_server_poll", "pfg_server_fetch", "pfg_server_stats_get", "pfg_server_destroy", "pfg_server_last_error",
     "pfg_dimacs_read", "pfg_dimacs_get_info", "pfg_dimacs_copy", "pfg_dimacs_error", "pfg_dimacs_free",
-    "pfg_map_vars", "pfg_map_lits", "pfg_extend_model",
+    "pfg_map_vars", "pfg_map_lits", "pfg_extend_model", "pfg_download_proof", "pfg_batch_download_proof",
+    "pfg_proof_text",
 )

@@ -42,6 +42,10 @@ constexpr uint32_t LBD_TIER1 = 2u;
 constexpr uint32_t USAGET3 = 1u;
 constexpr uint32_t NOREF = 0xFFFFFFFFu;
 constexpr uint32_t ERE_LANES = 32u;  // blockDim.x of the reference's ere_k
+// DRAT proof (src/gpu/constants.cuh:46, constants.hpp:45-46)
+constexpr uint32_t ADDEDPROOF_MAX = 0x3FFFFu;   // proof bytes one variable may add
+constexpr uint8_t PROOF_ADDED = 97u;            // 'a'
+constexpr uint8_t PROOF_DELETED = 100u;         // 'd'
 
 struct __align__(16) ClsHdr {
     uint32_t off;
@@ -86,6 +90,9 @@ struct DevCounters {
     uint32_t nbig_sub, nbig_ve1, nbig_ve3;   // variables too large for the warp stage
     unsigned long long ve_cls, ve_lits;      // store size after the last BVE emission
     uint32_t sort_warp;                      // lists sorted by one warp each
+    unsigned long long pf_words;             // proof line words reserved in the running pass
+    unsigned long long pf_need;              // proof words BVE emission needs
+    uint32_t pf_blocks;                      // proof blocks reserved in the running pass
 };
 
 constexpr uint32_t ERR_UNITS_OVERFLOW = 1u;
@@ -93,5 +100,6 @@ constexpr uint32_t ERR_STACK_OVERFLOW = 2u;
 constexpr uint32_t ERR_SLOT_MISMATCH = 4u;
 constexpr uint32_t ERR_BAD_LIT = 8u;
 constexpr uint32_t ERR_OT_OVERFLOW = 16u;
+constexpr uint32_t ERR_PROOF_OVERFLOW = 32u;
 
 }  // namespace pfg

@@ -37,6 +37,12 @@ struct EK {
     DevCounters* dc;
     uint32_t ve_clause_max, xor_max_arity, sub_max_occurs, ere_max_occurs, ere_clause_max;
     int ve_lbound_en, ve_inprocess;
+    int proof;                           // DRAT lines are written (proof_en)
+    uint32_t* pf_w;                      // proof line words of the running pass
+    unsigned long long pf_wcap;
+    ulonglong2* pf_b;                    // proof blocks {variable << 32 | sequence, first word}
+    uint32_t pf_bcap;
+    const uint8_t* lbyte;                // proof bytes per literal
 };
 
 PFG_D uint32_t* OLp(const EK& k, uint32_t lit) { return k.ot_ids + k.ot_off[lit]; }
@@ -184,6 +190,51 @@ PFG_D bool pair_ok(int kind, uint32_t mi, uint32_t mj) {
     return m_orig(mj) && (!m_molten(mi) || !m_molten(mj));
 }
 
+// mergeProof (elimination.cuh:162-213): proof bytes of the resolvent of c1 and
+// c2 on x, 0 for a tautology
+PFG_D uint32_t merge_bytes(const EK& k, uint32_t x, uint32_t c1, uint32_t c2) {
+    const ClsHdr h1 = k.hdr[c1], h2 = k.hdr[c2];
+    const uint32_t* a = k.lits + h1.off;
+    const uint32_t* b = k.lits + h2.off;
+    const int n1 = (int)h1.size, n2 = (int)h2.size;
+    int i = 0, j = 0;
+    uint32_t bytes = 2;
+    while (i < n1 && j < n2) {
+        const uint32_t l1 = a[i], l2 = b[j], v1 = ABSV(l1), v2 = ABSV(l2);
+        if (v1 == x) i++;
+        else if (v2 == x) j++;
+        else if ((l1 ^ l2) == 1u) return 0;
+        else if (v1 < v2) { i++; bytes += k.lbyte[l1]; }
+        else if (v2 < v1) { j++; bytes += k.lbyte[l2]; }
+        else { i++; j++; bytes += k.lbyte[l1]; }
+    }
+    while (i < n1) { const uint32_t l1 = a[i++]; if (ABSV(l1) != x) bytes += k.lbyte[l1]; }
+    while (j < n2) { const uint32_t l2 = b[j++]; if (ABSV(l2) != x) bytes += k.lbyte[l2]; }
+    return bytes;
+}
+
+// The guard the counting loops add when proofs are on (resolve.cuh:66-70,
+// elimination.cuh:445-447, function.cuh:233): more than ADDEDCLS_MAX unit
+// resolvents or more than ADDEDPROOF_MAX proof bytes rule x out. true = ruled out.
+PFG_D bool proof_guard(const EK& k, int kind, uint32_t x, uint32_t me, uint32_t other, uint32_t nE) {
+    if (nE > ADDEDCLS_MAX) return true;
+    const uint32_t* ml = OLp(k, me);
+    const uint32_t* ot = OLp(k, other);
+    const uint32_t ms = OLs(k, me), os = OLs(k, other);
+    unsigned long long bytes = 0;
+    for (uint32_t i = 0; i < ms; i++) {
+        const uint32_t ci = ml[i];
+        const uint32_t mi = META(k, ci);
+        if (m_learnt(mi)) continue;
+        for (uint32_t j = 0; j < os; j++) {
+            const uint32_t cj = ot[j];
+            if (!pair_ok(kind, mi, META(k, cj))) continue;
+            bytes += merge_bytes(k, x, ci, cj);
+        }
+    }
+    return bytes > ADDEDPROOF_MAX;
+}
+
 // countSubstituted / countCoreSubstituted: true = cannot substitute
 PFG_D bool count_subst(const EK& k, int kind, uint32_t x, uint32_t nClsBefore, uint32_t me, uint32_t other,
                        uint32_t& nE, uint32_t& nC, uint32_t& nL) {
@@ -212,6 +263,7 @@ PFG_D bool count_subst(const EK& k, int kind, uint32_t x, uint32_t nClsBefore, u
         const uint32_t before = count_lits_before(k, me) + count_lits_before(k, other);
         if (nL > before) return true;
     }
+    if (k.proof && proof_guard(k, kind, x, me, other, nE)) return true;
     return false;
 }
 
@@ -239,6 +291,7 @@ PFG_D bool count_res_unbounded(const EK& k, uint32_t x, uint32_t me, uint32_t ot
         }
     }
     if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return false;
+    if (k.proof && proof_guard(k, PAIR_RES, x, me, other, nE)) return false;
     return true;
 }
 
@@ -270,11 +323,56 @@ PFG_D bool count_res_bounded(const EK& k, uint32_t x, uint32_t nClsBefore, uint3
         const uint32_t before = count_lits_before(k, me) + count_lits_before(k, other);
         if (nL > before) return false;
     }
+    if (k.proof && proof_guard(k, PAIR_RES, x, me, other, nE)) return false;
     return true;
 }
 
 // ---- model stack (model.cuh:29-49) ----
 PFG_D uint32_t org_lit(const EK& k, uint32_t lit) { return (k.vorg[ABSV(lit)] << 1) | SIGNL(lit); }
+
+// ---- DRAT proof lines (proofutils.cuh:30-200) ----
+// Reserves `words` line words in one block keyed (x, seq); nullptr on overflow.
+PFG_D uint32_t* pf_reserve(const EK& k, uint32_t x, uint32_t seq, uint32_t words) {
+    const unsigned long long s = atomicAdd(&k.dc->pf_words, (unsigned long long)words);
+    const uint32_t b = atomicAdd(&k.dc->pf_blocks, 1u);
+    if (s + words > k.pf_wcap || b >= k.pf_bcap) { atomicOr(&k.dc->err, ERR_PROOF_OVERFLOW); return nullptr; }
+    k.pf_b[b] = make_ulonglong2(((unsigned long long)x << 32) | seq, s);
+    return k.pf_w + s;
+}
+
+// one line: header (bit 31 = deletion, low bits = length), then the literals in
+// original numbering (ORIGINIZELIT); returns the words written
+PFG_D uint32_t pf_put(const EK& k, uint32_t* dst, bool del, const uint32_t* l, uint32_t n) {
+    dst[0] = (del ? 0x80000000u : 0u) | n;
+    for (uint32_t i = 0; i < n; i++) dst[1 + i] = org_lit(k, l[i]);
+    return n + 1;
+}
+
+// saveProof over poss then negs after SUB of x (subsume.cuh:464-474,
+// proofutils.cuh:180-200): strengthened clauses are added, subsumed ones deleted
+PFG_D void proof_sub(const EK& k, uint32_t x, uint32_t p, uint32_t n) {
+    uint32_t words = 0;
+    for (int side = 0; side < 2; side++) {
+        const uint32_t lit = side ? n : p;
+        const uint32_t* ol = OLp(k, lit);
+        for (uint32_t i = 0; i < OLs(k, lit); i++) {
+            const ClsHdr h = k.hdr[ol[i]];
+            words += (m_molten(h.meta) ? h.size + 1 : 0u) + (m_deleted(h.meta) ? h.size + 1 : 0u);
+        }
+    }
+    if (!words) return;
+    uint32_t* d = pf_reserve(k, x, 0, words);
+    if (!d) return;
+    for (int side = 0; side < 2; side++) {
+        const uint32_t lit = side ? n : p;
+        const uint32_t* ol = OLp(k, lit);
+        for (uint32_t i = 0; i < OLs(k, lit); i++) {
+            const ClsHdr h = k.hdr[ol[i]];
+            if (m_molten(h.meta)) d += pf_put(k, d, false, k.lits + h.off, h.size);
+            if (m_deleted(h.meta)) d += pf_put(k, d, true, k.lits + h.off, h.size);
+        }
+    }
+}
 
 // original clauses of `side` (witness literal first) followed by [w, 1]
 PFG_D void save_side(const EK& k, uint32_t side, uint32_t witlit, uint32_t w) {
@@ -577,6 +675,28 @@ PFG_D void substitute_single(const EK& k, uint32_t p, uint32_t n, uint32_t def) 
         if (nNeg) append_units(k, n);
         if (nPos) append_units(k, p);
     }
+    if (k.proof) {   // addProof over negs, then poss (equivalence.cuh:100-111)
+        uint32_t words = 0;
+        for (int side = 0; side < 2; side++) {
+            const uint32_t lit = side ? p : n;
+            const uint32_t* ol = OLp(k, lit);
+            for (uint32_t i = 0; i < OLs(k, lit); i++) {
+                const ClsHdr h = k.hdr[ol[i]];
+                if (m_orig(h.meta)) words += h.size + 1;
+            }
+        }
+        uint32_t* d = words ? pf_reserve(k, ABSV(p), 0, words) : nullptr;
+        if (d) {
+            for (int side = 0; side < 2; side++) {
+                const uint32_t lit = side ? p : n;
+                const uint32_t* ol = OLp(k, lit);
+                for (uint32_t i = 0; i < OLs(k, lit); i++) {
+                    const ClsHdr h = k.hdr[ol[i]];
+                    if (m_orig(h.meta)) d += pf_put(k, d, false, k.lits + h.off, h.size);
+                }
+            }
+        }
+    }
 }
 
 PFG_D uint32_t find_sfanin(const EK& k, uint32_t gate_out) {
@@ -759,6 +879,7 @@ __global__ void sub_k(EK k, const uint32_t* elected, uint32_t nelected, const ui
             if (nPos) append_units(k, p);
             if (nNeg) append_units(k, n);
         }
+        if (k.proof) proof_sub(k, x, p, n);
         update_ol(k, p);
         update_ol(k, n);
     }
@@ -976,9 +1097,17 @@ __global__ void __launch_bounds__(128) ve1b_k(EK k, const uint32_t* elected, con
 }
 
 // ---- BVE phase 3 ----
+// proof words of x's resolvent lines: one line per clause resolvent and per
+// unit resolvent (emission may stop before the last units; the rest is padding)
+PFG_D uint32_t pf_res_words(uint32_t xinfo, uint32_t units) {
+    const uint32_t nC = (xinfo & 0xFFFCu) >> 2, nL = xinfo >> 16;
+    return nL + nC + 2 * units;
+}
+
 __global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint32_t nelected, const uint32_t* type,
-                                             const unsigned long long* rslot, const unsigned long long* rlit,
-                                             const uint8_t* fits, const uint32_t* list, const uint32_t* count) {
+                                             const uint32_t* ucnt, const unsigned long long* rslot,
+                                             const unsigned long long* rlit, const uint8_t* fits,
+                                             const uint32_t* list, const uint32_t* count) {
     const uint32_t nn = list_count(list, count, nelected);
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += gridDim.x * blockDim.x) {
         const uint32_t tid = list ? list[q] : q;
@@ -999,6 +1128,9 @@ __global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint
                 const uint32_t* ml = OLp(k, p);
                 const uint32_t* ol = OLp(k, n);
                 const uint32_t ms = OLs(k, p), os = OLs(k, n);
+                const uint32_t pwords = k.proof ? pf_res_words(xinfo, ucnt[tid]) : 0u;
+                uint32_t* pd = pwords ? pf_reserve(k, x, 0, pwords) : nullptr;
+                uint32_t* const pend = pd ? pd + pwords : nullptr;
                 for (uint32_t i = 0; i < ms && slot < checksum; i++) {
                     const uint32_t ci = ml[i];
                     const uint32_t mi = META(k, ci);
@@ -1012,9 +1144,15 @@ __global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint
                         uint32_t unit;
                         const int rsize = merge_cnt(k, x, ci, cj, unit);
                         if (!rsize) continue;
-                        if (rsize == 1) { push_unit(k, unit); continue; }
+                        if (pd && pd + rsize + 1 > pend) { atomicOr(&k.dc->err, ERR_PROOF_OVERFLOW); pd = nullptr; }
+                        if (rsize == 1) {
+                            push_unit(k, unit);
+                            if (pd) pd += pf_put(k, pd, false, &unit, 1);
+                            continue;
+                        }
                         uint32_t* out = k.lits + woff;
                         merge_out(k, x, ci, cj, out);
+                        if (pd) pd += pf_put(k, pd, false, out, (uint32_t)rsize);
                         uint32_t sig = 0;
                         for (int q = 0; q < rsize; q++) sig |= MAPHASH(out[q]);
                         ClsHdr h;
@@ -1028,6 +1166,7 @@ __global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint
                     }
                 }
                 if (slot != checksum) atomicOr(&k.dc->err, ERR_SLOT_MISMATCH);
+                if (pd) while (pd < pend) *pd++ = 0u;
                 toblivion(k, p, n);
                 k.elim[x] |= MELTING_MASK | ADDING_MASK;
             } else if (et != RES_MASK) {
@@ -1159,6 +1298,7 @@ __global__ void __launch_bounds__(128) ere_k(EK k, const uint32_t* elected, uint
     const uint32_t cmax = k.ere_clause_max;
     for (uint32_t q = blockIdx.x * 4 + wib; q < nelected; q += gridDim.x * 4) {
         const uint32_t v = elected[q], p = 2 * v, n = p | 1;
+        uint32_t pseq = 0;   // proof lines of v, in deletion order
         const uint32_t ds = OLs(k, p), fs = OLs(k, n);
         if (!(ds && fs && ds <= k.ere_max_occurs && fs <= k.ere_max_occurs)) continue;
         const uint32_t* pl = OLp(k, p);
@@ -1208,7 +1348,14 @@ __global__ void __launch_bounds__(128) ere_k(EK k, const uint32_t* elected, uint
                         for (int it = 0; it < 8; it++) {
                             if (m_deleted(old)) break;
                             const unsigned int prev = atomicCAS(mp, old, m_set_st(old, ST_DELETED));
-                            if (prev == old) { done |= bit; break; }
+                            if (prev == old) {
+                                done |= bit;
+                                if (k.proof) {   // redundancy.cuh:122-128
+                                    uint32_t* d = pf_reserve(k, v, pseq++, (uint32_t)mlen + 1);
+                                    if (d) pf_put(k, d, true, buf, (uint32_t)mlen);
+                                }
+                                break;
+                            }
                             old = prev;
                         }
                     }
@@ -1275,8 +1422,14 @@ __global__ void __launch_bounds__(128) bce_k(EK k, const uint32_t* elected, uint
             const uint32_t ex = warp_excl_scan(words, lane, total);
             if (!total) continue;
             unsigned long long base = 0;
-            if (lane == 0) base = stack_reserve(k, x, total);
+            uint32_t* pd = nullptr;
+            if (lane == 0) {
+                base = stack_reserve(k, x, total);
+                if (k.proof) pd = pf_reserve(k, x, b, total);   // one 'd' line per blocked clause (blocked.cuh:67-72)
+            }
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            pd = (uint32_t*)__shfl_sync(0xFFFFFFFFu, (unsigned long long)pd, 0);
+            if (blocked && pd) pf_put(k, pd + ex, true, k.lits + hi.off, hi.size);
             if (blocked && base != ~0ull) {
                 uint32_t* s = k.stack + base + ex;
                 const uint32_t* l = k.lits + hi.off;
@@ -1322,7 +1475,23 @@ EK make_ek(Ctx& c) {
     k.ere_clause_max = c.o.ere_clause_max;
     k.ve_lbound_en = c.o.ve_lbound_en;
     k.ve_inprocess = c.o.ve_inprocess;
+    k.proof = c.o.proof_en ? 1 : 0;
+    k.pf_w = c.pf_w;
+    k.pf_wcap = c.pf_wcap;
+    k.pf_b = c.pf_b;
+    k.pf_bcap = c.pf_bcap;
+    k.lbyte = c.lbyte;
     return k;
+}
+
+// proof words BVE emission needs: the resolvent lines of every variable whose slots fit
+__global__ void pf_need_k(const uint32_t* type, const uint32_t* ucnt, const uint8_t* fits, uint32_t E,
+                          unsigned long long* need) {
+    unsigned long long t = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < E; i += gridDim.x * blockDim.x)
+        if ((type[i] & 3u) && fits[i]) t += pf_res_words(type[i], ucnt[i]);
+    for (int d = 16; d > 0; d >>= 1) t += __shfl_down_sync(0xFFFFFFFFu, t, d);
+    if ((threadIdx.x & 31u) == 0 && t) atomicAdd(need, t);
 }
 
 // MEMORY_SAFE (bounded.cuh:279) per instance: gpos / gref are the exclusive
@@ -1365,20 +1534,23 @@ __global__ void inst_add_k(const unsigned long long* cslot, const unsigned long 
 
 }  // namespace
 
-void sub_pass(Ctx& c) {
+bool sub_pass(Ctx& c) {
     const uint32_t E = c.nve;
-    if (!E) return;
+    if (!E) return true;
+    if (c.o.proof_en && !proof_prepare(c, 2 * (c.lits_used + c.ncls))) return false;
     const EK k = make_ek(c);
     cudaMemsetAsync(&c.dc->nbig_sub, 0, sizeof(uint32_t), c.s);
     // warp per variable on the shared-memory stage; larger variables by one thread each
     PFG_LAUNCH(K_SUB, subw_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.veset, E,
                c.work_b, &c.dc->nbig_sub);
     PFG_LAUNCH(K_BIGVAR, sub_k, grid_for(E, 64, 8), 64, 0, c.s, k, c.veset, E, c.work_b, &c.dc->nbig_sub);
+    return !c.o.proof_en || proof_collect(c);
 }
 
 bool ve_pass(Ctx& c) {
     const uint32_t E = c.nve;
     if (!E) return true;
+    if (c.o.proof_en && !proof_prepare(c, 2 * (c.lits_used + c.ncls))) return false;
     const EK k = make_ek(c);
     bool any_vc = false;
     for (uint32_t i = 0; i < c.ninst; i++) any_vc |= c.ih[i].mode == 1 && c.ih[i].varcore_on;
@@ -1391,6 +1563,7 @@ bool ve_pass(Ctx& c) {
     if (any_vc)   // one warp per deferred variable; the grid walks the device-side count
         PFG_LAUNCH(K_VE1B, ve1b_k, grid_for((uint64_t)E * 32, 128, 16), 128, 0, c.s, k, c.veset, c.work,
                    &c.dc->nwork, c.type, c.ucnt, c.rpos, c.rref);
+    if (c.o.proof_en && !proof_collect(c)) return false;   // substitution lines (ve_k_1)
     if (!ensure_tmp(c, scan_temp_bytes(E))) return false;
     // vePhase2 (elimination.cu:74-100) per instance, then physical placement
     exclusive_scan_u64(c.rpos, c.rpos, E, 0ull, nullptr, c.tmp, c.s);
@@ -1403,10 +1576,19 @@ bool ve_pass(Ctx& c) {
                c.dout.add);
     cudaMemcpyAsync(&c.dc->ve_cls, c.rslot + E, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c.s);
     cudaMemcpyAsync(&c.dc->ve_lits, c.rlit + E, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c.s);
-    PFG_LAUNCH(K_VE3, ve3w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.veset, E,
-               c.type, c.rslot, c.rlit, c.winv, c.eligible_b, &c.dc->nbig_ve3);
-    PFG_LAUNCH(K_BIGVAR, ve3_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.veset, E, c.type, c.rslot, c.rlit, c.winv,
-               c.eligible_b, &c.dc->nbig_ve3);
+    EK k3 = k;
+    if (c.o.proof_en) {   // room for the resolvent lines
+        cudaMemsetAsync(&c.dc->pf_need, 0, sizeof(unsigned long long), c.s);
+        PFG_LAUNCH(K_SCAN, pf_need_k, grid_for(E, 256), 256, 0, c.s, c.type, c.ucnt, c.winv, E, &c.dc->pf_need);
+        sync_counters(c);
+        if (!proof_prepare(c, c.hc->pf_need)) return false;
+        k3 = make_ek(c);
+    }
+    PFG_LAUNCH(K_VE3, ve3w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k3, c.veset, E,
+               c.type, c.ucnt, c.rslot, c.rlit, c.winv, c.eligible_b, &c.dc->nbig_ve3);
+    PFG_LAUNCH(K_BIGVAR, ve3_k, grid_for(E, 128, 8), 128, 0, c.s, k3, c.veset, E, c.type, c.ucnt, c.rslot, c.rlit,
+               c.winv, c.eligible_b, &c.dc->nbig_ve3);
+    if (c.o.proof_en && !proof_collect(c)) return false;
     // resizeCNF_k (cnf.cu:55-80): the store ends after the last slot that fit
     pull_inst_out(c);
     if (!c.err.empty()) return false;
@@ -1423,10 +1605,12 @@ bool ve_pass(Ctx& c) {
     return cuda_ok(c, cudaGetLastError(), "ve");
 }
 
-void bce_pass(Ctx& c) {
-    if (!c.nve) return;
+bool bce_pass(Ctx& c) {
+    if (!c.nve) return true;
+    if (c.o.proof_en && !proof_prepare(c, 2 * (c.lits_used + c.ncls))) return false;
     PFG_LAUNCH(K_BCE, bce_k, grid_for((uint64_t)c.nve * 32, 128), 128, 0, c.s, make_ek(c), c.veset, c.nve,
                c.o.bce_max_occurs);
+    return !c.o.proof_en || proof_collect(c);
 }
 
 bool ere_pass(Ctx& c) {
@@ -1438,11 +1622,13 @@ bool ere_pass(Ctx& c) {
     uint32_t* table = nullptr;
     if (!dalloc_t(c, &table, cap)) { c.simpstate = PFG_OTALLOC_FAIL; return false; }
     const uint32_t mask = (uint32_t)(cap - 1);
+    if (c.o.proof_en && !proof_prepare(c, 2 * (c.lits_used + c.ncls))) { dfree(c, table); return false; }
     cudaMemsetAsync(table, 0xFF, cap * sizeof(uint32_t), c.s);
     PFG_LAUNCH(K_ERE, ere_table_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, table, mask);
     PFG_LAUNCH(K_ERE, ere_k, grid_for((uint64_t)c.nere * 32, 128), 128, 0, c.s, make_ek(c), c.ereset, c.nere, table,
                mask);
     dfree(c, table);
+    if (c.o.proof_en && !proof_collect(c)) return false;
     return cuda_ok(c, cudaGetLastError(), "ere");
 }
 

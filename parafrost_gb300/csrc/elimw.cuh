@@ -248,6 +248,48 @@ PFG_D bool ws_count_pairs(WS& w, int kind, uint32_t x, const Side& me, const Sid
     return true;
 }
 
+// mergeProof (elimination.cuh:162-213) on staged clauses: proof bytes of the
+// resolvent, 0 for a tautology
+PFG_D uint32_t ws_merge_bytes(const EK& k, WS& w, uint32_t x, uint32_t c1, uint32_t c2) {
+    const uint32_t* a = WL(w, c1);
+    const uint32_t* b = WL(w, c2);
+    const int n1 = (int)w.size[c1], n2 = (int)w.size[c2];
+    int i = 0, j = 0;
+    uint32_t bytes = 2;
+    while (i < n1 && j < n2) {
+        const uint32_t l1 = a[i], l2 = b[j], v1 = ABSV(l1), v2 = ABSV(l2);
+        if (v1 == x) i++;
+        else if (v2 == x) j++;
+        else if ((l1 ^ l2) == 1u) return 0;
+        else if (v1 < v2) { i++; bytes += k.lbyte[l1]; }
+        else if (v2 < v1) { j++; bytes += k.lbyte[l2]; }
+        else { i++; j++; bytes += k.lbyte[l1]; }
+    }
+    while (i < n1) { const uint32_t l1 = a[i++]; if (ABSV(l1) != x) bytes += k.lbyte[l1]; }
+    while (j < n2) { const uint32_t l2 = b[j++]; if (ABSV(l2) != x) bytes += k.lbyte[l2]; }
+    return bytes;
+}
+
+// proof_guard on the stage, 32 pairs per step: true = ruled out
+PFG_D bool ws_proof_guard(const EK& k, WS& w, int kind, uint32_t x, const Side& me, const Side& ot, uint32_t nE,
+                          unsigned lane) {
+    if (nE > ADDEDCLS_MAX) return true;
+    const uint32_t total = me.n * ot.n;
+    unsigned long long bytes = 0;
+    for (uint32_t q0 = 0; q0 < total; q0 += 32) {
+        const uint32_t q = q0 + lane;
+        uint32_t b = 0;
+        if (q < total) {
+            const uint32_t ci = me.b + q / ot.n, cj = ot.b + q % ot.n;
+            if (ws_pair_ok(kind, w.meta[ci], w.meta[cj])) b = ws_merge_bytes(k, w, x, ci, cj);
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) b += __shfl_xor_sync(FULL, b, d);
+        bytes += b;
+    }
+    return bytes > ADDEDPROOF_MAX;
+}
+
 PFG_D uint32_t ws_lits_before(const WS& w, const Side& s) {
     uint32_t t = 0;
     for (uint32_t i = 0; i < s.n; i++) if (m_orig(w.meta[s.b + i])) t += w.size[s.b + i];
@@ -260,13 +302,15 @@ PFG_D bool ws_count_subst(const EK& k, WS& w, int kind, uint32_t x, uint32_t nCl
     if (!ws_count_pairs(w, kind, x, me, ot, nClsBefore, k.ve_clause_max, nE, nC, nL, lane)) return true;
     if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return true;
     if (k.ve_lbound_en && nL > ws_lits_before(w, me) + ws_lits_before(w, ot)) return true;
+    if (k.proof && ws_proof_guard(k, w, kind, x, me, ot, nE, lane)) return true;
     return false;
 }
 
 PFG_D bool ws_count_res_unbounded(const EK& k, WS& w, uint32_t x, const Side& me, const Side& ot, uint32_t& nE,
                                   uint32_t& nC, uint32_t& nL, unsigned lane) {
     if (!ws_count_pairs(w, CNT_RES_UNBOUNDED, x, me, ot, 0, k.ve_clause_max, nE, nC, nL, lane)) return false;
-    return !(nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX);
+    if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return false;
+    return !(k.proof && ws_proof_guard(k, w, CNT_RES_UNBOUNDED, x, me, ot, nE, lane));
 }
 
 PFG_D bool ws_count_res_bounded(const EK& k, WS& w, uint32_t x, uint32_t nClsBefore, const Side& me, const Side& ot,
@@ -275,7 +319,7 @@ PFG_D bool ws_count_res_bounded(const EK& k, WS& w, uint32_t x, uint32_t nClsBef
     if (!ws_count_pairs(w, CNT_RES_BOUNDED, x, me, ot, nClsBefore, k.ve_clause_max, nE, nC, nL, lane)) return false;
     if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return false;
     if (k.ve_lbound_en && nL > ws_lits_before(w, me) + ws_lits_before(w, ot)) return false;
-    return true;
+    return !(k.proof && ws_proof_guard(k, w, CNT_RES_BOUNDED, x, me, ot, nE, lane));
 }
 
 // ---- model stack from the stage ----
@@ -603,6 +647,20 @@ PFG_D void ws_substitute_single(const EK& k, WS& w, const Side& P, const Side& N
             if (nNeg) for (uint32_t i = 0; i < N.n; i++) if (w.size[N.b + i] == 1) push_unit(k, WL(w, N.b + i)[0]);
             if (nPos) for (uint32_t i = 0; i < P.n; i++) if (w.size[P.b + i] == 1) push_unit(k, WL(w, P.b + i)[0]);
         }
+        if (k.proof) {   // addProof over negs, then poss (equivalence.cuh:100-111)
+            uint32_t words = 0;
+            for (int side = 0; side < 2; side++) {
+                const Side& S = side ? P : N;
+                for (uint32_t i = 0; i < S.n; i++) if (m_orig(w.meta[S.b + i])) words += w.size[S.b + i] + 1;
+            }
+            uint32_t* d = words ? pf_reserve(k, ABSV(P.lit), 0, words) : nullptr;
+            if (d)
+                for (int side = 0; side < 2; side++) {
+                    const Side& S = side ? P : N;
+                    for (uint32_t i = 0; i < S.n; i++)
+                        if (m_orig(w.meta[S.b + i])) d += pf_put(k, d, false, WL(w, S.b + i), w.size[S.b + i]);
+                }
+        }
     }
     __syncwarp();
 }
@@ -726,7 +784,8 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve1w_k(EK k, const uint32_t* el
 
 // ---- BVE phase 3 on the stage (bounded.cuh:69-258, 488-544) ----
 __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* elected, uint32_t nelected,
-                                                        const uint32_t* type, const unsigned long long* rslot,
+                                                        const uint32_t* type, const uint32_t* ucnt,
+                                                        const unsigned long long* rslot,
                                                         const unsigned long long* rlit, const uint8_t* fits,
                                                         uint32_t* big, uint32_t* nbig) {
     __shared__ WS stage[WS_WARPS];
@@ -755,6 +814,12 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
             unsigned long long woff = rlit[tid];
             uint32_t added = 0;
             const uint32_t total = P.n * N.n;
+            // proof: the resolvent lines in pair order into one block, the rest padding
+            const uint32_t pwords = k.proof ? pf_res_words(xinfo, ucnt[tid]) : 0u;
+            uint32_t* pd = nullptr;
+            if (pwords && lane == 0) pd = pf_reserve(k, x, 0, pwords);
+            pd = (uint32_t*)__shfl_sync(FULL, (unsigned long long)pd, 0);
+            uint32_t pused = 0;
             for (uint32_t q0 = 0; q0 < total && added < nAddedCls; q0 += 32) {
                 const uint32_t q = q0 + lane;
                 int rsize = 0;
@@ -778,10 +843,21 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
                 uint32_t ltot;
                 const uint32_t lex = warp_excl_scan(emit ? (uint32_t)rsize : 0u, lane, ltot);
                 const uint32_t ncl = __popc(__ballot_sync(FULL, emit));
+                uint32_t* pl = nullptr;
+                if (pd) {
+                    const uint32_t pw = (visited && rsize) ? (uint32_t)rsize + 1 : 0u;
+                    uint32_t ptot;
+                    const uint32_t pex = warp_excl_scan(pw, lane, ptot);
+                    if (pused + pex + pw <= pwords) pl = pd + pused + pex;
+                    else if (pw) atomicOr(&k.dc->err, ERR_PROOF_OVERFLOW);
+                    pused += ptot;
+                    if (visited && isun && pl) pf_put(k, pl, false, &unit, 1);
+                }
                 if (emit) {
                     const unsigned long long o = woff + lex;
                     uint32_t* out = k.lits + o;
                     ws_merge_out(w, x, ci, cj, out);
+                    if (pl) pf_put(k, pl, false, out, (uint32_t)rsize);
                     uint32_t sig = 0;
                     for (int t = 0; t < rsize; t++) sig |= MAPHASH(out[t]);
                     ClsHdr h;
@@ -796,6 +872,7 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
                 woff += ltot;
             }
             if (added != nAddedCls && lane == 0) atomicOr(&k.dc->err, ERR_SLOT_MISMATCH);
+            if (pd) for (uint32_t t = pused + lane; t < pwords; t += 32) pd[t] = 0u;
             ws_toblivion(k, w, P, N, lane);
             ws_flush(k, w, lane);
             if (lane == 0) k.elim[x] |= MELTING_MASK | ADDING_MASK;
@@ -923,6 +1000,40 @@ PFG_D void ws_subsume(WS& w, const Side& L, uint32_t end, uint32_t cand, unsigne
     }
 }
 
+// saveProof over poss then negs (subsume.cuh:464-474): the stage holds poss
+// then negs in list order; strengthened clauses are added, subsumed ones deleted
+PFG_D void ws_proof_sub(const EK& k, WS& w, uint32_t x, unsigned lane) {
+    __syncwarp();
+    const uint32_t nc = w.np + w.nn;
+    uint32_t total = 0;
+    for (uint32_t c0 = 0; c0 < nc; c0 += 32) {
+        const uint32_t i = c0 + lane;
+        uint32_t words = 0;
+        if (i < nc) words = (m_molten(w.meta[i]) ? w.size[i] + 1 : 0u) + (m_deleted(w.meta[i]) ? w.size[i] + 1 : 0u);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) words += __shfl_xor_sync(FULL, words, d);
+        total += words;
+    }
+    if (!total) return;
+    uint32_t* d = nullptr;
+    if (lane == 0) d = pf_reserve(k, x, 0, total);
+    d = (uint32_t*)__shfl_sync(FULL, (unsigned long long)d, 0);
+    if (!d) return;
+    uint32_t used = 0;
+    for (uint32_t c0 = 0; c0 < nc; c0 += 32) {
+        const uint32_t i = c0 + lane;
+        const bool m = i < nc && m_molten(w.meta[i]), del = i < nc && m_deleted(w.meta[i]);
+        const uint32_t words = (m ? w.size[i] + 1 : 0u) + (del ? w.size[i] + 1 : 0u);
+        uint32_t t;
+        const uint32_t ex = warp_excl_scan(words, lane, t);
+        uint32_t* o = d + used + ex;
+        if (m) o += pf_put(k, o, false, WL(w, i), w.size[i]);
+        if (del) pf_put(k, o, true, WL(w, i), w.size[i]);
+        used += t;
+    }
+    __syncwarp();
+}
+
 // updateOL (subsume.cuh:293-303) on the global list, order kept
 PFG_D void ws_update_ol(const EK& k, WS& w, const Side& L, unsigned lane) {
     __syncwarp();
@@ -983,6 +1094,7 @@ __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* el
             if (nPos) for (uint32_t i = 0; i < P.n; i++) if (w.size[P.b + i] == 1) push_unit(k, WL(w, P.b + i)[0]);
             if (nNeg) for (uint32_t i = 0; i < N.n; i++) if (w.size[N.b + i] == 1) push_unit(k, WL(w, N.b + i)[0]);
         }
+        if (k.proof) ws_proof_sub(k, w, x, lane);
         ws_update_ol(k, w, P, lane);
         ws_update_ol(k, w, N, lane);
         ws_flush(k, w, lane);

@@ -147,6 +147,68 @@ void pull_inst_out(Ctx& c) {
     sync_counters(c);
 }
 
+// ---- DRAT proof of a pass (the device side of cuPROOF, src/gpu/proof.cu:184-246) ----
+bool proof_prepare(Ctx& c, unsigned long long words) {
+    words += 64;
+    if (words > c.pf_wcap) {
+        dfree(c, c.pf_w);
+        dfree(c, c.pf_b);
+        c.pf_w = nullptr; c.pf_b = nullptr; c.pf_wcap = 0; c.pf_bcap = 0;
+        const unsigned long long cap = words + words / 4;
+        const unsigned long long bcap = cap / 2 + 1;   // a block holds a line: 2 words at least
+        if (bcap > 0xFFFFFFFFull) { c.err = "proof block table exceeds 2^32 entries"; return false; }
+        if (!dalloc_t(c, &c.pf_w, cap) || !dalloc_t(c, &c.pf_b, bcap)) return false;
+        c.pf_wcap = cap;
+        c.pf_bcap = (uint32_t)bcap;
+    }
+    cudaMemsetAsync(&c.dc->pf_words, 0, sizeof(unsigned long long), c.s);
+    cudaMemsetAsync(&c.dc->pf_blocks, 0, sizeof(uint32_t), c.s);
+    return true;
+}
+
+// The pass's blocks in (variable, sequence) order; each line becomes 'a' or 'd',
+// its literals as 7-bit groups (saveProofLiteral, proofutils.cuh:93-111), and a
+// zero byte, appended to the proof of the variable's instance.
+bool proof_collect(Ctx& c) {
+    sync_counters(c);
+    if (!c.err.empty()) return false;
+    const unsigned long long nw = c.hc->pf_words;
+    const uint32_t nb = c.hc->pf_blocks;
+    if (!nb) return true;
+    c.pf_hw.resize(nw);
+    c.pf_hb.resize(nb);
+    cudaMemcpyAsync(c.pf_hw.data(), c.pf_w, nw * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    cudaMemcpyAsync(c.pf_hb.data(), c.pf_b, nb * sizeof(ulonglong2), cudaMemcpyDeviceToHost, c.s);
+    if (!cuda_ok(c, cudaStreamSynchronize(c.s), "proof copy")) return false;
+    // blocks tile [0, nw) in reservation order: their ends are the next starts
+    std::vector<ulonglong2>& b = c.pf_hb;
+    std::sort(b.begin(), b.end(), [](const ulonglong2& a, const ulonglong2& z) { return a.y < z.y; });
+    std::vector<std::pair<unsigned long long, std::pair<unsigned long long, unsigned long long>>> blk(nb);
+    for (uint32_t i = 0; i < nb; i++) blk[i] = {b[i].x, {b[i].y, i + 1 < nb ? b[i + 1].y : nw}};
+    std::sort(blk.begin(), blk.end());
+    uint32_t inst = 0;
+    for (const auto& e : blk) {
+        const uint32_t x = (uint32_t)(e.first >> 32);
+        while (inst + 1 < c.ninst && c.ih[inst + 1].voff < x) inst++;
+        std::vector<uint8_t>& out = c.ih[inst].proof;
+        for (unsigned long long w = e.second.first; w < e.second.second;) {
+            const uint32_t h = c.pf_hw[w];
+            if (!h) { w++; continue; }                    // padding
+            const uint32_t n = h & 0x7FFFFFFFu;
+            if (w + 1 + n > e.second.second) { c.err = "malformed proof block"; return false; }
+            out.push_back((h >> 31) ? PROOF_DELETED : PROOF_ADDED);
+            for (uint32_t t = 0; t < n; t++) {
+                uint32_t v = c.pf_hw[w + 1 + t];
+                while (v >= 0x80u) { out.push_back((uint8_t)((v & 0x7Fu) | 0x80u)); v >>= 7; }
+                out.push_back((uint8_t)v);
+            }
+            out.push_back(0);
+            w += 1 + n;
+        }
+    }
+    return true;
+}
+
 namespace {
 
 // header of every uploaded clause; literals moved to their instance's variable range
@@ -192,6 +254,15 @@ __global__ void prep_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls) {
             for (uint32_t i = 0; i < h.size; i++) s |= MAPHASH(l[i]);
             hdr[c].sig = s;
         }
+    }
+}
+
+// proof bytes of every literal: 7-bit groups of its original (cnt_proof, proof.cu:49-85)
+__global__ void lbyte_k(const uint32_t* vorg, uint32_t V, uint8_t* lbyte) {
+    for (uint64_t l = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; l < 2ull * V + 2;
+         l += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = (uint32_t)(l >> 1);
+        lbyte[l] = v ? (uint8_t)varint_len((vorg[v] << 1) | (uint32_t)(l & 1)) : 0u;
     }
 }
 
@@ -568,6 +639,10 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
                    d_base, d_base + n + 1, c.di.voff, n, c.lits);
         PFG_LAUNCH(K_UPLOAD, prep_k, grid_for(Ctot, 128), 128, 0, c.s, c.hdr, c.lits, Ctot);
     }
+    if (c.o.proof_en) {
+        if (!dalloc_t(c, &c.lbyte, 2 * V1)) { free_all(o); return PFG_CNFALLOC_FAIL; }
+        PFG_LAUNCH(K_UPLOAD, lbyte_k, grid_for(2 * V1, 256), 256, 0, c.s, c.vorg, c.V, c.lbyte);
+    }
     cudaMemsetAsync(c.elim, 0, V1, c.s);
     cudaMemsetAsync(c.varcore, 0, V1 * sizeof(uint32_t), c.s);
     cudaMemsetAsync(c.dc, 0, sizeof(DevCounters), c.s);
@@ -685,7 +760,6 @@ extern "C" int pfg_create(pfg_ctx** out, const pfg_options* opts, size_t arena_b
     Ctx& c = o->c;
     if (opts) c.o = *opts; else pfg_default_options(&c.o);
     pfg_resolve_options(&c.o);
-    if (c.o.proof_en) { delete o; return PFG_INVALID; }   // proof emission is not built
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); delete o; return PFG_CUDA_ERROR; }
     c.device = dev;
@@ -922,7 +996,7 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         c.stats.literals_processed += Lin;
         if (c.o.sub_en || c.o.ve_plus_en) {
             PassTimer t(c, 3);
-            sub_pass(c);
+            if (!sub_pass(c)) break;
         }
         if (c.o.ve_en) {
             PassTimer t(c, 4);
@@ -930,7 +1004,7 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         }
         if (c.o.bce_en) {   // SUB(), VE(), BCE() (simplify.cu:173)
             PassTimer t(c, 7);
-            bce_pass(c);
+            if (!bce_pass(c)) break;
         }
         {
             PassTimer t(c, 6);
@@ -1063,6 +1137,7 @@ extern "C" int pfg_result_sizes_get(pfg_ctx* o, pfg_result_sizes* r) {
     r->stack_words = words;
     r->rounds = rounds;
     r->max_var = c.V;
+    for (uint32_t i = 0; i < c.ninst; i++) r->proof_bytes += c.ih[i].proof.size();
     return PFG_OK;
 }
 
@@ -1212,7 +1287,26 @@ extern "C" int pfg_batch_result_sizes(pfg_ctx* o, uint32_t i, pfg_result_sizes* 
     r->stack_words = c.hout.scount[i];
     r->rounds = h.round_ends.size();
     r->max_var = h.V;
+    r->proof_bytes = h.proof.size();
     return PFG_OK;
+}
+
+extern "C" int pfg_batch_download_proof(pfg_ctx* o, uint32_t i, uint8_t* out) {
+    if (!o) return PFG_INVALID;
+    Ctx& c = o->c;
+    if (!c.uploaded || i >= c.ninst) return PFG_INVALID;
+    const std::vector<uint8_t>& p = c.ih[i].proof;
+    if (!p.empty()) {
+        if (!out) return PFG_INVALID;
+        std::memcpy(out, p.data(), p.size());
+    }
+    return PFG_OK;
+}
+
+extern "C" int pfg_download_proof(pfg_ctx* o, uint8_t* out) {
+    if (!o) return PFG_INVALID;
+    if (o->c.ninst != 1) return PFG_INVALID;
+    return pfg_batch_download_proof(o, 0, out);
 }
 
 extern "C" int pfg_batch_download(pfg_ctx* o, uint32_t i, uint32_t* lits, uint64_t* cls_off, uint8_t* cls_learnt,

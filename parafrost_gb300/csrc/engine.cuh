@@ -40,6 +40,7 @@ struct InstHost {
     uint64_t processed_cls = 0, processed_lits = 0, resolvents = 0;
     std::vector<uint32_t> pending;  // units left unpropagated when it stopped
     std::vector<uint64_t> round_ends;
+    std::vector<uint8_t> proof;     // binary DRAT lines of its passes (proof_en)
 };
 
 // Per-instance kernel inputs, written by the host (one allocation, mirrored in
@@ -177,6 +178,18 @@ struct Ctx {
     void* tmp = nullptr; size_t tmp_cap = 0;
     uint32_t* tmp_u32 = nullptr; uint64_t tmp_u32_cap = 0;   // generic u32 scratch
 
+    // DRAT proof (proof_en): a pass writes its lines into pf_w in blocks, each
+    // block recorded in pf_b as {variable << 32 | sequence, first word}; a line
+    // is a header word (bit 31 = deletion, low bits = length) followed by its
+    // literals in original numbering, a zero word is padding. After the pass
+    // the host orders the blocks by key and appends the lines, as bytes, to
+    // the proof of the variable's instance.
+    uint32_t* pf_w = nullptr; unsigned long long pf_wcap = 0;
+    ulonglong2* pf_b = nullptr; uint32_t pf_bcap = 0;
+    uint8_t* lbyte = nullptr;    // 2V+2: proof bytes of each literal (7-bit groups of its original)
+    std::vector<uint32_t> pf_hw;
+    std::vector<ulonglong2> pf_hb;
+
     // per-kernel profiler (launch counts always; CUDA-event timing when enabled)
     Profiler prof;
 
@@ -228,10 +241,19 @@ bool bcp_prop(Ctx& c);
 // LCVE (lcve.cu) over the active instances; per-instance counts in dout.nelect
 bool lcve(Ctx& c);
 // SUB, BVE, ERE (elim.cu) over c.veset / c.ereset
-void sub_pass(Ctx& c);
+bool sub_pass(Ctx& c);
 bool ve_pass(Ctx& c);
 bool ere_pass(Ctx& c);
-void bce_pass(Ctx& c);   // blocked clause elimination over the surviving elected variables
+bool bce_pass(Ctx& c);   // blocked clause elimination over the surviving elected variables
+// DRAT proof of a pass (engine.cu): room for `words` line words before the pass,
+// then the pass's blocks appended to the instances' proofs
+bool proof_prepare(Ctx& c, unsigned long long words);
+bool proof_collect(Ctx& c);
+PFG_HD uint32_t varint_len(uint32_t x) {
+    uint32_t n = 1;
+    while (x >= 0x80u) { x >>= 7; n++; }
+    return n;
+}
 
 // device helper: instance of a global variable (binary search over voff[0..n])
 PFG_D uint32_t inst_search(const uint32_t* voff, uint32_t n, uint32_t v) {

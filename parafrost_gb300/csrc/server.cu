@@ -267,6 +267,7 @@ extern "C" int pfg_server_create(pfg_server** out, const pfg_options* opts, size
     *out = nullptr;
     pfg_server* s = new pfg_server();
     if (opts) s->opts = *opts; else pfg_default_options(&s->opts);
+    if (s->opts.proof_en) { delete s; return PFG_INVALID; }   // jobs carry no proof output
     s->slots = slots;
     s->max_batch = max_batch;
     if (cudaGetDevice(&s->device) != cudaSuccess) { cudaGetLastError(); delete s; return PFG_CUDA_ERROR; }

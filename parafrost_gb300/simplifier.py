@@ -41,6 +41,7 @@ class SimplifyResult:
     stack: np.ndarray                # model-reconstruction words
     round_ends: np.ndarray           # stack length after each SUB+BVE round
     stats: dict = field(default_factory=dict)
+    proof: bytes = b""               # binary DRAT lines of the passes (proof=True)
 
     def eliminated_vars(self) -> np.ndarray:
         e = self.eliminated
@@ -101,13 +102,16 @@ class Simplifier:
                                    _ptr(units, C.c_uint32), _ptr(pend, C.c_uint32), _ptr(stack, C.c_uint32),
                                    _ptr(rends, C.c_uint64))
         self._check(rc, "pfg_download")
+        proof = np.empty(max(sz.proof_bytes, 1), dtype=np.uint8)
+        self._check(self.lib.pfg_download_proof(self._ctx, _ptr(proof, C.c_uint8)), "pfg_download_proof")
         st = self.last_stats
         stats = {}
         if st is not None:
             stats = {f[0]: getattr(st, f[0]) for f in _abi.PfgStats._fields_ if f[0] != "pass_ms"}
             stats["pass_ms"] = dict(zip(_abi.PASS_NAMES, list(st.pass_ms)))
         return SimplifyResult(int(st.status) if st is not None else 0,
-                              Cnf(sz.max_var, lits, off, learnt, lbd, usage), elim, units, pend, stack, rends, stats)
+                              Cnf(sz.max_var, lits, off, learnt, lbd, usage), elim, units, pend, stack, rends, stats,
+                              proof[:sz.proof_bytes].tobytes())
 
     def simplify(self, cnf: Cnf, var_state=None, assumed=None, vorg=None) -> SimplifyResult:
         self.upload(cnf, var_state, assumed, vorg)
@@ -163,11 +167,19 @@ class Simplifier:
                                          _ptr(elim, C.c_uint8), _ptr(units, C.c_uint32), _ptr(pend, C.c_uint32),
                                          _ptr(stack, C.c_uint32), _ptr(rends, C.c_uint64))
         self._check(rc, "pfg_batch_download")
+        proof = self._proof_of(i, sz.proof_bytes)
         st = _abi.PfgStats()
         self._check(self.lib.pfg_batch_stats(self._ctx, i, C.byref(st)), "pfg_batch_stats")
         stats = {f[0]: getattr(st, f[0]) for f in _abi.PfgStats._fields_ if f[0] != "pass_ms"}
         return SimplifyResult(int(st.status), Cnf(sz.max_var, lits, off, learnt, lbd, usage), elim, units, pend,
-                              stack, rends, stats)
+                              stack, rends, stats, proof)
+
+    def _proof_of(self, i: int, nbytes: int) -> bytes:
+        if not nbytes:
+            return b""
+        buf = np.empty(nbytes, dtype=np.uint8)
+        self._check(self.lib.pfg_batch_download_proof(self._ctx, i, _ptr(buf, C.c_uint8)), "pfg_batch_download_proof")
+        return buf.tobytes()
 
     def download_all(self) -> list:
         """Results of every instance of the batch, one copy per output array
@@ -207,7 +219,8 @@ class Simplifier:
             cnf = Cnf(int(nvar[i]), lits[sl[i]:sl[i + 1]], off[so[i]:so[i + 1]], learnt[sc[i]:sc[i + 1]],
                       lbd[sc[i]:sc[i + 1]], usage[sc[i]:sc[i + 1]])
             out.append(SimplifyResult(int(st.status), cnf, elim[se[i]:se[i + 1]], units[su[i]:su[i + 1]],
-                                      pend[sp[i]:sp[i + 1]], stack[ss[i]:ss[i + 1]], rends[sr[i]:sr[i + 1]], stats))
+                                      pend[sp[i]:sp[i + 1]], stack[ss[i]:ss[i + 1]], rends[sr[i]:sr[i + 1]], stats,
+                                      self._proof_of(i, int(sizes[i].proof_bytes))))
         return out
 
     def simplify_batch(self, cnfs, var_states=None, assumeds=None, vorgs=None) -> list:
@@ -263,3 +276,18 @@ def simplify(cnf: Cnf, **options) -> SimplifyResult:
 def simplify_batch(cnfs, **options) -> list:
     with Simplifier(**options) as s:
         return s.simplify_batch(cnfs)
+
+
+def proof_text(proof: bytes) -> str:
+    """Text form of a binary DRAT proof ("d " before deletions, signed decimal
+    literals, "0" at the end of each line), as pfg_proof_text writes it."""
+    L = _lib.lib()
+    pb = np.frombuffer(proof, dtype=np.uint8) if proof else np.zeros(1, dtype=np.uint8)
+    pb = np.ascontiguousarray(pb)
+    n = C.c_uint64(0)
+    rc = L.pfg_proof_text(_ptr(pb, C.c_uint8), len(proof), None, 0, C.byref(n))
+    if rc != 0:
+        raise SimplifyError(rc, "malformed proof")
+    out = C.create_string_buffer(max(n.value, 1))
+    L.pfg_proof_text(_ptr(pb, C.c_uint8), len(proof), out, n.value, C.byref(n))
+    return out.raw[:n.value].decode("ascii")

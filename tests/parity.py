@@ -52,3 +52,35 @@ def assert_parity(cnf, var_state=None, assumed=None, vorg=None, **opts):
     d = diff(canon(res), canon(ref))
     assert not d, "engine differs from the oracle: " + "; ".join(d) + f" (oracle rounds {ref.round_stats})"
     return res, ref
+
+
+def decode_proof(proof: bytes):
+    """Binary DRAT lines as (kind, literals) with kind 'a' or 'd' and literals
+    in the 2v+s encoding."""
+    out, p, n = [], 0, len(proof)
+    while p < n:
+        kind = chr(proof[p]); p += 1
+        lits = []
+        while proof[p] != 0:
+            v, sh = 0, 0
+            while True:
+                b = proof[p]; p += 1
+                v |= (b & 0x7F) << sh
+                sh += 7
+                if not b & 0x80:
+                    break
+            lits.append(v)
+        p += 1
+        out.append((kind, tuple(lits)))
+    return out
+
+
+def proof_diff(engine: bytes, oracle: bytes) -> str:
+    """'' when equal, else the first differing line."""
+    if engine == oracle:
+        return ""
+    a, b = decode_proof(engine), decode_proof(oracle)
+    for i, (x, y) in enumerate(zip(a, b)):
+        if x != y:
+            return f"line {i}: engine {x} vs oracle {y} ({len(a)} vs {len(b)} lines)"
+    return f"{len(a)} vs {len(b)} lines"
