@@ -10,11 +10,12 @@ from .cnf import (Cnf, generate, lit_to_int, int_to_lit, parse_dimacs, random_ks
                   write_dimacs)
 from .simplifier import SimplifyError, SimplifyResult, Simplifier, proof_text, simplify, simplify_batch
 from .server import JobInfo, Server
+from .incremental import Incremental
 from .writeback import Mapped, map_result, reconstruct_model
 
 __all__ = [
     "Cnf", "Simplifier", "SimplifyResult", "SimplifyError", "simplify", "generate", "random_ksat", "tseitin",
     "scale_free", "read_dimacs", "write_dimacs", "lit_to_int", "int_to_lit", "default_options", "options_from",
     "simplify_batch", "proof_text", "Server", "JobInfo", "parse_dimacs", "Mapped", "map_result", "reconstruct_model",
-    "options_dict", "PfgOptions", "PfgStats", "PFG_SAT", "PFG_UNSAT", "PFG_UNKNOWN",
+    "options_dict", "Incremental", "PfgOptions", "PfgStats", "PFG_SAT", "PFG_UNSAT", "PFG_UNKNOWN",
 ]
