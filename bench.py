@@ -525,11 +525,16 @@ def run_gpu_batch(a, world, rank, local):
         plain_proc += st.clauses_processed
         plain_launches += st.kernel_launches
     barrier()
-    # ---- end to end through the C ABI with host buffers ----
+    # ---- end to end through the C ABI with host buffers: inputs and results in
+    # page-locked host memory, uploaded and downloaded inside the timed region ----
+    from parafrost_gb300 import pinned
+    pcnfs = [c.pinned() for c in cnfs]
+    rbuf = pinned.ResultBuffers()
+    sim.simplify_batch(pcnfs, into=rbuf)          # sizes the result buffers (untimed)
     e2e_s, e2e_proc, h2d, d2h = 0.0, 0, 0, 0
     for _ in range(a.steps):
         t1 = time.perf_counter()
-        outs = sim.simplify_batch(cnfs)
+        outs = sim.simplify_batch(pcnfs, into=rbuf)
         e2e_s += time.perf_counter() - t1
         e2e_proc += sum(int(o.stats["clauses_processed"]) for o in outs)
         h2d = sum(c.lits.nbytes + c.off.nbytes for c in cnfs)
@@ -537,7 +542,7 @@ def run_gpu_batch(a, world, rank, local):
     barrier()
     pe2e_s, pe2e_proc = 0.0, 0
     t1 = time.perf_counter()
-    for cnf in cnfs:
+    for cnf in pcnfs:
         res = sim.simplify(cnf)
         pe2e_proc += int(res.stats["clauses_processed"])
     pe2e_s = time.perf_counter() - t1

@@ -376,6 +376,12 @@ int  pfg_map_vars(uint32_t max_var, const uint8_t* eliminated, uint32_t* new_of_
 int  pfg_map_lits(const uint32_t* new_of_old, uint32_t max_var, uint64_t n, const uint32_t* in, uint32_t* out);
 int  pfg_extend_model(uint64_t nstack, const uint32_t* stack, uint32_t max_var, uint8_t* value);
 
+/* Page-locked host memory for input and result buffers (cuMM::allocPinned,
+   src/gpu/memory.cu:505-523): uploads from and downloads into it are direct
+   DMA transfers. NULL when it cannot be allocated. */
+void* pfg_host_alloc(size_t bytes);
+void  pfg_host_free(void* p);
+
 /* Release all device memory of the context. Replaces Solver::freeSimp (simplify.cu:254). */
 void pfg_destroy(pfg_ctx* ctx);
 

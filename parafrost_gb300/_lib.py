@@ -94,6 +94,10 @@ def lib():
     L.pfg_batch_download_proof.restype = C.c_int
     L.pfg_proof_text.argtypes = [u8p, C.c_uint64, C.c_char_p, C.c_uint64, u64p]
     L.pfg_proof_text.restype = C.c_int
+    L.pfg_host_alloc.argtypes = [C.c_size_t]
+    L.pfg_host_alloc.restype = C.c_void_p
+    L.pfg_host_free.argtypes = [C.c_void_p]
+    L.pfg_host_free.restype = None
     L.pfg_destroy.argtypes = [C.c_void_p]
     L.pfg_destroy.restype = None
     L.pfg_last_error.argtypes = [C.c_void_p]
@@ -127,5 +131,5 @@ EXPORTED = (
     "pfg_server_poll", "pfg_server_fetch", "pfg_server_stats_get", "pfg_server_destroy", "pfg_server_last_error",
     "pfg_dimacs_read", "pfg_dimacs_get_info", "pfg_dimacs_copy", "pfg_dimacs_error", "pfg_dimacs_free",
     "pfg_map_vars", "pfg_map_lits", "pfg_extend_model", "pfg_download_proof", "pfg_batch_download_proof",
-    "pfg_proof_text",
+    "pfg_proof_text", "pfg_host_alloc", "pfg_host_free",
 )

@@ -50,6 +50,13 @@ class Cnf:
     def clause(self, i: int) -> np.ndarray:
         return self.lits[int(self.off[i]):int(self.off[i + 1])]
 
+    def pinned(self) -> "Cnf":
+        """A copy whose arrays live in page-locked host memory (uploads from it
+        are direct DMA transfers)."""
+        from . import pinned as pm
+        cp = lambda a: None if a is None else pm.copy(a)
+        return Cnf(self.max_var, pm.copy(self.lits), pm.copy(self.off), cp(self.learnt), cp(self.lbd), cp(self.usage))
+
     def clauses(self) -> List[List[int]]:
         """Clauses as lists of DIMACS integers."""
         out = []

@@ -708,6 +708,19 @@ uint32_t select_mode(Ctx& c, uint8_t want, uint32_t*& out) {
 
 using namespace pfg;
 
+// Page-locked host memory for callers' input and result buffers: copies from
+// and to it run as DMA at link speed instead of through staging buffers
+// (cuMM::allocPinned, src/gpu/memory.cu:505-523).
+extern "C" void* pfg_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return p;
+}
+
+extern "C" void pfg_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
 extern "C" void pfg_abi_sizes(size_t* options, size_t* stats, size_t* result_sizes) {
     if (options) *options = sizeof(pfg_options);
     if (stats) *stats = sizeof(pfg_stats);

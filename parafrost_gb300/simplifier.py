@@ -181,25 +181,28 @@ class Simplifier:
         self._check(self.lib.pfg_batch_download_proof(self._ctx, i, _ptr(buf, C.c_uint8)), "pfg_batch_download_proof")
         return buf.tobytes()
 
-    def download_all(self) -> list:
+    def download_all(self, into=None) -> list:
         """Results of every instance of the batch, one copy per output array
-        (each instance's arrays are views into them)."""
+        (each instance's arrays are views into them). `into`: a
+        pinned.ResultBuffers to download into (page-locked, reused across calls)."""
         n = self.batch_size()
         sizes = (_abi.PfgResultSizes * max(n, 1))()
         self._check(self.lib.pfg_batch_result_sizes_all(self._ctx, sizes), "pfg_batch_result_sizes_all")
         f = lambda name: np.array([getattr(sizes[i], name) for i in range(n)], dtype=np.int64)
         ncls, nlit, nvar = f("clauses"), f("literals"), f("max_var")
         nun, npend, nstk, nrnd = f("units"), f("pending_units"), f("stack_words"), f("rounds")
-        lits = np.empty(int(nlit.sum()), dtype=np.uint32)
-        off = np.empty(int((ncls + 1).sum()), dtype=np.uint64)
-        learnt = np.empty(int(ncls.sum()), dtype=np.uint8)
-        lbd = np.empty(int(ncls.sum()), dtype=np.uint32)
-        usage = np.empty(int(ncls.sum()), dtype=np.uint8)
-        elim = np.empty(int((nvar + 1).sum()), dtype=np.uint8)
-        units = np.empty(int(nun.sum()), dtype=np.uint32)
-        pend = np.empty(int(npend.sum()), dtype=np.uint32)
-        stack = np.empty(int(nstk.sum()), dtype=np.uint32)
-        rends = np.empty(int(nrnd.sum()), dtype=np.uint64)
+        alloc = (lambda name, k, dt: np.empty(k, dtype=dt)) if into is None else \
+            (lambda name, k, dt: into.get(name, k))
+        lits = alloc("lits", int(nlit.sum()), np.uint32)
+        off = alloc("off", int((ncls + 1).sum()), np.uint64)
+        learnt = alloc("learnt", int(ncls.sum()), np.uint8)
+        lbd = alloc("lbd", int(ncls.sum()), np.uint32)
+        usage = alloc("usage", int(ncls.sum()), np.uint8)
+        elim = alloc("elim", int((nvar + 1).sum()), np.uint8)
+        units = alloc("units", int(nun.sum()), np.uint32)
+        pend = alloc("pend", int(npend.sum()), np.uint32)
+        stack = alloc("stack", int(nstk.sum()), np.uint32)
+        rends = alloc("rends", int(nrnd.sum()), np.uint64)
         rc = self.lib.pfg_batch_download_all(self._ctx, _ptr(lits, C.c_uint32), _ptr(off, C.c_uint64),
                                              _ptr(learnt, C.c_uint8), _ptr(lbd, C.c_uint32), _ptr(usage, C.c_uint8),
                                              _ptr(elim, C.c_uint8), _ptr(units, C.c_uint32), _ptr(pend, C.c_uint32),
@@ -223,11 +226,12 @@ class Simplifier:
                                       self._proof_of(i, int(sizes[i].proof_bytes))))
         return out
 
-    def simplify_batch(self, cnfs, var_states=None, assumeds=None, vorgs=None) -> list:
-        """Simplify every CNF of `cnfs` in one device store; one result per instance."""
+    def simplify_batch(self, cnfs, var_states=None, assumeds=None, vorgs=None, into=None) -> list:
+        """Simplify every CNF of `cnfs` in one device store; one result per
+        instance (views into `into`, a pinned.ResultBuffers, when given)."""
         self.upload_batch(cnfs, var_states, assumeds, vorgs)
         self.run()
-        return self.download_all()
+        return self.download_all(into)
 
     def profile(self, on: bool = True) -> None:
         """Per-kernel CUDA-event timing of the following simplify calls."""

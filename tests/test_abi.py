@@ -103,3 +103,14 @@ def test_planted_scalefree_is_satisfied_by_construction():
 def test_invalid_generator_arguments():
     with pytest.raises(ValueError):
         pg.generate(9, 1, 1, 1, 1)
+
+
+def test_pinned_arrays_fall_back_without_a_device():
+    from parafrost_gb300 import pinned
+    a = pinned.empty(10, np.uint32)
+    a[:] = np.arange(10)
+    assert a.dtype == np.uint32 and a.sum() == 45
+    b = pinned.copy(np.arange(5, dtype=np.uint64))
+    assert b.tolist() == [0, 1, 2, 3, 4]
+    buf = pinned.ResultBuffers()
+    assert buf.get("lits", 7).size == 7 and buf.get("lits", 3).size == 3

@@ -157,3 +157,21 @@ def test_bulk_and_per_instance_downloads_agree():
                      (a.round_ends, b.round_ends)):
             assert np.array_equal(x, y)
         assert a.status == b.status and a.stats["clauses_out"] == b.stats["clauses_out"]
+
+
+def test_download_into_pinned_buffers():
+    from parafrost_gb300 import pinned
+    buf = pinned.ResultBuffers()
+    for seeds in ([61, 62], [63, 64, 65, 66, 67]):
+        cnfs = [inst(s, scale=2).pinned() for s in seeds]
+        assert all(pinned.is_pinned(c.lits) for c in cnfs)
+        with pg.Simplifier() as s:
+            s.upload_batch(cnfs)
+            s.run()
+            ref = s.download_all()
+            got = s.download_all(into=buf)
+        for a, b in zip(got, ref):
+            for x, y in ((a.cnf.lits, b.cnf.lits), (a.cnf.off, b.cnf.off), (a.eliminated, b.eliminated),
+                         (a.units, b.units), (a.stack, b.stack), (a.round_ends, b.round_ends)):
+                assert np.array_equal(x, y)
+        assert pinned.is_pinned(got[0].cnf.lits)
