@@ -211,10 +211,29 @@ bool proof_collect(Ctx& c) {
 
 namespace {
 
+// Offsets of every uploaded clause: the first clause of an instance starts at
+// 0, every clause ends at least 2 literals after its start and no later than
+// the instance's literal count. The smallest failing clause lands in *bad.
+__global__ void check_off_k(const unsigned long long* off, uint64_t ncls, const unsigned long long* clsbase,
+                            const unsigned long long* litbase, uint32_t ninst, unsigned long long* bad) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = ninst;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (clsbase[mid] <= c) lo = mid; else hi = mid;
+        }
+        const uint64_t L = litbase[lo + 1] - litbase[lo];
+        const uint64_t b = off[c];
+        const uint64_t e = (c + 1 < clsbase[lo + 1]) ? off[c + 1] : L;
+        if ((c == clsbase[lo] && b != 0) || e < b + 2 || e > L) atomicMin(bad, (unsigned long long)c);
+    }
+}
+
 // header of every uploaded clause; literals moved to their instance's variable range
 __global__ void init_hdr_k(ClsHdr* hdr, const unsigned long long* off, uint64_t ncls, const uint8_t* learnt,
                            const uint32_t* lbd, const uint8_t* usage, const unsigned long long* clsbase,
-                           const unsigned long long* litbase, const uint32_t* voff, uint32_t ninst, uint32_t* lits) {
+                           const unsigned long long* litbase, const uint32_t* voff, uint32_t ninst,
+                           const uint32_t* vmax, uint32_t* lits, unsigned long long* bad) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t lo = 0, hi = ninst;   // largest i with clsbase[i] <= c
         while (hi - lo > 1) {
@@ -232,14 +251,21 @@ __global__ void init_hdr_k(ClsHdr* hdr, const unsigned long long* off, uint64_t 
         h.meta = l ? m_make(ST_LEARNT, 0, 0, usage ? (usage[c] & 3u) : 0u, lbd ? (lbd[c] & 0x03FFFFFFu) : 0u)
                    : m_make(ST_ORIGINAL, 0, 0, 0, 0);
         hdr[c] = h;
-        const uint32_t shift = 2u * voff[inst];
-        if (shift)
-            for (uint64_t k = b; k < e; k++) lits[k] += shift;
+        const uint32_t shift = 2u * voff[inst], vm = vmax[inst];
+        bool ok = true;
+        for (uint64_t k = b; k < e; k++) {
+            const uint32_t v = lits[k] >> 1;
+            ok &= v >= 1 && v <= vm;
+            lits[k] += shift;
+        }
+        if (!ok) atomicMin(bad, (unsigned long long)c);
     }
 }
 
 // prep_cnf_k (cnf.cu:45-53): sort literals of every clause, compute its signature
-__global__ void prep_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls) {
+// literals of every clause sorted, signature computed; a variable that occurs
+// twice in a clause (repeated literal or a literal and its negation) lands in *bad
+__global__ void prep_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls, unsigned long long* bad) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         const ClsHdr h = hdr[c];
         uint32_t* l = lits + h.off;
@@ -249,6 +275,8 @@ __global__ void prep_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls) {
             while (j > 0 && t < l[j - 1]) { l[j] = l[j - 1]; j--; }
             l[j] = t;
         }
+        for (uint32_t i = 1; i < h.size; i++)
+            if ((l[i] >> 1) == (l[i - 1] >> 1)) { atomicMin(bad, (unsigned long long)c); break; }
         if (h.size > 1) {
             uint32_t s = 0;
             for (uint32_t i = 0; i < h.size; i++) s |= MAPHASH(l[i]);
@@ -412,33 +440,25 @@ struct PassTimer {
 
 // Host checks of one instance (literal range, clause size >= 2, no duplicate or
 // complementary literals); also counts its original clauses and literals.
-bool valid_instance(uint32_t idx, const pfg_instance& q, std::vector<uint64_t>& seen, std::string& err,
-                    uint64_t& orig_cls, uint64_t& orig_lits) {
+// Host checks of one instance that cost O(1), plus its original (non-learnt)
+// clause and literal counts (a pass over the learnt flags when there are any).
+// Offsets, literal ranges and repeated variables are checked on the device
+// while the clauses are prepared.
+bool valid_instance(uint32_t idx, const pfg_instance& q, std::string& err, uint64_t& orig_cls, uint64_t& orig_lits) {
     const std::string who = "instance " + std::to_string(idx) + ": ";
     orig_cls = orig_lits = 0;
     if (q.max_var == 0 || q.max_var > 0x7FFFFFF0u || (q.num_clauses && (!q.lits || !q.cls_off))) {
         err = who + "invalid arguments";
         return false;
     }
-    if (q.num_clauses && q.cls_off[0] != 0) { err = who + "cls_off[0] must be 0"; return false; }
-    const uint64_t nlits = q.num_clauses ? q.cls_off[q.num_clauses] : 0;
-    seen.assign((size_t)q.max_var + 1, ~0ull);
-    for (uint64_t i = 0; i < q.num_clauses; i++) {
-        const uint64_t b = q.cls_off[i], e = q.cls_off[i + 1];
-        if (e < b + 2 || e > nlits) { err = who + "clause " + std::to_string(i) + " has fewer than 2 literals"; return false; }
-        for (uint64_t k = b; k < e; k++) {
-            const uint32_t l = q.lits[k], v = l >> 1;
-            if (v == 0 || v > q.max_var) { err = who + "literal out of range in clause " + std::to_string(i); return false; }
-            if (seen[v] == i) { err = who + "repeated variable in clause " + std::to_string(i); return false; }
-            seen[v] = i;
-        }
-        if (!(q.cls_learnt && q.cls_learnt[i])) { orig_cls++; orig_lits += e - b; }
-    }
+    if (!q.num_clauses) return true;
+    if (q.cls_off[0] != 0) { err = who + "cls_off[0] must be 0"; return false; }
+    const uint64_t nlits = q.cls_off[q.num_clauses];
+    if (!q.cls_learnt) { orig_cls = q.num_clauses; orig_lits = nlits; return true; }
+    for (uint64_t i = 0; i < q.num_clauses; i++)
+        if (!q.cls_learnt[i]) { orig_cls++; orig_lits += q.cls_off[i + 1] - q.cls_off[i]; }
     return true;
 }
-
-// valid_instance over all instances on the host's cores; the first failing
-// instance (lowest index) is reported
 bool valid_instances(Ctx& c, uint32_t n, const pfg_instance* in, std::vector<uint64_t>& orig_cls,
                      std::vector<uint64_t>& orig_lits) {
     orig_cls.assign(n, 0);
@@ -447,9 +467,8 @@ bool valid_instances(Ctx& c, uint32_t n, const pfg_instance* in, std::vector<uin
     std::vector<uint8_t> ok(n, 1);
     std::atomic<uint32_t> next{0};
     auto work = [&]() {
-        std::vector<uint64_t> seen;
         for (uint32_t i = next.fetch_add(1); i < n; i = next.fetch_add(1))
-            ok[i] = valid_instance(i, in[i], seen, errs[i], orig_cls[i], orig_lits[i]) ? 1 : 0;
+            ok[i] = valid_instance(i, in[i], errs[i], orig_cls[i], orig_lits[i]) ? 1 : 0;
     };
     const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
     const uint32_t nt = std::min<uint32_t>(n, std::min<uint32_t>(hw, 64));
@@ -605,7 +624,7 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
     uint8_t* d_learnt = nullptr;
     uint32_t* d_lbd = nullptr;
     uint8_t* d_usage = nullptr;
-    ok = dalloc_t(c, &d_off, Ctot + 1) && dalloc_t(c, &d_base, 2 * ((size_t)n + 1));
+    ok = dalloc_t(c, &d_off, Ctot + 1) && dalloc_t(c, &d_base, 2 * ((size_t)n + 1) + 2 + ((size_t)n + 1) / 2);
     if (ok && any_learnt) ok = dalloc_t(c, &d_learnt, Ctot + 1);
     if (ok && any_lbd) ok = dalloc_t(c, &d_lbd, Ctot + 1);
     if (ok && any_usage) ok = dalloc_t(c, &d_usage, Ctot + 1);
@@ -613,9 +632,17 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
     if (any_learnt) cudaMemsetAsync(d_learnt, 0, Ctot + 1, c.s);
     if (any_lbd) cudaMemsetAsync(d_lbd, 0, (Ctot + 1) * sizeof(uint32_t), c.s);
     if (any_usage) cudaMemsetAsync(d_usage, 0, Ctot + 1, c.s);
+    // d_base: clsbase (n+1), litbase (n+1), two error words (first bad clause of
+    // the offset check and of the literal checks), then max_var per instance
+    const size_t nb2 = 2 * ((size_t)n + 1);
+    unsigned long long* d_bad = d_base + nb2;
+    uint32_t* d_vmax = reinterpret_cast<uint32_t*>(d_base + nb2 + 2);
     {
-        std::vector<unsigned long long> bases(2 * ((size_t)n + 1));
+        std::vector<unsigned long long> bases(nb2 + 2 + ((size_t)n + 1) / 2, 0);
         for (uint32_t i = 0; i <= n; i++) { bases[i] = clsbase[i]; bases[n + 1 + i] = litbase[i]; }
+        bases[nb2] = bases[nb2 + 1] = ~0ull;
+        uint32_t* vm = reinterpret_cast<uint32_t*>(bases.data() + nb2 + 2);
+        for (uint32_t i = 0; i < n; i++) vm[i] = in[i].max_var;
         cudaMemcpy(d_base, bases.data(), bases.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice);
     }
     cudaMemsetAsync(c.vstate, 0, V1, c.s);
@@ -634,10 +661,19 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
         if (q.assumed) cudaMemcpyAsync(c.assumed + vo + 1, q.assumed + 1, q.max_var, cudaMemcpyHostToDevice, c.s);
         if (q.vorg) cudaMemcpyAsync(c.vorg + vo + 1, q.vorg + 1, q.max_var * sizeof(uint32_t), cudaMemcpyHostToDevice, c.s);
     }
+    unsigned long long hbad[2] = {~0ull, ~0ull};
     if (Ctot) {
-        PFG_LAUNCH(K_UPLOAD, init_hdr_k, grid_for(Ctot, 256), 256, 0, c.s, c.hdr, d_off, Ctot, d_learnt, d_lbd, d_usage,
-                   d_base, d_base + n + 1, c.di.voff, n, c.lits);
-        PFG_LAUNCH(K_UPLOAD, prep_k, grid_for(Ctot, 128), 128, 0, c.s, c.hdr, c.lits, Ctot);
+        // offsets first: the header kernel reads literals between them
+        PFG_LAUNCH(K_UPLOAD, check_off_k, grid_for(Ctot, 256), 256, 0, c.s, d_off, Ctot, d_base, d_base + n + 1, n,
+                   d_bad);
+        cudaMemcpyAsync(hbad, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.s);
+        cuda_ok(c, cudaStreamSynchronize(c.s), "upload");
+        if (hbad[0] == ~0ull && c.err.empty()) {
+            PFG_LAUNCH(K_UPLOAD, init_hdr_k, grid_for(Ctot, 256), 256, 0, c.s, c.hdr, d_off, Ctot, d_learnt, d_lbd,
+                       d_usage, d_base, d_base + n + 1, c.di.voff, n, d_vmax, c.lits, d_bad + 1);
+            PFG_LAUNCH(K_UPLOAD, prep_k, grid_for(Ctot, 128), 128, 0, c.s, c.hdr, c.lits, Ctot, d_bad + 1);
+            cudaMemcpyAsync(hbad + 1, d_bad + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.s);
+        }
     }
     if (c.o.proof_en) {
         if (!dalloc_t(c, &c.lbyte, 2 * V1)) { free_all(o); return PFG_CNFALLOC_FAIL; }
@@ -651,6 +687,17 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
     c.launches += g_launches - base_launches;
     g_prof = nullptr;
     if (!c.err.empty()) return PFG_CUDA_ERROR;
+    for (int k = 0; k < 2; k++) {
+        if (hbad[k] == ~0ull) continue;
+        const uint64_t bad = hbad[k];
+        const uint32_t i = (uint32_t)(std::upper_bound(clsbase.begin(), clsbase.end(), bad) - clsbase.begin() - 1);
+        const std::string msg = "instance " + std::to_string(i) + ": clause " + std::to_string(bad - clsbase[i]) +
+                                (k == 0 ? " has fewer than 2 literals or offsets out of order"
+                                        : " has a literal out of range or a repeated variable");
+        free_all(o);
+        c.err = msg;
+        return PFG_INVALID;
+    }
     c.uploaded = true;
     c.simplified = false;
     c.cache_ready = false;
@@ -1217,6 +1264,26 @@ namespace {
 // kept), literals back in the instance's numbering, offsets relative to the
 // instance. Per-instance eliminated / forced counts come from one copy of the
 // eliminated bytes.
+// per instance: variables eliminated (any bit but FORCED) and forced, with one
+// atomic per warp and instance
+__global__ void elim_counts_k(const uint8_t* elim, const uint32_t* vinst, uint32_t V, unsigned long long* cnt) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x; b < (uint64_t)V + 1; b += stride) {
+        const uint64_t v = b + threadIdx.x;
+        const bool in = v >= 1 && v <= V;
+        const uint8_t e = in ? elim[v] : 0u;
+        const uint32_t inst = in ? vinst[v] : 0xFFFFFFFFu;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, inst);
+        const unsigned fb = __ballot_sync(0xFFFFFFFFu, (e & FORCED_MASK) != 0) & peers;
+        const unsigned eb = __ballot_sync(0xFFFFFFFFu, e && !(e & FORCED_MASK)) & peers;
+        if (in && lane == (unsigned)(__ffs(peers) - 1)) {
+            if (eb) atomicAdd(&cnt[2 * (uint64_t)inst], (unsigned long long)__popc(eb));
+            if (fb) atomicAdd(&cnt[2 * (uint64_t)inst + 1], (unsigned long long)__popc(fb));
+        }
+    }
+}
+
 int build_cache(Ctx& c) {
     if (c.cache_ready) return PFG_OK;
     const uint32_t n = c.ninst;
@@ -1258,22 +1325,22 @@ int build_cache(Ctx& c) {
         cudaMemcpyAsync(bases, c.cache_lit_base.data(), ((size_t)n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, c.s);
         PFG_LAUNCH(K_DOWNLOAD, relative_off_k, grid_for(C, 256), 256, 0, c.s, keys, C, bases, c.pk_roff);
     }
-    std::vector<uint8_t> el((size_t)c.V + 1);
-    cudaMemcpyAsync(el.data(), c.elim, (size_t)c.V + 1, cudaMemcpyDeviceToHost, c.s);
+    // eliminated and forced variables per instance, counted on the device
+    unsigned long long* ecnt = nullptr;
+    if (!dalloc_t(c, &ecnt, 2 * (size_t)n)) { release(); return PFG_CNFALLOC_FAIL; }
+    cudaMemsetAsync(ecnt, 0, 2 * (size_t)n * sizeof(unsigned long long), c.s);
+    PFG_LAUNCH(K_DOWNLOAD, elim_counts_k, grid_for(c.V, 256), 256, 0, c.s, c.elim, c.vinst, c.V, ecnt);
+    std::vector<unsigned long long> hcnt(2 * (size_t)n);
+    cudaMemcpyAsync(hcnt.data(), ecnt, hcnt.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.s);
     const bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "batch write-back");
     release();
+    dfree(c, ecnt);
     if (!synced) return PFG_CUDA_ERROR;
     c.cache_elim_cnt.assign(n, 0);
     c.cache_forced_cnt.assign(n, 0);
     for (uint32_t i = 0; i < n; i++) {
-        const InstHost& h = c.ih[i];
-        uint64_t ne = 0, nf = 0;
-        for (uint32_t v = h.voff + 1; v <= h.voff + h.V; v++) {
-            if (el[v] & FORCED_MASK) nf++;
-            else if (el[v]) ne++;
-        }
-        c.cache_elim_cnt[i] = ne;
-        c.cache_forced_cnt[i] = nf;
+        c.cache_elim_cnt[i] = hcnt[2 * i];
+        c.cache_forced_cnt[i] = hcnt[2 * i + 1];
     }
     c.cache_ready = true;
     return PFG_OK;
@@ -1410,6 +1477,18 @@ __global__ void regions_all_k(const uint32_t* src, const unsigned long long* src
     }
 }
 
+// instance of every gathered unit (its region in dst_base)
+__global__ void region_ids_k(const unsigned long long* dst_base, uint32_t n, uint64_t total, uint32_t* out) {
+    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (uint64_t)gridDim.x * blockDim.x)
+        out[q] = region_of(dst_base, n, q);
+}
+
+uint32_t bits_for(uint64_t x) {
+    uint32_t b = 1;
+    while (b < 32 && (x >> b)) b++;
+    return b;
+}
+
 }  // namespace
 }  // namespace pfg
 
@@ -1479,9 +1558,30 @@ extern "C" int pfg_batch_download_all(pfg_ctx* o, uint32_t* lits, uint64_t* cls_
         PFG_LAUNCH(K_DOWNLOAD, offsets_all_k, grid_for(C + n, 256), 256, 0, c.s, c.pk_roff, C, d_cb, d_lb, n, doff);
     if (eliminated)
         PFG_LAUNCH(K_DOWNLOAD, elim_all_k, grid_for(eb[n], 256), 256, 0, c.s, c.elim, d_eb, c.di.voff, n, eb[n], delim);
-    if (units && ub[n])
-        PFG_LAUNCH(K_DOWNLOAD, regions_all_k, grid_for(ub[n], 256), 256, 0, c.s, c.trail, d_tsrc, d_ub, dshift, n,
-                   ub[n], dunits);
+    uint32_t* units_sorted = dunits;
+    uint32_t *uk1 = nullptr, *uv0 = nullptr, *uv1 = nullptr;
+    if (units && ub[n]) {
+        // every instance's units sorted ascending on the device: a stable sort by
+        // literal, then a stable sort by instance
+        const uint64_t N = ub[n];
+        PFG_LAUNCH(K_DOWNLOAD, regions_all_k, grid_for(N, 256), 256, 0, c.s, c.trail, d_tsrc, d_ub, dshift, n, N,
+                   dunits);
+        uint32_t vmax = 0;
+        for (uint32_t i = 0; i < n; i++) vmax = std::max(vmax, c.ih[i].V);
+        if (!dalloc_t(c, &uk1, N) || !dalloc_t(c, &uv0, N) || !dalloc_t(c, &uv1, N) ||
+            !ensure_tmp(c, radix_temp_bytes(N))) {
+            release(); dfree(c, uk1); dfree(c, uv0); dfree(c, uv1);
+            return finish(c, nullptr, base_launches, PFG_CNFALLOC_FAIL);
+        }
+        PFG_LAUNCH(K_DOWNLOAD, region_ids_k, grid_for(N, 256), 256, 0, c.s, d_ub, n, N, uv0);
+        const int r1 = radix_sort_pairs(dunits, uv0, uk1, uv1, N, 0, (int)bits_for(2ull * vmax + 1), c.tmp, c.s);
+        uint32_t* lk = r1 ? uk1 : dunits;     // literals, sorted
+        uint32_t* li = r1 ? uv1 : uv0;        // their instances
+        uint32_t* ak = r1 ? dunits : uk1;     // spare pair
+        uint32_t* ai = r1 ? uv0 : uv1;
+        const int r2 = radix_sort_pairs(li, lk, ai, ak, N, 0, (int)bits_for(n), c.tmp, c.s);
+        units_sorted = r2 ? ak : lk;
+    }
     if (stack && sb[n])
         PFG_LAUNCH(K_DOWNLOAD, regions_all_k, grid_for(sb[n], 256), 256, 0, c.s, c.stack, d_ssrc, d_sb,
                    (const uint32_t*)nullptr, n, sb[n], dstack);
@@ -1491,15 +1591,15 @@ extern "C" int pfg_batch_download_all(pfg_ctx* o, uint32_t* lits, uint64_t* cls_
     if (cls_lbd && C) cudaMemcpyAsync(cls_lbd, c.pk_lbd, C * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     if (cls_usage && C) cudaMemcpyAsync(cls_usage, c.pk_usage, C, cudaMemcpyDeviceToHost, c.s);
     if (eliminated) cudaMemcpyAsync(eliminated, delim, eb[n], cudaMemcpyDeviceToHost, c.s);
-    if (units && ub[n]) cudaMemcpyAsync(units, dunits, ub[n] * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (units && ub[n]) cudaMemcpyAsync(units, units_sorted, ub[n] * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     if (stack && sb[n]) cudaMemcpyAsync(stack, dstack, sb[n] * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     const bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "batch download");
     release();
+    dfree(c, uk1); dfree(c, uv0); dfree(c, uv1);
     if (!synced) return finish(c, nullptr, base_launches, PFG_CUDA_ERROR);
     uint64_t pend = 0, rends = 0;
     for (uint32_t i = 0; i < n; i++) {
         const InstHost& h = c.ih[i];
-        if (units) std::sort(units + ub[i], units + ub[i + 1]);
         if (pending_units && !h.pending.empty()) {
             for (size_t k = 0; k < h.pending.size(); k++) pending_units[pend + k] = h.pending[k] - 2u * h.voff;
             std::sort(pending_units + pend, pending_units + pend + h.pending.size());
