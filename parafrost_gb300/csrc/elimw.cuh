@@ -678,6 +678,25 @@ PFG_D void ws_elim_no_resolvents(const EK& k, WS& w, uint32_t x, const Side& P, 
     if (lane == 0) k.elim[x] |= MELTING_MASK;
 }
 
+// find_fun_gate maps the neighbours of x through varcore (their place in the
+// instance's frozen list) and builds truth tables over the first MAXFUNVAR
+// only: with one neighbour further down the list (in a clause that is not
+// learnt) it returns false before it changes anything (function.cuh:283-290),
+// and the variable goes straight on to n-by-m resolution.
+PFG_D bool ws_fun_possible(const EK& k, WS& w, uint32_t x, unsigned lane) {
+    const uint32_t nc = w.np + w.nn;
+    bool far = false;
+    for (uint32_t i = lane; i < nc && !far; i += 32) {
+        if (m_learnt(w.meta[i])) continue;
+        const uint32_t* l = WL(w, i);
+        for (uint32_t t = 0; t < w.size[i]; t++) {
+            const uint32_t v = ABSV(l[t]);
+            if (v != x && k.varcore[v] >= MAXFUNVAR) { far = true; break; }
+        }
+    }
+    return !__any_sync(FULL, far);
+}
+
 // BVE phase 1 for one staged variable (bounded.cuh:282-394)
 PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, uint32_t* ucnt,
                   unsigned long long* rpos, unsigned long long* rref, uint32_t* dlist, uint32_t* dcount,
@@ -745,7 +764,7 @@ PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
             ws_freeze_arities(w, lane);
         }
     }
-    if (vc_on(k, x) && !elimType && nClsBefore > 2) {
+    if (vc_on(k, x) && !elimType && nClsBefore > 2 && ws_fun_possible(k, w, x, lane)) {
         ws_flush(k, w, lane);
         if (lane == 0) {
             dlist[atomicAdd(dcount, 1u)] = tid;
