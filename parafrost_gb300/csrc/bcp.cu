@@ -2,7 +2,9 @@
 //
 // Replaces Solver::prop (src/gpu/elimbcp.cu:144-215): a BFS over falsified
 // literals whose frontier lives on the device; one warp scans one frontier
-// literal's occurrence list. Assignments are claimed with atomicCAS, so the
+// literal's occurrence list, and the lists longer than BCP_LONG (hub literals
+// of skewed instances) are spread over every thread of the grid instead, so
+// one long list does not hold up its level. Assignments are claimed with atomicCAS, so the
 // fixpoint (and a conflict) is independent of the schedule. Every level is a
 // kernel launch; the host reads the frontier size only every 1, 2, 4 .. 64
 // levels, and the level loop is bounded. With several instances, each one
@@ -26,8 +28,12 @@ struct BK {
     uint32_t* conflict;
     uint32_t* trail;
     DevCounters* dc;
+    const uint32_t* ot_size;
+    uint32_t* long_next;     // frontier literals with long lists, next level
     uint32_t V;
 };
+
+constexpr uint32_t BCP_LONG = 1024;   // lists longer than this are split over the grid
 
 PFG_D uint32_t litval(const uint8_t* st, uint32_t lit) {
     const uint8_t s = st[ABSV(lit)];
@@ -62,7 +68,9 @@ PFG_D void assign_unit(const BK& k, uint32_t unit, uint32_t* front_next) {
             k.elim[v] |= FORCED_MASK;
             const uint32_t t = atomicAdd(&k.tcount[inst], 1u);
             if (t < k.tcap[inst]) k.trail[k.tbase[inst] + t] = unit; else atomicOr(&k.dc->err, ERR_UNITS_OVERFLOW);
-            front_next[atomicAdd(&k.dc->bcp_next, 1u)] = FLIPL(unit);
+            const uint32_t f = FLIPL(unit);
+            if (k.ot_size[f] > BCP_LONG) k.long_next[atomicAdd(&k.dc->bcp_lnext, 1u)] = f;
+            else front_next[atomicAdd(&k.dc->bcp_next, 1u)] = f;
             return;
         }
         old = prev;
@@ -84,6 +92,8 @@ __global__ void bcp_seed_k(BK k, const uint32_t* units, const unsigned long long
 __global__ void bcp_advance_k(DevCounters* dc) {
     dc->bcp_curr = dc->bcp_next;
     dc->bcp_next = 0;
+    dc->bcp_lcurr = dc->bcp_lnext;
+    dc->bcp_lnext = 0;
     dc->bcp_level++;
 }
 
@@ -91,51 +101,68 @@ __global__ void bcp_advance_k(DevCounters* dc) {
 constexpr uint32_t BCP_GROUP = 32;
 constexpr uint32_t BCP_HEAD = 4;
 
+// one clause of a falsified literal's list: conflict, unit or nothing
+PFG_D void bcp_clause(const BK& k, const ClsHdr* hdr, const uint32_t* lits, uint32_t cid, uint32_t inst,
+                      uint32_t* nxt) {
+    const ClsHdr h = hdr[cid];
+    if (m_deleted(h.meta)) return;
+    uint32_t unit = 0;
+    int nunset = 0;
+    bool sat = false;
+    // the first BCP_HEAD literals and their values are loaded together
+    const uint32_t* cl = lits + h.off;
+    uint32_t hl[BCP_HEAD];
+    uint32_t hv[BCP_HEAD];
+#pragma unroll
+    for (uint32_t q = 0; q < BCP_HEAD; q++) hl[q] = q < h.size ? cl[q] : 0u;
+#pragma unroll
+    for (uint32_t q = 0; q < BCP_HEAD; q++) hv[q] = q < h.size ? litval(k.st, hl[q]) : BCP_FALSE;
+#pragma unroll
+    for (uint32_t q = 0; q < BCP_HEAD; q++) {
+        if (hv[q] == BCP_TRUE) sat = true;
+        else if (hv[q] == BCP_UNSET) { unit = hl[q]; nunset++; }
+    }
+    for (uint32_t q = BCP_HEAD; q < h.size && !sat && nunset < 2; q++) {
+        const uint32_t l = cl[q];
+        const uint32_t ve = litval(k.st, l);
+        if (ve == BCP_TRUE) { sat = true; break; }
+        if (ve == BCP_UNSET) { unit = l; nunset++; }
+    }
+    if (sat) return;
+    if (!nunset) set_conflict(k, inst);
+    else if (nunset == 1) assign_unit(k, unit, nxt);
+}
+
 __global__ void bcp_propagate_k(BK k, const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off,
                                 const uint32_t* ot_size, const uint32_t* ot_ids, const uint32_t* front_a,
-                                uint32_t* front_b) {
+                                uint32_t* front_b, const uint32_t* long_a, uint32_t* long_b) {
     DevCounters* dc = k.dc;
     const uint32_t level = dc->bcp_level;
     const uint32_t* cur = (level & 1u) ? front_b : (uint32_t*)front_a;
     uint32_t* nxt = (level & 1u) ? (uint32_t*)front_a : front_b;
+    const uint32_t* lcur = (level & 1u) ? long_b : (uint32_t*)long_a;
+    k.long_next = (level & 1u) ? (uint32_t*)long_a : long_b;
     const uint32_t n = dc->bcp_curr;
-    const uint32_t group = (blockIdx.x * blockDim.x + threadIdx.x) / BCP_GROUP;
-    const uint32_t ngroups = (gridDim.x * blockDim.x) / BCP_GROUP;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    const uint32_t group = tid / BCP_GROUP;
+    const uint32_t ngroups = nthreads / BCP_GROUP;
     const uint32_t lane = threadIdx.x % BCP_GROUP;
     for (uint32_t fi = group; fi < n; fi += ngroups) {
         const uint32_t f = cur[fi];
         const uint32_t inst = k.vinst[ABSV(f)];
         if (k.conflict[inst]) continue;       // this instance is UNSAT: stop propagating it
         const uint32_t o = ot_off[f], sz = ot_size[f];
-        for (uint32_t j = lane; j < sz; j += BCP_GROUP) {
-            const ClsHdr h = hdr[ot_ids[o + j]];
-            if (m_deleted(h.meta)) continue;
-            uint32_t unit = 0;
-            int nunset = 0;
-            bool sat = false;
-            // the first BCP_HEAD literals and their values are loaded together
-            const uint32_t* cl = lits + h.off;
-            uint32_t hl[BCP_HEAD];
-            uint32_t hv[BCP_HEAD];
-#pragma unroll
-            for (uint32_t q = 0; q < BCP_HEAD; q++) hl[q] = q < h.size ? cl[q] : 0u;
-#pragma unroll
-            for (uint32_t q = 0; q < BCP_HEAD; q++) hv[q] = q < h.size ? litval(k.st, hl[q]) : BCP_FALSE;
-#pragma unroll
-            for (uint32_t q = 0; q < BCP_HEAD; q++) {
-                if (hv[q] == BCP_TRUE) sat = true;
-                else if (hv[q] == BCP_UNSET) { unit = hl[q]; nunset++; }
-            }
-            for (uint32_t q = BCP_HEAD; q < h.size && !sat && nunset < 2; q++) {
-                const uint32_t l = cl[q];
-                const uint32_t ve = litval(k.st, l);
-                if (ve == BCP_TRUE) { sat = true; break; }
-                if (ve == BCP_UNSET) { unit = l; nunset++; }
-            }
-            if (sat) continue;
-            if (!nunset) set_conflict(k, inst);
-            else if (nunset == 1) assign_unit(k, unit, nxt);
-        }
+        for (uint32_t j = lane; j < sz; j += BCP_GROUP) bcp_clause(k, hdr, lits, ot_ids[o + j], inst, nxt);
+    }
+    // long lists: every thread of the grid takes a share of each
+    const uint32_t nl = dc->bcp_lcurr;
+    for (uint32_t li = 0; li < nl; li++) {
+        const uint32_t f = lcur[li];
+        const uint32_t inst = k.vinst[ABSV(f)];
+        if (k.conflict[inst]) continue;
+        const uint32_t o = ot_off[f], sz = ot_size[f];
+        for (uint32_t j = tid; j < sz; j += nthreads) bcp_clause(k, hdr, lits, ot_ids[o + j], inst, nxt);
     }
 }
 
@@ -173,10 +200,12 @@ bool bcp_prop(Ctx& c) {
     cudaMemsetAsync(&c.dc->conflict, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(c.dout.conflict, 0, c.ninst * sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->bcp_curr, 0, 3 * sizeof(uint32_t), c.s);
+    cudaMemsetAsync(&c.dc->bcp_lcurr, 0, 2 * sizeof(uint32_t), c.s);
     BK k;
     k.st = c.bstate; k.elim = c.elim; k.vinst = c.vinst;
     k.tbase = c.di.tbase; k.tcap = c.di.tcap; k.tcount = c.dout.tcount;
     k.conflict = c.dout.conflict; k.trail = c.trail; k.dc = c.dc; k.V = c.V;
+    k.ot_size = c.ot_size; k.long_next = c.long_a;
     uint64_t maxu = 0;
     for (uint32_t i = 0; i < c.ninst; i++)
         if (c.hi.bcp[i]) maxu = std::max<uint64_t>(maxu, c.ih[i].nUnits);
@@ -194,13 +223,13 @@ bool bcp_prop(Ctx& c) {
     for (int batch = 1;; batch = std::min(batch << 1, 64)) {
         for (int b = 0; b < batch; b++) {
             PFG_LAUNCH(K_BCP, bcp_propagate_k, grid, 256, 0, c.s, k, c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids,
-                       c.front_a, c.front_b);
+                       c.front_a, c.front_b, c.long_a, c.long_b);
             PFG_LAUNCH(K_BCP, bcp_advance_k, 1, 1, 0, c.s, c.dc);
         }
         levels += batch;
         sync_counters(c);
         if (!c.err.empty()) return false;
-        if ((single && c.hc->conflict) || !c.hc->bcp_curr) break;
+        if ((single && c.hc->conflict) || !(c.hc->bcp_curr | c.hc->bcp_lcurr)) break;
         if (levels > max_levels) { c.err = "device unit propagation did not converge"; c.simpstate = PFG_TIMEOUT; return false; }
     }
     if (c.hc->err) { c.err = "device error during unit propagation"; return false; }

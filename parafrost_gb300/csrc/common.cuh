@@ -86,6 +86,7 @@ struct DevCounters {
     uint32_t nfrozen;
     uint32_t conflict;             // BCP conflict flag
     uint32_t bcp_curr, bcp_next, bcp_level;
+    uint32_t bcp_lcurr, bcp_lnext;           // frontier literals with long lists
     uint32_t big_lists;
     uint32_t nbig_sub, nbig_ve1, nbig_ve3;   // variables too large for the warp stage
     unsigned long long ve_cls, ve_lits;      // store size after the last BVE emission

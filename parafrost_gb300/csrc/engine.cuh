@@ -169,6 +169,8 @@ struct Ctx {
     uint8_t* bstate = nullptr;
     uint32_t* front_a = nullptr;
     uint32_t* front_b = nullptr;
+    uint32_t* long_a = nullptr;   // frontier literals whose lists are split over the grid
+    uint32_t* long_b = nullptr;
 
     // counters
     DevCounters* dc = nullptr;   // device
