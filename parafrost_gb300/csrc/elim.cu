@@ -43,6 +43,7 @@ struct EK {
     ulonglong2* pf_b;                    // proof blocks {variable << 32 | sequence, first word}
     uint32_t pf_bcap;
     const uint8_t* lbyte;                // proof bytes per literal
+    uint8_t* cnew;                       // clauses added or rewritten in place (occurrence-table update)
 };
 
 PFG_D uint32_t* OLp(const EK& k, uint32_t lit) { return k.ot_ids + k.ot_off[lit]; }
@@ -639,6 +640,7 @@ PFG_D bool has_lit(const EK& k, uint32_t c, uint32_t lit) {
 }
 
 PFG_D void substitute_one(const EK& k, uint32_t dx, uint32_t def, uint32_t c, uint32_t& nUnits) {
+    k.cnew[c] = 1;
     const ClsHdr h = k.hdr[c];
     uint32_t* l = k.lits + h.off;
     uint32_t j = 0;
@@ -1161,6 +1163,7 @@ __global__ void __launch_bounds__(128) ve3_k(EK k, const uint32_t* elected, uint
                         h.sig = sig;
                         h.meta = m_make(ST_ORIGINAL, 0, 1, 0, 0);
                         k.hdr[slot] = h;
+                        k.cnew[slot] = 1;
                         slot++;
                         woff += (unsigned long long)rsize;
                     }
@@ -1481,6 +1484,7 @@ EK make_ek(Ctx& c) {
     k.pf_b = c.pf_b;
     k.pf_bcap = c.pf_bcap;
     k.lbyte = c.lbyte;
+    k.cnew = c.cnew;
     return k;
 }
 

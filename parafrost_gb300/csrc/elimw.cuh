@@ -634,6 +634,7 @@ PFG_D void ws_substitute_single(const EK& k, WS& w, const Side& P, const Side& N
                 }
                 w.size[c] = j;
                 w.dirty[c] = 1;
+                k.cnew[w.id[c]] = 1;
                 if (j == 1) cnt++;
                 else {
                     sort_small(l, j);
@@ -885,6 +886,7 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
                     h.sig = sig;
                     h.meta = m_make(ST_ORIGINAL, 0, 1, 0, 0);
                     k.hdr[slot + excl] = h;
+                    k.cnew[slot + excl] = 1;
                 }
                 added += ncl;
                 slot += ncl;

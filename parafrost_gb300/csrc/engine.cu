@@ -601,7 +601,7 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
          dalloc_t(c, &c.rlit, V1 + 1) && dalloc_t(c, &c.units, c.units_total) &&
          dalloc_t(c, &c.trail, c.trail_total) && dalloc_t(c, &c.stack, c.stack_total) &&
          dalloc_t(c, &c.front_a, V1) && dalloc_t(c, &c.front_b, V1) && dalloc_t(c, &c.long_a, V1) &&
-         dalloc_t(c, &c.long_b, V1);
+         dalloc_t(c, &c.long_b, V1) && dalloc_t(c, &c.cnew, c.hdr_cap) && dalloc_t(c, &c.ot_off2, c.nlist + 1);
     if (any_assumed) ok = ok && dalloc_t(c, &c.assumed, V1 + 8);
     if (!ok) {
         if (c.err.empty()) c.err = "device allocation failed";
@@ -681,6 +681,7 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
         PFG_LAUNCH(K_UPLOAD, lbyte_k, grid_for(2 * V1, 256), 256, 0, c.s, c.vorg, c.V, c.lbyte);
     }
     cudaMemsetAsync(c.elim, 0, V1, c.s);
+    cudaMemsetAsync(c.cnew, 0, c.hdr_cap, c.s);
     cudaMemsetAsync(c.varcore, 0, V1 * sizeof(uint32_t), c.s);
     cudaMemsetAsync(c.dc, 0, sizeof(DevCounters), c.s);
     dfree(c, d_off); dfree(c, d_base); dfree(c, d_learnt); dfree(c, d_lbd); dfree(c, d_usage);
@@ -938,13 +939,22 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         std::vector<uint32_t> act = active_ids(c);
         if (act.empty() || !c.err.empty()) break;
         const int times = c.phase + 1;
+        // after the first round the table is updated, not rebuilt: pruned on the
+        // old clause ids, then moved (through the compaction map) and completed
+        if (c.ot_valid) {
+            PassTimer t(c, 0);
+            if (!ot_prune(c)) break;
+        }
         if (times > 1 && times != c.o.phases && c.o.shrink_rate > 0 && (times % c.o.shrink_rate) == 0) {
             PassTimer t(c, 6);
             if (!compact_cnf(c)) break;
         }
         {
             PassTimer t(c, 0);
-            if (!ot_build(c)) break;
+            if (!(c.ot_valid ? ot_update(c) : ot_build(c))) break;
+            dfree(c, c.cmap);
+            c.cmap = nullptr;
+            c.ot_valid = true;
         }
         bool any_units = false;
         for (uint32_t i = 0; i < n; i++) {

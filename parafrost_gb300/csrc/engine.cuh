@@ -116,6 +116,16 @@ struct Ctx {
     uint32_t* ot_fill = nullptr; // nlist (fill cursors)
     uint32_t* ot_ids = nullptr;
     uint64_t ot_cap = 0;
+    // Between rounds the table is updated instead of rebuilt: a clause whose
+    // literals were replaced in place (substitution) or that was added (a
+    // resolvent) is flagged in cnew; every other change either deletes a clause
+    // or removes it from the one list it left (SUB strengthening, updateOL).
+    bool ot_valid = false;           // lists hold every live clause except those flagged in cnew
+    uint8_t* cnew = nullptr;         // hdr_cap
+    uint32_t* ot_ids2 = nullptr;     // second id array / offsets of the update
+    uint64_t ot_cap2 = 0;
+    uint32_t* ot_off2 = nullptr;     // nlist + 1
+    uint32_t* cmap = nullptr;        // old clause id -> new id of the last compaction (n + 1)
     // big-list sort scratch
     uint32_t* big_lists = nullptr;   // nlist (worst case)
     uint32_t* mid_desc = nullptr;    // descriptors (offset, size) pairs
@@ -235,9 +245,15 @@ bool ot_build(Ctx& c);          // histogram + CSR offsets + unsorted fill (clau
 // lists of every variable in vlist[0..nv)
 bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist = nullptr, uint32_t nv = 0);
 bool ot_filter(Ctx& c, const uint8_t* assigned);   // drop what unit propagation removed from the lists
+// Incremental table between rounds: ot_prune drops deleted and flagged clauses and
+// the lists of eliminated variables (run before a compaction, on the old ids);
+// ot_update then moves the kept entries into a fresh CSR (through cmap when the
+// store was compacted) and appends the flagged clauses.
+bool ot_prune(Ctx& c);
+bool ot_update(Ctx& c);
 // counting + compaction (gc.cu)
 void count_live(Ctx& c);        // totals into counters, per instance into dout.cnt (read after a sync)
-bool compact_cnf(Ctx& c);       // Solver::reallocCNF(true) (cnf.cu:129-144, recycle.cu:60)
+bool compact_cnf(Ctx& c);       // Solver::reallocCNF(true) (cnf.cu:129-144, recycle.cu:60); keeps cmap when ot_valid
 // device BCP (bcp.cu) of the instances flagged in di.bcp; conflicts land in dout.conflict
 bool bcp_prop(Ctx& c);
 // LCVE (lcve.cu) over the active instances; per-instance counts in dout.nelect

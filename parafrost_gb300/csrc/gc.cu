@@ -53,7 +53,7 @@ __global__ void live_flags_k(const ClsHdr* __restrict__ hdr, uint64_t ncls, uint
 // thread per clause: copy header and literals into the new store (clauses are short)
 __global__ void compact_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
                           const uint32_t* __restrict__ pos, const unsigned long long* __restrict__ loff,
-                          ClsHdr* nhdr, uint32_t* nlits) {
+                          ClsHdr* nhdr, uint32_t* nlits, const uint8_t* __restrict__ cnew, uint8_t* ncnew) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         const ClsHdr h = hdr[c];
         if (m_deleted(h.meta)) continue;
@@ -62,6 +62,7 @@ __global__ void compact_k(const ClsHdr* __restrict__ hdr, const uint32_t* __rest
         ClsHdr nh = h;
         nh.off = (uint32_t)o;
         nhdr[pos[c]] = nh;
+        ncnew[pos[c]] = cnew[c];
     }
 }
 
@@ -105,8 +106,9 @@ bool compact_cnf(Ctx& c) {
     }
     ClsHdr* nhdr = nullptr;
     uint32_t* nlits = nullptr;
-    if (!dalloc_t(c, &nhdr, clsCap + 1) || !dalloc_t(c, &nlits, phys_lits)) {
-        dfree(c, nhdr); dfree(c, nlits);
+    uint8_t* ncnew = nullptr;
+    if (!dalloc_t(c, &nhdr, clsCap + 1) || !dalloc_t(c, &nlits, phys_lits) || !dalloc_t(c, &ncnew, clsCap + 1)) {
+        dfree(c, nhdr); dfree(c, nlits); dfree(c, ncnew);
         c.simpstate = PFG_CNFALLOC_FAIL;
         return false;
     }
@@ -114,7 +116,7 @@ bool compact_cnf(Ctx& c) {
     uint32_t* pos = nullptr;
     unsigned long long* loff = nullptr;
     if (!dalloc_t(c, &pos, n + 1) || !dalloc_t(c, &loff, n + 1)) {
-        dfree(c, nhdr); dfree(c, nlits); dfree(c, pos); dfree(c, loff);
+        dfree(c, nhdr); dfree(c, nlits); dfree(c, ncnew); dfree(c, pos); dfree(c, loff);
         c.simpstate = PFG_CNFALLOC_FAIL;
         return false;
     }
@@ -122,11 +124,17 @@ bool compact_cnf(Ctx& c) {
     PFG_LAUNCH(K_COMPACT, live_flags_k, grid_for(n, 256), 256, 0, c.s, c.hdr, n, pos, loff);
     exclusive_scan_u32(pos, pos, n, 0u, nullptr, c.tmp, c.s);
     exclusive_scan_u64(loff, loff, n, 0ull, nullptr, c.tmp, c.s);
-    PFG_LAUNCH(K_COMPACT, compact_k, grid_for(n, 256), 256, 0, c.s, c.hdr, c.lits, n, pos, loff, nhdr, nlits);
-    dfree(c, pos); dfree(c, loff);
+    cudaMemsetAsync(ncnew, 0, clsCap + 1, c.s);
+    PFG_LAUNCH(K_COMPACT, compact_k, grid_for(n, 256), 256, 0, c.s, c.hdr, c.lits, n, pos, loff, nhdr, nlits, c.cnew,
+               ncnew);
+    // the occurrence-table update renumbers its kept entries through pos
+    dfree(c, c.cmap);
+    c.cmap = nullptr;
+    if (c.ot_valid) c.cmap = pos; else dfree(c, pos);
+    dfree(c, loff);
     c.prof.bytes[K_COMPACT] += 8 * (c.numLiterals + c.numClauses);
-    dfree(c, c.hdr); dfree(c, c.lits);
-    c.hdr = nhdr; c.lits = nlits;
+    dfree(c, c.hdr); dfree(c, c.lits); dfree(c, c.cnew);
+    c.hdr = nhdr; c.lits = nlits; c.cnew = ncnew;
     c.hdr_cap = clsCap + 1; c.lits_cap = phys_lits;
     c.ncls = c.numClauses;
     c.lits_used = c.numLiterals;

@@ -45,15 +45,75 @@ __global__ void fill_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restric
     }
 }
 
+// ---- incremental update between rounds ----
+// occurrences of the flagged (added or rewritten) live clauses
+__global__ void new_hist_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
+                           const uint8_t* __restrict__ cnew, uint32_t* hist) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        if (!cnew[c]) continue;
+        const ClsHdr h = hdr[c];
+        if (m_deleted(h.meta)) continue;
+        for (uint32_t k = 0; k < h.size; k++) atomicAdd(&hist[lits[h.off + k]], 1u);
+    }
+}
+
+__global__ void fill_new_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
+                           const uint8_t* __restrict__ cnew, uint32_t* fill, uint32_t* ids) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        if (!cnew[c]) continue;
+        const ClsHdr h = hdr[c];
+        if (m_deleted(h.meta)) continue;
+        for (uint32_t k = 0; k < h.size; k++) {
+            const uint32_t pos = atomicAdd(&fill[lits[h.off + k]], 1u);
+            ids[pos] = (uint32_t)c;
+        }
+    }
+}
+
+constexpr uint32_t MOVE_THREAD_MAX = 64;
+
+// kept entries of every list to its new offset, through the compaction map when
+// there is one; the append cursor of each list starts behind them
+__global__ void move_lists_k(uint64_t nlist, const uint32_t* __restrict__ off, const uint32_t* __restrict__ size,
+                             const uint32_t* __restrict__ ids, const uint32_t* __restrict__ off2, uint32_t* ids2,
+                             const uint32_t* __restrict__ map, uint32_t* fill, uint32_t* long_lists, uint32_t* nlong) {
+    for (uint64_t l = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlist; l += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t n = size[l];
+        const uint32_t o2 = off2[l];
+        fill[l] = o2 + n;
+        if (!n) continue;
+        if (n > MOVE_THREAD_MAX) { long_lists[atomicAdd(nlong, 1u)] = (uint32_t)l; continue; }
+        const uint32_t* src = ids + off[l];
+        for (uint32_t i = 0; i < n; i++) ids2[o2 + i] = map ? map[src[i]] : src[i];
+    }
+}
+
+__global__ void move_long_k(const uint32_t* __restrict__ off, const uint32_t* __restrict__ size,
+                            const uint32_t* __restrict__ ids, const uint32_t* __restrict__ off2, uint32_t* ids2,
+                            const uint32_t* __restrict__ map, const uint32_t* long_lists, const uint32_t* nlong) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t nlg = *nlong;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nlg; q += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t l = long_lists[q];
+        const uint32_t n = size[l];
+        const uint32_t* src = ids + off[l];
+        uint32_t* dst = ids2 + off2[l];
+        for (uint32_t i = lane; i < n; i += 32) dst[i] = map ? map[src[i]] : src[i];
+    }
+}
+
 // After unit propagation (bcp_apply_k) a list of an assigned variable is empty:
 // a true literal's clauses are satisfied and deleted, a false literal was
 // stripped from its clauses. Other lists only lose deleted clauses. Thread per
 // list, order kept; lists longer than FILTER_THREAD_MAX go to a warp each.
 constexpr uint32_t FILTER_THREAD_MAX = 64;
 
+// The same pass drops, between rounds, the clauses flagged in `cnew` (rewritten
+// or added; they are listed again by ot_update) and the lists of eliminated
+// variables (`assigned` is then the eliminated-byte array).
 __global__ void ot_filter_k(const ClsHdr* __restrict__ hdr, uint64_t nlist, const uint32_t* __restrict__ off,
                             uint32_t* size, uint32_t* hist, uint32_t* ids, const uint8_t* __restrict__ assigned,
-                            uint32_t* long_lists, uint32_t* nlong) {
+                            const uint8_t* __restrict__ cnew, uint32_t* long_lists, uint32_t* nlong) {
     for (uint64_t l = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlist; l += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t n = size[l];
         if (!n) continue;
@@ -63,7 +123,7 @@ __global__ void ot_filter_k(const ClsHdr* __restrict__ hdr, uint64_t nlist, cons
         uint32_t kept = 0;
         for (uint32_t i = 0; i < n; i++) {
             const uint32_t c = L[i];
-            if (!m_deleted(hdr[c].meta)) L[kept++] = c;
+            if (!m_deleted(hdr[c].meta) && !(cnew && cnew[c])) L[kept++] = c;
         }
         size[l] = kept;
         hist[l] = kept;
@@ -71,7 +131,8 @@ __global__ void ot_filter_k(const ClsHdr* __restrict__ hdr, uint64_t nlist, cons
 }
 
 __global__ void ot_filter_long_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ off, uint32_t* size,
-                                 uint32_t* hist, uint32_t* ids, const uint32_t* long_lists, const uint32_t* nlong) {
+                                 uint32_t* hist, uint32_t* ids, const uint8_t* __restrict__ cnew,
+                                 const uint32_t* long_lists, const uint32_t* nlong) {
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t nl = *nlong;
     for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nl; q += (gridDim.x * blockDim.x) >> 5) {
@@ -82,7 +143,7 @@ __global__ void ot_filter_long_k(const ClsHdr* __restrict__ hdr, const uint32_t*
         for (uint32_t b = 0; b < n; b += 32) {
             const uint32_t i = b + lane;
             const uint32_t c = i < n ? L[i] : 0u;
-            const bool keep = i < n && !m_deleted(hdr[c].meta);
+            const bool keep = i < n && !m_deleted(hdr[c].meta) && !(cnew && cnew[c]);
             const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
             __syncwarp();
             if (keep) L[kept + __popc(bal & ((1u << lane) - 1u))] = c;
@@ -336,16 +397,63 @@ bool ot_build(Ctx& c) {
     cudaMemcpyAsync(c.ot_fill, c.ot_off, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
     cudaMemcpyAsync(c.ot_size, c.hist, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
     PFG_LAUNCH(K_FILL, fill_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.ot_fill, c.ot_ids);
+    cudaMemsetAsync(c.cnew, 0, c.ncls, c.s);
     return cuda_ok(c, cudaGetLastError(), "ot_build");
 }
 
 bool ot_filter(Ctx& c, const uint8_t* assigned) {
     cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
     PFG_LAUNCH(K_FILL, ot_filter_k, grid_for(c.nlist, 256), 256, 0, c.s, c.hdr, c.nlist, c.ot_off, c.ot_size, c.hist,
-               c.ot_ids, assigned, c.big_lists, &c.dc->big_lists);
+               c.ot_ids, assigned, (const uint8_t*)nullptr, c.big_lists, &c.dc->big_lists);
     PFG_LAUNCH(K_FILL, ot_filter_long_k, grid_for((uint64_t)c.nlist * 32 / FILTER_THREAD_MAX, 256, 8), 256, 0, c.s,
-               c.hdr, c.ot_off, c.ot_size, c.hist, c.ot_ids, c.big_lists, &c.dc->big_lists);
+               c.hdr, c.ot_off, c.ot_size, c.hist, c.ot_ids, (const uint8_t*)nullptr, c.big_lists, &c.dc->big_lists);
     return cuda_ok(c, cudaGetLastError(), "ot_filter");
+}
+
+bool ot_prune(Ctx& c) {
+    cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
+    PFG_LAUNCH(K_FILL, ot_filter_k, grid_for(c.nlist, 256), 256, 0, c.s, c.hdr, c.nlist, c.ot_off, c.ot_size, c.hist,
+               c.ot_ids, c.elim, c.cnew, c.big_lists, &c.dc->big_lists);
+    PFG_LAUNCH(K_FILL, ot_filter_long_k, grid_for((uint64_t)c.nlist * 32 / FILTER_THREAD_MAX, 256, 8), 256, 0, c.s,
+               c.hdr, c.ot_off, c.ot_size, c.hist, c.ot_ids, c.cnew, c.big_lists, &c.dc->big_lists);
+    return cuda_ok(c, cudaGetLastError(), "ot_prune");
+}
+
+bool ot_update(Ctx& c) {
+    const uint64_t nl = c.nlist;
+    if (c.numLiterals > 0xFFFFFFF0ull) { c.simpstate = PFG_OTALLOC_FAIL; c.err = "occurrence table exceeds 2^32 entries"; return false; }
+    c.prof.bytes[K_HIST] += 4 * (c.numLiterals + c.numClauses);
+    c.prof.bytes[K_FILL] += 4 * (c.numLiterals + c.numClauses) + 4 * c.numLiterals;
+    // sizes: the kept entries plus the occurrences of the flagged clauses
+    cudaMemcpyAsync(c.hist, c.ot_size, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+    PFG_LAUNCH(K_HIST, new_hist_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.cnew, c.hist);
+    if (!ensure_tmp(c, scan_temp_bytes(nl))) return false;
+    exclusive_scan_u32(c.hist, c.ot_off2, nl, 0u, c.ot_off2 + nl, c.tmp, c.s);
+    uint32_t total = 0;
+    cudaMemcpyAsync(&total, c.ot_off2 + nl, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    if (!cuda_ok(c, cudaStreamSynchronize(c.s), "ot_update")) return false;
+    if (c.ot_cap2 < total) {   // the kept entries stay in ot_ids; only the target grows
+        dfree(c, c.ot_ids2);
+        c.ot_ids2 = nullptr;
+        const uint64_t cap = (uint64_t)total + total / 4 + 1024;
+        if (!dalloc_t(c, &c.ot_ids2, cap)) { c.simpstate = PFG_OTALLOC_FAIL; c.ot_cap2 = 0; return false; }
+        c.ot_cap2 = cap;
+    }
+    // kept entries move to the new offsets (renumbered after a compaction);
+    // the flagged clauses are appended behind them
+    cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
+    PFG_LAUNCH(K_FILL, move_lists_k, grid_for(nl, 256), 256, 0, c.s, nl, c.ot_off, c.ot_size, c.ot_ids, c.ot_off2,
+               c.ot_ids2, c.cmap, c.ot_fill, c.big_lists, &c.dc->big_lists);
+    PFG_LAUNCH(K_FILL, move_long_k, grid_for((uint64_t)nl * 32 / FILTER_THREAD_MAX, 256, 8), 256, 0, c.s, c.ot_off,
+               c.ot_size, c.ot_ids, c.ot_off2, c.ot_ids2, c.cmap, c.big_lists, &c.dc->big_lists);
+    PFG_LAUNCH(K_FILL, fill_new_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.cnew, c.ot_fill,
+               c.ot_ids2);
+    cudaMemcpyAsync(c.ot_size, c.hist, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+    cudaMemsetAsync(c.cnew, 0, c.ncls, c.s);
+    std::swap(c.ot_ids, c.ot_ids2);
+    std::swap(c.ot_cap, c.ot_cap2);
+    std::swap(c.ot_off, c.ot_off2);
+    return cuda_ok(c, cudaGetLastError(), "ot_update");
 }
 
 bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist, uint32_t nv) {
