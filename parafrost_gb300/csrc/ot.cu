@@ -70,86 +70,116 @@ __global__ void fill_new_k(const ClsHdr* __restrict__ hdr, const uint32_t* __res
     }
 }
 
-constexpr uint32_t MOVE_THREAD_MAX = 64;
-
-// kept entries of every list to its new offset, through the compaction map when
-// there is one; the append cursor of each list starts behind them
-__global__ void move_lists_k(uint64_t nlist, const uint32_t* __restrict__ off, const uint32_t* __restrict__ size,
-                             const uint32_t* __restrict__ ids, const uint32_t* __restrict__ off2, uint32_t* ids2,
-                             const uint32_t* __restrict__ map, uint32_t* fill, uint32_t* long_lists, uint32_t* nlong) {
-    for (uint64_t l = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlist; l += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t n = size[l];
-        const uint32_t o2 = off2[l];
-        fill[l] = o2 + n;
-        if (!n) continue;
-        if (n > MOVE_THREAD_MAX) { long_lists[atomicAdd(nlong, 1u)] = (uint32_t)l; continue; }
-        const uint32_t* src = ids + off[l];
-        for (uint32_t i = 0; i < n; i++) ids2[o2 + i] = map ? map[src[i]] : src[i];
+// Lists are processed 32 at a time by one warp: the lanes walk the entries of
+// the 32 lists back to back (the lists lie next to each other in the id array,
+// so the reads are nearly coalesced and a long list does not hold up one
+// thread), each lane finding its entry's list by a binary search over the
+// lists' starts.
+PFG_D uint32_t owner_lane(uint32_t pre, uint32_t e) {
+    uint32_t lo = 0, hi = 31;   // last lane whose list starts at or before e
+#pragma unroll
+    for (int it = 0; it < 5; it++) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        const uint32_t pm = __shfl_sync(0xFFFFFFFFu, pre, mid);
+        if (pm <= e) lo = mid; else hi = mid - 1;
     }
+    return lo;
 }
 
-__global__ void move_long_k(const uint32_t* __restrict__ off, const uint32_t* __restrict__ size,
-                            const uint32_t* __restrict__ ids, const uint32_t* __restrict__ off2, uint32_t* ids2,
-                            const uint32_t* __restrict__ map, const uint32_t* long_lists, const uint32_t* nlong) {
-    const unsigned lane = threadIdx.x & 31u;
-    const uint32_t nlg = *nlong;
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nlg; q += (gridDim.x * blockDim.x) >> 5) {
-        const uint32_t l = long_lists[q];
-        const uint32_t n = size[l];
-        const uint32_t* src = ids + off[l];
-        uint32_t* dst = ids2 + off2[l];
-        for (uint32_t i = lane; i < n; i += 32) dst[i] = map ? map[src[i]] : src[i];
-    }
+// flag[c] |= deleted: the list filters then read one byte per entry (an array
+// that stays in L2) instead of a clause header
+__global__ void mark_dead_k(const ClsHdr* __restrict__ hdr, uint64_t ncls, uint8_t* flag) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x)
+        if (m_deleted(hdr[c].meta)) flag[c] = 1;
 }
 
 // After unit propagation (bcp_apply_k) a list of an assigned variable is empty:
 // a true literal's clauses are satisfied and deleted, a false literal was
-// stripped from its clauses. Other lists only lose deleted clauses. Thread per
-// list, order kept; lists longer than FILTER_THREAD_MAX go to a warp each.
-constexpr uint32_t FILTER_THREAD_MAX = 64;
-
-// The same pass drops, between rounds, the clauses flagged in `cnew` (rewritten
-// or added; they are listed again by ot_update) and the lists of eliminated
-// variables (`assigned` is then the eliminated-byte array).
-__global__ void ot_filter_k(const ClsHdr* __restrict__ hdr, uint64_t nlist, const uint32_t* __restrict__ off,
-                            uint32_t* size, uint32_t* hist, uint32_t* ids, const uint8_t* __restrict__ assigned,
-                            const uint8_t* __restrict__ cnew, uint32_t* long_lists, uint32_t* nlong) {
-    for (uint64_t l = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlist; l += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t n = size[l];
-        if (!n) continue;
-        if (assigned[l >> 1]) { size[l] = 0; hist[l] = 0; continue; }
-        if (n > FILTER_THREAD_MAX) { long_lists[atomicAdd(nlong, 1u)] = (uint32_t)l; continue; }
-        uint32_t* L = ids + off[l];
-        uint32_t kept = 0;
-        for (uint32_t i = 0; i < n; i++) {
-            const uint32_t c = L[i];
-            if (!m_deleted(hdr[c].meta) && !(cnew && cnew[c])) L[kept++] = c;
+// stripped from its clauses. Other lists lose the clauses flagged in `drop`
+// (deleted ones; between rounds also the added and rewritten ones, listed again
+// by ot_update). `assigned` is then the eliminated-byte array: an eliminated
+// variable's lists are emptied. In place, order kept.
+__global__ void ot_filter_w_k(uint64_t nlist, const uint32_t* __restrict__ off, uint32_t* size, uint32_t* hist,
+                              uint32_t* ids, const uint8_t* __restrict__ assigned, const uint8_t* __restrict__ drop) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < nlist; w += nwarps) {
+        const uint64_t l = w * 32 + lane;
+        uint32_t n = 0, o = 0;
+        if (l < nlist) {
+            n = size[l];
+            if (n && assigned[l >> 1]) n = 0;
+            o = off[l];
         }
-        size[l] = kept;
-        hist[l] = kept;
+        uint32_t incl = n;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= (unsigned)d) incl += t;
+        }
+        const uint32_t pre = incl - n, T = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        uint32_t kept = 0;
+        for (uint32_t e0 = 0; e0 < T; e0 += 32) {
+            const uint32_t e = e0 + lane;
+            const uint32_t j = owner_lane(pre, e);
+            const uint32_t sj = __shfl_sync(0xFFFFFFFFu, pre, j);
+            const uint32_t oj = __shfl_sync(0xFFFFFFFFu, o, j);
+            const uint32_t kj = __shfl_sync(0xFFFFFFFFu, kept, j);
+            const bool valid = e < T;
+            const uint32_t c = valid ? ids[oj + (e - sj)] : 0u;
+            const bool keep = valid && !drop[c];
+            const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
+            // lanes of list j in this chunk start at lane max(sj - e0, 0)
+            const uint32_t first = sj > e0 ? sj - e0 : 0u;
+            const unsigned mine = ((1u << lane) - 1u) & ~((1u << first) - 1u);
+            if (keep) ids[oj + kj + __popc(bal & mine)] = c;
+            // this lane's own list: its entries in this chunk
+            const int64_t a = (int64_t)pre - (int64_t)e0, b = a + (int64_t)n;
+            const int lo = a < 0 ? 0 : (a > 32 ? 32 : (int)a);
+            const int hi = b < 0 ? 0 : (b > 32 ? 32 : (int)b);
+            if (hi > lo) {
+                const unsigned m = (hi - lo == 32) ? 0xFFFFFFFFu : (((1u << (hi - lo)) - 1u) << lo);
+                kept += __popc(bal & m);
+            }
+        }
+        if (l < nlist) { size[l] = kept; hist[l] = kept; }
     }
 }
 
-__global__ void ot_filter_long_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ off, uint32_t* size,
-                                 uint32_t* hist, uint32_t* ids, const uint8_t* __restrict__ cnew,
-                                 const uint32_t* long_lists, const uint32_t* nlong) {
+// kept entries of every list to its new offset, through the compaction map when
+// there is one; the append cursor of each list starts behind them
+__global__ void move_w_k(uint64_t nlist, const uint32_t* __restrict__ off, const uint32_t* __restrict__ size,
+                         const uint32_t* __restrict__ ids, const uint32_t* __restrict__ off2, uint32_t* ids2,
+                         const uint32_t* __restrict__ map, uint32_t* fill) {
     const unsigned lane = threadIdx.x & 31u;
-    const uint32_t nl = *nlong;
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nl; q += (gridDim.x * blockDim.x) >> 5) {
-        const uint32_t l = long_lists[q];
-        const uint32_t n = size[l];
-        uint32_t* L = ids + off[l];
-        uint32_t kept = 0;
-        for (uint32_t b = 0; b < n; b += 32) {
-            const uint32_t i = b + lane;
-            const uint32_t c = i < n ? L[i] : 0u;
-            const bool keep = i < n && !m_deleted(hdr[c].meta) && !(cnew && cnew[c]);
-            const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
-            __syncwarp();
-            if (keep) L[kept + __popc(bal & ((1u << lane) - 1u))] = c;
-            kept += __popc(bal);
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < nlist; w += nwarps) {
+        const uint64_t l = w * 32 + lane;
+        uint32_t n = 0, o = 0, o2 = 0;
+        if (l < nlist) {
+            n = size[l];
+            o = off[l];
+            o2 = off2[l];
+            fill[l] = o2 + n;
         }
-        if (lane == 0) { size[l] = kept; hist[l] = kept; }
+        uint32_t incl = n;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= (unsigned)d) incl += t;
+        }
+        const uint32_t pre = incl - n, T = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        for (uint32_t e0 = 0; e0 < T; e0 += 32) {
+            const uint32_t e = e0 + lane;
+            const uint32_t j = owner_lane(pre, e);
+            const uint32_t sj = __shfl_sync(0xFFFFFFFFu, pre, j);
+            const uint32_t oj = __shfl_sync(0xFFFFFFFFu, o, j);
+            const uint32_t o2j = __shfl_sync(0xFFFFFFFFu, o2, j);
+            if (e < T) {
+                const uint32_t c = ids[oj + (e - sj)];
+                ids2[o2j + (e - sj)] = map ? map[c] : c;
+            }
+        }
     }
 }
 
@@ -402,20 +432,16 @@ bool ot_build(Ctx& c) {
 }
 
 bool ot_filter(Ctx& c, const uint8_t* assigned) {
-    cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_FILL, ot_filter_k, grid_for(c.nlist, 256), 256, 0, c.s, c.hdr, c.nlist, c.ot_off, c.ot_size, c.hist,
-               c.ot_ids, assigned, (const uint8_t*)nullptr, c.big_lists, &c.dc->big_lists);
-    PFG_LAUNCH(K_FILL, ot_filter_long_k, grid_for((uint64_t)c.nlist * 32 / FILTER_THREAD_MAX, 256, 8), 256, 0, c.s,
-               c.hdr, c.ot_off, c.ot_size, c.hist, c.ot_ids, (const uint8_t*)nullptr, c.big_lists, &c.dc->big_lists);
+    PFG_LAUNCH(K_FILL, mark_dead_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.ncls, c.cnew);
+    PFG_LAUNCH(K_FILL, ot_filter_w_k, grid_for((c.nlist + 31) / 32 * 32, 256), 256, 0, c.s, c.nlist, c.ot_off,
+               c.ot_size, c.hist, c.ot_ids, assigned, c.cnew);
     return cuda_ok(c, cudaGetLastError(), "ot_filter");
 }
 
 bool ot_prune(Ctx& c) {
-    cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_FILL, ot_filter_k, grid_for(c.nlist, 256), 256, 0, c.s, c.hdr, c.nlist, c.ot_off, c.ot_size, c.hist,
-               c.ot_ids, c.elim, c.cnew, c.big_lists, &c.dc->big_lists);
-    PFG_LAUNCH(K_FILL, ot_filter_long_k, grid_for((uint64_t)c.nlist * 32 / FILTER_THREAD_MAX, 256, 8), 256, 0, c.s,
-               c.hdr, c.ot_off, c.ot_size, c.hist, c.ot_ids, c.cnew, c.big_lists, &c.dc->big_lists);
+    PFG_LAUNCH(K_FILL, mark_dead_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.ncls, c.cnew);
+    PFG_LAUNCH(K_FILL, ot_filter_w_k, grid_for((c.nlist + 31) / 32 * 32, 256), 256, 0, c.s, c.nlist, c.ot_off,
+               c.ot_size, c.hist, c.ot_ids, c.elim, c.cnew);
     return cuda_ok(c, cudaGetLastError(), "ot_prune");
 }
 
@@ -441,11 +467,8 @@ bool ot_update(Ctx& c) {
     }
     // kept entries move to the new offsets (renumbered after a compaction);
     // the flagged clauses are appended behind them
-    cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_FILL, move_lists_k, grid_for(nl, 256), 256, 0, c.s, nl, c.ot_off, c.ot_size, c.ot_ids, c.ot_off2,
-               c.ot_ids2, c.cmap, c.ot_fill, c.big_lists, &c.dc->big_lists);
-    PFG_LAUNCH(K_FILL, move_long_k, grid_for((uint64_t)nl * 32 / FILTER_THREAD_MAX, 256, 8), 256, 0, c.s, c.ot_off,
-               c.ot_size, c.ot_ids, c.ot_off2, c.ot_ids2, c.cmap, c.big_lists, &c.dc->big_lists);
+    PFG_LAUNCH(K_FILL, move_w_k, grid_for((nl + 31) / 32 * 32, 256), 256, 0, c.s, nl, c.ot_off, c.ot_size, c.ot_ids,
+               c.ot_off2, c.ot_ids2, c.cmap, c.ot_fill);
     PFG_LAUNCH(K_FILL, fill_new_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.cnew, c.ot_fill,
                c.ot_ids2);
     cudaMemcpyAsync(c.ot_size, c.hist, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
