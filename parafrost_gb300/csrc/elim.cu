@@ -23,6 +23,7 @@ struct EK {
     uint32_t* ot_ids;
     uint8_t* elim;
     const uint32_t* varcore;
+    const uint32_t* fcut;                // per instance: largest variable that varcore maps below MAXFUNVAR
     const uint32_t* vorg;
     const uint32_t* vinst;               // instance of a variable
     const uint8_t* vc_on;                // per instance: function-table gates on
@@ -1459,6 +1460,7 @@ EK make_ek(Ctx& c) {
     k.ot_ids = c.ot_ids;
     k.elim = c.elim;
     k.varcore = c.varcore;
+    k.fcut = c.fcut;
     k.vorg = c.vorg;
     k.vinst = c.vinst;
     k.vc_on = c.di.vc_on;

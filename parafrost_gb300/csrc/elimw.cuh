@@ -548,24 +548,54 @@ PFG_D bool ws_make_arity(WS& w, const Side& D, const Side& F, uint32_t& parity, 
     return true;
 }
 
-// find_xor_gate (xor.cuh:102-178) up to the substitution count
+// Original staged clauses other than ci over exactly ci's variables. An XOR
+// gate of arity a on ci needs 2^a - 1 of them (one per other parity), so with
+// fewer the search of makeArity fails on its first target or a later one.
+PFG_D uint32_t ws_xor_partners(const WS& w, uint32_t ci, unsigned lane) {
+    const uint32_t nc = w.np + w.nn, size = w.size[ci];
+    const uint32_t* a = w.lits + w.off[ci];
+    uint32_t cnt = 0;
+    for (uint32_t c0 = 0; c0 < nc; c0 += 32) {
+        const uint32_t c = c0 + lane;
+        bool same = false;
+        if (c < nc && c != ci && w.size[c] == size && m_orig(w.meta[c])) {
+            const uint32_t* b = w.lits + w.off[c];
+            same = true;
+            for (uint32_t q = 0; q < size; q++)
+                if ((a[q] >> 1) != (b[q] >> 1)) { same = false; break; }
+        }
+        cnt += __popc(__ballot_sync(FULL, same));
+    }
+    return cnt;
+}
+
+// find_xor_gate (xor.cuh:102-178) up to the substitution count. A clause of D
+// without the 2^a - 1 partners its gate needs is passed over without the
+// searches: they would fail before melting anything, and the freeze that
+// follows a failure (freezeArities) only changes state the first time, since
+// every later failure starts from a stage without molten clauses above size 2.
 PFG_D bool ws_find_xor_gate(const EK& k, WS& w, const Side& D, const Side& F, unsigned lane) {
     if (w.size[D.b + D.n - 1] == 2 || w.size[F.b + F.n - 1] == 2) return false;
     const int maxarity = (int)k.xor_max_arity;
     if ((int)w.size[D.b] - 1 > maxarity) return false;
     uint32_t* out = w.outs;
+    bool frozen = false;
     for (uint32_t i = 0; i < D.n; i++) {
         const uint32_t ci = D.b + i;
         if (!m_orig(w.meta[ci])) continue;
         const int size = (int)w.size[ci], arity = size - 1;
         if (size < 3 || arity > maxarity) continue;
+        if (ws_xor_partners(w, ci, lane) < (1u << arity) - 1u) {
+            if (!frozen) { ws_freeze_arities(w, lane); frozen = true; }
+            continue;
+        }
         __syncwarp();
         if (lane == 0) { const uint32_t* l = WL(w, ci); for (int q = 0; q < size; q++) out[q] = l[q]; }
         __syncwarp();
         uint32_t parity = 0;
         int itargets = 1 << arity;
         while (--itargets && ws_make_arity(w, D, F, parity, out, (uint32_t)size, lane)) {}
-        if (itargets) ws_freeze_arities(w, lane);
+        if (itargets) { ws_freeze_arities(w, lane); frozen = true; }
         else {
             ws_melt(w, ci, 1, lane);
             return true;
@@ -684,9 +714,22 @@ PFG_D void ws_elim_no_resolvents(const EK& k, WS& w, uint32_t x, const Side& P, 
 // only: with one neighbour further down the list (in a clause that is not
 // learnt) it returns false before it changes anything (function.cuh:283-290),
 // and the variable goes straight on to n-by-m resolution.
+// Every neighbour is frozen, and a frozen variable above the instance's cut
+// (fcut) has varcore >= MAXFUNVAR, so most variables are decided without
+// reading varcore.
 PFG_D bool ws_fun_possible(const EK& k, WS& w, uint32_t x, unsigned lane) {
     const uint32_t nc = w.np + w.nn;
+    const uint32_t cut = k.fcut[k.vinst[x]];
     bool far = false;
+    for (uint32_t i = lane; i < nc && !far; i += 32) {
+        if (m_learnt(w.meta[i])) continue;
+        const uint32_t* l = WL(w, i);
+        for (uint32_t t = 0; t < w.size[i]; t++) {
+            const uint32_t v = ABSV(l[t]);
+            if (v != x && v > cut) { far = true; break; }
+        }
+    }
+    if (__any_sync(FULL, far)) return false;
     for (uint32_t i = lane; i < nc && !far; i += 32) {
         if (m_learnt(w.meta[i])) continue;
         const uint32_t* l = WL(w, i);

@@ -601,7 +601,8 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
          dalloc_t(c, &c.rlit, V1 + 1) && dalloc_t(c, &c.units, c.units_total) &&
          dalloc_t(c, &c.trail, c.trail_total) && dalloc_t(c, &c.stack, c.stack_total) &&
          dalloc_t(c, &c.front_a, V1) && dalloc_t(c, &c.front_b, V1) && dalloc_t(c, &c.long_a, V1) &&
-         dalloc_t(c, &c.long_b, V1) && dalloc_t(c, &c.cnew, c.hdr_cap) && dalloc_t(c, &c.ot_off2, c.nlist + 1);
+         dalloc_t(c, &c.long_b, V1) && dalloc_t(c, &c.cnew, c.hdr_cap) && dalloc_t(c, &c.ot_off2, c.nlist + 1) &&
+         dalloc_t(c, &c.fcut, (size_t)n + 1);
     if (any_assumed) ok = ok && dalloc_t(c, &c.assumed, V1 + 8);
     if (!ok) {
         if (c.err.empty()) c.err = "device allocation failed";

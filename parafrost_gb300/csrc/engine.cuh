@@ -150,6 +150,7 @@ struct Ctx {
     uint32_t* eligible_b = nullptr;  // V+1
     uint32_t* rank = nullptr;    // V+1
     uint32_t* varcore = nullptr; // V+1
+    uint32_t* fcut = nullptr;    // n: largest frozen variable with varcore < 12, per instance
     uint32_t* elected = nullptr; // V+1
     uint32_t* work = nullptr;    // V+1 MIS worklist
     uint32_t* work_b = nullptr;  // V+1

@@ -184,6 +184,14 @@ __global__ void varcore_k(const uint8_t* frozen, uint32_t V, const uint32_t* pos
         if (frozen[v]) varcore[v] = pos[v] - fbase[vinst[v]];
 }
 
+// largest frozen variable of each instance inside the function-table core
+// (varcore < MAXFUNVAR): a neighbour above it cannot be mapped by find_fun_gate
+__global__ void fcut_k(const uint8_t* frozen, const uint32_t* varcore, uint32_t V, const uint32_t* vinst,
+                       uint32_t* fcut) {
+    for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x)
+        if (frozen[v] && varcore[v] < 12u) atomicMax(&fcut[vinst[v]], v);
+}
+
 // per-instance counts of a variable list (warp-aggregated over equal instances)
 __global__ void inst_count_k(const uint32_t* list, uint32_t n, const uint32_t* vinst, uint32_t* cnt) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -379,6 +387,10 @@ bool lcve(Ctx& c) {
         if (any_vc)
             PFG_LAUNCH(K_LCVE, mapfrozen_k, grid_for(V, 256), 256, 0, c.s, c.keys_b, V, c.di.voff, c.vinst,
                        c.dout.nfrozen, c.varcore);
+    }
+    if (any_vc) {
+        cudaMemsetAsync(c.fcut, 0, ninst * sizeof(uint32_t), c.s);
+        PFG_LAUNCH(K_LCVE, fcut_k, grid_for(V, 256), 256, 0, c.s, c.frozen, c.varcore, V, c.vinst, c.fcut);
     }
     pull_inst_out(c);
     if (!c.err.empty()) return false;
