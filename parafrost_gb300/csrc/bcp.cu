@@ -166,27 +166,54 @@ __global__ void bcp_propagate_k(BK k, const ClsHdr* hdr, const uint32_t* lits, c
     }
 }
 
-// strip false literals, delete satisfied clauses of the propagating, conflict-free instances
+// strip false literals, delete satisfied clauses of the propagating, conflict-free
+// instances, and count the live clauses and literals that remain (totals, and
+// per instance when there are several), as the count after prop() does
 __global__ void bcp_apply_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls, const uint8_t* st, const uint32_t* vinst,
-                            const uint8_t* bcp, const uint32_t* conflict) {
+                            const uint8_t* bcp, const uint32_t* conflict, int multi, unsigned long long* icnt,
+                            DevCounters* dc) {
+    unsigned long long nc = 0, nl = 0;
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         ClsHdr h = hdr[c];
-        if (m_deleted(h.meta) || !h.size) continue;
-        uint32_t* l = lits + h.off;
-        const uint32_t inst = vinst[ABSV(l[0])];
-        if (!bcp[inst] || conflict[inst]) continue;
-        uint32_t sig = 0, n = 0;
-        bool sat = false;
-        for (uint32_t q = 0; q < h.size; q++) {
-            const uint32_t lit = l[q];
-            const uint32_t ve = litval(st, lit);
-            if (ve == BCP_TRUE) { sat = true; break; }
-            if (ve == BCP_FALSE) continue;
-            l[n++] = lit;
-            sig |= MAPHASH(lit);
+        uint32_t inst = 0xFFFFFFFFu;
+        if (!m_deleted(h.meta)) {
+            uint32_t* l = lits + h.off;
+            inst = vinst[ABSV(l[0])];
+            if (h.size && bcp[inst] && !conflict[inst]) {
+                uint32_t sig = 0, n = 0;
+                bool sat = false;
+                for (uint32_t q = 0; q < h.size; q++) {
+                    const uint32_t lit = l[q];
+                    const uint32_t ve = litval(st, lit);
+                    if (ve == BCP_TRUE) { sat = true; break; }
+                    if (ve == BCP_FALSE) continue;
+                    l[n++] = lit;
+                    sig |= MAPHASH(lit);
+                }
+                if (sat) { hdr[c].meta = m_set_st(h.meta, ST_DELETED); inst = 0xFFFFFFFFu; }
+                else { hdr[c].sig = sig; hdr[c].size = n; h.size = n; }
+            }
         }
-        if (sat) hdr[c].meta = m_set_st(h.meta, ST_DELETED);
-        else { hdr[c].sig = sig; hdr[c].size = n; }
+        const bool live = inst != 0xFFFFFFFFu;
+        if (live) { nc++; nl += h.size; }
+        if (multi) {
+            const unsigned peers = __match_any_sync(__activemask(), inst);
+            const unsigned a = __reduce_add_sync(peers, live ? 1u : 0u);
+            const unsigned b = __reduce_add_sync(peers, live ? h.size : 0u);
+            if (live && (int)(threadIdx.x & 31u) == __ffs(peers) - 1) {
+                atomicAdd(&icnt[2 * inst], (unsigned long long)a);
+                atomicAdd(&icnt[2 * inst + 1], (unsigned long long)b);
+            }
+        }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        nc += __shfl_down_sync(0xFFFFFFFFu, nc, d);
+        nl += __shfl_down_sync(0xFFFFFFFFu, nl, d);
+    }
+    if ((threadIdx.x & 31u) == 0 && (nc || nl)) {
+        atomicAdd(&dc->live_cls, nc);
+        atomicAdd(&dc->live_lits, nl);
     }
 }
 
@@ -233,9 +260,17 @@ bool bcp_prop(Ctx& c) {
         if (levels > max_levels) { c.err = "device unit propagation did not converge"; c.simpstate = PFG_TIMEOUT; return false; }
     }
     if (c.hc->err) { c.err = "device error during unit propagation"; return false; }
-    if (!(single && c.hc->conflict))
-        PFG_LAUNCH(K_BCP, bcp_apply_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.bstate, c.vinst,
-                   c.di.bcp, c.dout.conflict);
+    // rewrite (conflict-free instances) and count: the live counts land in the
+    // counters and dout.cnt as count_live leaves them
+    const int multi = c.ninst > 1;
+    cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
+    if (multi) cudaMemsetAsync(c.dout.cnt, 0, 2 * c.ninst * sizeof(unsigned long long), c.s);
+    c.prof.bytes[K_COUNT] += 8 * c.ncls;
+    if (c.ncls)
+        PFG_LAUNCH(K_BCP, bcp_apply_k, grid_for(c.ncls, 256, 8), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.bstate, c.vinst,
+                   c.di.bcp, c.dout.conflict, multi, c.dout.cnt, c.dc);
+    if (!multi)
+        cudaMemcpyAsync(c.dout.cnt, &c.dc->live_cls, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c.s);
     return cuda_ok(c, cudaGetLastError(), "bcp");
 }
 

@@ -94,6 +94,7 @@ struct DevCounters {
     unsigned long long pf_words;             // proof line words reserved in the running pass
     unsigned long long pf_need;              // proof words BVE emission needs
     uint32_t pf_blocks;                      // proof blocks reserved in the running pass
+    uint32_t mis_done;                       // a MIS round found nothing undecided: later rounds return at once
 };
 
 constexpr uint32_t ERR_UNITS_OVERFLOW = 1u;

@@ -965,8 +965,7 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         if (any_units) {
             PassTimer t(c, 1);
             push_inst_in(c);
-            if (!bcp_prop(c)) break;
-            count_live(c);
+            if (!bcp_prop(c)) break;      // leaves the live counts as count_live does
             pull_inst_out(c);
             if (!c.err.empty()) break;
             c.numClauses = c.hc->live_cls;

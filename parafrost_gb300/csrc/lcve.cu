@@ -131,7 +131,8 @@ PFG_D void freeze_list(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* 
 // var-order round kernels: every variable checks its own state (coalesced)
 __global__ void mis_win3_k(uint32_t V, const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off,
                            const uint32_t* ot_size, const uint32_t* ot_ids, const uint32_t* rank,
-                           const uint8_t* mstate, uint8_t* winv, uint32_t* undecided) {
+                           const uint8_t* mstate, uint8_t* winv, uint32_t* undecided, const uint32_t* done) {
+    if (*done) return;   // an earlier round of this batch converged
     uint32_t cnt = 0;
     for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
         if (mstate[v] != MIS_UNDECIDED) continue;
@@ -146,7 +147,12 @@ __global__ void mis_win3_k(uint32_t V, const ClsHdr* hdr, const uint32_t* lits, 
 
 __global__ void mis_apply3_k(uint32_t V, const uint8_t* winv, uint32_t r, uint32_t* mround, const ClsHdr* hdr,
                              const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
-                             const uint32_t* ot_ids, uint8_t* frozen, uint8_t* mstate) {
+                             const uint32_t* ot_ids, uint8_t* frozen, uint8_t* mstate, const uint32_t* undecided,
+                             uint32_t* done) {
+    if (*undecided == 0) {   // nothing was undecided: no winner, and the rounds left have nothing to do
+        if (blockIdx.x == 0 && threadIdx.x == 0) *done = 1;
+        return;
+    }
     for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
         if (mstate[v] != MIS_UNDECIDED || !winv[v]) continue;
         mstate[v] = MIS_ELECTED;
@@ -314,13 +320,14 @@ bool lcve(Ctx& c) {
         uint32_t* mround = c.scores;     // scores are dead once the order is sorted
         uint32_t r = 0;
         bool done = nwork == 0;
+        cudaMemsetAsync(&c.dc->mis_done, 0, sizeof(uint32_t), c.s);
         for (int batch = 1; !done; batch = std::min(batch * 2, 16)) {
             for (int b = 0; b < batch; b++, r++) {
                 cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
                 PFG_LAUNCH(K_MIS_WIN, mis_win3_k, grid_for(V, 128), 128, 0, c.s, V, c.hdr, c.lits, c.ot_off,
-                           c.ot_size, c.ot_ids, c.rank, c.mstate, c.winv, &c.dc->nwin);
+                           c.ot_size, c.ot_ids, c.rank, c.mstate, c.winv, &c.dc->nwin, &c.dc->mis_done);
                 PFG_LAUNCH(K_MIS_APPLY, mis_apply3_k, grid_for(V, 128), 128, 0, c.s, V, c.winv, r, mround, c.hdr,
-                           c.lits, c.ot_off, c.ot_size, c.ot_ids, c.frozen, c.mstate);
+                           c.lits, c.ot_off, c.ot_size, c.ot_ids, c.frozen, c.mstate, &c.dc->nwin, &c.dc->mis_done);
             }
             sync_counters(c);
             if (!c.err.empty()) return false;
