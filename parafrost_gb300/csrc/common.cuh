@@ -95,9 +95,6 @@ struct DevCounters {
     unsigned long long pf_need;              // proof words BVE emission needs
     uint32_t pf_blocks;                      // proof blocks reserved in the running pass
     uint32_t mis_done;                       // a MIS round found nothing undecided: later rounds return at once
-    uint32_t mis_cnt[2];                     // undecided variables of the even / odd MIS round (persistent kernel)
-    uint32_t mis_rounds;                     // MIS rounds the persistent kernel ran
-    uint32_t bar_count, bar_gen;             // grid barrier of the persistent kernels
 };
 
 constexpr uint32_t ERR_UNITS_OVERFLOW = 1u;
@@ -106,37 +103,5 @@ constexpr uint32_t ERR_SLOT_MISMATCH = 4u;
 constexpr uint32_t ERR_BAD_LIT = 8u;
 constexpr uint32_t ERR_OT_OVERFLOW = 16u;
 constexpr uint32_t ERR_PROOF_OVERFLOW = 32u;
-constexpr uint32_t ERR_BARRIER_TIMEOUT = 64u;
-constexpr uint32_t ERR_NO_CONVERGENCE = 128u;
-
-// Grid barrier of a cooperative launch (every block resident). Thread 0 of the
-// last block to arrive resets the count and opens the next generation; the
-// others wait on the generation word with a bounded spin. On timeout the error
-// flag is set and false is returned: the caller leaves the kernel, and the
-// other blocks time out the same way, so the launch always ends.
-PFG_D bool grid_barrier(unsigned int* count, unsigned int* gen, unsigned int nblocks, uint32_t* err) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        const unsigned int g = *((volatile unsigned int*)gen);
-        __threadfence();
-        if (atomicAdd(count, 1u) == nblocks - 1) {
-            *((volatile unsigned int*)count) = 0u;
-            __threadfence();
-            atomicAdd(gen, 1u);
-        } else {
-            uint32_t it = 0;
-            while (*((volatile unsigned int*)gen) == g) {
-                if (++it > (1u << 24)) { atomicOr(err, ERR_BARRIER_TIMEOUT); ok = 0; break; }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
 
 }  // namespace pfg

@@ -162,101 +162,6 @@ __global__ void mis_apply3_k(uint32_t V, const uint8_t* winv, uint32_t r, uint32
     }
 }
 
-// ---- all MIS rounds in one cooperative launch ----
-// The win and apply phases of every round, separated by grid barriers, exactly
-// as the round kernels above run them one launch at a time. Between phases the
-// variable states are read through L2 (__ldcg): other blocks changed them.
-PFG_D bool blocked_cg(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
-                      const uint32_t* ot_ids, uint32_t lit, uint32_t cand, uint32_t r, const uint32_t* rank,
-                      const uint8_t* mstate) {
-    const uint32_t o = ot_off[lit], n = ot_size[lit];
-    ClsHdr next = n ? hdr[ot_ids[o]] : ClsHdr{0, 0, 0, 0};
-    for (uint32_t i = 0; i < n; i++) {
-        const ClsHdr h = next;
-        if (i + 1 < n) next = hdr[ot_ids[o + i + 1]];
-        if (m_deleted(h.meta)) continue;
-        const uint32_t* l = lits + h.off;
-        uint32_t u[MIS_HEAD];
-        uint8_t st[MIS_HEAD];
-#pragma unroll
-        for (uint32_t q = 0; q < MIS_HEAD; q++) u[q] = q < h.size ? ABSV(l[q]) : cand;
-#pragma unroll
-        for (uint32_t q = 0; q < MIS_HEAD; q++) st[q] = u[q] != cand ? __ldcg(mstate + u[q]) : MIS_NONE;
-#pragma unroll
-        for (uint32_t q = 0; q < MIS_HEAD; q++)
-            if (st[q] == MIS_UNDECIDED && rank[u[q]] < r) return true;
-        for (uint32_t k = MIS_HEAD; k < h.size; k++) {
-            const uint32_t v = ABSV(l[k]);
-            if (v != cand && __ldcg(mstate + v) == MIS_UNDECIDED && rank[v] < r) return true;
-        }
-    }
-    return false;
-}
-
-PFG_D void freeze_list_cg(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
-                          const uint32_t* ot_ids, uint32_t lit, uint32_t cand, uint8_t* frozen, uint8_t* mstate) {
-    const uint32_t o = ot_off[lit], n = ot_size[lit];
-    for (uint32_t i = 0; i < n; i++) {
-        const ClsHdr h = hdr[ot_ids[o + i]];
-        if (m_deleted(h.meta)) continue;
-        const uint32_t* l = lits + h.off;
-        for (uint32_t k = 0; k < h.size; k++) {
-            const uint32_t v = ABSV(l[k]);
-            if (v == cand) continue;
-            frozen[v] = 1;
-            if (__ldcg(mstate + v) == MIS_UNDECIDED) mstate[v] = MIS_FROZEN;
-        }
-    }
-}
-
-struct MisArgs {
-    uint32_t V, max_rounds;
-    const ClsHdr* hdr;
-    const uint32_t* lits;
-    const uint32_t* ot_off;
-    const uint32_t* ot_size;
-    const uint32_t* ot_ids;
-    const uint32_t* rank;
-    uint8_t* mstate;
-    uint8_t* winv;
-    uint8_t* frozen;
-    uint32_t* mround;
-    DevCounters* dc;
-};
-
-__global__ void __launch_bounds__(256) mis_rounds_k(MisArgs a) {
-    DevCounters* dc = a.dc;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t r = 0; r < a.max_rounds; r++) {
-        uint32_t cnt = 0;
-        for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= a.V; v += stride) {
-            if (__ldcg(a.mstate + v) != MIS_UNDECIDED) continue;
-            cnt++;
-            const uint32_t rk = a.rank[v];
-            a.winv[v] = !(blocked_cg(a.hdr, a.lits, a.ot_off, a.ot_size, a.ot_ids, 2 * v, v, rk, a.rank, a.mstate) ||
-                          blocked_cg(a.hdr, a.lits, a.ot_off, a.ot_size, a.ot_ids, 2 * v + 1, v, rk, a.rank, a.mstate));
-        }
-        for (int d = 16; d > 0; d >>= 1) cnt += __shfl_down_sync(0xFFFFFFFFu, cnt, d);
-        if ((threadIdx.x & 31u) == 0 && cnt) atomicAdd(&dc->mis_cnt[r & 1u], cnt);
-        if (!grid_barrier(&dc->bar_count, &dc->bar_gen, gridDim.x, &dc->err)) return;
-        if (__ldcg(&dc->mis_cnt[r & 1u]) == 0) {          // converged: round r found nothing undecided
-            if (blockIdx.x == 0 && threadIdx.x == 0) dc->mis_rounds = r + 1;
-            return;
-        }
-        // every block has read round r-1's counter: it becomes round r+1's
-        if (blockIdx.x == 0 && threadIdx.x == 0) dc->mis_cnt[(r + 1) & 1u] = 0;
-        for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= a.V; v += stride) {
-            if (__ldcg(a.mstate + v) != MIS_UNDECIDED || !__ldcg(a.winv + v)) continue;
-            a.mstate[v] = MIS_ELECTED;
-            a.mround[v] = r;
-            freeze_list_cg(a.hdr, a.lits, a.ot_off, a.ot_size, a.ot_ids, 2 * v, v, a.frozen, a.mstate);
-            freeze_list_cg(a.hdr, a.lits, a.ot_off, a.ot_size, a.ot_ids, 2 * v + 1, v, a.frozen, a.mstate);
-        }
-        if (!grid_barrier(&dc->bar_count, &dc->bar_gen, gridDim.x, &dc->err)) return;
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&dc->err, ERR_NO_CONVERGENCE);
-}
-
 __global__ void elected_flags_k(const uint32_t* work, uint32_t nwork, const uint8_t* mstate, uint8_t* flag) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwork; i += gridDim.x * blockDim.x)
         flag[i] = mstate[work[i]] == MIS_ELECTED;
@@ -415,37 +320,6 @@ bool lcve(Ctx& c) {
         uint32_t* mround = c.scores;     // scores are dead once the order is sorted
         uint32_t r = 0;
         bool done = nwork == 0;
-        // all rounds in one cooperative launch when the device runs them; the
-        // round-by-round launches below are the same rounds one kernel at a time
-        if (!done) {
-            int dev = 0, coop = 0, sms = 0, per_sm = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mis_rounds_k, 256, 0) == cudaSuccess &&
-                per_sm > 0) {
-                const uint64_t want = ((uint64_t)V + 255) / 256;
-                const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)per_sm * sms, want));
-                MisArgs a{V, nwork + 3, c.hdr, c.lits, c.ot_off, c.ot_size, c.ot_ids, c.rank, c.mstate, c.winv,
-                          c.frozen, mround, c.dc};
-                cudaMemsetAsync(&c.dc->mis_cnt[0], 0, 5 * sizeof(uint32_t), c.s);   // mis_cnt, mis_rounds, bar_count
-                void* kargs[] = {&a};
-                Profiler* pp = g_prof;
-                if (pp && pp->on) pp->begin(K_MIS_WIN, c.s);
-                const cudaError_t e = cudaLaunchCooperativeKernel((const void*)mis_rounds_k, dim3(grid), dim3(256),
-                                                                  kargs, 0, c.s);
-                g_launches++;
-                if (pp) { pp->launches[K_MIS_WIN]++; if (pp->on) pp->end(K_MIS_WIN, c.s); }
-                if (e == cudaSuccess) {
-                    sync_counters(c);
-                    if (!c.err.empty()) return false;
-                    r = c.hc->mis_rounds;
-                    done = true;
-                } else {
-                    cudaGetLastError();
-                }
-            }
-        }
         cudaMemsetAsync(&c.dc->mis_done, 0, sizeof(uint32_t), c.s);
         for (int batch = 1; !done; batch = std::min(batch * 2, 16)) {
             for (int b = 0; b < batch; b++, r++) {
