@@ -1122,6 +1122,31 @@ PFG_D void ws_update_ol(const EK& k, WS& w, const Side& L, unsigned lane) {
     __syncwarp();
 }
 
+// Screen of SUB on the stage, into w.outs: clause i can only be subsumed by an
+// earlier clause of its own list or strengthened by a clause of the other list
+// whose signature fits. Strengthening removes x's own literals only, so a
+// partner's signature without their bits (M) is contained in what it will be
+// when clause i's turn comes, and clause i's own signature does not change
+// before its turn; a clause with no fitting partner is left alone by both
+// searches, which are skipped for it.
+PFG_D void ws_sub_screen(WS& w, const Side& P, const Side& N, unsigned lane) {
+    const uint32_t M = MAPHASH(P.lit) | MAPHASH(N.lit);
+    const uint32_t nc = w.np + w.nn;
+    for (uint32_t i = lane; i < nc; i += 32) {
+        const bool inP = i < w.np;
+        const uint32_t sb = inP ? P.b : N.b;
+        const uint32_t ob = inP ? N.b : P.b, oe = ob + (inP ? N.n : P.n);
+        const uint32_t cs = w.sig[i];
+        bool maybe = false;
+        for (uint32_t j = sb; j < i && !maybe; j++)
+            maybe = w.size[j] > 1 && SUBSIG(w.sig[j] & ~M, cs);
+        for (uint32_t j = ob; j < oe && !maybe; j++)
+            maybe = w.size[j] > 1 && selfsub_sig(w.sig[j] & ~M, cs);
+        w.outs[i] = maybe ? 1u : 0u;
+    }
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* elected, uint32_t nelected,
                                                         uint32_t* big, uint32_t* nbig) {
     __shared__ WS stage[WS_WARPS];
@@ -1138,18 +1163,19 @@ __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* el
             continue;
         }
         const Side P{0, w.np, p}, N{w.np, w.nn, n};
+        ws_sub_screen(w, P, N, lane);
         uint32_t nPos = 0, nNeg = 0;
         for (uint32_t i = 0; i < P.n; i++) {
             const uint32_t c = P.b + i;
             if (w.size[c] > SUB_MAX_CL_SIZE) break;
-            if (m_deleted(w.meta[c])) continue;
+            if (m_deleted(w.meta[c]) || !w.outs[c]) continue;
             ws_selfsubsume(w, p, n, N, c, nPos, lane);
             ws_subsume(w, P, i, c, lane);
         }
         for (uint32_t i = 0; i < N.n; i++) {
             const uint32_t c = N.b + i;
             if (w.size[c] > SUB_MAX_CL_SIZE) break;
-            if (m_deleted(w.meta[c])) continue;
+            if (m_deleted(w.meta[c]) || !w.outs[c]) continue;
             ws_selfsubsume(w, n, p, P, c, nNeg, lane);
             ws_subsume(w, N, i, c, lane);
         }
