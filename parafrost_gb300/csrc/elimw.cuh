@@ -75,13 +75,15 @@ PFG_D bool ws_stage(const EK& k, WS& w, uint32_t p, uint32_t n, unsigned lane) {
     }
     if (base > WS_MAXL) return false;
     if (lane == 0) { w.np = np; w.nn = nn; w.nlit = base; }
-    // a lane per clause: its literals are contiguous (mostly one sector), and
-    // the loads of a clause are independent of each other
-    for (uint32_t i = lane; i < nc; i += 32) {
-        const uint32_t* src = k.lits + w.goff[i];
-        uint32_t* dst = w.lits + w.off[i];
-        const uint32_t sz = w.size[i];
-        for (uint32_t t = 0; t < sz; t++) dst[t] = src[t];
+    __syncwarp();
+    for (uint32_t g = lane; g < base; g += 32) {
+        // clause of literal word g: last staged clause whose offset is <= g
+        uint32_t lo = 0, hi = nc;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (w.off[mid] <= g) lo = mid; else hi = mid;
+        }
+        w.lits[g] = k.lits[w.goff[lo] + (g - w.off[lo])];
     }
     __syncwarp();
     return true;
