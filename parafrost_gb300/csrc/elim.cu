@@ -1553,7 +1553,7 @@ bool sub_pass(Ctx& c) {
     return !c.o.proof_en || proof_collect(c);
 }
 
-bool ve_pass(Ctx& c, bool with_sub) {
+bool ve_pass(Ctx& c) {
     const uint32_t E = c.nve;
     if (!E) return true;
     if (c.o.proof_en && !proof_prepare(c, 2 * (c.lits_used + c.ncls))) return false;
@@ -1562,16 +1562,8 @@ bool ve_pass(Ctx& c, bool with_sub) {
     for (uint32_t i = 0; i < c.ninst; i++) any_vc |= c.ih[i].mode == 1 && c.ih[i].varcore_on;
     cudaMemsetAsync(&c.dc->nwork, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->nbig_ve1, 0, 2 * sizeof(uint32_t), c.s);
-    if (with_sub) {
-        // SUB and phase 1 per variable on one stage; the variables too large for
-        // it get SUB, then phase 1, from the thread kernels
-        PFG_LAUNCH(K_VE1, subve1w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.veset,
-                   E, c.type, c.ucnt, c.rpos, c.rref, c.work, &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
-        PFG_LAUNCH(K_BIGVAR, sub_k, grid_for(E, 64, 8), 64, 0, c.s, k, c.veset, E, c.work_b, &c.dc->nbig_ve1);
-    } else {
-        PFG_LAUNCH(K_VE1, ve1w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.veset, E,
-                   c.type, c.ucnt, c.rpos, c.rref, c.work, &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
-    }
+    PFG_LAUNCH(K_VE1, ve1w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.veset, E,
+               c.type, c.ucnt, c.rpos, c.rref, c.work, &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
     PFG_LAUNCH(K_BIGVAR, ve1a_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.veset, E, c.type, c.ucnt, c.rpos, c.rref, c.work,
                &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
     if (any_vc)   // one warp per deferred variable; the grid walks the device-side count

@@ -1147,8 +1147,6 @@ PFG_D void ws_sub_screen(WS& w, const Side& P, const Side& N, unsigned lane) {
     __syncwarp();
 }
 
-PFG_D void ws_sub_var(const EK& k, WS& w, uint32_t x, unsigned lane);
-
 __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* elected, uint32_t nelected,
                                                         uint32_t* big, uint32_t* nbig) {
     __shared__ WS stage[WS_WARPS];
@@ -1164,50 +1162,6 @@ __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* el
             if (lane == 0) big[atomicAdd(nbig, 1u)] = e;
             continue;
         }
-        ws_sub_var(k, w, x, lane);
-    }
-}
-
-// SUB and BVE phase 1 of one variable after each other on one stage: the
-// variable's clauses are staged for SUB, written back, and staged again for
-// phase 1 while they are still in L1/L2. Elected variables share no clause,
-// so phase 1 of x only sees SUB of x, as after a separate SUB launch.
-// Variables that do not fit the stage go to the thread kernels of both.
-__global__ void __launch_bounds__(WS_WARPS * 32) subve1w_k(EK k, const uint32_t* elected, uint32_t nelected,
-                                                           uint32_t* type, uint32_t* ucnt, unsigned long long* rpos,
-                                                           unsigned long long* rref, uint32_t* dlist,
-                                                           uint32_t* dcount, uint32_t* big, uint32_t* nbig) {
-    __shared__ WS stage[WS_WARPS];
-    const unsigned lane = threadIdx.x & 31u;
-    WS& w = stage[threadIdx.x >> 5];
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected;
-         q += (gridDim.x * blockDim.x) >> 5) {
-        const uint32_t tid = q;
-        const uint32_t x = elected[tid];
-        const uint32_t p = 2 * x, n = p | 1;
-        if (!ws_stage(k, w, p, n, lane)) {
-            if (lane == 0) big[atomicAdd(nbig, 1u)] = tid;
-            continue;
-        }
-        if (w.np <= k.sub_max_occurs && w.nn <= k.sub_max_occurs) {
-            ws_sub_var(k, w, x, lane);
-            // the lists only shrank: they fit again
-            if (!ws_stage(k, w, p, n, lane)) {
-                if (lane == 0) atomicOr(&k.dc->err, ERR_SLOT_MISMATCH);
-                continue;
-            }
-        }
-        ws_ve1(k, w, tid, x, type, ucnt, rpos, rref, dlist, dcount, lane);
-        __syncwarp();
-    }
-}
-
-// SUB of one staged variable (subsume.cuh:402-484): strengthening and forward
-// subsumption over the positive then the negative list, units, proof lines,
-// then the lists and changed headers written back.
-PFG_D void ws_sub_var(const EK& k, WS& w, uint32_t x, unsigned lane) {
-    const uint32_t p = 2 * x, n = p | 1;
-    {
         const Side P{0, w.np, p}, N{w.np, w.nn, n};
         ws_sub_screen(w, P, N, lane);
         uint32_t nPos = 0, nNeg = 0;

@@ -1060,22 +1060,18 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
                 c.ih[i].processed_cls += c.ih[i].numClauses;
                 c.ih[i].processed_lits += c.ih[i].numLiterals;
             }
-        // SUB runs inside BVE phase 1 (one stage per variable) unless proof lines
-        // are written (they keep the pass order SUB, then BVE) or one of them is off
-        const bool sub_on = c.o.sub_en || c.o.ve_plus_en;
-        const bool fused = sub_on && c.o.ve_en && !c.o.proof_en;
-        c.prof.bytes[fused ? K_VE1 : K_SUB] += 4 * (LE + CE);
+        c.prof.bytes[K_SUB] += 4 * (LE + CE);
         c.prof.bytes[K_VE1] += 4 * (LE + CE);
         const uint64_t ncls0 = c.ncls, lits0 = c.lits_used;
         c.stats.clauses_processed += Cin;
         c.stats.literals_processed += Lin;
-        if (sub_on && !fused) {
+        if (c.o.sub_en || c.o.ve_plus_en) {
             PassTimer t(c, 3);
             if (!sub_pass(c)) break;
         }
         if (c.o.ve_en) {
             PassTimer t(c, 4);
-            if (!ve_pass(c, fused)) break;
+            if (!ve_pass(c)) break;
         }
         if (c.o.bce_en) {   // SUB(), VE(), BCE() (simplify.cu:173)
             PassTimer t(c, 7);

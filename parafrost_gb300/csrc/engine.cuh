@@ -261,7 +261,7 @@ bool bcp_prop(Ctx& c);
 bool lcve(Ctx& c);
 // SUB, BVE, ERE (elim.cu) over c.veset / c.ereset
 bool sub_pass(Ctx& c);
-bool ve_pass(Ctx& c, bool with_sub);   // with_sub: SUB runs inside, per variable before phase 1
+bool ve_pass(Ctx& c);
 bool ere_pass(Ctx& c);
 bool bce_pass(Ctx& c);   // blocked clause elimination over the surviving elected variables
 // DRAT proof of a pass (engine.cu): room for `words` line words before the pass,
