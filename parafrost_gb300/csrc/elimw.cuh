@@ -296,6 +296,19 @@ PFG_D uint32_t ws_lits_before(const WS& w, const Side& s) {
     return t;
 }
 
+// One resolvent count with the guards its loop has (resolve.cuh:28-198,
+// elimination.cuh:409-484): true = the variable can be eliminated this way.
+// The literal bound (velitsbound) applies to the bounded and substitution
+// counts; the proof guard to all three.
+PFG_D bool ws_count(const EK& k, WS& w, int kind, uint32_t x, const Side& me, const Side& ot, uint32_t nClsBefore,
+                    uint32_t& nE, uint32_t& nC, uint32_t& nL, unsigned lane) {
+    if (!ws_count_pairs(w, kind, x, me, ot, nClsBefore, k.ve_clause_max, nE, nC, nL, lane)) return false;
+    if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return false;
+    if (kind != CNT_RES_UNBOUNDED && k.ve_lbound_en && nL > ws_lits_before(w, me) + ws_lits_before(w, ot))
+        return false;
+    return !(k.proof && ws_proof_guard(k, w, kind, x, me, ot, nE, lane));
+}
+
 // countSubstituted / countCoreSubstituted: true = cannot substitute
 PFG_D bool ws_count_subst(const EK& k, WS& w, int kind, uint32_t x, uint32_t nClsBefore, const Side& me,
                           const Side& ot, uint32_t& nE, uint32_t& nC, uint32_t& nL, unsigned lane) {
@@ -764,37 +777,69 @@ PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
         if (lane == 0) k.elim[x] |= MELTING_MASK;
         return;
     }
-    if ((pOrgs == 1 || nOrgs == 1) && ws_count_res_unbounded(k, w, x, P, N, nE, nC, nL, lane)) {
-        if (nC) { ws_flush(k, w, lane); ws_store_info(tid, RES_MASK, nE, nC, nL, type, ucnt, rpos, rref, lane); }
-        else ws_elim_no_resolvents(k, w, x, P, N, pOrgs, nOrgs, lane);
-        return;
-    }
     const uint32_t nClsBefore = pOrgs + nOrgs;
-    elimType = 0; nE = 0; nC = 0; nL = 0;
-    // AND/OR gates for both definitions, then ITE and XOR gates for both
-    // (bounded.cuh:336-356); a second definition is tried only while no
-    // substitution was counted. The substitution of a found gate is counted
-    // here, at one call site for all detectors.
+    // Every resolvent count goes through the one call of ws_count below (the
+    // three loops inlined at three places made the kernel fetch-bound):
+    //   g = -1: single-occurrence resolution (resolve.cuh:28-109), tried first
+    //           when one side has one original clause;
+    //   g = 0..5: AND/OR gates for both definitions, then ITE and XOR gates for
+    //           both (bounded.cuh:336-356), each found gate's substitution
+    //           counted; a second definition is tried only while no
+    //           substitution was counted;
+    //   g = 6: the function-table gate is deferred to ve1b_k, else n-by-m
+    //           resolution (resolve.cuh:111-198) when nothing was counted.
 #pragma unroll 1
-    for (int g = 0; g < 6 && !elimType; g++) {
+    for (int g = (pOrgs == 1 || nOrgs == 1) ? -1 : 0; g <= 6; g++) {
+        int kind;
+        uint32_t ncb = nClsBefore;
         const int o = g & 1;
-        if (g < 2 ? nClsBefore <= 2 : nClsBefore <= 3) continue;
-        if (o && nC) continue;
         // AND/OR: (N, P) then (P, N); ITE and XOR: (P, N) then (N, P)
-        const bool pfirst = g < 2 ? o != 0 : o == 0;
+        const bool pfirst = g < 0 || g >= 6 ? true : (g < 2 ? o != 0 : o == 0);
         const Side& D = pfirst ? P : N;
         const Side& F = pfirst ? N : P;
         GateUndo undo{NOREF, NOREF, NOREF, NOREF};
-        bool found;
-        if (g < 2) found = (pfirst ? pOrgs : nOrgs) < SH_MAX_BVE_OUT1 && ws_find_ao_gate(k, w, D, F, undo, lane);
-        else if (g < 4) found = ws_find_ite_gate(k, w, D, F, undo, lane);
-        else found = ws_find_xor_gate(k, w, D, F, lane);
-        if (!found) continue;
-        nE = 0; nC = 0; nL = 0;
-        if (!ws_count_subst(k, w, CNT_SUBS, x, nClsBefore, D, F, nE, nC, nL, lane)) {
-            elimType = AOIX_MASK;
+        if (g < 0) {
+            kind = CNT_RES_UNBOUNDED;
+            ncb = 0;
+        } else if (g < 6) {
+            if (g < 2 ? nClsBefore <= 2 : nClsBefore <= 3) continue;
+            if (o && nC) continue;
+            bool found;
+            if (g < 2) found = (pfirst ? pOrgs : nOrgs) < SH_MAX_BVE_OUT1 && ws_find_ao_gate(k, w, D, F, undo, lane);
+            else if (g < 4) found = ws_find_ite_gate(k, w, D, F, undo, lane);
+            else found = ws_find_xor_gate(k, w, D, F, lane);
+            if (!found) continue;
+            nE = 0; nC = 0; nL = 0;
+            kind = CNT_SUBS;
+        } else {
+            if (vc_on(k, x) && nClsBefore > 2 && ws_fun_possible(k, w, x, lane)) {
+                ws_flush(k, w, lane);
+                if (lane == 0) {
+                    dlist[atomicAdd(dcount, 1u)] = tid;
+                    ucnt[tid] = nC;
+                    rpos[tid] = (unsigned long long)pOrgs | ((unsigned long long)nOrgs << 32);
+                }
+                return;
+            }
+            if (nC) break;
+            nE = 0; nC = 0; nL = 0;
+            kind = CNT_RES_BOUNDED;
+        }
+        const bool ok = ws_count(k, w, kind, x, D, F, ncb, nE, nC, nL, lane);
+        if (g < 0) {
+            if (ok) {
+                if (nC) { ws_flush(k, w, lane); ws_store_info(tid, RES_MASK, nE, nC, nL, type, ucnt, rpos, rref, lane); }
+                else ws_elim_no_resolvents(k, w, x, P, N, pOrgs, nOrgs, lane);
+                return;
+            }
+            nE = 0; nC = 0; nL = 0;
+            continue;
+        }
+        if (g >= 6) {
+            if (ok) elimType = RES_MASK;
             break;
         }
+        if (ok) { elimType = AOIX_MASK; break; }
         // too many resolvents: undo what the detector melted
         if (g < 2) {
             ws_melt(w, undo.a, 0, lane);
@@ -808,16 +853,6 @@ PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
             ws_freeze_arities(w, lane);
         }
     }
-    if (vc_on(k, x) && !elimType && nClsBefore > 2 && ws_fun_possible(k, w, x, lane)) {
-        ws_flush(k, w, lane);
-        if (lane == 0) {
-            dlist[atomicAdd(dcount, 1u)] = tid;
-            ucnt[tid] = nC;
-            rpos[tid] = (unsigned long long)pOrgs | ((unsigned long long)nOrgs << 32);
-        }
-        return;
-    }
-    if (!elimType && !nC && ws_count_res_bounded(k, w, x, nClsBefore, P, N, nE, nC, nL, lane)) elimType = RES_MASK;
     if (!nC) ws_elim_no_resolvents(k, w, x, P, N, pOrgs, nOrgs, lane);
     else {
         ws_flush(k, w, lane);
