@@ -384,8 +384,8 @@ PFG_D void ws_save_side(const EK& k, WS& w, const Side& s, uint32_t witlit, uint
 
 PFG_D void ws_save_resolved_orgs(const EK& k, WS& w, const Side& P, const Side& N, uint32_t pOrgs, uint32_t nOrgs,
                                  unsigned lane) {
-    if (pOrgs > nOrgs) ws_save_side(k, w, N, N.lit, P.lit, lane);
-    else ws_save_side(k, w, P, P.lit, N.lit, lane);
+    const Side& S = pOrgs > nOrgs ? N : P;     // one call site of ws_save_side
+    ws_save_side(k, w, S, S.lit, S.lit ^ 1u, lane);
 }
 
 // delete every staged clause, empty both lists (toblivion, elimination.cuh:540-549)
@@ -714,14 +714,6 @@ PFG_D void ws_store_info(uint32_t tid, uint32_t elimType, uint32_t nE, uint32_t 
     if (lane == 0) store_elim_info(tid, elimType, nE, nC, nL, type, ucnt, rpos, rref);
 }
 
-PFG_D void ws_elim_no_resolvents(const EK& k, WS& w, uint32_t x, const Side& P, const Side& N, uint32_t pOrgs,
-                                 uint32_t nOrgs, unsigned lane) {
-    ws_save_resolved_orgs(k, w, P, N, pOrgs, nOrgs, lane);
-    ws_toblivion(k, w, P, N, lane);
-    ws_flush(k, w, lane);
-    if (lane == 0) k.elim[x] |= MELTING_MASK;
-}
-
 // find_fun_gate maps the neighbours of x through varcore (their place in the
 // instance's frozen list) and builds truth tables over the first MAXFUNVAR
 // only: with one neighbour further down the list (in a clause that is not
@@ -767,93 +759,96 @@ PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
         for (uint32_t i = 0; i < N.n; i++) nOrgs += m_orig(w.meta[N.b + i]);
     }
     if (lane == 0) { type[tid] = 0; ucnt[tid] = 0; rpos[tid] = 0; rref[tid] = 0; }
-    uint32_t elimType = 0, nE = 0, nC = 0, nL = 0;
+    uint32_t elimType = 0, nE = 0, nC = 0, nL = 0, def = 0;
     // a pure literal goes straight to the common end: no resolvents
     if (pOrgs && nOrgs) {
-        const uint32_t def = ws_find_equ_gate(w, P, N, lane);
-        if (def) {
-            ws_save_resolved_orgs(k, w, P, N, pOrgs, nOrgs, lane);
-            ws_substitute_single(k, w, P, N, def, lane);
-            ws_flush(k, w, lane);
-            if (lane == 0) k.elim[x] |= MELTING_MASK;
-            return;
-        }
-        const uint32_t nClsBefore = pOrgs + nOrgs;
-        // Every resolvent count goes through the one call of ws_count below (the
-        // three loops inlined at three places made the kernel fetch-bound):
-        //   g = -1: single-occurrence resolution (resolve.cuh:28-109), tried first
-        //           when one side has one original clause;
-        //   g = 0..5: AND/OR gates for both definitions, then ITE and XOR gates for
-        //           both (bounded.cuh:336-356), each found gate's substitution
-        //           counted; a second definition is tried only while no
-        //           substitution was counted;
-        //   g = 6: the function-table gate is deferred to ve1b_k, else n-by-m
-        //           resolution (resolve.cuh:111-198) when nothing was counted.
+        def = ws_find_equ_gate(w, P, N, lane);
+        if (!def) {
+            const uint32_t nClsBefore = pOrgs + nOrgs;
+            // Every resolvent count goes through the one call of ws_count below (the
+            // three loops inlined at three places made the kernel fetch-bound):
+            //   g = -1: single-occurrence resolution (resolve.cuh:28-109), tried first
+            //           when one side has one original clause;
+            //   g = 0..5: AND/OR gates for both definitions, then ITE and XOR gates for
+            //           both (bounded.cuh:336-356), each found gate's substitution
+            //           counted; a second definition is tried only while no
+            //           substitution was counted;
+            //   g = 6: the function-table gate is deferred to ve1b_k, else n-by-m
+            //           resolution (resolve.cuh:111-198) when nothing was counted.
 #pragma unroll 1
-        for (int g = (pOrgs == 1 || nOrgs == 1) ? -1 : 0; g <= 6; g++) {
-            int kind;
-            uint32_t ncb = nClsBefore;
-            const int o = g & 1;
-            // AND/OR: (N, P) then (P, N); ITE and XOR: (P, N) then (N, P)
-            const bool pfirst = g < 0 || g >= 6 ? true : (g < 2 ? o != 0 : o == 0);
-            const Side& D = pfirst ? P : N;
-            const Side& F = pfirst ? N : P;
-            GateUndo undo{NOREF, NOREF, NOREF, NOREF};
-            if (g < 0) {
-                kind = CNT_RES_UNBOUNDED;
-                ncb = 0;
-            } else if (g < 6) {
-                if (g < 2 ? nClsBefore <= 2 : nClsBefore <= 3) continue;
-                if (o && nC) continue;
-                bool found;
-                if (g < 2) found = (pfirst ? pOrgs : nOrgs) < SH_MAX_BVE_OUT1 && ws_find_ao_gate(k, w, D, F, undo, lane);
-                else if (g < 4) found = ws_find_ite_gate(k, w, D, F, undo, lane);
-                else found = ws_find_xor_gate(k, w, D, F, lane);
-                if (!found) continue;
-                nE = 0; nC = 0; nL = 0;
-                kind = CNT_SUBS;
-            } else {
-                if (vc_on(k, x) && nClsBefore > 2 && ws_fun_possible(k, w, x, lane)) {
-                    ws_flush(k, w, lane);
-                    if (lane == 0) {
-                        dlist[atomicAdd(dcount, 1u)] = tid;
-                        ucnt[tid] = nC;
-                        rpos[tid] = (unsigned long long)pOrgs | ((unsigned long long)nOrgs << 32);
+            for (int g = (pOrgs == 1 || nOrgs == 1) ? -1 : 0; g <= 6; g++) {
+                int kind;
+                uint32_t ncb = nClsBefore;
+                const int o = g & 1;
+                // AND/OR: (N, P) then (P, N); ITE and XOR: (P, N) then (N, P)
+                const bool pfirst = g < 0 || g >= 6 ? true : (g < 2 ? o != 0 : o == 0);
+                const Side& D = pfirst ? P : N;
+                const Side& F = pfirst ? N : P;
+                GateUndo undo{NOREF, NOREF, NOREF, NOREF};
+                if (g < 0) {
+                    kind = CNT_RES_UNBOUNDED;
+                    ncb = 0;
+                } else if (g < 6) {
+                    if (g < 2 ? nClsBefore <= 2 : nClsBefore <= 3) continue;
+                    if (o && nC) continue;
+                    bool found;
+                    if (g < 2) found = (pfirst ? pOrgs : nOrgs) < SH_MAX_BVE_OUT1 && ws_find_ao_gate(k, w, D, F, undo, lane);
+                    else if (g < 4) found = ws_find_ite_gate(k, w, D, F, undo, lane);
+                    else found = ws_find_xor_gate(k, w, D, F, lane);
+                    if (!found) continue;
+                    nE = 0; nC = 0; nL = 0;
+                    kind = CNT_SUBS;
+                } else {
+                    if (vc_on(k, x) && nClsBefore > 2 && ws_fun_possible(k, w, x, lane)) {
+                        ws_flush(k, w, lane);
+                        if (lane == 0) {
+                            dlist[atomicAdd(dcount, 1u)] = tid;
+                            ucnt[tid] = nC;
+                            rpos[tid] = (unsigned long long)pOrgs | ((unsigned long long)nOrgs << 32);
+                        }
+                        return;
                     }
-                    return;
+                    if (nC) break;
+                    nE = 0; nC = 0; nL = 0;
+                    kind = CNT_RES_BOUNDED;
                 }
-                if (nC) break;
-                nE = 0; nC = 0; nL = 0;
-                kind = CNT_RES_BOUNDED;
-            }
-            const bool ok = ws_count(k, w, kind, x, D, F, ncb, nE, nC, nL, lane);
-            if (g < 0) {
-                if (ok) { elimType = RES_MASK; break; }   // resolvents (nC > 0) or none: the common end
-                nE = 0; nC = 0; nL = 0;
-                continue;
-            }
-            if (g >= 6) {
-                if (ok) elimType = RES_MASK;
-                break;
-            }
-            if (ok) { elimType = AOIX_MASK; break; }
-            // too many resolvents: undo what the detector melted
-            if (g < 2) {
-                ws_melt(w, undo.a, 0, lane);
-                ws_freeze_binaries(w, D, lane);
-            } else if (g < 4) {
-                ws_melt(w, undo.a, 0, lane);
-                ws_melt(w, undo.b, 0, lane);
-                if (undo.c != NOREF) ws_melt(w, undo.c, 0, lane);
-                if (undo.d != NOREF) ws_melt(w, undo.d, 0, lane);
-            } else {
-                ws_freeze_arities(w, lane);
+                const bool ok = ws_count(k, w, kind, x, D, F, ncb, nE, nC, nL, lane);
+                if (g < 0) {
+                    if (ok) { elimType = RES_MASK; break; }   // resolvents (nC > 0) or none: the common end
+                    nE = 0; nC = 0; nL = 0;
+                    continue;
+                }
+                if (g >= 6) {
+                    if (ok) elimType = RES_MASK;
+                    break;
+                }
+                if (ok) { elimType = AOIX_MASK; break; }
+                // too many resolvents: undo what the detector melted
+                if (g < 2) {
+                    ws_melt(w, undo.a, 0, lane);
+                    ws_freeze_binaries(w, D, lane);
+                } else if (g < 4) {
+                    ws_melt(w, undo.a, 0, lane);
+                    ws_melt(w, undo.b, 0, lane);
+                    if (undo.c != NOREF) ws_melt(w, undo.c, 0, lane);
+                    if (undo.d != NOREF) ws_melt(w, undo.d, 0, lane);
+                } else {
+                    ws_freeze_arities(w, lane);
+                }
             }
         }
     }
-    // common end: eliminated without resolvents, or the counts stored for
-    // emission (elimType set), or kept
-    if (!nC) ws_elim_no_resolvents(k, w, x, P, N, pOrgs, nOrgs, lane);
+    // common end: eliminated without resolvents (pure literal, no clause
+    // resolvent, or substituted by an equivalence: the side with fewer original
+    // clauses saved, then the clauses deleted or rewritten), or the counts
+    // stored for emission (elimType set), or kept
+    if (!nC) {
+        ws_save_resolved_orgs(k, w, P, N, pOrgs, nOrgs, lane);
+        if (def) ws_substitute_single(k, w, P, N, def, lane);
+        else ws_toblivion(k, w, P, N, lane);
+        ws_flush(k, w, lane);
+        if (lane == 0) k.elim[x] |= MELTING_MASK;
+    }
     else {
         ws_flush(k, w, lane);
         if (elimType) ws_store_info(tid, elimType, nE, nC, nL, type, ucnt, rpos, rref, lane);
