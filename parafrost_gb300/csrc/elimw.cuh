@@ -846,11 +846,12 @@ PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
         ws_save_resolved_orgs(k, w, P, N, pOrgs, nOrgs, lane);
         if (def) ws_substitute_single(k, w, P, N, def, lane);
         else ws_toblivion(k, w, P, N, lane);
+        ws_flush(k, w, lane);
+        if (lane == 0) k.elim[x] |= MELTING_MASK;
     }
-    ws_flush(k, w, lane);
-    if (lane == 0) {
-        if (!nC) k.elim[x] |= MELTING_MASK;
-        else if (elimType) store_elim_info(tid, elimType, nE, nC, nL, type, ucnt, rpos, rref);
+    else {
+        ws_flush(k, w, lane);
+        if (elimType) ws_store_info(tid, elimType, nE, nC, nL, type, ucnt, rpos, rref, lane);
     }
 }
 
@@ -1193,31 +1194,25 @@ __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* el
         }
         const Side P{0, w.np, p}, N{w.np, w.nn, n};
         ws_sub_screen(w, P, N, lane);
-        // positives against negatives, then negatives against positives, in one
-        // loop (one copy of the searches in the kernel's code)
-        uint32_t nUnits[2] = {0, 0};
-#pragma unroll 1
-        for (int side = 0; side < 2; side++) {
-            const Side& S = side ? N : P;
-            const Side& O = side ? P : N;
-            uint32_t cnt = 0;
-#pragma unroll 1
-            for (uint32_t i = 0; i < S.n; i++) {
-                const uint32_t c = S.b + i;
-                if (w.size[c] > SUB_MAX_CL_SIZE) break;
-                if (m_deleted(w.meta[c]) || !w.outs[c]) continue;
-                ws_selfsubsume(w, S.lit, O.lit, O, c, cnt, lane);
-                ws_subsume(w, S, i, c, lane);
-            }
-            nUnits[side] = cnt;
+        uint32_t nPos = 0, nNeg = 0;
+        for (uint32_t i = 0; i < P.n; i++) {
+            const uint32_t c = P.b + i;
+            if (w.size[c] > SUB_MAX_CL_SIZE) break;
+            if (m_deleted(w.meta[c]) || !w.outs[c]) continue;
+            ws_selfsubsume(w, p, n, N, c, nPos, lane);
+            ws_subsume(w, P, i, c, lane);
+        }
+        for (uint32_t i = 0; i < N.n; i++) {
+            const uint32_t c = N.b + i;
+            if (w.size[c] > SUB_MAX_CL_SIZE) break;
+            if (m_deleted(w.meta[c]) || !w.outs[c]) continue;
+            ws_selfsubsume(w, n, p, P, c, nNeg, lane);
+            ws_subsume(w, N, i, c, lane);
         }
         __syncwarp();
-        if ((nUnits[0] || nUnits[1]) && lane == 0) {
-            for (int side = 0; side < 2; side++) {
-                const Side& S = side ? N : P;
-                if (nUnits[side])
-                    for (uint32_t i = 0; i < S.n; i++) if (w.size[S.b + i] == 1) push_unit(k, WL(w, S.b + i)[0]);
-            }
+        if ((nPos || nNeg) && lane == 0) {
+            if (nPos) for (uint32_t i = 0; i < P.n; i++) if (w.size[P.b + i] == 1) push_unit(k, WL(w, P.b + i)[0]);
+            if (nNeg) for (uint32_t i = 0; i < N.n; i++) if (w.size[N.b + i] == 1) push_unit(k, WL(w, N.b + i)[0]);
         }
         if (k.proof) ws_proof_sub(k, w, x, lane);
         ws_update_ol(k, w, P, lane);
