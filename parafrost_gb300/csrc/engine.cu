@@ -711,19 +711,53 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
 }
 
 // instances leaving the round loop keep the units of their last round unpropagated
+__global__ void regions_all_k(const uint32_t* src, const unsigned long long* src_base,
+                              const unsigned long long* dst_base, const uint32_t* shift, uint32_t n, uint64_t total,
+                              uint32_t* out);
+
 void retire(Ctx& c, const std::vector<uint32_t>& ids) {
     bool need = false;
     for (uint32_t i : ids) need |= c.ih[i].nUnits > 0;
     if (need) pull_inst_out(c);
+    // the unit regions of the leaving instances, gathered back to back on the
+    // device and copied in one transfer
+    std::vector<uint32_t> with;
+    std::vector<unsigned long long> sb, db(1, 0);
     for (uint32_t i : ids) {
         InstHost& h = c.ih[i];
         h.active = false;
         if (!h.nUnits) continue;
         const uint64_t nu = std::min<uint64_t>(c.hout.ucount[i], c.hi.ucap[i]);
         h.pending.resize(nu);
-        if (nu) cudaMemcpy(h.pending.data(), c.units + c.hi.ubase[i], nu * sizeof(uint32_t), cudaMemcpyDeviceToHost);
         h.nUnits = 0;
+        if (!nu) continue;
+        with.push_back(i);
+        sb.push_back(c.hi.ubase[i]);
+        db.push_back(db.back() + nu);
     }
+    if (with.empty()) return;
+    const uint32_t m = (uint32_t)with.size();
+    const uint64_t total = db.back();
+    unsigned long long* dbases = nullptr;
+    uint32_t* dout = nullptr;
+    if (m > 1 && dalloc_t(c, &dbases, 2 * (size_t)m + 1) && dalloc_t(c, &dout, total)) {
+        std::vector<unsigned long long> hb(sb);
+        hb.insert(hb.end(), db.begin(), db.end());
+        cudaMemcpyAsync(dbases, hb.data(), hb.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, c.s);
+        PFG_LAUNCH(K_MISC, regions_all_k, grid_for(total, 256), 256, 0, c.s, c.units, dbases, dbases + m,
+                   (const uint32_t*)nullptr, m, total, dout);
+        std::vector<uint32_t> all(total);
+        cudaMemcpyAsync(all.data(), dout, total * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+        cuda_ok(c, cudaStreamSynchronize(c.s), "pending units");
+        for (uint32_t q = 0; q < m; q++)
+            std::copy(all.begin() + db[q], all.begin() + db[q + 1], c.ih[with[q]].pending.begin());
+    } else {
+        for (uint32_t q = 0; q < m; q++)
+            cudaMemcpy(c.ih[with[q]].pending.data(), c.units + sb[q], (db[q + 1] - db[q]) * sizeof(uint32_t),
+                       cudaMemcpyDeviceToHost);
+    }
+    dfree(c, dbases);
+    dfree(c, dout);
 }
 
 std::vector<uint32_t> active_ids(const Ctx& c) {
@@ -894,6 +928,12 @@ static int finish(Ctx& c, pfg_stats* st, uint64_t base_launches, int rc) {
     if (st) *st = c.stats;
     return rc;
 }
+
+namespace pfg {
+namespace {
+__global__ void elim_counts_k(const uint8_t* elim, const uint32_t* vinst, uint32_t V, unsigned long long* cnt);
+}  // namespace
+}  // namespace pfg
 
 // The round loop of Solver::simplifying (simplify.cu:159-186), run for every
 // instance at once. All instances still in the loop share the round counter
@@ -1117,23 +1157,28 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         }
     }
     cudaEventRecord(c.ev_end, c.s);
+    // eliminated / forced variables, counted per instance on the device
+    std::vector<unsigned long long> ecnt(2 * (size_t)n, 0);
+    {
+        unsigned long long* d_ecnt = nullptr;
+        if (dalloc_t(c, &d_ecnt, 2 * (size_t)n)) {
+            cudaMemsetAsync(d_ecnt, 0, 2 * (size_t)n * sizeof(unsigned long long), c.s);
+            PFG_LAUNCH(K_DOWNLOAD, elim_counts_k, grid_for(c.V, 256), 256, 0, c.s, c.elim, c.vinst, c.V, d_ecnt);
+            cudaMemcpyAsync(ecnt.data(), d_ecnt, ecnt.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            c.s);
+            dfree(c, d_ecnt);
+        }
+    }
     pull_inst_out(c);
     float ms = 0;
     cudaEventElapsedTime(&ms, c.ev_begin, c.ev_end);
     c.simplified = true;
-    // eliminated / forced counts per instance
-    std::vector<uint8_t> el(c.V + 1);
-    cudaMemcpy(el.data(), c.elim, c.V + 1, cudaMemcpyDeviceToHost);
     uint64_t tot_e = 0, tot_f = 0, tot_stack = 0;
     uint32_t max_rounds = 0;
     for (uint32_t i = 0; i < n; i++) {
         InstHost& h = c.ih[i];
-        uint64_t ne = 0, nf = 0;
-        for (uint32_t v = h.voff + 1; v <= h.voff + h.V; v++) {
-            if (el[v] & FORCED_MASK) nf++;
-            else if (el[v]) ne++;
-        }
-        tot_e += ne; tot_f += nf;
+        tot_e += ecnt[2 * i];
+        tot_f += ecnt[2 * i + 1];
         tot_stack += c.hout.scount[i];
         max_rounds = std::max(max_rounds, h.rounds);
     }
