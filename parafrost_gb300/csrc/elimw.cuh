@@ -117,24 +117,6 @@ PFG_D void ws_set_meta(WS& w, uint32_t c, uint32_t m, unsigned lane) {
 }
 PFG_D void ws_melt(WS& w, uint32_t c, uint32_t f, unsigned lane) { ws_set_meta(w, c, m_set_molten(w.meta[c], f), lane); }
 
-// staged index of global clause id (or NOREF)
-PFG_D uint32_t ws_find(const WS& w, uint32_t id, unsigned lane) {
-    const uint32_t nc = w.np + w.nn;
-    for (uint32_t c0 = 0; c0 < nc; c0 += 32) {
-        const uint32_t i = c0 + lane;
-        const unsigned b = __ballot_sync(FULL, i < nc && w.id[i] == id);
-        if (b) return c0 + __ffs(b) - 1;
-    }
-    return NOREF;
-}
-
-PFG_D uint32_t ws_meta_of(const EK& k, const WS& w, uint32_t id, unsigned lane) {
-    // called by one lane at a time with its own id: linear scan of the stage
-    const uint32_t nc = w.np + w.nn;
-    for (uint32_t i = 0; i < nc; i++) if (w.id[i] == id) return w.meta[i];
-    return k.hdr[id].meta;
-}
-
 PFG_D uint32_t warp_excl_scan(uint32_t v, unsigned lane, uint32_t& total) {
     uint32_t incl = v;
 #pragma unroll
@@ -307,32 +289,6 @@ PFG_D bool ws_count(const EK& k, WS& w, int kind, uint32_t x, const Side& me, co
     if (kind != CNT_RES_UNBOUNDED && k.ve_lbound_en && nL > ws_lits_before(w, me) + ws_lits_before(w, ot))
         return false;
     return !(k.proof && ws_proof_guard(k, w, kind, x, me, ot, nE, lane));
-}
-
-// countSubstituted / countCoreSubstituted: true = cannot substitute
-PFG_D bool ws_count_subst(const EK& k, WS& w, int kind, uint32_t x, uint32_t nClsBefore, const Side& me,
-                          const Side& ot, uint32_t& nE, uint32_t& nC, uint32_t& nL, unsigned lane) {
-    if (!ws_count_pairs(w, kind, x, me, ot, nClsBefore, k.ve_clause_max, nE, nC, nL, lane)) return true;
-    if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return true;
-    if (k.ve_lbound_en && nL > ws_lits_before(w, me) + ws_lits_before(w, ot)) return true;
-    if (k.proof && ws_proof_guard(k, w, kind, x, me, ot, nE, lane)) return true;
-    return false;
-}
-
-PFG_D bool ws_count_res_unbounded(const EK& k, WS& w, uint32_t x, const Side& me, const Side& ot, uint32_t& nE,
-                                  uint32_t& nC, uint32_t& nL, unsigned lane) {
-    if (!ws_count_pairs(w, CNT_RES_UNBOUNDED, x, me, ot, 0, k.ve_clause_max, nE, nC, nL, lane)) return false;
-    if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return false;
-    return !(k.proof && ws_proof_guard(k, w, CNT_RES_UNBOUNDED, x, me, ot, nE, lane));
-}
-
-PFG_D bool ws_count_res_bounded(const EK& k, WS& w, uint32_t x, uint32_t nClsBefore, const Side& me, const Side& ot,
-                                uint32_t& nE, uint32_t& nC, uint32_t& nL, unsigned lane) {
-    nE = 0; nC = 0; nL = 0;
-    if (!ws_count_pairs(w, CNT_RES_BOUNDED, x, me, ot, nClsBefore, k.ve_clause_max, nE, nC, nL, lane)) return false;
-    if (nC > ADDEDCLS_MAX || nL > ADDEDLITS_MAX) return false;
-    if (k.ve_lbound_en && nL > ws_lits_before(w, me) + ws_lits_before(w, ot)) return false;
-    return !(k.proof && ws_proof_guard(k, w, CNT_RES_BOUNDED, x, me, ot, nE, lane));
 }
 
 // ---- model stack from the stage ----
