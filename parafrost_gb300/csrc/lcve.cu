@@ -145,6 +145,51 @@ __global__ void mis_win3_k(uint32_t V, const ClsHdr* hdr, const uint32_t* lits, 
     if ((threadIdx.x & 31u) == 0 && cnt) atomicAdd(undecided, cnt);
 }
 
+// First MIS round through clause minima: with every candidate undecided, a
+// candidate is blocked exactly when one of its live clauses holds an undecided
+// variable of smaller rank, i.e. when the clause's smallest undecided rank is
+// below its own. One pass over the clauses records that minimum (a deleted
+// clause gets none); the candidates then read one word per occurrence instead
+// of the clause's header, literals and their states.
+__global__ void clause_min_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
+                             const uint32_t* __restrict__ rank, const uint8_t* __restrict__ mstate, uint32_t* cmin) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        const ClsHdr h = hdr[c];
+        uint32_t m = 0xFFFFFFFFu;
+        if (!m_deleted(h.meta)) {
+            const uint32_t* l = lits + h.off;
+            for (uint32_t k = 0; k < h.size; k++) {
+                const uint32_t v = ABSV(l[k]);
+                if (mstate[v] == MIS_UNDECIDED) m = min(m, rank[v]);
+            }
+        }
+        cmin[c] = m;
+    }
+}
+
+PFG_D bool blocked_min(const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids, const uint32_t* cmin,
+                       uint32_t lit, uint32_t r) {
+    const uint32_t o = ot_off[lit], n = ot_size[lit];
+    for (uint32_t i = 0; i < n; i++)
+        if (cmin[ot_ids[o + i]] < r) return true;
+    return false;
+}
+
+__global__ void mis_win_min_k(uint32_t V, const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids,
+                              const uint32_t* cmin, const uint32_t* rank, const uint8_t* mstate, uint8_t* winv,
+                              uint32_t* undecided) {
+    uint32_t cnt = 0;
+    for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
+        if (mstate[v] != MIS_UNDECIDED) continue;
+        cnt++;
+        const uint32_t r = rank[v];
+        winv[v] = !(blocked_min(ot_off, ot_size, ot_ids, cmin, 2 * v, r) ||
+                    blocked_min(ot_off, ot_size, ot_ids, cmin, 2 * v + 1, r));
+    }
+    for (int d = 16; d > 0; d >>= 1) cnt += __shfl_down_sync(0xFFFFFFFFu, cnt, d);
+    if ((threadIdx.x & 31u) == 0 && cnt) atomicAdd(undecided, cnt);
+}
+
 __global__ void mis_apply3_k(uint32_t V, const uint8_t* winv, uint32_t r, uint32_t* mround, const ClsHdr* hdr,
                              const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
                              const uint32_t* ot_ids, uint8_t* frozen, uint8_t* mstate, const uint32_t* undecided,
@@ -324,8 +369,15 @@ bool lcve(Ctx& c) {
         for (int batch = 1; !done; batch = std::min(batch * 2, 16)) {
             for (int b = 0; b < batch; b++, r++) {
                 cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
-                PFG_LAUNCH(K_MIS_WIN, mis_win3_k, grid_for(V, 128), 128, 0, c.s, V, c.hdr, c.lits, c.ot_off,
-                           c.ot_size, c.ot_ids, c.rank, c.mstate, c.winv, &c.dc->nwin, &c.dc->mis_done);
+                if (r == 0 && ensure_tmp_u32(c, c.ncls + 1)) {   // first round: every candidate undecided
+                    PFG_LAUNCH(K_MIS_WIN, clause_min_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls,
+                               c.rank, c.mstate, c.tmp_u32);
+                    PFG_LAUNCH(K_MIS_WIN, mis_win_min_k, grid_for(V, 128), 128, 0, c.s, V, c.ot_off, c.ot_size,
+                               c.ot_ids, c.tmp_u32, c.rank, c.mstate, c.winv, &c.dc->nwin);
+                } else {
+                    PFG_LAUNCH(K_MIS_WIN, mis_win3_k, grid_for(V, 128), 128, 0, c.s, V, c.hdr, c.lits, c.ot_off,
+                               c.ot_size, c.ot_ids, c.rank, c.mstate, c.winv, &c.dc->nwin, &c.dc->mis_done);
+                }
                 PFG_LAUNCH(K_MIS_APPLY, mis_apply3_k, grid_for(V, 128), 128, 0, c.s, V, c.winv, r, mround, c.hdr,
                            c.lits, c.ot_off, c.ot_size, c.ot_ids, c.frozen, c.mstate, &c.dc->nwin, &c.dc->mis_done);
             }
