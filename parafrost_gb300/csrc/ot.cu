@@ -119,14 +119,25 @@ __global__ void ot_filter_w_k(uint64_t nlist, const uint32_t* __restrict__ off, 
         }
         const uint32_t pre = incl - n, T = __shfl_sync(0xFFFFFFFFu, incl, 31);
         uint32_t kept = 0;
+        // the ids of the next chunk are loaded while this one is decided (every
+        // write goes to a position at or before the entry it keeps, so no write
+        // of a chunk reaches a later chunk's entries)
+        uint32_t nj = owner_lane(pre, lane);
+        uint32_t nsj = __shfl_sync(0xFFFFFFFFu, pre, nj);
+        uint32_t noj = __shfl_sync(0xFFFFFFFFu, o, nj);
+        uint32_t nc = lane < T ? ids[noj + (lane - nsj)] : 0u;
         for (uint32_t e0 = 0; e0 < T; e0 += 32) {
             const uint32_t e = e0 + lane;
-            const uint32_t j = owner_lane(pre, e);
-            const uint32_t sj = __shfl_sync(0xFFFFFFFFu, pre, j);
-            const uint32_t oj = __shfl_sync(0xFFFFFFFFu, o, j);
+            const uint32_t j = nj, sj = nsj, oj = noj, c = nc;
             const uint32_t kj = __shfl_sync(0xFFFFFFFFu, kept, j);
             const bool valid = e < T;
-            const uint32_t c = valid ? ids[oj + (e - sj)] : 0u;
+            if (e0 + 32 < T) {
+                const uint32_t e2 = e + 32;
+                nj = owner_lane(pre, e2);
+                nsj = __shfl_sync(0xFFFFFFFFu, pre, nj);
+                noj = __shfl_sync(0xFFFFFFFFu, o, nj);
+                nc = e2 < T ? ids[noj + (e2 - nsj)] : 0u;
+            }
             const bool keep = valid && !drop[c];
             const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
             // lanes of list j in this chunk start at lane max(sj - e0, 0)
@@ -169,16 +180,16 @@ __global__ void move_w_k(uint64_t nlist, const uint32_t* __restrict__ off, const
             if (lane >= (unsigned)d) incl += t;
         }
         const uint32_t pre = incl - n, T = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        for (uint32_t e0 = 0; e0 < T; e0 += 32) {
-            const uint32_t e = e0 + lane;
-            const uint32_t j = owner_lane(pre, e);
-            const uint32_t sj = __shfl_sync(0xFFFFFFFFu, pre, j);
-            const uint32_t oj = __shfl_sync(0xFFFFFFFFu, o, j);
-            const uint32_t o2j = __shfl_sync(0xFFFFFFFFu, o2, j);
-            if (e < T) {
-                const uint32_t c = ids[oj + (e - sj)];
-                ids2[o2j + (e - sj)] = map ? map[c] : c;
-            }
+        for (uint32_t e0 = 0; e0 < T; e0 += 64) {   // two chunks per step: their loads in flight together
+            const uint32_t ea = e0 + lane, eb = ea + 32;
+            const uint32_t ja = owner_lane(pre, ea), jb = owner_lane(pre, eb);
+            const uint32_t sa = __shfl_sync(0xFFFFFFFFu, pre, ja), sb = __shfl_sync(0xFFFFFFFFu, pre, jb);
+            const uint32_t oa = __shfl_sync(0xFFFFFFFFu, o, ja), ob = __shfl_sync(0xFFFFFFFFu, o, jb);
+            const uint32_t a2 = __shfl_sync(0xFFFFFFFFu, o2, ja), b2 = __shfl_sync(0xFFFFFFFFu, o2, jb);
+            const uint32_t ca = ea < T ? ids[oa + (ea - sa)] : 0u;
+            const uint32_t cb = eb < T ? ids[ob + (eb - sb)] : 0u;
+            if (ea < T) ids2[a2 + (ea - sa)] = map ? map[ca] : ca;
+            if (eb < T) ids2[b2 + (eb - sb)] = map ? map[cb] : cb;
         }
     }
 }
