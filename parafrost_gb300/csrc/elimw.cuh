@@ -42,6 +42,35 @@ struct Side {
 
 PFG_D uint32_t* WL(WS& w, uint32_t c) { return w.lits + w.off[c]; }
 
+// The next variable of a warp: its list bounds are loaded when the current
+// variable starts and its id lines are prefetched into L2 when it ends, so the
+// first two steps of its staging (list bounds, ids) do not wait on DRAM.
+struct NextLists {
+    uint32_t po, ps, no, ns;
+};
+
+PFG_D NextLists ws_next_lists(const EK& k, const uint32_t* elected, uint32_t qn, uint32_t nelected) {
+    NextLists nl{0, 0, 0, 0};
+    if (qn < nelected) {
+        const uint32_t xn = elected[qn];
+        nl.po = k.ot_off[2 * xn];
+        nl.ps = k.ot_size[2 * xn];
+        nl.no = k.ot_off[2 * xn + 1];
+        nl.ns = k.ot_size[2 * xn + 1];
+    }
+    return nl;
+}
+
+PFG_D void ws_prefetch_lists(const EK& k, const NextLists& nl, unsigned lane) {
+    if (nl.ps + nl.ns > WS_MAXC) return;      // it goes to the thread kernel
+    const uint32_t side = lane >> 4, line = lane & 15u;   // lanes 0-15: positives, 16-31: negatives
+    const uint32_t o = side ? nl.no : nl.po, n = side ? nl.ns : nl.ps;
+    if (line * 32u < n) {
+        const uint32_t* a = k.ot_ids + o + line * 32u;
+        asm volatile("prefetch.global.L2 [%0];" :: "l"(a));
+    }
+}
+
 // Loads both lists of x into the stage; false if they do not fit.
 PFG_D bool ws_stage(const EK& k, WS& w, uint32_t p, uint32_t n, unsigned lane) {
     const uint32_t np = OLs(k, p), nn = OLs(k, n), nc = np + nn;
@@ -818,15 +847,17 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve1w_k(EK k, const uint32_t* el
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected;
-         q += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t stride = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected; q += stride) {
         const uint32_t tid = q;
         const uint32_t x = elected[tid];
+        const NextLists nl = ws_next_lists(k, elected, q + stride, nelected);
         if (!ws_stage(k, w, 2 * x, 2 * x + 1, lane)) {
             if (lane == 0) big[atomicAdd(nbig, 1u)] = tid;
             continue;
         }
         ws_ve1(k, w, tid, x, type, ucnt, rpos, rref, dlist, dcount, lane);
+        ws_prefetch_lists(k, nl, lane);
         __syncwarp();
     }
 }
