@@ -840,7 +840,7 @@ PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
     }
 }
 
-__global__ void __launch_bounds__(WS_WARPS * 32, 10) ve1w_k(EK k, const uint32_t* elected, uint32_t nelected,
+__global__ void __launch_bounds__(WS_WARPS * 32) ve1w_k(EK k, const uint32_t* elected, uint32_t nelected,
                                                         uint32_t* type, uint32_t* ucnt, unsigned long long* rpos,
                                                         unsigned long long* rref, uint32_t* dlist, uint32_t* dcount,
                                                         uint32_t* big, uint32_t* nbig) {
