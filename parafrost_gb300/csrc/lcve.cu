@@ -190,6 +190,41 @@ __global__ void mis_win_min_k(uint32_t V, const uint32_t* ot_off, const uint32_t
     if ((threadIdx.x & 31u) == 0 && cnt) atomicAdd(undecided, cnt);
 }
 
+// First MIS round, applied through the same clause minima: a winner is the
+// smallest undecided variable of every clause it is in, so a live clause holds
+// a winner exactly when its minimum-rank variable won, and then every other
+// variable of the clause is its neighbour and is frozen (freeze_list over the
+// winner's lists reaches the same clauses). No other variable of such a clause
+// is a winner, so the freezing never meets an election.
+__global__ void mis_apply_min_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
+                                const uint32_t* __restrict__ cmin, const uint32_t* __restrict__ eligible,
+                                const uint8_t* __restrict__ winv, uint8_t* frozen, uint8_t* mstate) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t m = cmin[c];
+        if (m == 0xFFFFFFFFu) continue;
+        const uint32_t u = eligible[m];
+        if (!winv[u]) continue;
+        const ClsHdr h = hdr[c];
+        const uint32_t* l = lits + h.off;
+        for (uint32_t k = 0; k < h.size; k++) {
+            const uint32_t v = ABSV(l[k]);
+            if (v == u) continue;
+            frozen[v] = 1;
+            if (mstate[v] == MIS_UNDECIDED) mstate[v] = MIS_FROZEN;
+        }
+    }
+}
+
+__global__ void mis_elect_k(uint32_t V, const uint8_t* winv, uint32_t r, uint32_t* mround, uint8_t* mstate,
+                            const uint32_t* undecided) {
+    if (*undecided == 0) return;
+    for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
+        if (mstate[v] != MIS_UNDECIDED || !winv[v]) continue;
+        mstate[v] = MIS_ELECTED;
+        mround[v] = r;
+    }
+}
+
 __global__ void mis_apply3_k(uint32_t V, const uint8_t* winv, uint32_t r, uint32_t* mround, const ClsHdr* hdr,
                              const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
                              const uint32_t* ot_ids, uint8_t* frozen, uint8_t* mstate, const uint32_t* undecided,
@@ -374,10 +409,14 @@ bool lcve(Ctx& c) {
                                c.rank, c.mstate, c.tmp_u32);
                     PFG_LAUNCH(K_MIS_WIN, mis_win_min_k, grid_for(V, 128), 128, 0, c.s, V, c.ot_off, c.ot_size,
                                c.ot_ids, c.tmp_u32, c.rank, c.mstate, c.winv, &c.dc->nwin);
-                } else {
-                    PFG_LAUNCH(K_MIS_WIN, mis_win3_k, grid_for(V, 128), 128, 0, c.s, V, c.hdr, c.lits, c.ot_off,
-                               c.ot_size, c.ot_ids, c.rank, c.mstate, c.winv, &c.dc->nwin, &c.dc->mis_done);
+                    PFG_LAUNCH(K_MIS_APPLY, mis_apply_min_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits,
+                               c.ncls, c.tmp_u32, c.eligible, c.winv, c.frozen, c.mstate);
+                    PFG_LAUNCH(K_MIS_APPLY, mis_elect_k, grid_for(V, 256), 256, 0, c.s, V, c.winv, r, mround, c.mstate,
+                               &c.dc->nwin);
+                    continue;
                 }
+                PFG_LAUNCH(K_MIS_WIN, mis_win3_k, grid_for(V, 128), 128, 0, c.s, V, c.hdr, c.lits, c.ot_off,
+                           c.ot_size, c.ot_ids, c.rank, c.mstate, c.winv, &c.dc->nwin, &c.dc->mis_done);
                 PFG_LAUNCH(K_MIS_APPLY, mis_apply3_k, grid_for(V, 128), 128, 0, c.s, V, c.winv, r, mround, c.hdr,
                            c.lits, c.ot_off, c.ot_size, c.ot_ids, c.frozen, c.mstate, &c.dc->nwin, &c.dc->mis_done);
             }
