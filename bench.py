@@ -537,12 +537,14 @@ def run_gpu_batch(a, world, rank, local):
     rbuf = pinned.ResultBuffers()
     sim.simplify_batch(pcnfs, into=rbuf)          # sizes the result buffers (untimed)
     e2e_s, e2e_proc, h2d, d2h = 0.0, 0, 0, 0
+    e2e_steps = []
     gc.collect()
     gc.disable()     # no collector pause of this process inside the timed calls
     for _ in range(a.steps):
         t1 = time.perf_counter()
         outs = sim.simplify_batch(pcnfs, into=rbuf)
-        e2e_s += time.perf_counter() - t1
+        e2e_steps.append(time.perf_counter() - t1)
+        e2e_s += e2e_steps[-1]
         e2e_proc += sum(int(o.stats["clauses_processed"]) for o in outs)
         h2d = sum(c.lits.nbytes + c.off.nbytes for c in cnfs)
         d2h = sum(result_bytes(o) for o in outs)
@@ -602,7 +604,8 @@ def run_gpu_batch(a, world, rank, local):
         "batched_vs_plain": value / plain_value,
         "serving": serving,
         "e2e": {"value": e2e_total / e2e_max, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_max / a.steps},
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_max / a.steps,
+                "ms_steps": [round(1000 * t, 2) for t in e2e_steps]},
         "roofline": roofline,
         "gpu_launches": int(launches),
         "kernel_ms": {k: round(v["ms"] / a.steps, 4) for k, v in prof.items() if v["launches"]},
