@@ -630,8 +630,8 @@ def run_gpu_batch(a, world, rank, local):
 # DRAM traffic per launch of the dominant kernel group from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (workload, group).
 TRAFFIC = {
-    # profiles/ve1w_k_batched.md: 12.382 GB read + 1.007 GB written over the 5 launches of one step
-    ("batched", "ve_phase1"): (12.382e9 + 1.007e9) / 5,
+    # profiles/ve1w_k_batched.md: 11.884 GB read + 0.991 GB written over the 5 launches of one step
+    ("batched", "ve_phase1"): (11.884e9 + 0.991e9) / 5,
 }
 
 
