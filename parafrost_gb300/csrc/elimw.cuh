@@ -1169,13 +1169,12 @@ __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* el
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
-    const uint32_t stride = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected; q += stride) {
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected;
+         q += (gridDim.x * blockDim.x) >> 5) {
         const uint32_t e = q;
         const uint32_t x = elected[e];
         const uint32_t p = 2 * x, n = p | 1;
         if (OLs(k, p) > k.sub_max_occurs || OLs(k, n) > k.sub_max_occurs) continue;
-        const NextLists nl = ws_next_lists(k, elected, q + stride, nelected);
         if (!ws_stage(k, w, p, n, lane)) {
             if (lane == 0) big[atomicAdd(nbig, 1u)] = e;
             continue;
@@ -1206,6 +1205,5 @@ __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* el
         ws_update_ol(k, w, P, lane);
         ws_update_ol(k, w, N, lane);
         ws_flush(k, w, lane);
-        ws_prefetch_lists(k, nl, lane);
     }
 }
