@@ -37,27 +37,27 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    # configs[1]: plain GPU method on a Tseitin circuit (the default bench line)
+    # plain one-instance GPU path on a Tseitin circuit (the default single-instance line)
     "tseitin": dict(family=1, a=1_000_000, b=50_000, c=1_000, seed=1,
                     desc="Tseitin circuit: 1M 2-input gates (40% AND, 30% OR, 30% XOR) over 50k inputs, "
                          "1k outputs asserted and root-propagated"),
-    # configs[0]: uniform random 3-SAT, 20k vars, 85.2k clauses
+    # uniform random 3-SAT, 20k vars, 85.2k clauses (small enough for the CPU simplifier)
     "ksat": dict(family=0, a=20_000, b=85_200, c=3, seed=1,
                  desc="uniform random 3-SAT, 20,000 vars, 85,200 clauses"),
-    # configs[2]: scale-free, 4M vars, 16M clauses, planted model so all 5 rounds run
+    # scale-free, 4M vars, 16M clauses, planted model so all 5 rounds run
     "scalefree": dict(family=2, a=4_000_000, b=16_000_000, c=1, seed=1,
                       desc="scale-free CNF, 4M vars, 16M clauses, power-law exponent 2.5, "
                            "geometric lengths on [2,50] mean 4, planted model"),
 }
 
-# configs[3]: 512 instances per batch, sizes log-uniform on [1e3, 2e5] variables,
+# batched workload: 512 instances per batch, sizes log-uniform on [1e3, 2e5] variables,
 # generator per instance uniform over {3-SAT (ratio 4.26), Tseitin, scale-free
 # (ratio 4.0, planted)}, per-instance seeds
 BATCH = dict(n=512, vmin=1_000, vmax=200_000, seed=7,
              desc="512 instances per batch, log-uniform 1k..200k vars each, generator per instance uniform over "
                   "random 3-SAT (4.26 clauses/var), Tseitin (5% inputs) and scale-free (4 clauses/var, planted)")
 
-# configs[4]: Poisson stream of 10,000 jobs, clause counts log-uniform on [1e3, 1e6]
+# serving workload: Poisson stream of 10,000 jobs, clause counts log-uniform on [1e3, 1e6]
 # from the three generators, admitted by a 120 GB device-arena budget, 3 rounds each.
 # Jobs are drawn from a pool of seeded instances (with replacement).
 SERVE = dict(jobs=10_000, cmin=1_000, cmax=1_000_000, pool=256, rate=800.0, budget=120_000_000_000, phases=3,
