@@ -126,6 +126,7 @@ struct Ctx {
     uint64_t ot_cap2 = 0;
     uint32_t* ot_off2 = nullptr;     // nlist + 1
     uint32_t* cmap = nullptr;        // old clause id -> new id of the last compaction (n + 1)
+    uint8_t* cdrop = nullptr;        // drop bytes on the old clause ids, kept over a compaction
     // big-list sort scratch
     uint32_t* big_lists = nullptr;   // nlist (worst case)
     uint32_t* mid_desc = nullptr;    // descriptors (offset, size) pairs

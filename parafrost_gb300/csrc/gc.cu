@@ -133,7 +133,12 @@ bool compact_cnf(Ctx& c) {
     if (c.ot_valid) c.cmap = pos; else dfree(c, pos);
     dfree(c, loff);
     c.prof.bytes[K_COMPACT] += 8 * (c.numLiterals + c.numClauses);
-    dfree(c, c.hdr); dfree(c, c.lits); dfree(c, c.cnew);
+    dfree(c, c.hdr); dfree(c, c.lits);
+    // with a table to update, the old drop bytes (deleted or flagged clauses on
+    // the old ids) are read by its move
+    dfree(c, c.cdrop);
+    c.cdrop = nullptr;
+    if (c.ot_valid) c.cdrop = c.cnew; else dfree(c, c.cnew);
     c.hdr = nhdr; c.lits = nlits; c.cnew = ncnew;
     c.hdr_cap = clsCap + 1; c.lits_cap = phys_lits;
     c.ncls = c.numClauses;

@@ -157,11 +157,26 @@ __global__ void ot_filter_w_k(uint64_t nlist, const uint32_t* __restrict__ off, 
     }
 }
 
-// kept entries of every list to its new offset, through the compaction map when
-// there is one; the append cursor of each list starts behind them
-__global__ void move_w_k(uint64_t nlist, const uint32_t* __restrict__ off, const uint32_t* __restrict__ size,
-                         const uint32_t* __restrict__ ids, const uint32_t* __restrict__ off2, uint32_t* ids2,
-                         const uint32_t* __restrict__ map, uint32_t* fill) {
+// sizes of the update before the drops are known: a list's old size (nothing
+// for an eliminated variable's lists), new_hist_k adds the flagged clauses
+__global__ void hist_init_k(uint64_t nlist, const uint32_t* __restrict__ size, const uint8_t* __restrict__ elim,
+                            uint32_t* hist) {
+    for (uint64_t l = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlist; l += (uint64_t)gridDim.x * blockDim.x)
+        hist[l] = elim[l >> 1] ? 0u : size[l];
+}
+
+// Prune and move in one pass: the entries of every list that `drop` keeps
+// (not deleted, not flagged) go in order to the list's new offset, renumbered
+// through the compaction map when there is one; an eliminated variable's lists
+// keep nothing. The new offsets were sized for the whole old list, so a list
+// ends with the gap of its dropped entries; its size (and histogram count,
+// which the election reads) becomes the kept entries plus its flagged clauses,
+// and its append cursor starts behind the kept ones. Same warp layout as the
+// in-place filter, but reads and writes go to different arrays.
+__global__ void prune_move_w_k(uint64_t nlist, const uint32_t* __restrict__ off, uint32_t* size, uint32_t* hist,
+                               const uint32_t* __restrict__ ids, const uint8_t* __restrict__ elim,
+                               const uint8_t* __restrict__ drop, const uint32_t* __restrict__ off2,
+                               uint32_t* __restrict__ ids2, const uint32_t* __restrict__ map, uint32_t* fill) {
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < nlist; w += nwarps) {
@@ -169,9 +184,9 @@ __global__ void move_w_k(uint64_t nlist, const uint32_t* __restrict__ off, const
         uint32_t n = 0, o = 0, o2 = 0;
         if (l < nlist) {
             n = size[l];
+            if (n && elim[l >> 1]) n = 0;
             o = off[l];
             o2 = off2[l];
-            fill[l] = o2 + n;
         }
         uint32_t incl = n;
 #pragma unroll
@@ -180,16 +195,42 @@ __global__ void move_w_k(uint64_t nlist, const uint32_t* __restrict__ off, const
             if (lane >= (unsigned)d) incl += t;
         }
         const uint32_t pre = incl - n, T = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        for (uint32_t e0 = 0; e0 < T; e0 += 64) {   // two chunks per step: their loads in flight together
-            const uint32_t ea = e0 + lane, eb = ea + 32;
-            const uint32_t ja = owner_lane(pre, ea), jb = owner_lane(pre, eb);
-            const uint32_t sa = __shfl_sync(0xFFFFFFFFu, pre, ja), sb = __shfl_sync(0xFFFFFFFFu, pre, jb);
-            const uint32_t oa = __shfl_sync(0xFFFFFFFFu, o, ja), ob = __shfl_sync(0xFFFFFFFFu, o, jb);
-            const uint32_t a2 = __shfl_sync(0xFFFFFFFFu, o2, ja), b2 = __shfl_sync(0xFFFFFFFFu, o2, jb);
-            const uint32_t ca = ea < T ? ids[oa + (ea - sa)] : 0u;
-            const uint32_t cb = eb < T ? ids[ob + (eb - sb)] : 0u;
-            if (ea < T) ids2[a2 + (ea - sa)] = map ? map[ca] : ca;
-            if (eb < T) ids2[b2 + (eb - sb)] = map ? map[cb] : cb;
+        uint32_t kept = 0;
+        uint32_t nj = owner_lane(pre, lane);
+        uint32_t nsj = __shfl_sync(0xFFFFFFFFu, pre, nj);
+        uint32_t noj = __shfl_sync(0xFFFFFFFFu, o, nj);
+        uint32_t nc = lane < T ? ids[noj + (lane - nsj)] : 0u;
+        for (uint32_t e0 = 0; e0 < T; e0 += 32) {
+            const uint32_t e = e0 + lane;
+            const uint32_t j = nj, sj = nsj, c = nc;
+            const uint32_t kj = __shfl_sync(0xFFFFFFFFu, kept, j);
+            const uint32_t o2j = __shfl_sync(0xFFFFFFFFu, o2, j);
+            const bool valid = e < T;
+            if (e0 + 32 < T) {
+                const uint32_t e2 = e + 32;
+                nj = owner_lane(pre, e2);
+                nsj = __shfl_sync(0xFFFFFFFFu, pre, nj);
+                noj = __shfl_sync(0xFFFFFFFFu, o, nj);
+                nc = e2 < T ? ids[noj + (e2 - nsj)] : 0u;
+            }
+            const bool keep = valid && !drop[c];
+            const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
+            const uint32_t first = sj > e0 ? sj - e0 : 0u;
+            const unsigned mine = ((1u << lane) - 1u) & ~((1u << first) - 1u);
+            if (keep) ids2[o2j + kj + __popc(bal & mine)] = map ? map[c] : c;
+            const int64_t a = (int64_t)pre - (int64_t)e0, b = a + (int64_t)n;
+            const int lo = a < 0 ? 0 : (a > 32 ? 32 : (int)a);
+            const int hi = b < 0 ? 0 : (b > 32 ? 32 : (int)b);
+            if (hi > lo) {
+                const unsigned m = (hi - lo == 32) ? 0xFFFFFFFFu : (((1u << (hi - lo)) - 1u) << lo);
+                kept += __popc(bal & m);
+            }
+        }
+        if (l < nlist) {
+            const uint32_t total = kept + (hist[l] - n);
+            size[l] = total;
+            hist[l] = total;
+            fill[l] = o2 + kept;
         }
     }
 }
@@ -450,9 +491,9 @@ bool ot_filter(Ctx& c, const uint8_t* assigned) {
 }
 
 bool ot_prune(Ctx& c) {
+    // the deleted clauses join the flagged ones in the drop bytes; the lists
+    // are filtered when they move (ot_update), after any compaction
     PFG_LAUNCH(K_FILL, mark_dead_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.ncls, c.cnew);
-    PFG_LAUNCH(K_FILL, ot_filter_w_k, grid_for((c.nlist + 31) / 32 * 32, 256), 256, 0, c.s, c.nlist, c.ot_off,
-               c.ot_size, c.hist, c.ot_ids, c.elim, c.cnew);
     return cuda_ok(c, cudaGetLastError(), "ot_prune");
 }
 
@@ -461,8 +502,8 @@ bool ot_update(Ctx& c) {
     if (c.numLiterals > 0xFFFFFFF0ull) { c.simpstate = PFG_OTALLOC_FAIL; c.err = "occurrence table exceeds 2^32 entries"; return false; }
     c.prof.bytes[K_HIST] += 4 * (c.numLiterals + c.numClauses);
     c.prof.bytes[K_FILL] += 4 * (c.numLiterals + c.numClauses) + 4 * c.numLiterals;
-    // sizes: the kept entries plus the occurrences of the flagged clauses
-    cudaMemcpyAsync(c.hist, c.ot_size, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+    // room: the old entries of every list plus the occurrences of the flagged clauses
+    PFG_LAUNCH(K_HIST, hist_init_k, grid_for(nl, 256), 256, 0, c.s, nl, c.ot_size, c.elim, c.hist);
     PFG_LAUNCH(K_HIST, new_hist_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.cnew, c.hist);
     if (!ensure_tmp(c, scan_temp_bytes(nl))) return false;
     exclusive_scan_u32(c.hist, c.ot_off2, nl, 0u, c.ot_off2 + nl, c.tmp, c.s);
@@ -476,14 +517,16 @@ bool ot_update(Ctx& c) {
         if (!dalloc_t(c, &c.ot_ids2, cap)) { c.simpstate = PFG_OTALLOC_FAIL; c.ot_cap2 = 0; return false; }
         c.ot_cap2 = cap;
     }
-    // kept entries move to the new offsets (renumbered after a compaction);
-    // the flagged clauses are appended behind them
-    PFG_LAUNCH(K_FILL, move_w_k, grid_for((nl + 31) / 32 * 32, 256), 256, 0, c.s, nl, c.ot_off, c.ot_size, c.ot_ids,
-               c.ot_off2, c.ot_ids2, c.cmap, c.ot_fill);
+    // kept entries move to the new offsets (renumbered after a compaction, whose
+    // drop bytes are still on the old ids); the flagged clauses are appended
+    // behind them
+    PFG_LAUNCH(K_FILL, prune_move_w_k, grid_for((nl + 31) / 32 * 32, 256), 256, 0, c.s, nl, c.ot_off, c.ot_size,
+               c.hist, c.ot_ids, c.elim, c.cdrop ? c.cdrop : c.cnew, c.ot_off2, c.ot_ids2, c.cmap, c.ot_fill);
     PFG_LAUNCH(K_FILL, fill_new_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.cnew, c.ot_fill,
                c.ot_ids2);
-    cudaMemcpyAsync(c.ot_size, c.hist, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
     cudaMemsetAsync(c.cnew, 0, c.ncls, c.s);
+    dfree(c, c.cdrop);
+    c.cdrop = nullptr;
     std::swap(c.ot_ids, c.ot_ids2);
     std::swap(c.ot_cap, c.ot_cap2);
     std::swap(c.ot_off, c.ot_off2);
