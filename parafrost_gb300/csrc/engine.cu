@@ -376,24 +376,22 @@ __global__ void gathered_sizes_k(const ClsHdr* hdr, const uint32_t* ids, uint64_
         sz[j] = hdr[ids[j]].size;
 }
 
-// warp per clause; literals back to the instance's own numbering
-__global__ void gathered_pack_k(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ids, uint64_t n,
-                                const unsigned long long* loff, const uint32_t* vinst, const uint32_t* voff,
+// thread per clause (clauses are short, and neighbouring threads read and
+// write neighbouring ranges: the ids are sorted by instance, stably);
+// literals back to the instance's own numbering
+__global__ void gathered_pack_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits,
+                                const uint32_t* __restrict__ ids, const uint32_t* __restrict__ inst, uint64_t n,
+                                const unsigned long long* __restrict__ loff, const uint32_t* __restrict__ voff,
                                 uint32_t* olits, uint8_t* olearnt, uint32_t* olbd, uint8_t* ousage) {
-    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const unsigned lane = threadIdx.x & 31u;
-    for (uint64_t j = warp; j < n; j += nwarps) {
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
         const ClsHdr h = hdr[ids[j]];
         const uint32_t* l = lits + h.off;
-        const uint32_t shift = 2u * voff[vinst[ABSV(l[0])]];
-        const unsigned long long o = loff[j];
-        for (uint32_t k = lane; k < h.size; k += 32) olits[o + k] = l[k] - shift;
-        if (lane == 0) {
-            olearnt[j] = m_learnt(h.meta);
-            olbd[j] = m_lbd(h.meta);
-            ousage[j] = (uint8_t)m_usage(h.meta);
-        }
+        const uint32_t shift = 2u * voff[inst[j]];
+        uint32_t* out = olits + loff[j];
+        for (uint32_t k = 0; k < h.size; k++) out[k] = l[k] - shift;
+        olearnt[j] = m_learnt(h.meta);
+        olbd[j] = m_lbd(h.meta);
+        ousage[j] = (uint8_t)m_usage(h.meta);
     }
 }
 
@@ -418,6 +416,7 @@ void free_all(pfg_ctx* o) {
     fresh.o = c.o;
     fresh.device = c.device;
     fresh.s = c.s;
+    fresh.s_copy = c.s_copy; fresh.ev_copy = c.ev_copy;
     fresh.ev_begin = c.ev_begin; fresh.ev_end = c.ev_end; fresh.ev_a = c.ev_a; fresh.ev_b = c.ev_b;
     fresh.dc = nullptr; fresh.hc = c.hc;
     fresh.launches = c.launches;
@@ -1376,8 +1375,8 @@ int build_cache(Ctx& c) {
     if (C) {
         PFG_LAUNCH(K_DOWNLOAD, gathered_sizes_k, grid_for(C, 256), 256, 0, c.s, c.hdr, ids, C, c.pk_roff);
         exclusive_scan_u64(c.pk_roff, c.pk_roff, C, 0ull, c.pk_roff + C, c.tmp, c.s);
-        PFG_LAUNCH(K_DOWNLOAD, gathered_pack_k, grid_for(C * 32, 256), 256, 0, c.s, c.hdr, c.lits, ids, C,
-                   c.pk_roff, c.vinst, c.di.voff, c.pk_lits, c.pk_learnt, c.pk_lbd, c.pk_usage);
+        PFG_LAUNCH(K_DOWNLOAD, gathered_pack_k, grid_for(C, 256), 256, 0, c.s, c.hdr, c.lits, ids, keys, C,
+                   c.pk_roff, c.di.voff, c.pk_lits, c.pk_learnt, c.pk_lbd, c.pk_usage);
         cudaMemcpyAsync(bases, c.cache_lit_base.data(), ((size_t)n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, c.s);
         PFG_LAUNCH(K_DOWNLOAD, relative_off_k, grid_for(C, 256), 256, 0, c.s, keys, C, bases, c.pk_roff);
     }
@@ -1571,6 +1570,26 @@ extern "C" int pfg_batch_download_all(pfg_ctx* o, uint32_t* lits, uint64_t* cls_
     if (rc != PFG_OK) return finish(c, nullptr, base_launches, rc);
     const uint32_t n = c.ninst;
     const uint64_t C = c.cache_cls_base[n], L = c.cache_lit_base[n];
+    // the packed clauses are complete here: their copies go to the host on a
+    // second stream, beside the write-back kernels below
+    cudaStream_t cs = c.s;
+    if (!c.s_copy && cudaStreamCreateWithFlags(&c.s_copy, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        c.s_copy = nullptr;
+    }
+    if (c.s_copy && !c.ev_copy && cudaEventCreateWithFlags(&c.ev_copy, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        c.ev_copy = nullptr;
+    }
+    if (c.s_copy && c.ev_copy) {
+        cudaEventRecord(c.ev_copy, c.s);
+        cudaStreamWaitEvent(c.s_copy, c.ev_copy, 0);
+        cs = c.s_copy;
+    }
+    if (lits && L) cudaMemcpyAsync(lits, c.pk_lits, L * sizeof(uint32_t), cudaMemcpyDeviceToHost, cs);
+    if (cls_learnt && C) cudaMemcpyAsync(cls_learnt, c.pk_learnt, C, cudaMemcpyDeviceToHost, cs);
+    if (cls_lbd && C) cudaMemcpyAsync(cls_lbd, c.pk_lbd, C * sizeof(uint32_t), cudaMemcpyDeviceToHost, cs);
+    if (cls_usage && C) cudaMemcpyAsync(cls_usage, c.pk_usage, C, cudaMemcpyDeviceToHost, cs);
     // output starts of every instance: eliminated, units, stack
     std::vector<unsigned long long> hb(6 * ((size_t)n + 1), 0);
     unsigned long long* eb = hb.data();
@@ -1597,7 +1616,10 @@ extern "C" int pfg_batch_download_all(pfg_ctx* o, uint32_t* lits, uint64_t* cls_
     bool ok = dalloc_t(c, &dbases, hb.size() + (size_t)n + 1) && dalloc_t(c, &dshift, (size_t)n + 1) &&
               dalloc_t(c, &doff, C + n + 1) && dalloc_t(c, &delim, eb[n] + 1) && dalloc_t(c, &dunits, ub[n] + 1) &&
               dalloc_t(c, &dstack, sb[n] + 1);
-    auto release = [&]() { dfree(c, dbases); dfree(c, dshift); dfree(c, doff); dfree(c, delim); dfree(c, dunits); dfree(c, dstack); };
+    auto release = [&]() {
+        if (cs != c.s) cudaStreamSynchronize(cs);    // no copy into the caller's buffers outlives the call
+        dfree(c, dbases); dfree(c, dshift); dfree(c, doff); dfree(c, delim); dfree(c, dunits); dfree(c, dstack);
+    };
     if (!ok) { release(); return finish(c, nullptr, base_launches, PFG_CNFALLOC_FAIL); }
     cudaMemcpyAsync(dbases, hb.data(), hb.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, c.s);
     cudaMemcpyAsync(dbases + hb.size(), c.cache_lit_base.data(), ((size_t)n + 1) * sizeof(unsigned long long),
@@ -1641,15 +1663,12 @@ extern "C" int pfg_batch_download_all(pfg_ctx* o, uint32_t* lits, uint64_t* cls_
     if (stack && sb[n])
         PFG_LAUNCH(K_DOWNLOAD, regions_all_k, grid_for(sb[n], 256), 256, 0, c.s, c.stack, d_ssrc, d_sb,
                    (const uint32_t*)nullptr, n, sb[n], dstack);
-    if (lits && L) cudaMemcpyAsync(lits, c.pk_lits, L * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     if (cls_off) cudaMemcpyAsync(cls_off, doff, (C + n) * sizeof(uint64_t), cudaMemcpyDeviceToHost, c.s);
-    if (cls_learnt && C) cudaMemcpyAsync(cls_learnt, c.pk_learnt, C, cudaMemcpyDeviceToHost, c.s);
-    if (cls_lbd && C) cudaMemcpyAsync(cls_lbd, c.pk_lbd, C * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    if (cls_usage && C) cudaMemcpyAsync(cls_usage, c.pk_usage, C, cudaMemcpyDeviceToHost, c.s);
     if (eliminated) cudaMemcpyAsync(eliminated, delim, eb[n], cudaMemcpyDeviceToHost, c.s);
     if (units && ub[n]) cudaMemcpyAsync(units, units_sorted, ub[n] * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     if (stack && sb[n]) cudaMemcpyAsync(stack, dstack, sb[n] * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    const bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "batch download");
+    bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "batch download");
+    if (cs != c.s) synced = cuda_ok(c, cudaStreamSynchronize(cs), "batch download copies") && synced;
     release();
     dfree(c, uk1); dfree(c, uv0); dfree(c, uv1);
     if (!synced) return finish(c, nullptr, base_launches, PFG_CUDA_ERROR);
@@ -1696,6 +1715,8 @@ extern "C" void pfg_destroy(pfg_ctx* o) {
     for (auto& kv : o->sizes) ptrs.push_back(kv.first);
     for (void* p : ptrs) cudaFreeAsync(p, c.s);
     if (c.s) { cudaStreamSynchronize(c.s); cudaStreamDestroy(c.s); }
+    if (c.s_copy) { cudaStreamSynchronize(c.s_copy); cudaStreamDestroy(c.s_copy); }
+    if (c.ev_copy) cudaEventDestroy(c.ev_copy);
     if (c.ev_begin) cudaEventDestroy(c.ev_begin);
     if (c.ev_end) cudaEventDestroy(c.ev_end);
     if (c.ev_a) cudaEventDestroy(c.ev_a);

@@ -81,6 +81,8 @@ struct Ctx {
     pfg_options o{};
     int device = 0;
     cudaStream_t s = nullptr;
+    cudaStream_t s_copy = nullptr;   // write-back copies that overlap the last write-back kernels
+    cudaEvent_t ev_copy = nullptr;
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr, ev_a = nullptr, ev_b = nullptr;
     std::string err;
     uint64_t launches = 0;
