@@ -1540,6 +1540,25 @@ __global__ void inst_add_k(const unsigned long long* cslot, const unsigned long 
 
 }  // namespace
 
+// A persistent grid for a warp kernel: the blocks the GPU holds at once (from
+// the kernel's occupancy), no more than the variables need.
+template <typename Kern>
+static unsigned resident_blocks(Kern kern, unsigned threads) {
+    int nb = 0, sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) { cudaGetLastError(); sms = 152; }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, (int)threads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        nb = 1;
+    }
+    return (unsigned)std::max(1, nb) * (unsigned)std::max(1, sms);
+}
+
+static unsigned warp_grid(unsigned resident, uint32_t nvars) {
+    const uint64_t need = ((uint64_t)nvars + WS_WARPS - 1) / WS_WARPS;
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(need, resident));
+}
+
 bool sub_pass(Ctx& c) {
     const uint32_t E = c.nve;
     if (!E) return true;
@@ -1547,8 +1566,10 @@ bool sub_pass(Ctx& c) {
     const EK k = make_ek(c);
     cudaMemsetAsync(&c.dc->nbig_sub, 0, sizeof(uint32_t), c.s);
     // warp per variable on the shared-memory stage; larger variables by one thread each
-    PFG_LAUNCH(K_SUB, subw_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.veset, E,
-               c.work_b, &c.dc->nbig_sub);
+    static const unsigned sub_res = resident_blocks(subw_k, WS_WARPS * 32);
+    cudaMemsetAsync(&c.dc->steal[0], 0, sizeof(uint32_t), c.s);
+    PFG_LAUNCH(K_SUB, subw_k, warp_grid(sub_res, E), WS_WARPS * 32, 0, c.s, k, c.veset, E, c.work_b, &c.dc->nbig_sub,
+               &c.dc->steal[0]);
     PFG_LAUNCH(K_BIGVAR, sub_k, grid_for(E, 64, 8), 64, 0, c.s, k, c.veset, E, c.work_b, &c.dc->nbig_sub);
     return !c.o.proof_en || proof_collect(c);
 }
@@ -1562,8 +1583,10 @@ bool ve_pass(Ctx& c) {
     for (uint32_t i = 0; i < c.ninst; i++) any_vc |= c.ih[i].mode == 1 && c.ih[i].varcore_on;
     cudaMemsetAsync(&c.dc->nwork, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->nbig_ve1, 0, 2 * sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_VE1, ve1w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k, c.veset, E,
-               c.type, c.ucnt, c.rpos, c.rref, c.work, &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
+    static const unsigned ve1_res = resident_blocks(ve1w_k, WS_WARPS * 32);
+    cudaMemsetAsync(&c.dc->steal[1], 0, sizeof(uint32_t), c.s);
+    PFG_LAUNCH(K_VE1, ve1w_k, warp_grid(ve1_res, E), WS_WARPS * 32, 0, c.s, k, c.veset, E, c.type, c.ucnt, c.rpos,
+               c.rref, c.work, &c.dc->nwork, c.work_b, &c.dc->nbig_ve1, &c.dc->steal[1]);
     PFG_LAUNCH(K_BIGVAR, ve1a_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.veset, E, c.type, c.ucnt, c.rpos, c.rref, c.work,
                &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
     if (any_vc)   // one warp per deferred variable; the grid walks the device-side count
@@ -1590,8 +1613,10 @@ bool ve_pass(Ctx& c) {
         if (!proof_prepare(c, c.hc->pf_need)) return false;
         k3 = make_ek(c);
     }
-    PFG_LAUNCH(K_VE3, ve3w_k, grid_for((uint64_t)E * 32, WS_WARPS * 32, 16), WS_WARPS * 32, 0, c.s, k3, c.veset, E,
-               c.type, c.ucnt, c.rslot, c.rlit, c.winv, c.eligible_b, &c.dc->nbig_ve3);
+    static const unsigned ve3_res = resident_blocks(ve3w_k, WS_WARPS * 32);
+    cudaMemsetAsync(&c.dc->steal[2], 0, sizeof(uint32_t), c.s);
+    PFG_LAUNCH(K_VE3, ve3w_k, warp_grid(ve3_res, E), WS_WARPS * 32, 0, c.s, k3, c.veset, E, c.type, c.ucnt, c.rslot,
+               c.rlit, c.winv, c.eligible_b, &c.dc->nbig_ve3, &c.dc->steal[2]);
     PFG_LAUNCH(K_BIGVAR, ve3_k, grid_for(E, 128, 8), 128, 0, c.s, k3, c.veset, E, c.type, c.ucnt, c.rslot, c.rlit,
                c.winv, c.eligible_b, &c.dc->nbig_ve3);
     if (c.o.proof_en && !proof_collect(c)) return false;

@@ -71,6 +71,16 @@ PFG_D void ws_prefetch_lists(const EK& k, const NextLists& nl, unsigned lane) {
     }
 }
 
+// Work stealing: the grid is as large as the GPU holds at once and every warp
+// draws its next variable from one counter (lane 0 draws, the warp reads it by
+// shuffle), so a warp whose variables have long lists does not leave the rest
+// of its fixed share to the end of the launch.
+PFG_D uint32_t ws_ticket(uint32_t* ctr, unsigned lane) {
+    uint32_t t = 0;
+    if (lane == 0) t = atomicAdd(ctr, 1u);
+    return __shfl_sync(0xFFFFFFFFu, t, 0);
+}
+
 // Loads both lists of x into the stage; false if they do not fit.
 PFG_D bool ws_stage(const EK& k, WS& w, uint32_t p, uint32_t n, unsigned lane) {
     const uint32_t np = OLs(k, p), nn = OLs(k, n), nc = np + nn;
@@ -843,15 +853,16 @@ PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
 __global__ void __launch_bounds__(WS_WARPS * 32) ve1w_k(EK k, const uint32_t* elected, uint32_t nelected,
                                                         uint32_t* type, uint32_t* ucnt, unsigned long long* rpos,
                                                         unsigned long long* rref, uint32_t* dlist, uint32_t* dcount,
-                                                        uint32_t* big, uint32_t* nbig) {
+                                                        uint32_t* big, uint32_t* nbig, uint32_t* steal) {
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
-    const uint32_t stride = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected; q += stride) {
+    uint32_t qn;
+    for (uint32_t q = ws_ticket(steal, lane); q < nelected; q = qn) {
+        qn = ws_ticket(steal, lane);     // drawn ahead: its lists are prefetched while this one runs
         const uint32_t tid = q;
         const uint32_t x = elected[tid];
-        const NextLists nl = ws_next_lists(k, elected, q + stride, nelected);
+        const NextLists nl = ws_next_lists(k, elected, qn, nelected);
         if (!ws_stage(k, w, 2 * x, 2 * x + 1, lane)) {
             if (lane == 0) big[atomicAdd(nbig, 1u)] = tid;
             continue;
@@ -867,12 +878,11 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
                                                         const uint32_t* type, const uint32_t* ucnt,
                                                         const unsigned long long* rslot,
                                                         const unsigned long long* rlit, const uint8_t* fits,
-                                                        uint32_t* big, uint32_t* nbig) {
+                                                        uint32_t* big, uint32_t* nbig, uint32_t* steal) {
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected;
-         q += (gridDim.x * blockDim.x) >> 5) {
+    for (uint32_t q = ws_ticket(steal, lane); q < nelected; q = ws_ticket(steal, lane)) {
         const uint32_t tid = q;
         const uint32_t x = elected[tid];
         const uint32_t xinfo = type[tid];
@@ -1165,12 +1175,11 @@ PFG_D void ws_sub_screen(WS& w, const Side& P, const Side& N, unsigned lane) {
 }
 
 __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* elected, uint32_t nelected,
-                                                        uint32_t* big, uint32_t* nbig) {
+                                                        uint32_t* big, uint32_t* nbig, uint32_t* steal) {
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nelected;
-         q += (gridDim.x * blockDim.x) >> 5) {
+    for (uint32_t q = ws_ticket(steal, lane); q < nelected; q = ws_ticket(steal, lane)) {
         const uint32_t e = q;
         const uint32_t x = elected[e];
         const uint32_t p = 2 * x, n = p | 1;
