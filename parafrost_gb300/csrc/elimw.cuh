@@ -75,6 +75,8 @@ PFG_D void ws_prefetch_lists(const EK& k, const NextLists& nl, unsigned lane) {
 // draws its next variable from one counter (lane 0 draws, the warp reads it by
 // shuffle), so a warp whose variables have long lists does not leave the rest
 // of its fixed share to the end of the launch.
+constexpr uint32_t VE3_CHUNK = 16;
+
 PFG_D uint32_t ws_ticket(uint32_t* ctr, unsigned lane) {
     uint32_t t = 0;
     if (lane == 0) t = atomicAdd(ctr, 1u);
@@ -882,7 +884,11 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
-    for (uint32_t q = ws_ticket(steal, lane); q < nelected; q = ws_ticket(steal, lane)) {
+    // tickets of VE3_CHUNK variables: most elected variables emit nothing and
+    // are passed over at once, so one draw per variable would queue on the counter
+    const uint32_t nchunks = (nelected + VE3_CHUNK - 1) / VE3_CHUNK;
+    for (uint32_t t = ws_ticket(steal, lane); t < nchunks; t = ws_ticket(steal, lane))
+    for (uint32_t q = t * VE3_CHUNK, qe = min(q + VE3_CHUNK, nelected); q < qe; q++) {
         const uint32_t tid = q;
         const uint32_t x = elected[tid];
         const uint32_t xinfo = type[tid];
