@@ -20,6 +20,10 @@ namespace pfg {
 namespace {
 
 constexpr uint8_t MIS_NONE = 0, MIS_UNDECIDED = 1, MIS_ELECTED = 2, MIS_FROZEN = 3;
+// rank[v] is v's place in the (score, var) order while v is undecided and
+// NO_RANK otherwise (not a candidate, elected or frozen), so "an undecided
+// neighbour of smaller rank" is one load per neighbour: rank[u] < r
+constexpr uint32_t NO_RANK = 0xFFFFFFFFu;
 
 __global__ void scores_k(const uint32_t* hist, uint32_t V, uint32_t* scores, uint32_t* keys, uint32_t* vals,
                          DevCounters* dc) {
@@ -52,7 +56,6 @@ __global__ void mis_init_k(const uint32_t* eligible, uint32_t V, uint32_t* rank,
                            const uint32_t* vinst, const uint8_t* active) {
     for (uint32_t ei = blockIdx.x * blockDim.x + threadIdx.x; ei < V; ei += gridDim.x * blockDim.x) {
         const uint32_t v = eligible[ei];
-        rank[v] = ei;
         uint8_t st = MIS_NONE;
         if (active[vinst[v]] && !vstate[v] && !(assumed && assumed[v])) {
             const uint32_t p = 2 * v, n = p | 1;
@@ -61,18 +64,19 @@ __global__ void mis_init_k(const uint32_t* eligible, uint32_t V, uint32_t* rank,
                 st = MIS_UNDECIDED;
         }
         mstate[v] = st;
+        rank[v] = st == MIS_UNDECIDED ? ei : NO_RANK;
         cand[ei] = st == MIS_UNDECIDED;
     }
 }
 
 // The first MIS_HEAD literals of a clause are loaded together, then their
-// states, then the ranks of the undecided ones: independent loads in flight
-// instead of one dependent chain per literal (most clauses are that short).
+// ranks: independent loads in flight instead of one dependent chain per
+// literal (most clauses are that short). The candidate's own rank is r, never
+// below it.
 constexpr uint32_t MIS_HEAD = 4;
 
 PFG_D bool blocked(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
-                   const uint32_t* ot_ids, uint32_t lit, uint32_t cand, uint32_t r, const uint32_t* rank,
-                   const uint8_t* mstate) {
+                   const uint32_t* ot_ids, uint32_t lit, uint32_t r, const uint32_t* rank) {
     const uint32_t o = ot_off[lit], n = ot_size[lit];
     ClsHdr next = n ? hdr[ot_ids[o]] : ClsHdr{0, 0, 0, 0};
     for (uint32_t i = 0; i < n; i++) {
@@ -81,24 +85,23 @@ PFG_D bool blocked(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_o
         if (m_deleted(h.meta)) continue;
         const uint32_t* l = lits + h.off;
         uint32_t u[MIS_HEAD];
-        uint8_t st[MIS_HEAD];
+        uint32_t rk[MIS_HEAD];
 #pragma unroll
-        for (uint32_t q = 0; q < MIS_HEAD; q++) u[q] = q < h.size ? ABSV(l[q]) : cand;
+        for (uint32_t q = 0; q < MIS_HEAD; q++) u[q] = q < h.size ? ABSV(l[q]) : 0u;
 #pragma unroll
-        for (uint32_t q = 0; q < MIS_HEAD; q++) st[q] = u[q] != cand ? mstate[u[q]] : MIS_NONE;
+        for (uint32_t q = 0; q < MIS_HEAD; q++) rk[q] = q < h.size ? rank[u[q]] : NO_RANK;
 #pragma unroll
         for (uint32_t q = 0; q < MIS_HEAD; q++)
-            if (st[q] == MIS_UNDECIDED && rank[u[q]] < r) return true;
-        for (uint32_t k = MIS_HEAD; k < h.size; k++) {
-            const uint32_t v = ABSV(l[k]);
-            if (v != cand && mstate[v] == MIS_UNDECIDED && rank[v] < r) return true;
-        }
+            if (rk[q] < r) return true;
+        for (uint32_t k = MIS_HEAD; k < h.size; k++)
+            if (rank[ABSV(l[k])] < r) return true;
     }
     return false;
 }
 
 PFG_D void freeze_list(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
-                       const uint32_t* ot_ids, uint32_t lit, uint32_t cand, uint8_t* frozen, uint8_t* mstate) {
+                       const uint32_t* ot_ids, uint32_t lit, uint32_t cand, uint8_t* frozen, uint8_t* mstate,
+                       uint32_t* rank) {
     const uint32_t o = ot_off[lit], n = ot_size[lit];
     ClsHdr next = n ? hdr[ot_ids[o]] : ClsHdr{0, 0, 0, 0};
     for (uint32_t i = 0; i < n; i++) {
@@ -116,13 +119,13 @@ PFG_D void freeze_list(const ClsHdr* hdr, const uint32_t* lits, const uint32_t* 
         for (uint32_t q = 0; q < MIS_HEAD; q++) {
             if (u[q] == cand) continue;
             frozen[u[q]] = 1;
-            if (st[q] == MIS_UNDECIDED) mstate[u[q]] = MIS_FROZEN;
+            if (st[q] == MIS_UNDECIDED) { mstate[u[q]] = MIS_FROZEN; rank[u[q]] = NO_RANK; }
         }
         for (uint32_t k = MIS_HEAD; k < h.size; k++) {
             const uint32_t v = ABSV(l[k]);
             if (v != cand) {
                 frozen[v] = 1;
-                if (mstate[v] == MIS_UNDECIDED) mstate[v] = MIS_FROZEN;
+                if (mstate[v] == MIS_UNDECIDED) { mstate[v] = MIS_FROZEN; rank[v] = NO_RANK; }
             }
         }
     }
@@ -138,8 +141,8 @@ __global__ void mis_win3_k(uint32_t V, const ClsHdr* hdr, const uint32_t* lits, 
         if (mstate[v] != MIS_UNDECIDED) continue;
         cnt++;
         const uint32_t r = rank[v];
-        winv[v] = !(blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, v, r, rank, mstate) ||
-                    blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v + 1, v, r, rank, mstate));
+        winv[v] = !(blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, r, rank) ||
+                    blocked(hdr, lits, ot_off, ot_size, ot_ids, 2 * v + 1, r, rank));
     }
     for (int d = 16; d > 0; d >>= 1) cnt += __shfl_down_sync(0xFFFFFFFFu, cnt, d);
     if ((threadIdx.x & 31u) == 0 && cnt) atomicAdd(undecided, cnt);
@@ -152,16 +155,13 @@ __global__ void mis_win3_k(uint32_t V, const ClsHdr* hdr, const uint32_t* lits, 
 // clause gets none); the candidates then read one word per occurrence instead
 // of the clause's header, literals and their states.
 __global__ void clause_min_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
-                             const uint32_t* __restrict__ rank, const uint8_t* __restrict__ mstate, uint32_t* cmin) {
+                             const uint32_t* __restrict__ rank, uint32_t* cmin) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         const ClsHdr h = hdr[c];
         uint32_t m = 0xFFFFFFFFu;
         if (!m_deleted(h.meta)) {
             const uint32_t* l = lits + h.off;
-            for (uint32_t k = 0; k < h.size; k++) {
-                const uint32_t v = ABSV(l[k]);
-                if (mstate[v] == MIS_UNDECIDED) m = min(m, rank[v]);
-            }
+            for (uint32_t k = 0; k < h.size; k++) m = min(m, rank[ABSV(l[k])]);
         }
         cmin[c] = m;
     }
@@ -198,7 +198,7 @@ __global__ void mis_win_min_k(uint32_t V, const uint32_t* ot_off, const uint32_t
 // is a winner, so the freezing never meets an election.
 __global__ void mis_apply_min_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
                                 const uint32_t* __restrict__ cmin, const uint32_t* __restrict__ eligible,
-                                const uint8_t* __restrict__ winv, uint8_t* frozen, uint8_t* mstate) {
+                                const uint8_t* __restrict__ winv, uint8_t* frozen, uint8_t* mstate, uint32_t* rank) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t m = cmin[c];
         if (m == 0xFFFFFFFFu) continue;
@@ -210,25 +210,26 @@ __global__ void mis_apply_min_k(const ClsHdr* __restrict__ hdr, const uint32_t* 
             const uint32_t v = ABSV(l[k]);
             if (v == u) continue;
             frozen[v] = 1;
-            if (mstate[v] == MIS_UNDECIDED) mstate[v] = MIS_FROZEN;
+            if (mstate[v] == MIS_UNDECIDED) { mstate[v] = MIS_FROZEN; rank[v] = NO_RANK; }
         }
     }
 }
 
 __global__ void mis_elect_k(uint32_t V, const uint8_t* winv, uint32_t r, uint32_t* mround, uint8_t* mstate,
-                            const uint32_t* undecided) {
+                            uint32_t* rank, const uint32_t* undecided) {
     if (*undecided == 0) return;
     for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
         if (mstate[v] != MIS_UNDECIDED || !winv[v]) continue;
         mstate[v] = MIS_ELECTED;
+        rank[v] = NO_RANK;
         mround[v] = r;
     }
 }
 
 __global__ void mis_apply3_k(uint32_t V, const uint8_t* winv, uint32_t r, uint32_t* mround, const ClsHdr* hdr,
                              const uint32_t* lits, const uint32_t* ot_off, const uint32_t* ot_size,
-                             const uint32_t* ot_ids, uint8_t* frozen, uint8_t* mstate, const uint32_t* undecided,
-                             uint32_t* done) {
+                             const uint32_t* ot_ids, uint8_t* frozen, uint8_t* mstate, uint32_t* rank,
+                             const uint32_t* undecided, uint32_t* done) {
     if (*undecided == 0) {   // nothing was undecided: no winner, and the rounds left have nothing to do
         if (blockIdx.x == 0 && threadIdx.x == 0) *done = 1;
         return;
@@ -236,9 +237,10 @@ __global__ void mis_apply3_k(uint32_t V, const uint8_t* winv, uint32_t r, uint32
     for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
         if (mstate[v] != MIS_UNDECIDED || !winv[v]) continue;
         mstate[v] = MIS_ELECTED;
+        rank[v] = NO_RANK;
         mround[v] = r;
-        freeze_list(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, v, frozen, mstate);
-        freeze_list(hdr, lits, ot_off, ot_size, ot_ids, 2 * v + 1, v, frozen, mstate);
+        freeze_list(hdr, lits, ot_off, ot_size, ot_ids, 2 * v, v, frozen, mstate, rank);
+        freeze_list(hdr, lits, ot_off, ot_size, ot_ids, 2 * v + 1, v, frozen, mstate, rank);
     }
 }
 
@@ -406,19 +408,20 @@ bool lcve(Ctx& c) {
                 cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
                 if (r == 0 && ensure_tmp_u32(c, c.ncls + 1)) {   // first round: every candidate undecided
                     PFG_LAUNCH(K_MIS_WIN, clause_min_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls,
-                               c.rank, c.mstate, c.tmp_u32);
+                               c.rank, c.tmp_u32);
                     PFG_LAUNCH(K_MIS_WIN, mis_win_min_k, grid_for(V, 128), 128, 0, c.s, V, c.ot_off, c.ot_size,
                                c.ot_ids, c.tmp_u32, c.rank, c.mstate, c.winv, &c.dc->nwin);
                     PFG_LAUNCH(K_MIS_APPLY, mis_apply_min_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits,
-                               c.ncls, c.tmp_u32, c.eligible, c.winv, c.frozen, c.mstate);
+                               c.ncls, c.tmp_u32, c.eligible, c.winv, c.frozen, c.mstate, c.rank);
                     PFG_LAUNCH(K_MIS_APPLY, mis_elect_k, grid_for(V, 256), 256, 0, c.s, V, c.winv, r, mround, c.mstate,
-                               &c.dc->nwin);
+                               c.rank, &c.dc->nwin);
                     continue;
                 }
                 PFG_LAUNCH(K_MIS_WIN, mis_win3_k, grid_for(V, 128), 128, 0, c.s, V, c.hdr, c.lits, c.ot_off,
                            c.ot_size, c.ot_ids, c.rank, c.mstate, c.winv, &c.dc->nwin, &c.dc->mis_done);
                 PFG_LAUNCH(K_MIS_APPLY, mis_apply3_k, grid_for(V, 128), 128, 0, c.s, V, c.winv, r, mround, c.hdr,
-                           c.lits, c.ot_off, c.ot_size, c.ot_ids, c.frozen, c.mstate, &c.dc->nwin, &c.dc->mis_done);
+                           c.lits, c.ot_off, c.ot_size, c.ot_ids, c.frozen, c.mstate, c.rank, &c.dc->nwin,
+                           &c.dc->mis_done);
             }
             sync_counters(c);
             if (!c.err.empty()) return false;
