@@ -175,16 +175,19 @@ PFG_D bool blocked_min(const uint32_t* ot_off, const uint32_t* ot_size, const ui
     return false;
 }
 
+// the outcome is also kept by rank (winr), the index a clause minimum holds
 __global__ void mis_win_min_k(uint32_t V, const uint32_t* ot_off, const uint32_t* ot_size, const uint32_t* ot_ids,
                               const uint32_t* cmin, const uint32_t* rank, const uint8_t* mstate, uint8_t* winv,
-                              uint32_t* undecided) {
+                              uint8_t* winr, uint32_t* undecided) {
     uint32_t cnt = 0;
     for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
         if (mstate[v] != MIS_UNDECIDED) continue;
         cnt++;
         const uint32_t r = rank[v];
-        winv[v] = !(blocked_min(ot_off, ot_size, ot_ids, cmin, 2 * v, r) ||
-                    blocked_min(ot_off, ot_size, ot_ids, cmin, 2 * v + 1, r));
+        const bool win = !(blocked_min(ot_off, ot_size, ot_ids, cmin, 2 * v, r) ||
+                           blocked_min(ot_off, ot_size, ot_ids, cmin, 2 * v + 1, r));
+        winv[v] = win;
+        winr[r] = win;
     }
     for (int d = 16; d > 0; d >>= 1) cnt += __shfl_down_sync(0xFFFFFFFFu, cnt, d);
     if ((threadIdx.x & 31u) == 0 && cnt) atomicAdd(undecided, cnt);
@@ -198,12 +201,11 @@ __global__ void mis_win_min_k(uint32_t V, const uint32_t* ot_off, const uint32_t
 // is a winner, so the freezing never meets an election.
 __global__ void mis_apply_min_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
                                 const uint32_t* __restrict__ cmin, const uint32_t* __restrict__ eligible,
-                                const uint8_t* __restrict__ winv, uint8_t* frozen, uint8_t* mstate, uint32_t* rank) {
+                                const uint8_t* __restrict__ winr, uint8_t* frozen, uint8_t* mstate, uint32_t* rank) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t m = cmin[c];
-        if (m == 0xFFFFFFFFu) continue;
+        if (m == NO_RANK || !winr[m]) continue;
         const uint32_t u = eligible[m];
-        if (!winv[u]) continue;
         const ClsHdr h = hdr[c];
         const uint32_t* l = lits + h.off;
         for (uint32_t k = 0; k < h.size; k++) {
@@ -409,10 +411,11 @@ bool lcve(Ctx& c) {
                 if (r == 0 && ensure_tmp_u32(c, c.ncls + 1)) {   // first round: every candidate undecided
                     PFG_LAUNCH(K_MIS_WIN, clause_min_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls,
                                c.rank, c.tmp_u32);
+                    // flag8 (the candidate flags, consumed above) holds the outcomes by rank
                     PFG_LAUNCH(K_MIS_WIN, mis_win_min_k, grid_for(V, 128), 128, 0, c.s, V, c.ot_off, c.ot_size,
-                               c.ot_ids, c.tmp_u32, c.rank, c.mstate, c.winv, &c.dc->nwin);
+                               c.ot_ids, c.tmp_u32, c.rank, c.mstate, c.winv, c.flag8, &c.dc->nwin);
                     PFG_LAUNCH(K_MIS_APPLY, mis_apply_min_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits,
-                               c.ncls, c.tmp_u32, c.eligible, c.winv, c.frozen, c.mstate, c.rank);
+                               c.ncls, c.tmp_u32, c.eligible, c.flag8, c.frozen, c.mstate, c.rank);
                     PFG_LAUNCH(K_MIS_APPLY, mis_elect_k, grid_for(V, 256), 256, 0, c.s, V, c.winv, r, mround, c.mstate,
                                c.rank, &c.dc->nwin);
                     continue;
