@@ -492,6 +492,8 @@ def run_gpu_batch(a, world, rank, local):
     cls_in = sum(int(c.num_clauses) for c in cnfs)
     sim = pg.Simplifier()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    # launch shapes picked by the engine's autotuner on this batch (untimed)
+    tuning = sim.autotune(cnfs) if not a.no_autotune else sim.tuning
     for _ in range(a.warmup):
         sim.upload_batch(cnfs)
         sim.run()
@@ -595,6 +597,7 @@ def run_gpu_batch(a, world, rank, local):
                    "literals_in": int(sum(int(c.num_literals) for c in cnfs)),
                    "clauses_out": int(last.clauses_out), "max_rounds": int(last.rounds),
                    "options": "reference defaults (phases=5, ERE on)",
+                   "tuning": dict(tuning, source="pfg_autotune on this batch" if not a.no_autotune else "built-in"),
                    "l2": "256 MB buffer written before every timed simplify call (batched and plain)",
                    "parallelism": "replicas only" if world > 1 else "single GPU"},
         "plain": {"value": plain_value, "unit": UNIT, "ms_per_pass": plain_max,
@@ -646,6 +649,8 @@ def main():
     ap.add_argument("--workload", default="batched", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving stream of the batched line")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batched line: built-in launch shapes instead of the autotuner's")
     ap.add_argument("--serve-jobs", type=int, default=SERVE["jobs"])
     ap.add_argument("--batch-n", type=int, default=None,
                     help="with --single-step: only the first N instances of the batch (small profiling case)")

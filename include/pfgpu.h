@@ -405,6 +405,43 @@ const char* pfg_profile_name(int id);
 int  pfg_profile_get(pfg_ctx* ctx, int id, uint64_t* launches, double* ms, uint64_t* alg_bytes);
 
 /*
+ * Launch shapes per pass, and the autotuner that picks them. Replaces the
+ * reference's launch-configuration macros, which size grids from the device
+ * properties alone (OPTIMIZEBLOCKS, OPTIMIZEBLOCKSELIM, OPTIMIZEBLOCKSERE,
+ * OPTIMIZEBLOCKS2, OPTIMIZESHARED, src/gpu/grid.cuh:137-240, and the
+ * veminthreads-style options, src/gpu/options.cu:36-47). A zero field means
+ * the built-in choice (shown in brackets). No field changes any result: the
+ * passes are schedule-independent, only their speed moves.
+ */
+typedef struct pfg_tuning {
+    uint32_t sub_blocks_per_sm;  /* SUB warp kernel: blocks per SM of its persistent grid [all the SM holds] */
+    uint32_t ve1_blocks_per_sm;  /* BVE phase 1 warp kernel, likewise [all] */
+    uint32_t ve3_blocks_per_sm;  /* BVE phase 3 warp kernel, likewise [all] */
+    uint32_t ve3_ticket;         /* variables per work-stealing draw in BVE phase 3 [16] */
+    uint32_t mis_threads;        /* block size of the MIS round kernels (multiple of 32, <= 1024) [128] */
+    uint32_t list_threads;       /* block size of the occurrence-list passes (multiple of 32, <= 1024) [256] */
+    uint32_t bcp_blocks_per_sm;  /* blocks per SM of each propagation level [8] */
+    uint32_t _reserved[9];
+} pfg_tuning;
+
+/* The context's launch shapes (kept across uploads). Set rejects a field out
+ * of range with PFG_INVALID and changes nothing then. */
+int pfg_tuning_get(pfg_ctx* ctx, pfg_tuning* out);
+int pfg_tuning_set(pfg_ctx* ctx, const pfg_tuning* t);
+
+/*
+ * Measured choice of the launch shapes on the caller's instances: every trial
+ * uploads the n instances, simplifies them with per-kernel timing and reads
+ * each tuned pass's own kernel time; the knobs of different passes are swept
+ * together (one trial per candidate), then the BVE phase 3 ticket with the
+ * best grid. `repeats` trials per candidate, the fastest counts. The best
+ * shapes are set on the context and written to *out (if not NULL). The
+ * context holds the last trial's result afterwards: upload again before the
+ * next simplify. Profiling is left as it was.
+ */
+int pfg_autotune(pfg_ctx* ctx, uint32_t n, const pfg_instance* instances, uint32_t repeats, pfg_tuning* out);
+
+/*
  * Host-side synthetic CNF generators (the seeded families used by the
  * benchmark and the tests). They write into caller buffers; call once with
  * lits == NULL to get the sizes.

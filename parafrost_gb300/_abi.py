@@ -151,6 +151,20 @@ class PfgDimacsInfo(C.Structure):
     ]
 
 
+class PfgTuning(C.Structure):
+    """pfg_tuning: launch shapes per pass (0 = the built-in choice)."""
+    _fields_ = [
+        ("sub_blocks_per_sm", C.c_uint32),
+        ("ve1_blocks_per_sm", C.c_uint32),
+        ("ve3_blocks_per_sm", C.c_uint32),
+        ("ve3_ticket", C.c_uint32),
+        ("mis_threads", C.c_uint32),
+        ("list_threads", C.c_uint32),
+        ("bcp_blocks_per_sm", C.c_uint32),
+        ("_reserved", C.c_uint32 * 9),
+    ]
+
+
 PFG_PENDING = 7
 
 PASS_NAMES = ("ot", "bcp", "lcve", "sub", "ve", "ere", "gc", "other")

@@ -6,7 +6,8 @@ implementation to fall back to, so a missing or broken library raises.
 import ctypes as C
 import os
 
-from ._abi import PfgDimacsInfo, PfgInstance, PfgJobInfo, PfgOptions, PfgResultSizes, PfgServerStats, PfgStats
+from ._abi import (PfgDimacsInfo, PfgInstance, PfgJobInfo, PfgOptions, PfgResultSizes, PfgServerStats, PfgStats,
+                   PfgTuning)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libpfgpu.so")
@@ -98,6 +99,12 @@ def lib():
     L.pfg_host_alloc.restype = C.c_void_p
     L.pfg_host_free.argtypes = [C.c_void_p]
     L.pfg_host_free.restype = None
+    L.pfg_tuning_get.argtypes = [C.c_void_p, C.POINTER(PfgTuning)]
+    L.pfg_tuning_get.restype = C.c_int
+    L.pfg_tuning_set.argtypes = [C.c_void_p, C.POINTER(PfgTuning)]
+    L.pfg_tuning_set.restype = C.c_int
+    L.pfg_autotune.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(PfgInstance), C.c_uint32, C.POINTER(PfgTuning)]
+    L.pfg_autotune.restype = C.c_int
     L.pfg_destroy.argtypes = [C.c_void_p]
     L.pfg_destroy.restype = None
     L.pfg_last_error.argtypes = [C.c_void_p]
@@ -131,5 +138,5 @@ EXPORTED = (
     "pfg_server_poll", "pfg_server_fetch", "pfg_server_stats_get", "pfg_server_destroy", "pfg_server_last_error",
     "pfg_dimacs_read", "pfg_dimacs_get_info", "pfg_dimacs_copy", "pfg_dimacs_error", "pfg_dimacs_free",
     "pfg_map_vars", "pfg_map_lits", "pfg_extend_model", "pfg_download_proof", "pfg_batch_download_proof",
-    "pfg_proof_text", "pfg_host_alloc", "pfg_host_free",
+    "pfg_proof_text", "pfg_host_alloc", "pfg_host_free", "pfg_tuning_get", "pfg_tuning_set", "pfg_autotune",
 )

@@ -17,7 +17,7 @@ INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(HERE, "libpfgpu.so")
 BUILD_DIR = os.path.join(HERE, "_build")
 
-CU_SOURCES = ["prims.cu", "ot.cu", "gc.cu", "bcp.cu", "lcve.cu", "elim.cu", "engine.cu", "server.cu"]
+CU_SOURCES = ["prims.cu", "ot.cu", "gc.cu", "bcp.cu", "lcve.cu", "elim.cu", "engine.cu", "server.cu", "tune.cu"]
 CPP_SOURCES = ["gen.cpp", "dimacs.cpp", "vmap.cpp", "proof.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

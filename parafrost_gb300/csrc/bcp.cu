@@ -243,7 +243,7 @@ bool bcp_prop(Ctx& c) {
     PFG_LAUNCH(K_BCP, bcp_advance_k, 1, 1, 0, c.s, c.dc);
     // make level parity start at 0 with the seeds in front_a
     cudaMemsetAsync(&c.dc->bcp_level, 0, sizeof(uint32_t), c.s);
-    const unsigned grid = 152 * 8;
+    const unsigned grid = sm_count() * tuned(c.tune.bcp_blocks_per_sm, BCP_BLOCKS_PER_SM);
     uint32_t levels = 0;
     const uint32_t max_levels = c.V + 2;   // every level assigns at least one new variable
     const bool single = c.ninst == 1;

@@ -1540,23 +1540,23 @@ __global__ void inst_add_k(const unsigned long long* cslot, const unsigned long 
 
 }  // namespace
 
-// A persistent grid for a warp kernel: the blocks the GPU holds at once (from
-// the kernel's occupancy), no more than the variables need.
+// A persistent grid for a warp kernel: the blocks per SM the kernel's
+// occupancy allows (or fewer, as the tuning asks) on every SM, no more blocks
+// than the variables need.
 template <typename Kern>
-static unsigned resident_blocks(Kern kern, unsigned threads) {
-    int nb = 0, sms = 0, dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) { cudaGetLastError(); sms = 152; }
+static unsigned blocks_per_sm(Kern kern, unsigned threads) {
+    int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, (int)threads, 0) != cudaSuccess) {
         cudaGetLastError();
         nb = 1;
     }
-    return (unsigned)std::max(1, nb) * (unsigned)std::max(1, sms);
+    return (unsigned)std::max(1, nb);
 }
 
-static unsigned warp_grid(unsigned resident, uint32_t nvars) {
+static unsigned warp_grid(unsigned occ, uint32_t want, uint32_t nvars) {
+    const uint64_t per_sm = want ? std::min<unsigned>(want, occ) : occ;
     const uint64_t need = ((uint64_t)nvars + WS_WARPS - 1) / WS_WARPS;
-    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(need, resident));
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(need, per_sm * sm_count()));
 }
 
 bool sub_pass(Ctx& c) {
@@ -1566,9 +1566,9 @@ bool sub_pass(Ctx& c) {
     const EK k = make_ek(c);
     cudaMemsetAsync(&c.dc->nbig_sub, 0, sizeof(uint32_t), c.s);
     // warp per variable on the shared-memory stage; larger variables by one thread each
-    static const unsigned sub_res = resident_blocks(subw_k, WS_WARPS * 32);
+    static const unsigned sub_occ = blocks_per_sm(subw_k, WS_WARPS * 32);
     cudaMemsetAsync(&c.dc->steal[0], 0, sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_SUB, subw_k, warp_grid(sub_res, E), WS_WARPS * 32, 0, c.s, k, c.veset, E, c.work_b, &c.dc->nbig_sub,
+    PFG_LAUNCH(K_SUB, subw_k, warp_grid(sub_occ, c.tune.sub_blocks_per_sm, E), WS_WARPS * 32, 0, c.s, k, c.veset, E, c.work_b, &c.dc->nbig_sub,
                &c.dc->steal[0]);
     PFG_LAUNCH(K_BIGVAR, sub_k, grid_for(E, 64, 8), 64, 0, c.s, k, c.veset, E, c.work_b, &c.dc->nbig_sub);
     return !c.o.proof_en || proof_collect(c);
@@ -1583,9 +1583,9 @@ bool ve_pass(Ctx& c) {
     for (uint32_t i = 0; i < c.ninst; i++) any_vc |= c.ih[i].mode == 1 && c.ih[i].varcore_on;
     cudaMemsetAsync(&c.dc->nwork, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->nbig_ve1, 0, 2 * sizeof(uint32_t), c.s);
-    static const unsigned ve1_res = resident_blocks(ve1w_k, WS_WARPS * 32);
+    static const unsigned ve1_occ = blocks_per_sm(ve1w_k, WS_WARPS * 32);
     cudaMemsetAsync(&c.dc->steal[1], 0, sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_VE1, ve1w_k, warp_grid(ve1_res, E), WS_WARPS * 32, 0, c.s, k, c.veset, E, c.type, c.ucnt, c.rpos,
+    PFG_LAUNCH(K_VE1, ve1w_k, warp_grid(ve1_occ, c.tune.ve1_blocks_per_sm, E), WS_WARPS * 32, 0, c.s, k, c.veset, E, c.type, c.ucnt, c.rpos,
                c.rref, c.work, &c.dc->nwork, c.work_b, &c.dc->nbig_ve1, &c.dc->steal[1]);
     PFG_LAUNCH(K_BIGVAR, ve1a_k, grid_for(E, 128, 8), 128, 0, c.s, k, c.veset, E, c.type, c.ucnt, c.rpos, c.rref, c.work,
                &c.dc->nwork, c.work_b, &c.dc->nbig_ve1);
@@ -1613,10 +1613,11 @@ bool ve_pass(Ctx& c) {
         if (!proof_prepare(c, c.hc->pf_need)) return false;
         k3 = make_ek(c);
     }
-    static const unsigned ve3_res = resident_blocks(ve3w_k, WS_WARPS * 32);
+    static const unsigned ve3_occ = blocks_per_sm(ve3w_k, WS_WARPS * 32);
     cudaMemsetAsync(&c.dc->steal[2], 0, sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_VE3, ve3w_k, warp_grid(ve3_res, E), WS_WARPS * 32, 0, c.s, k3, c.veset, E, c.type, c.ucnt, c.rslot,
-               c.rlit, c.winv, c.eligible_b, &c.dc->nbig_ve3, &c.dc->steal[2]);
+    PFG_LAUNCH(K_VE3, ve3w_k, warp_grid(ve3_occ, c.tune.ve3_blocks_per_sm, E), WS_WARPS * 32, 0, c.s, k3, c.veset, E,
+               c.type, c.ucnt, c.rslot, c.rlit, c.winv, c.eligible_b, &c.dc->nbig_ve3, &c.dc->steal[2],
+               c.tune.ve3_ticket ? c.tune.ve3_ticket : VE3_TICKET);
     PFG_LAUNCH(K_BIGVAR, ve3_k, grid_for(E, 128, 8), 128, 0, c.s, k3, c.veset, E, c.type, c.ucnt, c.rslot, c.rlit,
                c.winv, c.eligible_b, &c.dc->nbig_ve3);
     if (c.o.proof_en && !proof_collect(c)) return false;

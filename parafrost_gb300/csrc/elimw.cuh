@@ -75,8 +75,6 @@ PFG_D void ws_prefetch_lists(const EK& k, const NextLists& nl, unsigned lane) {
 // draws its next variable from one counter (lane 0 draws, the warp reads it by
 // shuffle), so a warp whose variables have long lists does not leave the rest
 // of its fixed share to the end of the launch.
-constexpr uint32_t VE3_CHUNK = 16;
-
 PFG_D uint32_t ws_ticket(uint32_t* ctr, unsigned lane) {
     uint32_t t = 0;
     if (lane == 0) t = atomicAdd(ctr, 1u);
@@ -880,15 +878,16 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
                                                         const uint32_t* type, const uint32_t* ucnt,
                                                         const unsigned long long* rslot,
                                                         const unsigned long long* rlit, const uint8_t* fits,
-                                                        uint32_t* big, uint32_t* nbig, uint32_t* steal) {
+                                                        uint32_t* big, uint32_t* nbig, uint32_t* steal,
+                                                        uint32_t ticket) {
     __shared__ WS stage[WS_WARPS];
     const unsigned lane = threadIdx.x & 31u;
     WS& w = stage[threadIdx.x >> 5];
-    // tickets of VE3_CHUNK variables: most elected variables emit nothing and
-    // are passed over at once, so one draw per variable would queue on the counter
-    const uint32_t nchunks = (nelected + VE3_CHUNK - 1) / VE3_CHUNK;
+    // tickets of `ticket` variables (>= 1): most elected variables emit nothing
+    // and are passed over at once, so one draw per variable would queue on the counter
+    const uint32_t nchunks = (nelected + ticket - 1) / ticket;
     for (uint32_t t = ws_ticket(steal, lane); t < nchunks; t = ws_ticket(steal, lane))
-    for (uint32_t q = t * VE3_CHUNK, qe = min(q + VE3_CHUNK, nelected); q < qe; q++) {
+    for (uint32_t q = t * ticket, qe = min(q + ticket, nelected); q < qe; q++) {
         const uint32_t tid = q;
         const uint32_t x = elected[tid];
         const uint32_t xinfo = type[tid];

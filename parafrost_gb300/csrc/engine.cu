@@ -34,6 +34,19 @@ bool cuda_ok(Ctx& c, cudaError_t e, const char* what) {
     return false;
 }
 
+unsigned sm_count() {
+    static const unsigned n = [] {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            sms = 152;
+        }
+        return (unsigned)std::max(1, sms);
+    }();
+    return n;
+}
+
 bool dalloc(Ctx& c, void** p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
@@ -416,6 +429,7 @@ void free_all(pfg_ctx* o) {
     fresh.o = c.o;
     fresh.device = c.device;
     fresh.s = c.s;
+    fresh.tune = c.tune;
     fresh.s_copy = c.s_copy; fresh.ev_copy = c.ev_copy;
     fresh.ev_begin = c.ev_begin; fresh.ev_end = c.ev_end; fresh.ev_a = c.ev_a; fresh.ev_b = c.ev_b;
     fresh.dc = nullptr; fresh.hc = c.hc;
@@ -1684,6 +1698,32 @@ extern "C" int pfg_batch_download_all(pfg_ctx* o, uint32_t* lits, uint64_t* cls_
         rends += h.round_ends.size();
     }
     return finish(c, nullptr, base_launches, PFG_OK);
+}
+
+bool pfg::profiling(pfg_ctx* o) { return o && o->c.prof.on; }
+
+void pfg::set_error(pfg_ctx* o, const std::string& e) {
+    if (o) o->c.err = e;
+}
+
+extern "C" int pfg_tuning_get(pfg_ctx* o, pfg_tuning* out) {
+    if (!o || !out) return PFG_INVALID;
+    *out = o->c.tune;
+    return PFG_OK;
+}
+
+extern "C" int pfg_tuning_set(pfg_ctx* o, const pfg_tuning* t) {
+    if (!o || !t) return PFG_INVALID;
+    auto threads_ok = [](uint32_t v) { return v == 0 || (v % 32 == 0 && v <= 1024); };
+    if (t->sub_blocks_per_sm > 64 || t->ve1_blocks_per_sm > 64 || t->ve3_blocks_per_sm > 64 ||
+        t->bcp_blocks_per_sm > 64 || t->ve3_ticket > 65536 || !threads_ok(t->mis_threads) ||
+        !threads_ok(t->list_threads)) {
+        o->c.err = "tuning field out of range (blocks per SM <= 64, ticket <= 65536, threads a multiple of 32 "
+                   "up to 1024)";
+        return PFG_INVALID;
+    }
+    o->c.tune = *t;
+    return PFG_OK;
 }
 
 extern "C" int pfg_profile_enable(pfg_ctx* o, int on) {

@@ -79,6 +79,7 @@ size_t inst_out_layout(uint32_t n, char* base, InstOut* p);
 
 struct Ctx {
     pfg_options o{};
+    pfg_tuning tune{};               // launch shapes (zero: built-in), kept across uploads
     int device = 0;
     cudaStream_t s = nullptr;
     cudaStream_t s_copy = nullptr;   // write-back copies that overlap the last write-back kernels
@@ -229,6 +230,16 @@ struct Ctx {
     std::vector<uint64_t> cache_lit_base;       // n+1: first packed literal of each instance
     std::vector<uint64_t> cache_elim_cnt, cache_forced_cnt;
 };
+
+// ---- launch shapes: the built-in choices of the pfg_tuning fields left zero ----
+constexpr uint32_t VE3_TICKET = 16;
+constexpr uint32_t MIS_THREADS = 128;
+constexpr uint32_t LIST_THREADS = 256;
+constexpr uint32_t BCP_BLOCKS_PER_SM = 8;
+unsigned sm_count();            // SMs of the current device (read once)
+bool profiling(pfg_ctx* o);     // per-kernel timing on (engine.cu)
+void set_error(pfg_ctx* o, const std::string& e);
+inline unsigned tuned(uint32_t v, uint32_t dflt) { return v ? v : dflt; }
 
 // ---- memory helpers (engine.cu) ----
 bool dalloc(Ctx& c, void** p, size_t bytes);

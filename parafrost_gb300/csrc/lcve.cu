@@ -402,6 +402,7 @@ bool lcve(Ctx& c) {
         // Rounds run without compaction; each winner records its round. The host
         // reads the undecided count only every 1, 2, 4 .. 16 rounds.
         uint32_t* mround = c.scores;     // scores are dead once the order is sorted
+        const unsigned mt = tuned(c.tune.mis_threads, MIS_THREADS);
         uint32_t r = 0;
         bool done = nwork == 0;
         cudaMemsetAsync(&c.dc->mis_done, 0, sizeof(uint32_t), c.s);
@@ -412,7 +413,7 @@ bool lcve(Ctx& c) {
                     PFG_LAUNCH(K_MIS_WIN, clause_min_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls,
                                c.rank, c.tmp_u32);
                     // flag8 (the candidate flags, consumed above) holds the outcomes by rank
-                    PFG_LAUNCH(K_MIS_WIN, mis_win_min_k, grid_for(V, 128), 128, 0, c.s, V, c.ot_off, c.ot_size,
+                    PFG_LAUNCH(K_MIS_WIN, mis_win_min_k, grid_for(V, mt), mt, 0, c.s, V, c.ot_off, c.ot_size,
                                c.ot_ids, c.tmp_u32, c.rank, c.mstate, c.winv, c.flag8, &c.dc->nwin);
                     PFG_LAUNCH(K_MIS_APPLY, mis_apply_min_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits,
                                c.ncls, c.tmp_u32, c.eligible, c.flag8, c.frozen, c.mstate, c.rank);
@@ -420,9 +421,9 @@ bool lcve(Ctx& c) {
                                c.rank, &c.dc->nwin);
                     continue;
                 }
-                PFG_LAUNCH(K_MIS_WIN, mis_win3_k, grid_for(V, 128), 128, 0, c.s, V, c.hdr, c.lits, c.ot_off,
+                PFG_LAUNCH(K_MIS_WIN, mis_win3_k, grid_for(V, mt), mt, 0, c.s, V, c.hdr, c.lits, c.ot_off,
                            c.ot_size, c.ot_ids, c.rank, c.mstate, c.winv, &c.dc->nwin, &c.dc->mis_done);
-                PFG_LAUNCH(K_MIS_APPLY, mis_apply3_k, grid_for(V, 128), 128, 0, c.s, V, c.winv, r, mround, c.hdr,
+                PFG_LAUNCH(K_MIS_APPLY, mis_apply3_k, grid_for(V, mt), mt, 0, c.s, V, c.winv, r, mround, c.hdr,
                            c.lits, c.ot_off, c.ot_size, c.ot_ids, c.frozen, c.mstate, c.rank, &c.dc->nwin,
                            &c.dc->mis_done);
             }

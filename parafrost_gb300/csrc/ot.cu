@@ -485,7 +485,8 @@ bool ot_build(Ctx& c) {
 
 bool ot_filter(Ctx& c, const uint8_t* assigned) {
     PFG_LAUNCH(K_FILL, mark_dead_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.ncls, c.cnew);
-    PFG_LAUNCH(K_FILL, ot_filter_w_k, grid_for((c.nlist + 31) / 32 * 32, 256), 256, 0, c.s, c.nlist, c.ot_off,
+    const unsigned lt = tuned(c.tune.list_threads, LIST_THREADS);
+    PFG_LAUNCH(K_FILL, ot_filter_w_k, grid_for((c.nlist + 31) / 32 * 32, lt), lt, 0, c.s, c.nlist, c.ot_off,
                c.ot_size, c.hist, c.ot_ids, assigned, c.cnew);
     return cuda_ok(c, cudaGetLastError(), "ot_filter");
 }
@@ -520,7 +521,8 @@ bool ot_update(Ctx& c) {
     // kept entries move to the new offsets (renumbered after a compaction, whose
     // drop bytes are still on the old ids); the flagged clauses are appended
     // behind them
-    PFG_LAUNCH(K_FILL, prune_move_w_k, grid_for((nl + 31) / 32 * 32, 256), 256, 0, c.s, nl, c.ot_off, c.ot_size,
+    const unsigned lt = tuned(c.tune.list_threads, LIST_THREADS);
+    PFG_LAUNCH(K_FILL, prune_move_w_k, grid_for((nl + 31) / 32 * 32, lt), lt, 0, c.s, nl, c.ot_off, c.ot_size,
                c.hist, c.ot_ids, c.elim, c.cdrop ? c.cdrop : c.cnew, c.ot_off2, c.ot_ids2, c.cmap, c.ot_fill);
     PFG_LAUNCH(K_FILL, fill_new_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.cnew, c.ot_fill,
                c.ot_ids2);

@@ -121,6 +121,13 @@ class Simplifier:
     # ---- batches: n instances simplified together, results per instance ----
 
     def upload_batch(self, cnfs, var_states=None, assumeds=None, vorgs=None) -> None:
+        arr, keep = self._instances(cnfs, var_states, assumeds, vorgs)
+        self._check(self.lib.pfg_batch_upload(self._ctx, len(cnfs), arr), "pfg_batch_upload")
+
+    @staticmethod
+    def _instances(cnfs, var_states=None, assumeds=None, vorgs=None):
+        """The pfg_instance array of `cnfs` and the arrays it points into (keep
+        both alive across the call)."""
         n = len(cnfs)
         arr = (_abi.PfgInstance * max(n, 1))()
         keep = []   # the arrays must outlive the call
@@ -144,7 +151,33 @@ class Simplifier:
             q.var_state = _ptr(opt(var_states, i, np.uint8), C.c_uint8)
             q.assumed = _ptr(opt(assumeds, i, np.uint8), C.c_uint8)
             q.vorg = _ptr(opt(vorgs, i, np.uint32), C.c_uint32)
-        self._check(self.lib.pfg_batch_upload(self._ctx, n, arr), "pfg_batch_upload")
+        return arr, keep
+
+    # ---- launch shapes (pfg_tuning) ----
+
+    @property
+    def tuning(self) -> dict:
+        """Launch shapes per pass; 0 is the built-in choice."""
+        t = _abi.PfgTuning()
+        self._check(self.lib.pfg_tuning_get(self._ctx, C.byref(t)), "pfg_tuning_get")
+        return {f[0]: getattr(t, f[0]) for f in _abi.PfgTuning._fields_ if not f[0].startswith("_")}
+
+    @tuning.setter
+    def tuning(self, values: dict) -> None:
+        t = _abi.PfgTuning()
+        for k, v in values.items():
+            if k.startswith("_") or not any(f[0] == k for f in _abi.PfgTuning._fields_):
+                raise KeyError(f"unknown tuning field {k!r}")
+            setattr(t, k, int(v))
+        self._check(self.lib.pfg_tuning_set(self._ctx, C.byref(t)), "pfg_tuning_set")
+
+    def autotune(self, cnfs, repeats: int = 1) -> dict:
+        """Measure the launch shapes on `cnfs` (pfg_autotune) and keep the best;
+        returns them. Upload again before the next simplify."""
+        arr, keep = self._instances(cnfs)
+        t = _abi.PfgTuning()
+        self._check(self.lib.pfg_autotune(self._ctx, len(cnfs), arr, int(repeats), C.byref(t)), "pfg_autotune")
+        return {f[0]: getattr(t, f[0]) for f in _abi.PfgTuning._fields_ if not f[0].startswith("_")}
 
     def batch_size(self) -> int:
         return int(self.lib.pfg_batch_size(self._ctx))

@@ -114,3 +114,12 @@ def test_pinned_arrays_fall_back_without_a_device():
     assert b.tolist() == [0, 1, 2, 3, 4]
     buf = pinned.ResultBuffers()
     assert buf.get("lits", 7).size == 7 and buf.get("lits", 3).size == 3
+
+
+def test_tuning_struct_layout():
+    # pfg_tuning: seven uint32 knobs and nine reserved words, in header order
+    src = open(os.path.join(ROOT, "include", "pfgpu.h")).read()
+    body = src[src.index("typedef struct pfg_tuning {"):src.index("} pfg_tuning;")]
+    names = re.findall(r"uint32_t\s+([a-z_0-9]+)", body)
+    assert names == [f[0] for f in _abi.PfgTuning._fields_]
+    assert C.sizeof(_abi.PfgTuning) == 64
