@@ -408,7 +408,7 @@ int  pfg_profile_get(pfg_ctx* ctx, int id, uint64_t* launches, double* ms, uint6
  * Launch shapes per pass, and the autotuner that picks them. Replaces the
  * reference's launch-configuration macros, which size grids from the device
  * properties alone (OPTIMIZEBLOCKS, OPTIMIZEBLOCKSELIM, OPTIMIZEBLOCKSERE,
- * OPTIMIZEBLOCKS2, OPTIMIZESHARED, src/gpu/grid.cuh:137-240, and the
+ * OPTIMIZEBLOCKS2, OPTIMIZESHARED, src/gpu/grid.cuh:137-232, and the
  * veminthreads-style options, src/gpu/options.cu:36-47). A zero field means
  * the built-in choice (shown in brackets). No field changes any result: the
  * passes are schedule-independent, only their speed moves.

@@ -1,7 +1,7 @@
 // Autotuner of the launch shapes (pfg_tuning).
 //
 // Replaces the reference's launch-configuration macros (OPTIMIZEBLOCKS and
-// its variants, src/gpu/grid.cuh:137-240), which size every grid from the
+// its variants, src/gpu/grid.cuh:137-232), which size every grid from the
 // device properties alone, by measurement on the caller's own instances:
 // each trial uploads them, simplifies with per-kernel timing, and reads the
 // time of every tuned pass's kernel group. Passes whose knobs belong to
