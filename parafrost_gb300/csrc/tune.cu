@@ -16,8 +16,6 @@
 
 namespace {
 
-using pfg::KernelId;
-
 struct Knob {
     uint32_t pfg_tuning::*field;
     std::vector<uint32_t> cand;       // candidates; 0 is the built-in choice
