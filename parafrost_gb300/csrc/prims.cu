@@ -268,6 +268,17 @@ void excl_scan(const T* in, T* out, uint64_t n, T init, T* total_out, void* tmp,
     PFG_LAUNCH(K_SCAN, scan_lookback_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, in, out, n, init, total_out, lb, nt);
 }
 
+bool scan_gave_up(cudaStream_t s) {
+    uint32_t v = 0;
+    cudaMemcpyFromSymbolAsync(&v, g_scan_gaveup, sizeof(v), 0, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (v) {
+        const uint32_t z = 0;
+        cudaMemcpyToSymbolAsync(g_scan_gaveup, &z, sizeof(z), 0, cudaMemcpyHostToDevice, s);
+        cudaStreamSynchronize(s);
+    }
+    return v != 0;
+}
 
 // ---------------- radix sort ----------------
 constexpr int RS_THREADS = 256;
@@ -346,18 +357,6 @@ __global__ void select_scatter_k(const uint32_t* in, const uint8_t* flags, const
 }
 
 }  // namespace
-
-bool scan_gave_up(cudaStream_t s) {
-    uint32_t v = 0;
-    cudaMemcpyFromSymbolAsync(&v, g_scan_gaveup, sizeof(v), 0, cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    if (v) {
-        const uint32_t z = 0;
-        cudaMemcpyToSymbolAsync(g_scan_gaveup, &z, sizeof(z), 0, cudaMemcpyHostToDevice, s);
-        cudaStreamSynchronize(s);
-    }
-    return v != 0;
-}
 
 size_t scan_temp_bytes(uint64_t n) {
     const uint64_t nt = (n + SCAN_TILE - 1) / SCAN_TILE + 1;
