@@ -935,10 +935,6 @@ extern "C" int pfg_batch_upload(pfg_ctx* o, uint32_t n, const pfg_instance* inst
 extern "C" uint32_t pfg_batch_size(pfg_ctx* o) { return (o && o->c.uploaded) ? o->c.ninst : 0; }
 
 static int finish(Ctx& c, pfg_stats* st, uint64_t base_launches, int rc) {
-    if (c.s && scan_gave_up(c.s) && rc == PFG_OK) {
-        c.err = "a prefix scan gave up waiting for an earlier tile; the results are not valid";
-        rc = PFG_CUDA_ERROR;
-    }
     if (c.prof.on) c.prof.resolve();
     g_prof = nullptr;
     c.launches += g_launches - base_launches;

@@ -93,6 +93,65 @@ __device__ __forceinline__ T block_excl_scan(T v, T& total) {
     return excl;
 }
 
+// Phase 1: scan each tile locally, emit tile totals.
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_tiles_k(const T* in, T* out, uint64_t n, T* tile_sums) {
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    __shared__ T sh[SCAN_TILE];
+    // coalesced striped load into shared memory
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
+        sh[i * SCAN_THREADS + threadIdx.x] = idx < n ? in[idx] : T(0);
+    }
+    __syncthreads();
+    T loc[SCAN_ITEMS];
+    T sum = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        loc[i] = sum;
+        sum += sh[threadIdx.x * SCAN_ITEMS + i];
+    }
+    T total;
+    const T excl = block_excl_scan<T>(sum, total);
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) sh[threadIdx.x * SCAN_ITEMS + i] = loc[i] + excl;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
+        if (idx < n) out[idx] = sh[i * SCAN_THREADS + threadIdx.x];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// Phase 2: one block scans the tile totals sequentially in chunks.
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_sums_k(T* sums, uint64_t nt, T init, T* total_out) {
+    T carry = init;
+    for (uint64_t b = 0; b < nt; b += SCAN_THREADS) {
+        const uint64_t i = b + threadIdx.x;
+        const T v = i < nt ? sums[i] : T(0);
+        T tot;
+        const T ex = block_excl_scan<T>(v, tot);
+        if (i < nt) sums[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0 && total_out) *total_out = carry;
+}
+
+// Phase 3: add the tile offsets.
+template <typename T>
+__global__ void scan_add_k(T* out, uint64_t n, const T* sums) {
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    const T add = sums[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
+        if (idx < n) out[idx] += add;
+    }
+}
+
 // Small arrays: one block walks the tiles in order, carrying the prefix (one launch).
 template <typename T>
 __global__ void __launch_bounds__(SCAN_THREADS) scan_single_k(const T* in, T* out, uint64_t n, T init, T* total_out) {
@@ -130,128 +189,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_single_k(const T* in, T* ou
 
 constexpr uint64_t SCAN_SINGLE_MAX_TILES = 16;
 
-// ---- single pass, decoupled look-back (larger arrays) ----
-// Tiles take their number from a counter in launch order, so every smaller
-// tile belongs to a block that is already running and never waits on a later
-// one. A tile publishes its own sum (state 1), then, once it knows the sum of
-// everything before it, its inclusive prefix (state 2); warp 0 of the next
-// tiles reads 32 predecessors at a time and stops at the nearest inclusive
-// prefix. Values are stored before their state with a fence between, and read
-// after it the same way. Every wait is bounded: a tile that gives up counts its
-// predecessor as zero and sets scan_gaveup, which the host reads after the call.
-constexpr uint32_t LB_AGG = 1, LB_INCL = 2;
-constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;
-
-__device__ uint32_t g_scan_gaveup;
-
-struct LookBack {
-    uint32_t* counter;
-    volatile uint32_t* state;        // nt
-    volatile unsigned long long* agg;   // nt
-    volatile unsigned long long* incl;  // nt
-};
-
-__host__ __device__ inline size_t lb_align(size_t x) { return (x + 255) & ~(size_t)255; }
-
-inline LookBack lb_layout(void* tmp, uint64_t nt) {
-    char* b = (char*)tmp;
-    LookBack l;
-    l.counter = (uint32_t*)b;
-    l.state = (volatile uint32_t*)(b + 256);
-    l.agg = (volatile unsigned long long*)(b + 256 + lb_align(nt * 4));
-    l.incl = l.agg + nt;
-    return l;
-}
-
-template <typename T>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_k(const T* in, T* out, uint64_t n, T init,
-                                                              T* total_out, LookBack lb, uint64_t nt) {
-    __shared__ T sh[SCAN_TILE];
-    __shared__ uint32_t tile_sh;
-    __shared__ T prefix_sh;
-    if (threadIdx.x == 0) tile_sh = atomicAdd(lb.counter, 1u);
-    __syncthreads();
-    const uint64_t tile = tile_sh;
-    const uint64_t base = tile * SCAN_TILE;
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; i++) {
-        const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
-        sh[i * SCAN_THREADS + threadIdx.x] = idx < n ? in[idx] : T(0);
-    }
-    __syncthreads();
-    T loc[SCAN_ITEMS];
-    T sum = 0;
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; i++) {
-        loc[i] = sum;
-        sum += sh[threadIdx.x * SCAN_ITEMS + i];
-    }
-    T total;
-    const T excl = block_excl_scan<T>(sum, total);
-    if (threadIdx.x < 32) {
-        const unsigned lane = threadIdx.x;
-        T run = 0;
-        if (tile == 0) {
-            if (lane == 0) {
-                lb.incl[0] = (unsigned long long)total;
-                __threadfence();
-                lb.state[0] = LB_INCL;
-            }
-        } else {
-            if (lane == 0) {
-                lb.agg[tile] = (unsigned long long)total;
-                __threadfence();
-                lb.state[tile] = LB_AGG;
-            }
-            int64_t end = (int64_t)tile;     // predecessors [end-32, end) this step
-            bool gave_up = false;
-            while (true) {
-                const int64_t j = end - 1 - (int64_t)lane;
-                uint32_t st = LB_INCL;
-                T v = 0;
-                if (j >= 0) {
-                    st = lb.state[j];
-                    for (uint32_t it = 0; st == 0 && it < LB_SPIN_LIMIT; it++) {
-                        __nanosleep(64);
-                        st = lb.state[j];
-                    }
-                    if (st == 0) { gave_up = true; st = LB_INCL; }
-                    else {
-                        __threadfence();
-                        v = (T)(st == LB_INCL ? lb.incl[j] : lb.agg[j]);
-                    }
-                }
-                const unsigned incl_mask = __ballot_sync(0xFFFFFFFFu, st == LB_INCL);
-                const int first = incl_mask ? __ffs(incl_mask) - 1 : 32;   // nearest inclusive predecessor
-                T c = (int)lane <= first ? v : T(0);
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, d);
-                run += __shfl_sync(0xFFFFFFFFu, c, 0);
-                if (incl_mask) break;
-                end -= 32;
-            }
-            if (__any_sync(0xFFFFFFFFu, gave_up) && lane == 0) atomicOr(&g_scan_gaveup, 1u);
-            if (lane == 0) {
-                lb.incl[tile] = (unsigned long long)(run + total);
-                __threadfence();
-                lb.state[tile] = LB_INCL;
-            }
-        }
-        if (lane == 0) prefix_sh = run;
-    }
-    __syncthreads();
-    const T off = init + prefix_sh + excl;
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; i++) sh[threadIdx.x * SCAN_ITEMS + i] = off + loc[i];
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; i++) {
-        const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
-        if (idx < n) out[idx] = sh[i * SCAN_THREADS + threadIdx.x];
-    }
-    if (tile == nt - 1 && threadIdx.x == 0 && total_out) *total_out = init + prefix_sh + total;
-}
-
 template <typename T>
 void excl_scan(const T* in, T* out, uint64_t n, T init, T* total_out, void* tmp, cudaStream_t s) {
     if (n == 0) {
@@ -263,21 +200,10 @@ void excl_scan(const T* in, T* out, uint64_t n, T init, T* total_out, void* tmp,
         PFG_LAUNCH(K_SCAN, scan_single_k<T>, 1, SCAN_THREADS, 0, s, in, out, n, init, total_out);
         return;
     }
-    const LookBack lb = lb_layout(tmp, nt);
-    cudaMemsetAsync(tmp, 0, 256 + lb_align(nt * 4), s);   // counter and tile states
-    PFG_LAUNCH(K_SCAN, scan_lookback_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, in, out, n, init, total_out, lb, nt);
-}
-
-bool scan_gave_up(cudaStream_t s) {
-    uint32_t v = 0;
-    cudaMemcpyFromSymbolAsync(&v, g_scan_gaveup, sizeof(v), 0, cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    if (v) {
-        const uint32_t z = 0;
-        cudaMemcpyToSymbolAsync(g_scan_gaveup, &z, sizeof(z), 0, cudaMemcpyHostToDevice, s);
-        cudaStreamSynchronize(s);
-    }
-    return v != 0;
+    T* sums = (T*)tmp;
+    PFG_LAUNCH(K_SCAN, scan_tiles_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, in, out, n, sums);
+    PFG_LAUNCH(K_SCAN, scan_sums_k<T>, 1, SCAN_THREADS, 0, s, sums, nt, init, total_out);
+    PFG_LAUNCH(K_SCAN, scan_add_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, out, n, sums);
 }
 
 // ---------------- radix sort ----------------
@@ -359,8 +285,7 @@ __global__ void select_scatter_k(const uint32_t* in, const uint8_t* flags, const
 }  // namespace
 
 size_t scan_temp_bytes(uint64_t n) {
-    const uint64_t nt = (n + SCAN_TILE - 1) / SCAN_TILE + 1;
-    return 256 + lb_align(nt * 4) + 2 * nt * sizeof(unsigned long long) + 256;
+    return ((n + SCAN_TILE - 1) / SCAN_TILE + 1) * sizeof(unsigned long long) + 256;
 }
 
 size_t radix_temp_bytes(uint64_t n) {

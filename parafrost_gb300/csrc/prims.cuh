@@ -51,10 +51,6 @@ extern thread_local Profiler* g_prof;
                    if (_pp->on) _pp->end(::pfg::ID, (STREAM)); }                \
     } while (0)
 
-// True (once) when a scan's look-back gave up waiting for a predecessor tile
-// since the last call; that scan's output is wrong. Synchronizes `s`.
-bool scan_gave_up(cudaStream_t s);
-
 // Scratch bytes needed by the scans / sorts below for n elements.
 size_t scan_temp_bytes(uint64_t n);
 size_t radix_temp_bytes(uint64_t n);
