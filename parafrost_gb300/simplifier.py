@@ -157,7 +157,8 @@ class Simplifier:
 
     @property
     def tuning(self) -> dict:
-        """Launch shapes per pass; 0 is the built-in choice."""
+        """Launch shapes per pass (pfg_tuning); 0 is the built-in choice.
+        Assigning a dict sets every field: the ones it leaves out go back to 0."""
         t = _abi.PfgTuning()
         self._check(self.lib.pfg_tuning_get(self._ctx, C.byref(t)), "pfg_tuning_get")
         return {f[0]: getattr(t, f[0]) for f in _abi.PfgTuning._fields_ if not f[0].startswith("_")}
