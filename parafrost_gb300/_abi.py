@@ -95,19 +95,22 @@ class PfgResultSizes(C.Structure):
 
 
 class PfgInstance(C.Structure):
-    """One instance of a batch (pfg_instance)."""
+    """One instance of a batch (pfg_instance). The array pointers are plain
+    addresses (c_void_p, the same layout as the typed pointers of the header):
+    a host filling hundreds of these per call assigns integers instead of
+    building ctypes pointer objects."""
     _fields_ = [
         ("max_var", C.c_uint32),
         ("_pad", C.c_uint32),
         ("num_clauses", C.c_uint64),
-        ("lits", C.POINTER(C.c_uint32)),
-        ("cls_off", C.POINTER(C.c_uint64)),
-        ("cls_learnt", C.POINTER(C.c_uint8)),
-        ("cls_lbd", C.POINTER(C.c_uint32)),
-        ("cls_usage", C.POINTER(C.c_uint8)),
-        ("var_state", C.POINTER(C.c_uint8)),
-        ("assumed", C.POINTER(C.c_uint8)),
-        ("vorg", C.POINTER(C.c_uint32)),
+        ("lits", C.c_void_p),          # const uint32_t*
+        ("cls_off", C.c_void_p),       # const uint64_t*
+        ("cls_learnt", C.c_void_p),    # const uint8_t*
+        ("cls_lbd", C.c_void_p),       # const uint32_t*
+        ("cls_usage", C.c_void_p),     # const uint8_t*
+        ("var_state", C.c_void_p),     # const uint8_t*
+        ("assumed", C.c_void_p),       # const uint8_t*
+        ("vorg", C.c_void_p),          # const uint32_t*
     ]
 
 

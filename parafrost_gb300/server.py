@@ -16,7 +16,7 @@ import numpy as np
 
 from . import _abi, _lib
 from .cnf import Cnf
-from .simplifier import SimplifyError, SimplifyResult, _ptr
+from .simplifier import SimplifyError, SimplifyResult, _addr, _ptr
 
 
 @dataclass
@@ -58,14 +58,14 @@ class Server:
         q = _abi.PfgInstance()
         q.max_var = cnf.max_var
         q.num_clauses = cnf.num_clauses
-        q.lits = _ptr(cnf.lits, C.c_uint32)
-        q.cls_off = _ptr(cnf.off, C.c_uint64)
-        q.cls_learnt = _ptr(cnf.learnt, C.c_uint8)
-        q.cls_lbd = _ptr(cnf.lbd, C.c_uint32)
-        q.cls_usage = _ptr(cnf.usage, C.c_uint8)
-        q.var_state = _ptr(arr(var_state, np.uint8), C.c_uint8)
-        q.assumed = _ptr(arr(assumed, np.uint8), C.c_uint8)
-        q.vorg = _ptr(arr(vorg, np.uint32), C.c_uint32)
+        q.lits = _addr(cnf.lits)
+        q.cls_off = _addr(cnf.off)
+        q.cls_learnt = _addr(cnf.learnt)
+        q.cls_lbd = _addr(cnf.lbd)
+        q.cls_usage = _addr(cnf.usage)
+        q.var_state = _addr(arr(var_state, np.uint8))
+        q.assumed = _addr(arr(assumed, np.uint8))
+        q.vorg = _addr(arr(vorg, np.uint32))
         t = C.c_uint64()
         rc = self.lib.pfg_server_submit(self._srv, C.byref(q), C.byref(t))
         if rc != 0:

@@ -31,6 +31,11 @@ def _ptr(a, t):
     return None if a is None else a.ctypes.data_as(C.POINTER(t))
 
 
+def _addr(a):
+    """Address of a contiguous numpy array (or None), for PfgInstance fields."""
+    return None if a is None else a.ctypes.data
+
+
 @dataclass
 class SimplifyResult:
     status: int                      # 0 unknown, 10 SAT (no clause left), 20 UNSAT
@@ -143,14 +148,14 @@ class Simplifier:
             q = arr[i]
             q.max_var = cnf.max_var
             q.num_clauses = cnf.num_clauses
-            q.lits = _ptr(cnf.lits, C.c_uint32)
-            q.cls_off = _ptr(cnf.off, C.c_uint64)
-            q.cls_learnt = _ptr(cnf.learnt, C.c_uint8)
-            q.cls_lbd = _ptr(cnf.lbd, C.c_uint32)
-            q.cls_usage = _ptr(cnf.usage, C.c_uint8)
-            q.var_state = _ptr(opt(var_states, i, np.uint8), C.c_uint8)
-            q.assumed = _ptr(opt(assumeds, i, np.uint8), C.c_uint8)
-            q.vorg = _ptr(opt(vorgs, i, np.uint32), C.c_uint32)
+            q.lits = _addr(cnf.lits)
+            q.cls_off = _addr(cnf.off)
+            q.cls_learnt = _addr(cnf.learnt)
+            q.cls_lbd = _addr(cnf.lbd)
+            q.cls_usage = _addr(cnf.usage)
+            q.var_state = _addr(opt(var_states, i, np.uint8))
+            q.assumed = _addr(opt(assumeds, i, np.uint8))
+            q.vorg = _addr(opt(vorgs, i, np.uint32))
         return arr, keep
 
     # ---- launch shapes (pfg_tuning) ----
