@@ -330,6 +330,11 @@ int  pfg_server_fetch(pfg_server* server, uint64_t ticket, uint32_t* lits, uint6
                       uint8_t* cls_learnt, uint32_t* cls_lbd, uint8_t* cls_usage,
                       uint8_t* eliminated, uint32_t* units, uint32_t* pending_units,
                       uint32_t* stack, uint64_t* round_ends);
+/* copy the binary DRAT proof of a finished job (info.sizes.proof_bytes bytes;
+   nothing without proof_en) and keep the job: call it before pfg_server_fetch.
+   The lines are the ones pfg_batch_download_proof gives for the instance, so
+   the same as the instance simplified alone. */
+int  pfg_server_fetch_proof(pfg_server* server, uint64_t ticket, uint8_t* out);
 int  pfg_server_stats_get(pfg_server* server, pfg_server_stats* stats);
 /* finish every queued job, stop the workers and free everything */
 void pfg_server_destroy(pfg_server* server);

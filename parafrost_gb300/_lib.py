@@ -105,6 +105,8 @@ def lib():
     L.pfg_tuning_set.restype = C.c_int
     L.pfg_autotune.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(PfgInstance), C.c_uint32, C.POINTER(PfgTuning)]
     L.pfg_autotune.restype = C.c_int
+    L.pfg_server_fetch_proof.argtypes = [C.c_void_p, C.c_uint64, u8p]
+    L.pfg_server_fetch_proof.restype = C.c_int
     L.pfg_destroy.argtypes = [C.c_void_p]
     L.pfg_destroy.restype = None
     L.pfg_last_error.argtypes = [C.c_void_p]
@@ -139,4 +141,5 @@ EXPORTED = (
     "pfg_dimacs_read", "pfg_dimacs_get_info", "pfg_dimacs_copy", "pfg_dimacs_error", "pfg_dimacs_free",
     "pfg_map_vars", "pfg_map_lits", "pfg_extend_model", "pfg_download_proof", "pfg_batch_download_proof",
     "pfg_proof_text", "pfg_host_alloc", "pfg_host_free", "pfg_tuning_get", "pfg_tuning_set", "pfg_autotune",
+    "pfg_server_fetch_proof",
 )

@@ -57,6 +57,7 @@ struct Job {
     bool done = false;
     pfg_job_info info{};
     std::shared_ptr<BatchResult> res;   // results, from `at`
+    std::vector<uint8_t> proof;         // binary DRAT lines of the job (proof_en)
     Slice at;
 };
 
@@ -192,7 +193,11 @@ void run_batch(pfg_server* s, pfg_ctx* ctx, uint32_t slot, std::vector<Job*>& ba
         in.sizes = z[i];
         j->res = res;
         pfg_stats st;
-        const int r = pfg_batch_stats(ctx, i, &st);
+        int r = pfg_batch_stats(ctx, i, &st);
+        if (r == PFG_OK && z[i].proof_bytes) {    // the instance's own proof, as pfg_batch_download_proof gives it
+            j->proof.resize(z[i].proof_bytes);
+            r = pfg_batch_download_proof(ctx, i, j->proof.data());
+        }
         in.rc = r;
         if (r == PFG_OK) {
             in.status = st.status;
@@ -267,7 +272,6 @@ extern "C" int pfg_server_create(pfg_server** out, const pfg_options* opts, size
     *out = nullptr;
     pfg_server* s = new pfg_server();
     if (opts) s->opts = *opts; else pfg_default_options(&s->opts);
-    if (s->opts.proof_en) { delete s; return PFG_INVALID; }   // jobs carry no proof output
     s->slots = slots;
     s->max_batch = max_batch;
     if (cudaGetDevice(&s->device) != cudaSuccess) { cudaGetLastError(); delete s; return PFG_CUDA_ERROR; }
@@ -372,6 +376,18 @@ extern "C" int pfg_server_fetch(pfg_server* s, uint64_t ticket, uint32_t* lits, 
     put(pending_units, r.pending, a.pending, z.pending_units);
     put(stack, r.stack, a.stack, z.stack_words);
     put(round_ends, r.rends, a.rends, z.rounds);
+    return PFG_OK;
+}
+
+extern "C" int pfg_server_fetch_proof(pfg_server* s, uint64_t ticket, uint8_t* out) {
+    if (!s) return PFG_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(ticket);
+    if (it == s->jobs.end()) return PFG_INVALID;
+    const Job& j = *it->second;
+    if (!j.done) return PFG_PENDING;
+    if (j.info.rc != PFG_OK) return j.info.rc;
+    if (out && !j.proof.empty()) std::copy(j.proof.begin(), j.proof.end(), out);
     return PFG_OK;
 }
 

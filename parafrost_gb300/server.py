@@ -111,6 +111,13 @@ class Server:
         pend = np.empty(sz.pending_units, dtype=np.uint32)
         stack = np.empty(sz.stack_words, dtype=np.uint32)
         rends = np.empty(sz.rounds, dtype=np.uint64)
+        proof = b""
+        if sz.proof_bytes:       # before the fetch, which forgets the job
+            pb = np.empty(sz.proof_bytes, dtype=np.uint8)
+            rc = self.lib.pfg_server_fetch_proof(self._srv, ticket, _ptr(pb, C.c_uint8))
+            if rc != 0:
+                raise SimplifyError(rc, f"pfg_server_fetch_proof({ticket})")
+            proof = pb.tobytes()
         rc = self.lib.pfg_server_fetch(self._srv, ticket, _ptr(lits, C.c_uint32), _ptr(off, C.c_uint64),
                                        _ptr(learnt, C.c_uint8), _ptr(lbd, C.c_uint32), _ptr(usage, C.c_uint8),
                                        _ptr(elim, C.c_uint8), _ptr(units, C.c_uint32), _ptr(pend, C.c_uint32),
@@ -119,7 +126,7 @@ class Server:
             raise SimplifyError(rc, f"pfg_server_fetch({ticket})")
         stats = {"clauses_processed": info.clauses_processed, "batch_size": info.batch_size, "slot": info.slot}
         return SimplifyResult(int(info.status), Cnf(sz.max_var, lits, off, learnt, lbd, usage), elim, units, pend,
-                              stack, rends, stats)
+                              stack, rends, stats, proof)
 
     def stats(self) -> dict:
         st = _abi.PfgServerStats()

@@ -86,3 +86,21 @@ def test_unknown_ticket():
     with pg.Server(slots=1) as srv:
         with pytest.raises(pg.SimplifyError):
             srv.poll(12345)
+
+
+def test_served_proofs_are_the_ones_alone():
+    # proof lines per job (pfg_server_fetch_proof): byte for byte the oracle's
+    # and the instance's alone, whatever batch the job ran in
+    from tests.parity import proof_diff
+    opts = dict(phases=3, proof=True)
+    cnfs = jobs(12, base=700)
+    with pg.Server(slots=2, max_batch=4, **opts) as srv:
+        tickets = [srv.submit(c) for c in cnfs]
+        outs = [srv.fetch(t) for t in tickets]
+    assert any(len(r.proof) for r in outs)
+    for i, (cnf, res) in enumerate(zip(cnfs, outs)):
+        ref = po.simplify(cnf, pg.options_from(**opts))
+        assert not proof_diff(res.proof, ref.proof), f"job {i}: " + proof_diff(res.proof, ref.proof)
+        with pg.Simplifier(**opts) as s:
+            one = s.simplify(cnf)
+        assert res.proof == one.proof, f"job {i}: served proof differs from the instance alone"
