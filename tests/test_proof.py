@@ -115,8 +115,8 @@ def test_proof_text_writer():
             pg.proof_text(bad)
 
 
-def test_server_rejects_proofs():
+def test_server_proof_fetch_checks_its_arguments():
+    # served jobs carry their proof (pfg_server_fetch_proof, GPU-tested in
+    # test_gpu_serving.py); without a server the call is rejected, not run
     L = pg._lib.lib()
-    o = pg.options_from(proof=True)
-    srv = C.c_void_p()
-    assert L.pfg_server_create(C.byref(srv), C.byref(o), 0, 1, 1) == 5
+    assert L.pfg_server_fetch_proof(None, 0, None) == 5
