@@ -18,8 +18,9 @@ request loop (throughput, p50/p99 latency). `tseitin`, `ksat` and
   e2e   : the same metric through the C ABI with host buffers: upload (H2D),
           simplify and download (D2H) inside the timed region.
 
-`--impl reference` times the CPU restatement of the same passes (the oracle
-port; the reference's GPU simplifier cannot run here) on all host cores.
+`--impl reference` times the reference's own CPU simplifier (Solver::sigmify
+of src/cpu, built by oracle/ref_build.py) on every instance of the same
+workload on all host cores; where it is not built, the oracle port.
 """
 import argparse
 import gc
@@ -27,6 +28,7 @@ import concurrent.futures as cf
 import json
 import multiprocessing as mp
 import os
+import shutil
 import statistics
 import subprocess
 import sys
@@ -239,42 +241,115 @@ def dist_setup():
     return world, rank, local
 
 
-def oracle_run(args):
-    """One replica of the CPU restatement (run in a spawned worker)."""
-    wname, opts = args
+# ---- CPU side: the reference's own CPU simplifier (Solver::sigmify of src/cpu,
+# built by oracle/ref_build.py with the timing harness oracle/refcpu/time_main.cpp)
+# where it is built, else the oracle port (oracle/pfo.c). Inputs are generated and
+# written before any timing; only the simplify calls are timed. ----
+
+REF_CPU_BIN = os.path.join(ROOT, "oracle", "_ref", "pfref_cpu_time")
+
+
+def _write_instance(args):
+    """Generate one instance and write it as DIMACS (spawned worker; loads only
+    the host-only generator library)."""
+    spec, path = args
     sys.path.insert(0, ROOT)
     import parafrost_gb300 as pg
-    from oracle import pyoracle as po
-    cnf = make_cnf(WORKLOADS[wname])
-    t0 = time.perf_counter()
-    r = po.simplify(cnf, pg.options_from(**opts))
-    dt = time.perf_counter() - t0
-    processed = sum(s["clauses_before"] for s in r.round_stats)
-    return processed, dt
-
-
-def cpu_baseline(wname, opts, cores):
-    """Oracle port timed on host cores: `cores` independent replicas at once."""
-    ctx = mp.get_context("spawn")
-    with cf.ProcessPoolExecutor(cores, mp_context=ctx) as pool:
-        t0 = time.perf_counter()
-        res = list(pool.map(oracle_run, [(wname, opts)] * cores))
-        wall = time.perf_counter() - t0
-    processed = sum(r[0] for r in res)
-    return processed, wall, res
-
-
-def oracle_run_spec(args):
-    """The CPU restatement on one generated instance (run in a spawned worker)."""
-    spec, opts = args
-    sys.path.insert(0, ROOT)
-    import parafrost_gb300 as pg
-    from oracle import pyoracle as po
     cnf = pg.generate(*spec)
-    t0 = time.perf_counter()
-    r = po.simplify(cnf, pg.options_from(**opts))
-    dt = time.perf_counter() - t0
-    return sum(s["clauses_before"] for s in r.round_stats), dt
+    pg.write_dimacs(cnf, path)
+    return int(cnf.num_clauses)
+
+
+def _spec_clauses(spec):
+    """Clause count of a generated instance (spawned worker)."""
+    sys.path.insert(0, ROOT)
+    import parafrost_gb300 as pg
+    return int(pg.generate(*spec).num_clauses)
+
+
+def _port_group(specs):
+    """The oracle port on a group of instances, one after another (spawned
+    worker): returns (seconds of the simplify calls, clauses processed)."""
+    sys.path.insert(0, ROOT)
+    import parafrost_gb300 as pg
+    from oracle import pyoracle as po
+    secs, proc = 0.0, 0
+    opts = pg.options_from()
+    for sp in specs:
+        cnf = pg.generate(*sp)
+        t0 = time.perf_counter()
+        r = po.simplify(cnf, opts)
+        secs += time.perf_counter() - t0
+        proc += sum(s["clauses_before"] for s in r.round_stats)
+    return secs, proc
+
+
+def lpt_groups(sizes, k):
+    """Longest-processing-time assignment of items to k workers by size."""
+    groups, loads = [[] for _ in range(k)], [0] * k
+    for i in sorted(range(len(sizes)), key=lambda i: -sizes[i]):
+        j = min(range(k), key=loads.__getitem__)
+        groups[j].append(i)
+        loads[j] += sizes[i]
+    return [g for g in groups if g]
+
+
+class CpuSimplifier:
+    """A set of instances simplified on the host cores: `cores` workers, each
+    running its share of the instances one after another (one reference
+    process per instance). A step's time is the largest sum of simplify times
+    over the workers, which run at the same time."""
+
+    def __init__(self, specs, cores):
+        self.specs = list(specs)
+        self.cores = max(1, min(cores, len(self.specs)))
+        self.kind = "reference" if os.path.exists(REF_CPU_BIN) else "port"
+        ctx = mp.get_context("spawn")
+        uniq = sorted(set(self.specs))
+        with cf.ProcessPoolExecutor(min(self.cores, len(uniq)), mp_context=ctx) as pool:
+            if self.kind == "reference":
+                self.tmp = tempfile.mkdtemp(prefix="pfref_")
+                paths = {sp: os.path.join(self.tmp, f"i{k}.cnf") for k, sp in enumerate(uniq)}
+                sizes = dict(zip(uniq, pool.map(_write_instance, [(sp, paths[sp]) for sp in uniq])))
+                self.paths = [paths[sp] for sp in self.specs]
+            else:
+                sizes = dict(zip(uniq, pool.map(_spec_clauses, uniq)))
+        self.sizes = [sizes[sp] for sp in self.specs]
+        self.groups = lpt_groups(self.sizes, self.cores)
+
+    def _run_group(self, idx):
+        secs, proc = 0.0, 0
+        for i in idx:
+            p = subprocess.run([REF_CPU_BIN, self.paths[i], "--verbose=0"], capture_output=True, text=True)
+            line = next((x for x in p.stdout.splitlines() if x.startswith("pfref_cpu ")), None)
+            if line is None:
+                raise RuntimeError(f"reference CPU simplifier gave no result ({p.returncode}): {p.stderr[-500:]}")
+            kv = dict(t.split("=") for t in line.split()[1:])
+            secs += float(kv["seconds"])
+            proc += int(kv["processed"])
+        return secs, proc
+
+    def step(self):
+        """(seconds, clauses processed, wall seconds) of one pass over the set."""
+        t0 = time.perf_counter()
+        if self.kind == "reference":
+            with cf.ThreadPoolExecutor(len(self.groups)) as ex:
+                res = list(ex.map(self._run_group, self.groups))
+        else:
+            ctx = mp.get_context("spawn")
+            with cf.ProcessPoolExecutor(len(self.groups), mp_context=ctx) as pool:
+                res = list(pool.map(_port_group, [[self.specs[i] for i in g] for g in self.groups]))
+        wall = time.perf_counter() - t0
+        return max(r[0] for r in res), sum(r[1] for r in res), wall
+
+    def what(self):
+        if self.kind == "reference":
+            return "the reference's CPU simplifier (Solver::sigmify of src/cpu, oracle/_ref/pfref_cpu_time)"
+        return "the oracle port (oracle/pfo.c)"
+
+    def close(self):
+        if self.kind == "reference":
+            shutil.rmtree(self.tmp, ignore_errors=True)
 
 
 def batch_sample(specs, every):
@@ -282,64 +357,68 @@ def batch_sample(specs, every):
     return [sp for i, sp in enumerate(specs) if i % every == 0]
 
 
-def run_reference_batch(a, world, rank):
-    cores = os.cpu_count() or 1
-    specs = batch_sample(batch_specs(0), 4)
-    ctx = mp.get_context("spawn")
-    times, proc = [], 0
-    # a worker that dies raises BrokenProcessPool here instead of hanging the run
-    with cf.ProcessPoolExecutor(cores, mp_context=ctx) as pool:
-        for step in range(a.warmup + a.steps):
-            t0 = time.perf_counter()
-            res = list(pool.map(oracle_run_spec, [(sp, {}) for sp in specs], chunksize=1))
-            wall = time.perf_counter() - t0
-            if step >= a.warmup:
-                times.append(wall)
-                proc += sum(r[0] for r in res)
-    total = sum(times)
-    value = proc / total
-    line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": 1000.0 * total / a.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generators)",
-        "config": {"workload": "batched", "desc": BATCH["desc"], "options": "reference defaults"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"every 4th instance of the batch ({len(specs)} instances) per step, one "
-                                   f"instance per worker process on {cores} cores (oracle/pfo.c)"},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
-    return 0
+def batch_config():
+    """The batched workload as both arms report it."""
+    specs = batch_specs(0)
+    return {"workload": "batched", "desc": BATCH["desc"], "instances": len(specs),
+            "generator_seed": BATCH["seed"], "options": "reference defaults (phases=5, ERE on)"}
+
+
+def single_config(wname):
+    return {"workload": wname, "desc": WORKLOADS[wname]["desc"], "options": "reference defaults (phases=5, ERE on)"}
 
 
 def run_reference(a, world, rank):
+    """The reference's own CPU implementation of the path on all host cores,
+    on the same workload as the GPU arm (every instance of the batch, or one
+    replica of the single instance per core), each step one full pass."""
     if rank != 0:
         return 0
-    if a.workload == "batched":
-        return run_reference_batch(a, world, rank)
     cores = os.cpu_count() or 1
-    opts = {}
+    if a.workload == "batched":
+        specs = batch_specs(0)[:a.batch_n]
+        config = batch_config()
+        if a.batch_n:
+            config["instances"] = len(specs)
+        sample = f"all {len(specs)} instances of the batch per step"
+    else:
+        w = WORKLOADS[a.workload]
+        specs = [(w["family"], w["a"], w["b"], w["c"], w["seed"])] * cores
+        config = single_config(a.workload)
+        sample = f"{cores} concurrent replicas of the instance per step"
+    cpu = CpuSimplifier(specs, cores)
     for _ in range(a.warmup):
-        cpu_baseline(a.workload, opts, cores)
-    times, proc = [], 0
+        cpu.step()
+    total, proc, walls = 0.0, 0, []
     for _ in range(a.steps):
-        p, wall, _ = cpu_baseline(a.workload, opts, cores)
+        secs, p, wall = cpu.step()
+        total += secs
         proc += p
-        times.append(wall)
-    total = sum(times)
+        walls.append(wall)
+    cpu.close()
     value = proc / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1000.0 * total / a.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator)",
-        "config": {"workload": a.workload, "desc": WORKLOADS[a.workload]["desc"], "options": "reference defaults"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} concurrent replicas of the full workload per step (oracle/pfo.c, "
-                                   f"single-threaded each)"},
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generators)", "config": config,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu.cores, "kind": cpu.kind,
+                         "sample": f"{sample}: {cpu.what()}, {len(cpu.groups)} workers on {cores} host cores, each "
+                                   f"running its share one instance at a time; a step's time is the largest "
+                                   f"per-worker sum of simplify times (parsing and process start excluded)",
+                         "wall_ms_per_step": round(1000.0 * statistics.mean(walls), 1)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def cpu_baseline_line(specs, cores, sample):
+    cpu = CpuSimplifier(specs, cores)
+    secs, proc, wall = cpu.step()
+    cpu.close()
+    return {"value": proc / secs, "unit": UNIT, "cores": cpu.cores, "kind": cpu.kind,
+            "sample": f"{sample}: {cpu.what()}, {len(cpu.groups)} workers, one pass",
+            "wall_ms": round(1000.0 * wall, 1)}
 
 
 def run_gpu(a, world, rank, local):
@@ -441,13 +520,12 @@ def run_gpu(a, world, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": dev_ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic (seeded generator)",
-        "config": {"workload": a.workload, "desc": WORKLOADS[a.workload]["desc"],
-                   "options": "reference defaults (phases=5, ERE on)",
-                   "clauses_in": int(cnf.num_clauses), "literals_in": int(cnf.num_literals),
-                   "clauses_out": int(last.clauses_out), "rounds": int(last.rounds),
-                   "l2": "256 MB buffer written between steps; instance working set > L2",
-                   "parallelism": "replicas only" if world > 1 else "single GPU",
-                   "wall_ms_per_step_incl_upload": wall_ms / a.steps},
+        "config": single_config(a.workload),
+        "run": {"clauses_in": int(cnf.num_clauses), "literals_in": int(cnf.num_literals),
+                "clauses_out": int(last.clauses_out), "rounds": int(last.rounds),
+                "l2": "256 MB buffer written between steps; instance working set > L2",
+                "parallelism": "replicas only" if world > 1 else "single GPU",
+                "wall_ms_per_step_incl_upload": wall_ms / a.steps},
         "e2e": {"value": e2e_total / e2e_max, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_max / a.steps},
         "roofline": roofline,
@@ -456,9 +534,8 @@ def run_gpu(a, world, rank, local):
         "clocks": clk,
     }
     if not a.no_cpu_baseline:
-        p, wall, _ = cpu_baseline(a.workload, {}, 1)
-        line["cpu_baseline"] = {"value": p / wall, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": "the full workload once (oracle/pfo.c, one thread)"}
+        spec = (w["family"], w["a"], w["b"], w["c"], w["seed"])
+        line["cpu_baseline"] = cpu_baseline_line([spec], 1, "the full instance once on one core")
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -593,13 +670,12 @@ def run_gpu_batch(a, world, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": dev_ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic (seeded generators)",
-        "config": {"workload": "batched", "desc": BATCH["desc"], "instances": n, "clauses_in": cls_in,
-                   "literals_in": int(sum(int(c.num_literals) for c in cnfs)),
-                   "clauses_out": int(last.clauses_out), "max_rounds": int(last.rounds),
-                   "options": "reference defaults (phases=5, ERE on)",
-                   "tuning": dict(tuning, source="pfg_autotune on this batch" if not a.no_autotune else "built-in"),
-                   "l2": "256 MB buffer written before every timed simplify call (batched and plain)",
-                   "parallelism": "replicas only" if world > 1 else "single GPU"},
+        "config": batch_config(),
+        "run": {"instances": n, "clauses_in": cls_in, "literals_in": int(sum(int(c.num_literals) for c in cnfs)),
+                "clauses_out": int(last.clauses_out), "max_rounds": int(last.rounds),
+                "tuning": dict(tuning, source="pfg_autotune on this batch" if not a.no_autotune else "built-in"),
+                "l2": "256 MB buffer written before every timed simplify call (batched and plain)",
+                "parallelism": "replicas only" if world > 1 else "single GPU"},
         "plain": {"value": plain_value, "unit": UNIT, "ms_per_pass": plain_max,
                   "gpu_launches": int(plain_launches),
                   "e2e": {"value": pe2e_total / pe2e_max, "unit": UNIT, "ms_per_pass": 1000 * pe2e_max},
@@ -615,15 +691,9 @@ def run_gpu_batch(a, world, rank, local):
         "clocks": clk,
     }
     if not a.no_cpu_baseline:
-        specs = batch_sample(batch_specs(0), 16)
-        t0 = time.perf_counter()
-        p = 0
-        for sp in specs:
-            p += oracle_run_spec((sp, {}))[0]
-        wall = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": p / wall, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"every 16th instance of the batch ({len(specs)} instances), oracle/pfo.c "
-                                          f"on one thread"}
+        specs = batch_sample(batch_specs(0), 4)
+        line["cpu_baseline"] = cpu_baseline_line(specs, os.cpu_count() or 1,
+                                                 f"every 4th instance of the batch ({len(specs)} instances)")
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -653,7 +723,8 @@ def main():
                     help="batched line: built-in launch shapes instead of the autotuner's")
     ap.add_argument("--serve-jobs", type=int, default=SERVE["jobs"])
     ap.add_argument("--batch-n", type=int, default=None,
-                    help="with --single-step: only the first N instances of the batch (small profiling case)")
+                    help="with --single-step or --impl reference: only the first N instances of the batch "
+                         "(a small case for profiling and tests)")
     ap.add_argument("--single-step", action="store_true",
                     help="one simplify call of the workload, nothing timed (the command profiled by ncu)")
     a = ap.parse_args()

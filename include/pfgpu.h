@@ -8,8 +8,10 @@
  * (`Solver::simplifying`, src/gpu/simplify.cu:136-241) uploads the clause
  * database (`awaken`, simplify.cu:77-134), runs the round loop
  * (simplify.cu:163-186) and writes results back (simplify.cu:190-240).
- * The entry points below replace that body; the host adapter that a
- * maintainer drops into `Solver::simplifying` is shown in INTEGRATION.md.
+ * The entry points below replace that body: a host adapter inside
+ * `Solver::simplifying` calls pfg_upload after its rootify/shrinkTop, then
+ * pfg_simplify, pfg_result_sizes_get and pfg_download, and writes the
+ * clauses, units, eliminated variables and model stack back into the solver.
  *
  * Conventions
  *  - Literals use the reference's internal encoding: lit = 2*v | sign,
@@ -270,9 +272,13 @@ int  pfg_proof_text(const uint8_t* bin, uint64_t n, char* out, uint64_t cap, uin
  *
  * Scratch is one static 16 MiB device array per device, enough for a clause
  * store of about 1.3 million slots (live or deleted); a larger store is
- * rejected with PFG_INVALID and pfg_last_error says the limit. The first call
- * on a device looks the array up with cudaGetSymbolAddress, which may load
- * the module: make that first call before any stream capture. No scratch word
+ * rejected with PFG_INVALID and pfg_last_error says the limit. Every device
+ * that loads the library holds the array until the process exits, whether or
+ * not this call is used. Each call looks the array's address up with
+ * cudaGetSymbolAddress in the current context; the first call on a device
+ * may load the module, so make that first call before any stream capture.
+ * The context's device must be the current device (PFG_CUDA_ERROR
+ * otherwise). No scratch word
  * has to start at zero (each call writes every word before reading it). Calls
  * that overlap in time on one device -- from two threads, or on two contexts
  * whose streams run at once -- share the array and corrupt each other's
@@ -433,6 +439,20 @@ typedef struct pfg_tuning {
  * of range with PFG_INVALID and changes nothing then. */
 int pfg_tuning_get(pfg_ctx* ctx, pfg_tuning* out);
 int pfg_tuning_set(pfg_ctx* ctx, const pfg_tuning* t);
+
+/*
+ * Bounds of the two host-driven device loops of a simplify call: levels of
+ * device unit propagation (the loop of Solver::prop, src/gpu/elimbcp.cu:168-177)
+ * and Luby MIS rounds of one election (the loop of Solver::LCVE,
+ * src/gpu/lcve.cu:356-363). The reference loops until they converge; the
+ * engine gives up beyond a bound and pfg_simplify returns PFG_TIMEOUT with
+ * pfg_last_error naming the loop. 0 (the default) keeps the built-in bounds,
+ * max_var + 2 levels and (candidates + 2) rounds, which a correct run never
+ * reaches. A caller with a latency budget may set lower ones; a context that
+ * returned PFG_TIMEOUT holds a partial result and takes a new upload (or
+ * pfg_destroy). Kept across uploads.
+ */
+int pfg_set_loop_limits(pfg_ctx* ctx, uint32_t max_bcp_levels, uint32_t max_mis_rounds);
 
 /*
  * Measured choice of the launch shapes on the caller's instances: every trial

@@ -11,7 +11,9 @@ from ._abi import (PfgDimacsInfo, PfgInstance, PfgJobInfo, PfgOptions, PfgResult
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libpfgpu.so")
+GEN_LIB_PATH = os.path.join(_HERE, "libpfgen.so")
 _lib = None
+_gen = None
 
 u8p = C.POINTER(C.c_uint8)
 u32p = C.POINTER(C.c_uint32)
@@ -101,6 +103,8 @@ def lib():
     L.pfg_host_free.restype = None
     L.pfg_tuning_get.argtypes = [C.c_void_p, C.POINTER(PfgTuning)]
     L.pfg_tuning_get.restype = C.c_int
+    L.pfg_set_loop_limits.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32]
+    L.pfg_set_loop_limits.restype = C.c_int
     L.pfg_tuning_set.argtypes = [C.c_void_p, C.POINTER(PfgTuning)]
     L.pfg_tuning_set.restype = C.c_int
     L.pfg_autotune.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(PfgInstance), C.c_uint32, C.POINTER(PfgTuning)]
@@ -130,6 +134,22 @@ def lib():
     return L
 
 
+def gen_lib():
+    """The host-only generator library (pfg_generate without the engine)."""
+    global _gen
+    if _gen is not None:
+        return _gen
+    if not os.path.exists(GEN_LIB_PATH):
+        raise RuntimeError(
+            f"{GEN_LIB_PATH} is missing: build first (python -c 'import __graft_entry__ as g; g.build()')")
+    G = C.CDLL(GEN_LIB_PATH)
+    G.pfg_generate.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64,
+                               u32p, u64p, u64p, u32p, u64p]
+    G.pfg_generate.restype = C.c_int
+    _gen = G
+    return G
+
+
 # C-ABI entry points declared in include/pfgpu.h (checked by the CPU tests)
 EXPORTED = (
     "pfg_abi_sizes", "pfg_default_options", "pfg_resolve_options", "pfg_create", "pfg_upload", "pfg_simplify",
@@ -141,5 +161,6 @@ EXPORTED = (
     "pfg_dimacs_read", "pfg_dimacs_get_info", "pfg_dimacs_copy", "pfg_dimacs_error", "pfg_dimacs_free",
     "pfg_map_vars", "pfg_map_lits", "pfg_extend_model", "pfg_download_proof", "pfg_batch_download_proof",
     "pfg_proof_text", "pfg_host_alloc", "pfg_host_free", "pfg_tuning_get", "pfg_tuning_set", "pfg_autotune",
+    "pfg_set_loop_limits",
     "pfg_server_fetch_proof",
 )

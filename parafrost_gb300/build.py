@@ -3,6 +3,11 @@
 Every CUDA translation unit is compiled by nvcc in parallel with
 `-gencode arch=compute_103a,code=sm_103a`, then linked with the host
 generator code into one shared library next to this file.
+
+The seeded instance generators (csrc/gen.cpp) are also linked alone into
+`libpfgen.so`, a host-only library without CUDA: CPU-side users of the
+generators (the reference arm of bench.py, fixture scripts) load that one, so
+they never map the engine.
 """
 import concurrent.futures as cf
 import os
@@ -15,6 +20,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(HERE, "libpfgpu.so")
+GEN_LIB = os.path.join(HERE, "libpfgen.so")
 BUILD_DIR = os.path.join(HERE, "_build")
 
 CU_SOURCES = ["prims.cu", "ot.cu", "gc.cu", "bcp.cu", "lcve.cu", "elim.cu", "engine.cu", "server.cu", "tune.cu"]
@@ -36,9 +42,9 @@ def _deps():
 
 
 def _up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(GEN_LIB):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(GEN_LIB))
     return all(os.path.getmtime(f) <= t for f in _deps())
 
 
@@ -73,6 +79,9 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     tmp = LIB + ".tmp"
     _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs])
     os.replace(tmp, LIB)
+    gen_obj = os.path.join(BUILD_DIR, "gen.o")
+    _run(["g++", "-shared", "-o", GEN_LIB + ".tmp", gen_obj])
+    os.replace(GEN_LIB + ".tmp", GEN_LIB)
     if verbose or ptxas_info:
         sys.stderr.write("".join(logs))
     return LIB

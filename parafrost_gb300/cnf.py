@@ -85,8 +85,9 @@ def lit_to_int(lit: int) -> int:
 
 
 def generate(family: int, a: int, b: int, c: int, seed: int) -> Cnf:
-    """Seeded instance from the engine's C generators (pfg_generate)."""
-    lib = _lib.lib()
+    """Seeded instance from the C generators (pfg_generate of the host-only
+    libpfgen.so, the same code libpfgpu.so exports)."""
+    lib = _lib.gen_lib()
     mv = C.c_uint32()
     nc = C.c_uint64()
     nl = C.c_uint64()
@@ -116,14 +117,20 @@ def scale_free(num_vars: int, num_clauses: int, seed: int = 1, planted: bool = F
 
 
 def write_dimacs(cnf: Cnf, path: str, extra_units: Iterable[int] = ()) -> None:
+    """DIMACS text of `cnf` (clause order kept), then `extra_units` as unit
+    clauses. The literals and 0 terminators are laid out in one array first,
+    so the text is formatted in one pass."""
     units = list(extra_units)
+    lits = np.asarray(cnf.lits, dtype=np.int64)
+    ints = np.where(lits & 1, -(lits >> 1), lits >> 1)
+    n = cnf.num_clauses
+    lens = np.diff(np.asarray(cnf.off, dtype=np.int64))
+    words = np.zeros(len(ints) + n, dtype=np.int64)
+    words[np.arange(len(ints)) + np.repeat(np.arange(n), lens)] = ints
     with open(path, "w") as f:
-        f.write(f"p cnf {cnf.max_var} {cnf.num_clauses + len(units)}\n")
-        lits = cnf.lits
-        off = cnf.off
-        ints = np.where(lits & 1, -(lits >> 1).astype(np.int64), (lits >> 1).astype(np.int64))
-        for i in range(cnf.num_clauses):
-            f.write(" ".join(map(str, ints[int(off[i]):int(off[i + 1])].tolist())) + " 0\n")
+        f.write(f"p cnf {cnf.max_var} {n + len(units)}\n")
+        if n:
+            f.write(" ".join(map(str, words.tolist())).replace(" 0 ", " 0\n") + "\n")
         for u in units:
             f.write(f"{u} 0\n")
 

@@ -245,7 +245,8 @@ bool bcp_prop(Ctx& c) {
     cudaMemsetAsync(&c.dc->bcp_level, 0, sizeof(uint32_t), c.s);
     const unsigned grid = sm_count() * tuned(c.tune.bcp_blocks_per_sm, BCP_BLOCKS_PER_SM);
     uint32_t levels = 0;
-    const uint32_t max_levels = c.V + 2;   // every level assigns at least one new variable
+    // every level assigns at least one new variable, so V + 2 levels always suffice
+    const uint32_t max_levels = c.lim_bcp_levels ? c.lim_bcp_levels : c.V + 2;
     const bool single = c.ninst == 1;
     for (int batch = 1;; batch = std::min(batch << 1, 64)) {
         for (int b = 0; b < batch; b++) {

@@ -8,7 +8,6 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -1712,6 +1711,13 @@ extern "C" int pfg_tuning_get(pfg_ctx* o, pfg_tuning* out) {
     return PFG_OK;
 }
 
+extern "C" int pfg_set_loop_limits(pfg_ctx* o, uint32_t max_bcp_levels, uint32_t max_mis_rounds) {
+    if (!o) return PFG_INVALID;
+    o->c.lim_bcp_levels = max_bcp_levels;
+    o->c.lim_mis_rounds = max_mis_rounds;
+    return PFG_OK;
+}
+
 extern "C" int pfg_tuning_set(pfg_ctx* o, const pfg_tuning* t) {
     if (!o || !t) return PFG_INVALID;
     auto threads_ok = [](uint32_t v) { return v == 0 || (v % 32 == 0 && v <= 1024); };
@@ -1778,10 +1784,6 @@ namespace {
 constexpr size_t NOALLOC_SCRATCH_BYTES = 16ull << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
-
 size_t noalloc_bytes(uint64_t n) {
     return align_up(4 * (n + 1)) + align_up(8 * (n + 1)) + scan_temp_bytes(n + 1);
 }
@@ -1796,24 +1798,22 @@ uint64_t noalloc_max_slots() {
     return lo;
 }
 
-// device address of the scratch array; looked up once per device
+// Device address of the scratch array in the current context. The lookup is
+// made on every call (it allocates nothing once the module is loaded), so an
+// address never outlives the context it belongs to (a device reset or a
+// re-created primary context gives the array a new address).
 bool noalloc_scratch(Ctx& c, char** out) {
     int dev = -1;
     if (!cuda_ok(c, cudaGetDevice(&dev), "cudaGetDevice")) return false;
     if (dev != c.device) { c.err = "the context's device is not the current device"; return false; }
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) { c.err = "device index out of range"; return false; }
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            c.err = std::string("cudaGetSymbolAddress of the download scratch failed: ") + cudaGetErrorString(e);
-            return false;
-        }
-        g_noalloc_ptr[dev] = p;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        c.err = std::string("cudaGetSymbolAddress of the download scratch failed: ") + cudaGetErrorString(e);
+        return false;
     }
-    *out = (char*)g_noalloc_ptr[dev];
+    *out = (char*)p;
     return true;
 }
 

@@ -213,6 +213,8 @@ struct Ctx {
     // round state
     int simpstate = 0;
     uint32_t mis_rounds = 0;
+    // host-side bounds of the device loops (0: the built-in bound from V)
+    uint32_t lim_bcp_levels = 0, lim_mis_rounds = 0;
     pfg_stats stats{};
     double pass_ms[8] = {0};
 

@@ -430,7 +430,9 @@ bool lcve(Ctx& c) {
             sync_counters(c);
             if (!c.err.empty()) return false;
             if (c.hc->nwin == 0) done = true;          // the last round found nothing undecided
-            else if (r > nwork + 2) { c.err = "MIS did not converge"; c.simpstate = PFG_TIMEOUT; return false; }
+            else if (r > (c.lim_mis_rounds ? (uint64_t)c.lim_mis_rounds : (uint64_t)nwork + 2)) {
+                c.err = "MIS did not converge"; c.simpstate = PFG_TIMEOUT; return false;
+            }
         }
         c.mis_rounds = r;
         // elected in (instance, round, rank) order: select in rank order, then a

@@ -290,6 +290,13 @@ class Simplifier:
             out[self.lib.pfg_profile_name(i).decode()] = {"launches": n.value, "ms": ms.value, "alg_bytes": b.value}
         return out
 
+    def set_loop_limits(self, max_bcp_levels: int = 0, max_mis_rounds: int = 0) -> None:
+        """Bounds of the device propagation levels and MIS rounds of a simplify
+        call (pfg_set_loop_limits); beyond one the call raises SimplifyError
+        with code PFG_TIMEOUT. 0 keeps the built-in bound."""
+        self._check(self.lib.pfg_set_loop_limits(self._ctx, int(max_bcp_levels), int(max_mis_rounds)),
+                    "pfg_set_loop_limits")
+
     def kernel_launches(self) -> int:
         return int(self.lib.pfg_kernel_launches(self._ctx))
 

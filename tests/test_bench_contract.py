@@ -1,5 +1,6 @@
 """CPU checks of bench.py's contract: the reference arm's JSON line (it runs the
-oracle port on the host cores, no GPU) and the traffic table's kernel groups."""
+reference's CPU simplifier, or the oracle port where that is not built, on the
+host cores, no GPU) and the traffic table's kernel groups."""
 import json
 import os
 import subprocess
@@ -13,7 +14,7 @@ sys.path.insert(0, ROOT)
 
 def test_reference_arm_line():
     p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "0"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+                        "--warmup", "0", "--batch-n", "24"], capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert p.returncode == 0, p.stderr[-2000:]
     line = json.loads(p.stdout.strip().splitlines()[-1])
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",

@@ -87,3 +87,34 @@ def test_batch_context_is_rejected():
     with pg.Simplifier() as sim:
         sim.upload_batch([inst(1), inst(2)])
         assert sim.lib.pfg_download_device_noalloc(sim._ctx, None, None, None, None, None) == 5
+
+
+def test_second_call_allocates_no_device_memory():
+    """Device memory in use is the same before and after a call: the caller's
+    buffers are made first, one call warms the module up, then the free bytes
+    the driver reports and torch's allocator counters must not move."""
+    import torch
+    cnf = with_learnts(inst(4, scale=2), 4)
+    with pg.Simplifier() as sim:
+        sim.upload(cnf)
+        sim.run()
+        want = expected(sim.download())
+        sz = _abi.PfgResultSizes()
+        assert sim.lib.pfg_result_sizes_get(sim._ctx, C.byref(sz)) == 0
+        nc, nl = int(sz.clauses), int(sz.literals)
+        lits = torch.empty(max(nl, 1), dtype=torch.int32, device="cuda")
+        off = torch.empty(nc + 1, dtype=torch.int64, device="cuda")
+
+        def call():
+            return sim.lib.pfg_download_device_noalloc(sim._ctx, lits.data_ptr(), off.data_ptr(), None, None, None)
+
+        assert call() == 0, sim.lib.pfg_last_error(sim._ctx)
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        alloc0, reserved0 = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+        assert call() == 0, sim.lib.pfg_last_error(sim._ctx)
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0, "free device memory changed across the call"
+        assert torch.cuda.memory_allocated() == alloc0 and torch.cuda.memory_reserved() == reserved0
+        assert np.array_equal(lits.cpu().numpy().view(np.uint32)[:nl], want["lits"])
+        assert np.array_equal(off.cpu().numpy().view(np.uint64), want["off"])
