@@ -51,7 +51,8 @@ def input_digest(cnf: Cnf) -> str:
     for i in range(cnf.num_clauses):
         a, b = int(off[i]), int(off[i + 1])
         lits[a:b].sort()
-    return _h(off, lits, np.asarray(cnf.learnt, np.uint8))
+    learnt = np.zeros(cnf.num_clauses, np.uint8) if cnf.learnt is None else np.asarray(cnf.learnt, np.uint8)
+    return _h(off, lits, learnt)
 
 
 def canon(status: int, cnf: Cnf | None, elim, units, pending, stack, rounds: int) -> dict:
