@@ -62,12 +62,13 @@ BATCH = dict(n=512, vmin=1_000, vmax=200_000, seed=7,
 # serving workload: Poisson stream of 10,000 jobs, clause counts log-uniform on [1e3, 1e6]
 # from the three generators, admitted by a 120 GB device-arena budget, 3 rounds each.
 # Jobs are drawn from a pool of seeded instances (with replacement).
-SERVE = dict(jobs=10_000, cmin=1_000, cmax=1_000_000, pool=1024, rates=(800.0, 1600.0, 3200.0, 6400.0),
-             budget=120_000_000_000, tight_budget=4_000_000_000, phases=3, slots=4, max_batch=512, seed=11,
+SERVE = dict(jobs=10_000, cmin=1_000, cmax=1_000_000, pool=1024, rates=(800.0, 1600.0, 3200.0, 6400.0, 12800.0),
+             budget=120_000_000_000, tight_budget=500_000_000, phases=3, slots=4, max_batch=512, clients=8,
+             seed=11,
              desc="Poisson arrivals of 10,000 jobs at fixed offered rates, swept until the loop saturates; clause "
                   "counts log-uniform 1e3..1e6 from random 3-SAT / Tseitin / scale-free generators (pool of 1024 "
-                  "seeded instances drawn with replacement); admission by a 120 GB device-arena budget, and once "
-                  "at saturation by a 4 GB budget that binds; 3 rounds per job")
+                  "seeded instances drawn with replacement) submitted by 8 client threads; admission by a 120 GB "
+                  "device-arena budget, and once at saturation by a 0.5 GB budget that binds; 3 rounds per job")
 
 METRIC = "inprocessing clauses/s (BVE+SUB)"
 UNIT = "clauses/s"
@@ -129,7 +130,10 @@ def serve_pool(rank=0):
 
 def serve_stream(pool, jobs, rate, rank=0, budget=None):
     """Submit `jobs` jobs drawn from `pool` with Poisson arrivals at `rate` jobs/s;
-    returns throughput, latency percentiles and the server's counters."""
+    returns throughput, latency percentiles and the server's counters. The
+    stream is driven by SERVE["clients"] client threads: client t submits the
+    jobs k = t mod clients at their arrival times and fetches their results in
+    order, as independent clients of one service would."""
     import threading
     import numpy as np
     import parafrost_gb300 as pg
@@ -139,27 +143,36 @@ def serve_stream(pool, jobs, rate, rank=0, budget=None):
     arrivals = np.cumsum(gaps) - gaps[0]
     infos = [None] * jobs
     tickets = [None] * jobs
-    have = threading.Semaphore(0)
+    P = SERVE["clients"]
+    have = [threading.Semaphore(0) for _ in range(P)]
+    late = [0.0] * P
     with pg.Server(arena_bytes=budget or SERVE["budget"], slots=SERVE["slots"], max_batch=SERVE["max_batch"],
                    phases=SERVE["phases"]) as srv:
-        def collect():
-            for k in range(jobs):
-                have.acquire()
+        def collect(t):
+            for k in range(t, jobs, P):
+                have[t].acquire()
                 infos[k] = srv.wait(tickets[k])
                 srv.fetch(tickets[k])
-        th = threading.Thread(target=collect)
-        th.start()
+
+        def produce(t, t0):
+            for k in range(t, jobs, P):
+                dt = t0 + arrivals[k] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                else:
+                    late[t] = max(late[t], -dt)
+                tickets[k] = srv.submit(pool[picks[k]])
+                have[t].release()
+
+        cols = [threading.Thread(target=collect, args=(t,)) for t in range(P)]
+        for th in cols:
+            th.start()
         t0 = time.perf_counter()
-        late = 0.0
-        for k in range(jobs):
-            dt = t0 + arrivals[k] - time.perf_counter()
-            if dt > 0:
-                time.sleep(dt)
-            else:
-                late = max(late, -dt)
-            tickets[k] = srv.submit(pool[picks[k]])
-            have.release()
-        th.join()
+        prods = [threading.Thread(target=produce, args=(t, t0)) for t in range(P)]
+        for th in prods:
+            th.start()
+        for th in prods + cols:
+            th.join()
         st = srv.stats()
     lat = np.array([i.latency_s for i in infos]) * 1e3
     qlat = np.array([i.queue_s for i in infos]) * 1e3
@@ -175,7 +188,8 @@ def serve_stream(pool, jobs, rate, rank=0, budget=None):
         "mean_batch": float(np.mean([i.batch_size for i in infos])),
         "max_in_flight_batches": st["max_in_flight_batches"], "max_jobs_in_flight": st["max_jobs_in_flight"],
         "peak_admitted_gb": st["peak_est_bytes"] / 1e9, "budget_gb": st["budget_bytes"] / 1e9,
-        "slots": SERVE["slots"], "max_batch": SERVE["max_batch"], "producer_max_lateness_s": late,
+        "slots": SERVE["slots"], "max_batch": SERVE["max_batch"], "clients": P,
+        "producer_max_lateness_s": max(late),
         "latency": "submit to result on the host (admission wait, upload, rounds, download)",
     }
 
@@ -751,14 +765,26 @@ def main():
                          "(a small case for profiling and tests)")
     ap.add_argument("--single-step", action="store_true",
                     help="one simplify call of the workload, nothing timed (the command profiled by ncu)")
+    ap.add_argument("--groups", action="store_true",
+                    help="with --single-step: print each kernel group's launches, event-timed ms and "
+                         "algorithmic bytes")
     a = ap.parse_args()
     world, rank, local = dist_setup()
     if a.single_step and a.workload == "batched":
         import parafrost_gb300 as pg
+        cnfs = make_batch(0, a.batch_n)
         with pg.Simplifier() as sim:
-            outs = sim.simplify_batch(make_batch(0, a.batch_n))
-        print(json.dumps({"workload": "batched", "instances": len(outs),
-                          "clauses_out": int(sum(o.cnf.num_clauses for o in outs))}))
+            if a.groups:
+                sim.profile(True)
+            outs = sim.simplify_batch(cnfs)
+            groups = sim.profile_report() if a.groups else None
+        line = {"workload": "batched", "instances": len(outs),
+                "clauses_in": int(sum(c.num_clauses for c in cnfs)),
+                "literals_in": int(sum(c.num_literals for c in cnfs)),
+                "clauses_out": int(sum(o.cnf.num_clauses for o in outs))}
+        if groups:
+            line["groups"] = {k: v for k, v in groups.items() if v["launches"]}
+        print(json.dumps(line))
         return 0
     if a.single_step:
         import parafrost_gb300 as pg

@@ -96,7 +96,6 @@ struct DevCounters {
     uint32_t pf_blocks;                      // proof blocks reserved in the running pass
     uint32_t mis_done;                       // a MIS round found nothing undecided: later rounds return at once
     uint32_t steal[4];                       // next variable of the warp kernels (SUB, BVE 1, BVE 3)
-    unsigned long long rec_bump;             // stage-record words handed out in the running round
 };
 
 constexpr uint32_t ERR_UNITS_OVERFLOW = 1u;

@@ -45,12 +45,6 @@ struct EK {
     uint32_t pf_bcap;
     const uint8_t* lbyte;                // proof bytes per literal
     uint8_t* cnew;                       // clauses added or rewritten in place (occurrence-table update)
-    // stage records (elimw.cuh): per elected index the word offset of its
-    // variable's staged lists in rec_store, or REC_NONE
-    uint32_t* rec_store;
-    unsigned long long rec_cap;          // words
-    unsigned long long* rec_bump;        // words handed out
-    unsigned long long* rec;
 };
 
 PFG_D uint32_t* OLp(const EK& k, uint32_t lit) { return k.ot_ids + k.ot_off[lit]; }
@@ -1493,13 +1487,8 @@ EK make_ek(Ctx& c) {
     k.pf_bcap = c.pf_bcap;
     k.lbyte = c.lbyte;
     k.cnew = c.cnew;
-    k.rec_store = c.rec_store;
-    k.rec_cap = c.rec_cap;
-    k.rec_bump = &c.dc->rec_bump;
-    k.rec = c.rec;
     return k;
 }
-
 
 // proof words BVE emission needs: the resolvent lines of every variable whose slots fit
 __global__ void pf_need_k(const uint32_t* type, const uint32_t* ucnt, const uint8_t* fits, uint32_t E,
@@ -1568,40 +1557,6 @@ static unsigned warp_grid(unsigned occ, uint32_t want, uint32_t nvars) {
     const uint64_t per_sm = want ? std::min<unsigned>(want, occ) : occ;
     const uint64_t need = ((uint64_t)nvars + WS_WARPS - 1) / WS_WARPS;
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(need, per_sm * sm_count()));
-}
-
-// Stage records for the SUB and BVE passes of a round: room for one record of
-// every elected variable (4 header words + 5 words per clause + its literals,
-// rounded to 4 words; the lists only shrink between the volume count and the
-// passes), every record offset cleared. Without the room the passes gather
-// from the clause store as before.
-bool rec_prepare(Ctx& c) {
-    const uint64_t E = c.nve;
-    const uint64_t words = 7 * E + 5 * c.ve_CE + c.ve_LE + 64;
-    if (words > c.rec_cap) {
-        if (c.rec_store) dfree(c, c.rec_store);
-        c.rec_store = nullptr;
-        c.rec_cap = 0;
-        const uint64_t want = words + words / 4;
-        if (!dalloc_t(c, &c.rec_store, want)) { c.err.clear(); cudaGetLastError(); }
-        else c.rec_cap = want;
-    }
-    if (E > c.rec_slots) {
-        if (c.rec) dfree(c, c.rec);
-        c.rec = nullptr;
-        c.rec_slots = 0;
-        const uint64_t want = E + E / 4 + 1024;
-        if (!dalloc_t(c, &c.rec, want)) { c.err.clear(); cudaGetLastError(); }
-        else c.rec_slots = want;
-    }
-    if (!c.rec_store || !c.rec) {
-        c.rec_cap = 0;
-        if (c.rec) { dfree(c, c.rec); c.rec = nullptr; c.rec_slots = 0; }
-        return true;
-    }
-    cudaMemsetAsync(c.rec, 0xFF, E * sizeof(unsigned long long), c.s);
-    cudaMemsetAsync(&c.dc->rec_bump, 0, sizeof(unsigned long long), c.s);
-    return true;
 }
 
 bool sub_pass(Ctx& c) {

@@ -149,6 +149,13 @@ PFG_D void ws_flush(const EK& k, WS& w, unsigned lane) {
     __syncwarp();
 }
 
+PFG_D void ws_set_meta(WS& w, uint32_t c, uint32_t m, unsigned lane) {
+    __syncwarp();
+    if (lane == 0) w.meta[c] = m;
+    __syncwarp();
+}
+PFG_D void ws_melt(WS& w, uint32_t c, uint32_t f, unsigned lane) { ws_set_meta(w, c, m_set_molten(w.meta[c], f), lane); }
+
 PFG_D uint32_t warp_excl_scan(uint32_t v, unsigned lane, uint32_t& total) {
     uint32_t incl = v;
 #pragma unroll
@@ -159,141 +166,6 @@ PFG_D uint32_t warp_excl_scan(uint32_t v, unsigned lane, uint32_t& total) {
     total = __shfl_sync(FULL, incl, 31);
     return incl - v;
 }
-
-// ---- stage records ----
-// What a pass leaves on the stage of a variable is what the next pass on that
-// variable would gather back from the clause store: SUB's clauses still in
-// the two lists after updateOL, in list order, and BVE phase 1's stage of a
-// variable that goes on to emission. Elected variables share no clause, so
-// nothing else changes those clauses in between. Each is written as one
-// contiguous record, which the next pass reads with coalesced loads instead
-// of gathering 16-byte headers and a few literals per clause id.
-// Record (words, 16-byte aligned): np, nn, nlit, nc, then id[nc], meta[nc],
-// size[nc], sig[nc], goff[nc], then the nlit literal words in stage order.
-constexpr unsigned long long REC_NONE = ~0ull;
-
-PFG_D unsigned long long rec_words(uint32_t nc, uint32_t nlit) {
-    return (4ull + 5ull * nc + nlit + 3ull) & ~3ull;
-}
-
-PFG_D unsigned long long rec_get(const EK& k, uint32_t e) { return k.rec ? k.rec[e] : REC_NONE; }
-
-PFG_D void rec_set(const EK& k, uint32_t e, unsigned long long r, unsigned lane) {
-    if (k.rec && lane == 0) k.rec[e] = r;
-}
-
-// Writes the stage as the record of elected index e. With `compact`, only
-// the clauses whose w.outs word has bit 0 set are written (in stage order).
-PFG_D void ws_store_rec(const EK& k, WS& w, uint32_t e, bool compact, unsigned lane) {
-    __syncwarp();
-    if (!k.rec) return;
-    const uint32_t nc0 = w.np + w.nn;
-    uint32_t np = 0, nc = 0, nlit = 0;
-    // new index and literal offset of every kept clause, packed into w.outs:
-    // bit 0 kept, bits 1-7 index (< 96), bits 8-31 literal offset (< 448)
-    for (uint32_t c0 = 0; c0 < nc0; c0 += 32) {
-        const uint32_t i = c0 + lane;
-        const bool kp = i < nc0 && (!compact || (w.outs[i] & 1u));
-        const uint32_t sz = kp ? w.size[i] : 0u;
-        uint32_t t, lt;
-        const uint32_t ex = warp_excl_scan(kp ? 1u : 0u, lane, t);
-        const uint32_t lex = warp_excl_scan(sz, lane, lt);
-        np += __popc(__ballot_sync(FULL, kp && i < w.np));
-        if (i < nc0) w.outs[i] = kp ? (1u | ((nc + ex) << 1) | ((nlit + lex) << 8)) : 0u;
-        nc += t;
-        nlit += lt;
-    }
-    __syncwarp();
-    const unsigned long long words = rec_words(nc, nlit);
-    unsigned long long r = 0;
-    if (lane == 0) {
-        r = atomicAdd(k.rec_bump, words);
-        if (r + words > k.rec_cap) r = REC_NONE;
-    }
-    r = __shfl_sync(FULL, r, 0);
-    if (r == REC_NONE) { rec_set(k, e, REC_NONE, lane); return; }
-    uint32_t* R = k.rec_store + r;
-    if (lane == 0) *reinterpret_cast<uint4*>(R) = make_uint4(np, nc - np, nlit, nc);
-    uint32_t* A = R + 4;
-    uint32_t* L = A + 5 * nc;
-    for (uint32_t i = lane; i < nc0; i += 32) {
-        const uint32_t o = w.outs[i];
-        if (!(o & 1u)) continue;
-        const uint32_t j = (o >> 1) & 0x7Fu, lo = o >> 8;
-        A[j] = w.id[i];
-        A[nc + j] = w.meta[i];
-        A[2 * nc + j] = w.size[i];
-        A[3 * nc + j] = w.sig[i];
-        A[4 * nc + j] = w.goff[i];
-        const uint32_t* src = WL(w, i);
-        for (uint32_t t = 0; t < w.size[i]; t++) L[lo + t] = src[t];
-    }
-    rec_set(k, e, r, lane);
-    __syncwarp();
-}
-
-// Loads record r into the stage (the inverse of ws_store_rec).
-PFG_D void ws_load_rec(const EK& k, WS& w, unsigned long long r, unsigned lane) {
-    const uint32_t* R = k.rec_store + r;
-    const uint4 h = *reinterpret_cast<const uint4*>(R);
-    const uint32_t nc = h.w, nlit = h.z;
-    const uint32_t* A = R + 4;
-    const uint32_t* L = A + 5 * nc;
-    for (uint32_t i = lane; i < nc; i += 32) {
-        w.id[i] = A[i];
-        const uint32_t m = A[nc + i];
-        w.meta[i] = m;
-        w.meta0[i] = m;
-        w.size[i] = A[2 * nc + i];
-        w.sig[i] = A[3 * nc + i];
-        w.goff[i] = A[4 * nc + i];
-        w.dirty[i] = 0;
-    }
-    __syncwarp();
-    uint32_t base = 0;
-    for (uint32_t c0 = 0; c0 < nc; c0 += 32) {
-        const uint32_t i = c0 + lane;
-        uint32_t t;
-        const uint32_t ex = warp_excl_scan(i < nc ? w.size[i] : 0u, lane, t);
-        if (i < nc) w.off[i] = base + ex;
-        base += t;
-    }
-    for (uint32_t g = lane; g < nlit; g += 32) w.lits[g] = L[g];
-    if (lane == 0) { w.np = h.x; w.nn = h.y; w.nlit = nlit; }
-    __syncwarp();
-}
-
-// The stage of elected index e: its record when there is one, else gathered
-// from the clause store. False if the lists do not fit the stage.
-PFG_D bool ws_stage_e(const EK& k, WS& w, uint32_t e, uint32_t p, uint32_t n, unsigned lane) {
-    const unsigned long long r = rec_get(k, e);
-    if (r != REC_NONE) { ws_load_rec(k, w, r, lane); return true; }
-    return ws_stage(k, w, p, n, lane);
-}
-
-// Rewrites the meta words of record r from the stage (same clauses, same order).
-PFG_D void ws_rec_meta(const EK& k, const WS& w, unsigned long long r, unsigned lane) {
-    __syncwarp();
-    uint32_t* A = k.rec_store + r + 4;
-    const uint32_t nc = w.np + w.nn;
-    for (uint32_t i = lane; i < nc; i += 32) A[nc + i] = w.meta[i];
-    __syncwarp();
-}
-
-// L2 prefetch of the first lines of elected index e's record.
-PFG_D void rec_prefetch(const EK& k, uint32_t e, unsigned lane) {
-    const unsigned long long r = rec_get(k, e);
-    if (r == REC_NONE || lane >= 8) return;
-    const unsigned long long wo = r + 32ull * lane;
-    if (wo < k.rec_cap) asm volatile("prefetch.global.L2 [%0];" :: "l"(k.rec_store + wo));
-}
-
-PFG_D void ws_set_meta(WS& w, uint32_t c, uint32_t m, unsigned lane) {
-    __syncwarp();
-    if (lane == 0) w.meta[c] = m;
-    __syncwarp();
-}
-PFG_D void ws_melt(WS& w, uint32_t c, uint32_t f, unsigned lane) { ws_set_meta(w, c, m_set_molten(w.meta[c], f), lane); }
 
 // merge(x, c1, c2, unit) on staged clauses (elimination.cuh:242-270)
 PFG_D int ws_merge_cnt(WS& w, uint32_t x, uint32_t c1, uint32_t c2, uint32_t& unit) {
@@ -870,9 +742,7 @@ PFG_D bool ws_fun_possible(const EK& k, WS& w, uint32_t x, unsigned lane) {
 }
 
 // BVE phase 1 for one staged variable (bounded.cuh:282-394)
-// Returns true when the variable's counts were stored for emission (BVE phase 3
-// reads its stage again).
-PFG_D bool ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, uint32_t* ucnt,
+PFG_D void ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, uint32_t* ucnt,
                   unsigned long long* rpos, unsigned long long* rref, uint32_t* dlist, uint32_t* dcount,
                   unsigned lane) {
     const uint32_t p = 2 * x, n = p | 1;
@@ -931,7 +801,7 @@ PFG_D bool ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
                             ucnt[tid] = nC;
                             rpos[tid] = (unsigned long long)pOrgs | ((unsigned long long)nOrgs << 32);
                         }
-                        return false;
+                        return;
                     }
                     if (nC) break;
                     nE = 0; nC = 0; nL = 0;
@@ -973,11 +843,11 @@ PFG_D bool ws_ve1(const EK& k, WS& w, uint32_t tid, uint32_t x, uint32_t* type, 
         else ws_toblivion(k, w, P, N, lane);
         ws_flush(k, w, lane);
         if (lane == 0) k.elim[x] |= MELTING_MASK;
-        return false;
     }
-    ws_flush(k, w, lane);
-    if (elimType) ws_store_info(tid, elimType, nE, nC, nL, type, ucnt, rpos, rref, lane);
-    return elimType != 0;
+    else {
+        ws_flush(k, w, lane);
+        if (elimType) ws_store_info(tid, elimType, nE, nC, nL, type, ucnt, rpos, rref, lane);
+    }
 }
 
 __global__ void __launch_bounds__(WS_WARPS * 32) ve1w_k(EK k, const uint32_t* elected, uint32_t nelected,
@@ -992,23 +862,13 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve1w_k(EK k, const uint32_t* el
         qn = ws_ticket(steal, lane);     // drawn ahead: its lists are prefetched while this one runs
         const uint32_t tid = q;
         const uint32_t x = elected[tid];
-        const unsigned long long r = rec_get(k, tid);
-        const bool next_rec = qn < nelected && rec_get(k, qn) != REC_NONE;
-        const NextLists nl = next_rec ? NextLists{0, 0, 0, 0} : ws_next_lists(k, elected, qn, nelected);
-        if (r != REC_NONE) ws_load_rec(k, w, r, lane);
-        else if (!ws_stage(k, w, 2 * x, 2 * x + 1, lane)) {
+        const NextLists nl = ws_next_lists(k, elected, qn, nelected);
+        if (!ws_stage(k, w, 2 * x, 2 * x + 1, lane)) {
             if (lane == 0) big[atomicAdd(nbig, 1u)] = tid;
             continue;
         }
-        // the stage goes on to phase 3 as a record; any other outcome drops it
-        if (ws_ve1(k, w, tid, x, type, ucnt, rpos, rref, dlist, dcount, lane)) {
-            if (r != REC_NONE) ws_rec_meta(k, w, r, lane);
-            else ws_store_rec(k, w, tid, false, lane);
-        } else if (r != REC_NONE) {
-            rec_set(k, tid, REC_NONE, lane);
-        }
-        if (next_rec) rec_prefetch(k, qn, lane);
-        else ws_prefetch_lists(k, nl, lane);
+        ws_ve1(k, w, tid, x, type, ucnt, rpos, rref, dlist, dcount, lane);
+        ws_prefetch_lists(k, nl, lane);
         __syncwarp();
     }
 }
@@ -1034,7 +894,7 @@ __global__ void __launch_bounds__(WS_WARPS * 32) ve3w_k(EK k, const uint32_t* el
         const uint32_t et = xinfo & 3u;
         if (!et) continue;
         const uint32_t p = 2 * x, n = p | 1;
-        if (!ws_stage_e(k, w, tid, p, n, lane)) {
+        if (!ws_stage(k, w, p, n, lane)) {
             if (lane == 0) big[atomicAdd(nbig, 1u)] = tid;
             continue;
         }
@@ -1284,7 +1144,6 @@ PFG_D void ws_update_ol(const EK& k, WS& w, const Side& L, unsigned lane) {
             const uint32_t m = w.meta[c];
             if (m_molten(m)) w.meta[c] = m_set_molten(m, 0);
             else keepit = !m_deleted(m);
-            w.outs[c] = keepit ? 1u : 0u;     // what stays in the list: the stage record's clauses
         }
         uint32_t t;
         const uint32_t ex = warp_excl_scan(keepit ? 1u : 0u, lane, t);
@@ -1360,6 +1219,5 @@ __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* el
         ws_update_ol(k, w, P, lane);
         ws_update_ol(k, w, N, lane);
         ws_flush(k, w, lane);
-        ws_store_rec(k, w, e, true, lane);
     }
 }

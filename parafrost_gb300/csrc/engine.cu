@@ -1106,9 +1106,6 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
                    c.ot_size, c.ot_ids, &c.dc->live_cls);
         sync_counters(c);
         const uint64_t CE = c.hc->live_cls, LE = c.hc->live_lits;
-        c.ve_CE = CE;
-        c.ve_LE = LE;
-        rec_prepare(c);
         uint64_t Cin = 0, Lin = 0;
         for (uint32_t i = 0; i < n; i++)
             if (c.ih[i].mode == 1) {

@@ -215,13 +215,6 @@ struct Ctx {
     uint32_t mis_rounds = 0;
     // host-side bounds of the device loops (0: the built-in bound from V)
     uint32_t lim_bcp_levels = 0, lim_mis_rounds = 0;
-    // stage records of SUB and BVE (elimw.cuh): store, its capacity in words,
-    // and one record offset per elected variable; C_E, L_E of the round
-    uint32_t* rec_store = nullptr;
-    unsigned long long rec_cap = 0;
-    unsigned long long* rec = nullptr;
-    uint64_t rec_slots = 0;
-    uint64_t ve_CE = 0, ve_LE = 0;
     pfg_stats stats{};
     double pass_ms[8] = {0};
 
@@ -283,7 +276,6 @@ bool bcp_prop(Ctx& c);
 // LCVE (lcve.cu) over the active instances; per-instance counts in dout.nelect
 bool lcve(Ctx& c);
 // SUB, BVE, ERE (elim.cu) over c.veset / c.ereset
-bool rec_prepare(Ctx& c);  // stage records of the round's SUB and BVE passes
 bool sub_pass(Ctx& c);
 bool ve_pass(Ctx& c);
 bool ere_pass(Ctx& c);
