@@ -517,14 +517,19 @@ def run_gpu(a, world, rank, local):
     # ---- end-to-end through the C ABI with host buffers ----
     barrier()
     e2e_s, e2e_proc, h2d, d2h = 0.0, 0, 0, 0
-    pcnf = cnf.pinned()     # inputs in page-locked host memory, as for the batch
+    pcnf = cnf.pinned()     # inputs and results in page-locked host memory, as for the batch
+    from parafrost_gb300 import pinned
+    rbuf = pinned.ResultBuffers()
+    sim.upload(pcnf)
+    sim.run()
+    sim.download(into=rbuf)  # sizes the result buffers (untimed)
     gc.collect()
     gc.disable()
     for _ in range(a.steps):
         t1 = time.perf_counter()
         sim.upload(pcnf)
         st = sim.run()
-        res = sim.download()
+        res = sim.download(into=rbuf)
         e2e_s += time.perf_counter() - t1
         e2e_proc += st.clauses_processed
         h2d = cnf.lits.nbytes + cnf.off.nbytes

@@ -96,6 +96,7 @@ struct DevCounters {
     uint32_t pf_blocks;                      // proof blocks reserved in the running pass
     uint32_t mis_done;                       // a MIS round found nothing undecided: later rounds return at once
     uint32_t steal[4];                       // next variable of the warp kernels (SUB, BVE 1, BVE 3)
+    uint32_t ot_long;                        // lists the list passes hand to whole blocks
 };
 
 constexpr uint32_t ERR_UNITS_OVERFLOW = 1u;

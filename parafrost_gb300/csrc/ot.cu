@@ -20,6 +20,11 @@ namespace pfg {
 namespace {
 
 constexpr uint32_t SMALL_MAX = 16;
+// The list passes give a warp 32 consecutive lists; a list longer than this
+// (the hub literals of skewed instances) is handed to a whole block instead,
+// so one warp does not walk it 32 entries at a time while the grid waits.
+constexpr uint32_t OT_LONG = 1024;
+constexpr int LONG_THREADS = 1024;
 constexpr uint32_t WARP_MAX = 64;
 constexpr uint32_t MID_MAX = 2048;
 constexpr int MID_THREADS = 256;
@@ -100,16 +105,23 @@ __global__ void mark_dead_k(const ClsHdr* __restrict__ hdr, uint64_t ncls, uint8
 // by ot_update). `assigned` is then the eliminated-byte array: an eliminated
 // variable's lists are emptied. In place, order kept.
 __global__ void ot_filter_w_k(uint64_t nlist, const uint32_t* __restrict__ off, uint32_t* size, uint32_t* hist,
-                              uint32_t* ids, const uint8_t* __restrict__ assigned, const uint8_t* __restrict__ drop) {
+                              uint32_t* ids, const uint8_t* __restrict__ assigned, const uint8_t* __restrict__ drop,
+                              uint32_t* longs, uint32_t* nlong) {
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < nlist; w += nwarps) {
         const uint64_t l = w * 32 + lane;
         uint32_t n = 0, o = 0;
+        bool is_long = false;
         if (l < nlist) {
             n = size[l];
             if (n && assigned[l >> 1]) n = 0;
             o = off[l];
+            if (n > OT_LONG) {   // ot_filter_long_k filters it
+                longs[atomicAdd(nlong, 1u)] = (uint32_t)l;
+                is_long = true;
+                n = 0;
+            }
         }
         uint32_t incl = n;
 #pragma unroll
@@ -153,7 +165,60 @@ __global__ void ot_filter_w_k(uint64_t nlist, const uint32_t* __restrict__ off, 
                 kept += __popc(bal & m);
             }
         }
-        if (l < nlist) { size[l] = kept; hist[l] = kept; }
+        if (l < nlist && !is_long) { size[l] = kept; hist[l] = kept; }
+    }
+}
+
+// Exclusive prefix of one flag per thread over a block of LONG_THREADS
+// threads; *total gets the block's count. `sh` holds 33 words.
+PFG_D uint32_t block_flag_scan(bool f, uint32_t* sh, uint32_t* total) {
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const unsigned bal = __ballot_sync(0xFFFFFFFFu, f);
+    if (lane == 0) sh[warp] = __popc(bal);
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t v = lane < (blockDim.x >> 5) ? sh[lane] : 0u;
+        uint32_t incl = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= (unsigned)d) incl += t;
+        }
+        sh[lane] = incl - v;
+        if (lane == 31) sh[32] = incl;
+    }
+    __syncthreads();
+    const uint32_t pre = sh[warp] + __popc(bal & ((1u << lane) - 1u));
+    *total = sh[32];
+    __syncthreads();
+    return pre;
+}
+
+// The long lists ot_filter_w_k handed over: one block per list, a tile of
+// LONG_THREADS entries at a time, order kept. In place: a tile's entries are
+// read before any of its kept entries is written, and they go to positions
+// at or before their own.
+__global__ void __launch_bounds__(LONG_THREADS) ot_filter_long_k(const uint32_t* __restrict__ off, uint32_t* size,
+                                                                 uint32_t* hist, uint32_t* ids,
+                                                                 const uint8_t* __restrict__ drop,
+                                                                 const uint32_t* longs, const uint32_t* nlong) {
+    __shared__ uint32_t sh[33];
+    const uint32_t count = *nlong;
+    for (uint32_t b = blockIdx.x; b < count; b += gridDim.x) {
+        const uint32_t l = longs[b];
+        const uint32_t n = size[l], o = off[l];
+        uint32_t kept = 0;
+        for (uint32_t t0 = 0; t0 < n; t0 += blockDim.x) {
+            const uint32_t i = t0 + threadIdx.x;
+            const uint32_t c = i < n ? ids[o + i] : 0u;
+            const bool keep = i < n && !drop[c];
+            uint32_t total;
+            const uint32_t pre = block_flag_scan(keep, sh, &total);   // synchronises after the reads
+            if (keep) ids[o + kept + pre] = c;
+            kept += total;
+        }
+        if (threadIdx.x == 0) { size[l] = kept; hist[l] = kept; }
+        __syncthreads();
     }
 }
 
@@ -176,17 +241,24 @@ __global__ void hist_init_k(uint64_t nlist, const uint32_t* __restrict__ size, c
 __global__ void prune_move_w_k(uint64_t nlist, const uint32_t* __restrict__ off, uint32_t* size, uint32_t* hist,
                                const uint32_t* __restrict__ ids, const uint8_t* __restrict__ elim,
                                const uint8_t* __restrict__ drop, const uint32_t* __restrict__ off2,
-                               uint32_t* __restrict__ ids2, const uint32_t* __restrict__ map, uint32_t* fill) {
+                               uint32_t* __restrict__ ids2, const uint32_t* __restrict__ map, uint32_t* fill,
+                               uint32_t* longs, uint32_t* nlong) {
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < nlist; w += nwarps) {
         const uint64_t l = w * 32 + lane;
         uint32_t n = 0, o = 0, o2 = 0;
+        bool is_long = false;
         if (l < nlist) {
             n = size[l];
             if (n && elim[l >> 1]) n = 0;
             o = off[l];
             o2 = off2[l];
+            if (n > OT_LONG) {   // prune_move_long_k moves it
+                longs[atomicAdd(nlong, 1u)] = (uint32_t)l;
+                is_long = true;
+                n = 0;
+            }
         }
         uint32_t incl = n;
 #pragma unroll
@@ -226,12 +298,47 @@ __global__ void prune_move_w_k(uint64_t nlist, const uint32_t* __restrict__ off,
                 kept += __popc(bal & m);
             }
         }
-        if (l < nlist) {
+        if (l < nlist && !is_long) {
             const uint32_t total = kept + (hist[l] - n);
             size[l] = total;
             hist[l] = total;
             fill[l] = o2 + kept;
         }
+    }
+}
+
+// The long lists prune_move_w_k handed over: one block per list, a tile of
+// LONG_THREADS entries at a time, order kept, into the new layout.
+__global__ void __launch_bounds__(LONG_THREADS) prune_move_long_k(const uint32_t* __restrict__ off, uint32_t* size,
+                                                                  uint32_t* hist, const uint32_t* __restrict__ ids,
+                                                                  const uint8_t* __restrict__ drop,
+                                                                  const uint32_t* __restrict__ off2,
+                                                                  uint32_t* __restrict__ ids2,
+                                                                  const uint32_t* __restrict__ map, uint32_t* fill,
+                                                                  const uint32_t* longs, const uint32_t* nlong) {
+    __shared__ uint32_t sh[33];
+    const uint32_t count = *nlong;
+    for (uint32_t b = blockIdx.x; b < count; b += gridDim.x) {
+        const uint32_t l = longs[b];
+        const uint32_t n = size[l], o = off[l], o2 = off2[l];
+        uint32_t kept = 0;
+        for (uint32_t t0 = 0; t0 < n; t0 += blockDim.x) {
+            const uint32_t i = t0 + threadIdx.x;
+            const uint32_t c = i < n ? ids[o + i] : 0u;
+            const bool keep = i < n && !drop[c];
+            uint32_t total;
+            const uint32_t pre = block_flag_scan(keep, sh, &total);
+            if (keep) ids2[o2 + kept + pre] = map ? map[c] : c;
+            kept += total;
+        }
+        if (threadIdx.x == 0) {
+            // the list's old size n was counted in hist by hist_init_k
+            const uint32_t total = kept + (hist[l] - n);
+            size[l] = total;
+            hist[l] = total;
+            fill[l] = o2 + kept;
+        }
+        __syncthreads();
     }
 }
 
@@ -486,8 +593,11 @@ bool ot_build(Ctx& c) {
 bool ot_filter(Ctx& c, const uint8_t* assigned) {
     PFG_LAUNCH(K_FILL, mark_dead_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.ncls, c.cnew);
     const unsigned lt = tuned(c.tune.list_threads, LIST_THREADS);
+    cudaMemsetAsync(&c.dc->ot_long, 0, sizeof(uint32_t), c.s);
     PFG_LAUNCH(K_FILL, ot_filter_w_k, grid_for((c.nlist + 31) / 32 * 32, lt), lt, 0, c.s, c.nlist, c.ot_off,
-               c.ot_size, c.hist, c.ot_ids, assigned, c.cnew);
+               c.ot_size, c.hist, c.ot_ids, assigned, c.cnew, c.big_lists, &c.dc->ot_long);
+    PFG_LAUNCH(K_FILL, ot_filter_long_k, 2 * sm_count(), LONG_THREADS, 0, c.s, c.ot_off, c.ot_size, c.hist,
+               c.ot_ids, c.cnew, c.big_lists, &c.dc->ot_long);
     return cuda_ok(c, cudaGetLastError(), "ot_filter");
 }
 
@@ -522,8 +632,13 @@ bool ot_update(Ctx& c) {
     // drop bytes are still on the old ids); the flagged clauses are appended
     // behind them
     const unsigned lt = tuned(c.tune.list_threads, LIST_THREADS);
+    const uint8_t* drop = c.cdrop ? c.cdrop : c.cnew;
+    cudaMemsetAsync(&c.dc->ot_long, 0, sizeof(uint32_t), c.s);
     PFG_LAUNCH(K_FILL, prune_move_w_k, grid_for((nl + 31) / 32 * 32, lt), lt, 0, c.s, nl, c.ot_off, c.ot_size,
-               c.hist, c.ot_ids, c.elim, c.cdrop ? c.cdrop : c.cnew, c.ot_off2, c.ot_ids2, c.cmap, c.ot_fill);
+               c.hist, c.ot_ids, c.elim, drop, c.ot_off2, c.ot_ids2, c.cmap, c.ot_fill, c.big_lists,
+               &c.dc->ot_long);
+    PFG_LAUNCH(K_FILL, prune_move_long_k, 2 * sm_count(), LONG_THREADS, 0, c.s, c.ot_off, c.ot_size, c.hist,
+               c.ot_ids, drop, c.ot_off2, c.ot_ids2, c.cmap, c.ot_fill, c.big_lists, &c.dc->ot_long);
     PFG_LAUNCH(K_FILL, fill_new_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.cnew, c.ot_fill,
                c.ot_ids2);
     cudaMemsetAsync(c.cnew, 0, c.ncls, c.s);

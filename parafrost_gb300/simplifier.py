@@ -89,19 +89,24 @@ class Simplifier:
         self._check(rc, "pfg_simplify")
         return st
 
-    def download(self) -> SimplifyResult:
+    def download(self, into=None) -> SimplifyResult:
+        """Results of a one-instance context. `into`: a pinned.ResultBuffers to
+        download into (page-locked, reused across calls; the result's arrays
+        are views into it, valid until the next download into it)."""
         sz = _abi.PfgResultSizes()
         self._check(self.lib.pfg_result_sizes_get(self._ctx, C.byref(sz)), "pfg_result_sizes_get")
-        lits = np.empty(sz.literals, dtype=np.uint32)
-        off = np.empty(sz.clauses + 1, dtype=np.uint64)
-        learnt = np.empty(sz.clauses, dtype=np.uint8)
-        lbd = np.empty(sz.clauses, dtype=np.uint32)
-        usage = np.empty(sz.clauses, dtype=np.uint8)
-        elim = np.empty(sz.max_var + 1, dtype=np.uint8)
-        units = np.empty(sz.units, dtype=np.uint32)
-        pend = np.empty(sz.pending_units, dtype=np.uint32)
-        stack = np.empty(sz.stack_words, dtype=np.uint32)
-        rends = np.empty(sz.rounds, dtype=np.uint64)
+        alloc = (lambda name, k, dt: np.empty(k, dtype=dt)) if into is None else \
+            (lambda name, k, dt: into.get(name, k))
+        lits = alloc("lits", sz.literals, np.uint32)
+        off = alloc("off", sz.clauses + 1, np.uint64)
+        learnt = alloc("learnt", sz.clauses, np.uint8)
+        lbd = alloc("lbd", sz.clauses, np.uint32)
+        usage = alloc("usage", sz.clauses, np.uint8)
+        elim = alloc("elim", sz.max_var + 1, np.uint8)
+        units = alloc("units", sz.units, np.uint32)
+        pend = alloc("pend", sz.pending_units, np.uint32)
+        stack = alloc("stack", sz.stack_words, np.uint32)
+        rends = alloc("rends", sz.rounds, np.uint64)
         rc = self.lib.pfg_download(self._ctx, _ptr(lits, C.c_uint32), _ptr(off, C.c_uint64), _ptr(learnt, C.c_uint8),
                                    _ptr(lbd, C.c_uint32), _ptr(usage, C.c_uint8), _ptr(elim, C.c_uint8),
                                    _ptr(units, C.c_uint32), _ptr(pend, C.c_uint32), _ptr(stack, C.c_uint32),
@@ -118,10 +123,10 @@ class Simplifier:
                               Cnf(sz.max_var, lits, off, learnt, lbd, usage), elim, units, pend, stack, rends, stats,
                               proof[:sz.proof_bytes].tobytes())
 
-    def simplify(self, cnf: Cnf, var_state=None, assumed=None, vorg=None) -> SimplifyResult:
+    def simplify(self, cnf: Cnf, var_state=None, assumed=None, vorg=None, into=None) -> SimplifyResult:
         self.upload(cnf, var_state, assumed, vorg)
         self.run()
-        return self.download()
+        return self.download(into)
 
     # ---- batches: n instances simplified together, results per instance ----
 
