@@ -748,8 +748,6 @@ def run_gpu_batch(a, world, rank, local):
 TRAFFIC = {
     # profiles/ve1w_k_batched.md: 7.447 GB read + 0.932 GB written over the 5 launches of one step
     ("batched", "ve_phase1"): (7.447e9 + 0.932e9) / 5,
-    # profiles/launches_batched_512.md: 32.805 GB read + 15.952 GB written over the 22 launches of one step
-    ("batched", "ot_fill"): (32.805e9 + 15.952e9) / 22,
 }
 
 
