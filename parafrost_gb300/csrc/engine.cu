@@ -1315,10 +1315,31 @@ extern "C" int pfg_download(pfg_ctx* o, uint32_t* lits, uint64_t* cls_off, uint8
     const uint32_t ntrail = c.hout.tcount[0];
     const uint64_t nstack = c.hout.scount[0];
     if (eliminated) cudaMemcpyAsync(eliminated, c.elim, c.V + 1, cudaMemcpyDeviceToHost, c.s);
-    if (units && ntrail) cudaMemcpyAsync(units, c.trail, ntrail * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
+    // forced units ascending: a long trail is radix-sorted on the device (a host
+    // sort of millions of literals costs more than the whole simplify call),
+    // a short one on the host after the copy
+    const uint32_t* usrc = c.trail;
+    bool host_sort = units && ntrail;
+    uint32_t *uk0 = nullptr, *uk1 = nullptr, *uv0 = nullptr, *uv1 = nullptr;
+    if (units && ntrail > 4096) {
+        if (dalloc_t(c, &uk0, ntrail) && dalloc_t(c, &uk1, ntrail) && dalloc_t(c, &uv0, ntrail) &&
+            dalloc_t(c, &uv1, ntrail) && ensure_tmp(c, radix_temp_bytes(ntrail))) {
+            cudaMemcpyAsync(uk0, c.trail, ntrail * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+            cudaMemsetAsync(uv0, 0, ntrail * sizeof(uint32_t), c.s);
+            int bits = 0;
+            while (bits < 32 && ((2ull * c.V + 1) >> bits)) bits++;
+            usrc = radix_sort_pairs(uk0, uv0, uk1, uv1, ntrail, 0, bits, c.tmp, c.s) ? uk1 : uk0;
+            host_sort = false;
+        } else {
+            c.err.clear();   // no room for the sort buffers: sort on the host instead
+        }
+    }
+    if (units && ntrail) cudaMemcpyAsync(units, usrc, ntrail * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     if (stack && nstack) cudaMemcpyAsync(stack, c.stack, nstack * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    if (!cuda_ok(c, cudaStreamSynchronize(c.s), "download")) return finish(c, nullptr, base_launches, PFG_CUDA_ERROR);
-    if (units && ntrail) std::sort(units, units + ntrail);
+    const bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "download");
+    dfree(c, uk0); dfree(c, uk1); dfree(c, uv0); dfree(c, uv1);
+    if (!synced) return finish(c, nullptr, base_launches, PFG_CUDA_ERROR);
+    if (host_sort) std::sort(units, units + ntrail);
     if (pending_units && !h.pending.empty()) {
         std::copy(h.pending.begin(), h.pending.end(), pending_units);
         std::sort(pending_units, pending_units + h.pending.size());

@@ -28,6 +28,9 @@ def hub_instance(seed):
 def test_long_lists_alone(seed):
     res, ref = assert_parity(hub_instance(seed))
     assert len(ref.units) > 10_000 and len(ref.round_ends) >= 3
+    # a trail this long is sorted on the device by pfg_download; the ABI promises ascending units
+    u = np.asarray(res.units)
+    assert np.all(u[1:] > u[:-1])
 
 
 def test_long_lists_in_a_batch():
