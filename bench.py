@@ -746,8 +746,9 @@ def run_gpu_batch(a, world, rank, local):
 # DRAM traffic per launch of the dominant kernel group from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (workload, group).
 TRAFFIC = {
-    # profiles/ve1w_k_batched.md: 7.447 GB read + 0.932 GB written over the 5 launches of one step
-    ("batched", "ve_phase1"): (7.447e9 + 0.932e9) / 5,
+    # profiles/ve1w_k_batched.md: all 5 launches on the 64-instance case move 7.65x their algorithmic
+    # bytes; a full-batch launch has 218.2 MB algorithmic, so 1.669 GB
+    ("batched", "ve_phase1"): 7.645 * 218.2e6,
 }
 
 
