@@ -995,7 +995,7 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         if (act.empty() || !c.err.empty()) break;
         const int times = c.phase + 1;
         // after the first round the table is updated, not rebuilt: pruned on the
-        // old clause ids, then moved (through the compaction map) and completed
+        // old clause ids, then moved (through the compaction words) and completed
         if (c.ot_valid) {
             PassTimer t(c, 0);
             if (!ot_prune(c)) break;
@@ -1007,8 +1007,8 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         {
             PassTimer t(c, 0);
             if (!(c.ot_valid ? ot_update(c) : ot_build(c))) break;
-            dfree(c, c.cmap);
-            c.cmap = nullptr;
+            dfree(c, c.cbits);
+            c.cbits = nullptr;
             c.ot_valid = true;
         }
         bool any_units = false;

@@ -128,8 +128,11 @@ struct Ctx {
     uint32_t* ot_ids2 = nullptr;     // second id array / offsets of the update
     uint64_t ot_cap2 = 0;
     uint32_t* ot_off2 = nullptr;     // nlist + 1
-    uint32_t* cmap = nullptr;        // old clause id -> new id of the last compaction (n + 1)
-    uint8_t* cdrop = nullptr;        // drop bytes on the old clause ids, kept over a compaction
+    // the last compaction, on the old clause ids, one word per 32 ids: bits of
+    // the live clauses, bits of the kept ones (live and not flagged), and the
+    // live clauses before the word's first id (its new id is that plus the
+    // live bits below it); read by the table update, ~1 bit per clause
+    uint4* cbits = nullptr;
     // big-list sort scratch
     uint32_t* big_lists = nullptr;   // nlist (worst case)
     uint32_t* mid_desc = nullptr;    // descriptors (offset, size) pairs
@@ -264,13 +267,13 @@ bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist = nullptr, uint32_t nv = 
 bool ot_filter(Ctx& c, const uint8_t* assigned);   // drop what unit propagation removed from the lists
 // Incremental table between rounds: ot_prune drops deleted and flagged clauses and
 // the lists of eliminated variables (run before a compaction, on the old ids);
-// ot_update then moves the kept entries into a fresh CSR (through cmap when the
+// ot_update then moves the kept entries into a fresh CSR (through cbits when the
 // store was compacted) and appends the flagged clauses.
 bool ot_prune(Ctx& c);
 bool ot_update(Ctx& c);
 // counting + compaction (gc.cu)
 void count_live(Ctx& c);        // totals into counters, per instance into dout.cnt (read after a sync)
-bool compact_cnf(Ctx& c);       // Solver::reallocCNF(true) (cnf.cu:129-144, recycle.cu:60); keeps cmap when ot_valid
+bool compact_cnf(Ctx& c);       // Solver::reallocCNF(true) (cnf.cu:129-144, recycle.cu:60); keeps cbits when ot_valid
 // device BCP (bcp.cu) of the instances flagged in di.bcp; conflicts land in dout.conflict
 bool bcp_prop(Ctx& c);
 // LCVE (lcve.cu) over the active instances; per-instance counts in dout.nelect

@@ -66,6 +66,26 @@ __global__ void compact_k(const ClsHdr* __restrict__ hdr, const uint32_t* __rest
     }
 }
 
+// One word per 32 old clause ids for the table update after a compaction:
+// live bits, kept bits (live and not flagged in the drop bytes), and the new id
+// of the word's first live clause (the exclusive scan of the live flags).
+__global__ void drop_bits_k(const ClsHdr* __restrict__ hdr, const uint8_t* __restrict__ drop,
+                            const uint32_t* __restrict__ pos, uint64_t n, uint4* bits) {
+    const uint64_t nw = (n + 31) / 32;
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += nwarps) {
+        const uint64_t c = w * 32 + lane;
+        bool live = false, keep = false;
+        if (c < n) {
+            live = !m_deleted(hdr[c].meta);
+            keep = live && !drop[c];
+        }
+        const unsigned lb = __ballot_sync(0xFFFFFFFFu, live), kb = __ballot_sync(0xFFFFFFFFu, keep);
+        if (lane == 0) bits[w] = make_uint4(lb, kb, pos[w * 32], 0u);
+    }
+}
+
 }  // namespace
 
 void count_live(Ctx& c) {
@@ -127,18 +147,26 @@ bool compact_cnf(Ctx& c) {
     cudaMemsetAsync(ncnew, 0, clsCap + 1, c.s);
     PFG_LAUNCH(K_COMPACT, compact_k, grid_for(n, 256), 256, 0, c.s, c.hdr, c.lits, n, pos, loff, nhdr, nlits, c.cnew,
                ncnew);
-    // the occurrence-table update renumbers its kept entries through pos
-    dfree(c, c.cmap);
-    c.cmap = nullptr;
-    if (c.ot_valid) c.cmap = pos; else dfree(c, pos);
+    // the occurrence-table update keeps and renumbers its entries through
+    // these words (the drop bytes, c.cnew, are on the old ids)
+    dfree(c, c.cbits);
+    c.cbits = nullptr;
+    if (c.ot_valid) {
+        const uint64_t nw = (n + 31) / 32;
+        if (!dalloc_t(c, &c.cbits, nw + 1)) {
+            dfree(c, nhdr); dfree(c, nlits); dfree(c, ncnew); dfree(c, pos); dfree(c, loff);
+            c.simpstate = PFG_CNFALLOC_FAIL;
+            return false;
+        }
+        cudaMemsetAsync(c.cbits, 0, (nw + 1) * sizeof(uint4), c.s);
+        if (n)
+            PFG_LAUNCH(K_COMPACT, drop_bits_k, grid_for(nw * 32, 256), 256, 0, c.s, c.hdr, c.cnew, pos, n, c.cbits);
+    }
+    dfree(c, pos);
     dfree(c, loff);
     c.prof.bytes[K_COMPACT] += 8 * (c.numLiterals + c.numClauses);
     dfree(c, c.hdr); dfree(c, c.lits);
-    // with a table to update, the old drop bytes (deleted or flagged clauses on
-    // the old ids) are read by its move
-    dfree(c, c.cdrop);
-    c.cdrop = nullptr;
-    if (c.ot_valid) c.cdrop = c.cnew; else dfree(c, c.cnew);
+    dfree(c, c.cnew);
     c.hdr = nhdr; c.lits = nlits; c.cnew = ncnew;
     c.hdr_cap = clsCap + 1; c.lits_cap = phys_lits;
     c.ncls = c.numClauses;

@@ -38,15 +38,32 @@ __global__ void hist_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restric
     }
 }
 
+// One clause's entries: its literals are loaded FILL_BURST at a time and their
+// cursor increments issued together, so the atomics' round trips to L2
+// overlap instead of each one waiting for the previous store.
+constexpr uint32_t FILL_BURST = 8;
+
+PFG_D void fill_clause(const ClsHdr& h, const uint32_t* __restrict__ lits, uint32_t c, uint32_t* fill,
+                       uint32_t* ids) {
+    for (uint32_t k0 = 0; k0 < h.size; k0 += FILL_BURST) {
+        uint32_t l[FILL_BURST], pos[FILL_BURST];
+#pragma unroll
+        for (uint32_t q = 0; q < FILL_BURST; q++) l[q] = k0 + q < h.size ? lits[h.off + k0 + q] : 0u;
+#pragma unroll
+        for (uint32_t q = 0; q < FILL_BURST; q++)
+            if (k0 + q < h.size) pos[q] = atomicAdd(&fill[l[q]], 1u);
+#pragma unroll
+        for (uint32_t q = 0; q < FILL_BURST; q++)
+            if (k0 + q < h.size) ids[pos[q]] = c;
+    }
+}
+
 __global__ void fill_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
                        uint32_t* fill, uint32_t* ids) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         const ClsHdr h = hdr[c];
         if (m_deleted(h.meta)) continue;
-        for (uint32_t k = 0; k < h.size; k++) {
-            const uint32_t pos = atomicAdd(&fill[lits[h.off + k]], 1u);
-            ids[pos] = (uint32_t)c;
-        }
+        fill_clause(h, lits, (uint32_t)c, fill, ids);
     }
 }
 
@@ -68,10 +85,7 @@ __global__ void fill_new_k(const ClsHdr* __restrict__ hdr, const uint32_t* __res
         if (!cnew[c]) continue;
         const ClsHdr h = hdr[c];
         if (m_deleted(h.meta)) continue;
-        for (uint32_t k = 0; k < h.size; k++) {
-            const uint32_t pos = atomicAdd(&fill[lits[h.off + k]], 1u);
-            ids[pos] = (uint32_t)c;
-        }
+        fill_clause(h, lits, (uint32_t)c, fill, ids);
     }
 }
 
@@ -230,9 +244,23 @@ __global__ void hist_init_k(uint64_t nlist, const uint32_t* __restrict__ size, c
         hist[l] = elim[l >> 1] ? 0u : size[l];
 }
 
+// Whether the table update keeps clause c, and its id in the new store: after
+// a compaction from the words of drop_bits_k (kept bit; live clauses before
+// the word plus the live bits below c), else from the drop bytes (id kept).
+PFG_D bool entry_kept(const uint8_t* __restrict__ drop, const uint4* __restrict__ bits, uint32_t c, uint32_t& id) {
+    if (bits) {
+        const uint4 b = bits[c >> 5];
+        const uint32_t bit = c & 31u;
+        id = b.z + __popc(b.x & ((1u << bit) - 1u));
+        return (b.y >> bit) & 1u;
+    }
+    id = c;
+    return !drop[c];
+}
+
 // Prune and move in one pass: the entries of every list that `drop` keeps
 // (not deleted, not flagged) go in order to the list's new offset, renumbered
-// through the compaction map when there is one; an eliminated variable's lists
+// through the compaction words when the store was compacted; an eliminated variable's lists
 // keep nothing. The new offsets were sized for the whole old list, so a list
 // ends with the gap of its dropped entries; its size (and histogram count,
 // which the election reads) becomes the kept entries plus its flagged clauses,
@@ -241,7 +269,7 @@ __global__ void hist_init_k(uint64_t nlist, const uint32_t* __restrict__ size, c
 __global__ void prune_move_w_k(uint64_t nlist, const uint32_t* __restrict__ off, uint32_t* size, uint32_t* hist,
                                const uint32_t* __restrict__ ids, const uint8_t* __restrict__ elim,
                                const uint8_t* __restrict__ drop, const uint32_t* __restrict__ off2,
-                               uint32_t* __restrict__ ids2, const uint32_t* __restrict__ map, uint32_t* fill,
+                               uint32_t* __restrict__ ids2, const uint4* __restrict__ bits, uint32_t* fill,
                                uint32_t* longs, uint32_t* nlong) {
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -285,11 +313,12 @@ __global__ void prune_move_w_k(uint64_t nlist, const uint32_t* __restrict__ off,
                 noj = __shfl_sync(0xFFFFFFFFu, o, nj);
                 nc = e2 < T ? ids[noj + (e2 - nsj)] : 0u;
             }
-            const bool keep = valid && !drop[c];
+            uint32_t id = c;
+            const bool keep = valid && entry_kept(drop, bits, c, id);
             const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
             const uint32_t first = sj > e0 ? sj - e0 : 0u;
             const unsigned mine = ((1u << lane) - 1u) & ~((1u << first) - 1u);
-            if (keep) ids2[o2j + kj + __popc(bal & mine)] = map ? map[c] : c;
+            if (keep) ids2[o2j + kj + __popc(bal & mine)] = id;
             const int64_t a = (int64_t)pre - (int64_t)e0, b = a + (int64_t)n;
             const int lo = a < 0 ? 0 : (a > 32 ? 32 : (int)a);
             const int hi = b < 0 ? 0 : (b > 32 ? 32 : (int)b);
@@ -314,7 +343,7 @@ __global__ void __launch_bounds__(LONG_THREADS) prune_move_long_k(const uint32_t
                                                                   const uint8_t* __restrict__ drop,
                                                                   const uint32_t* __restrict__ off2,
                                                                   uint32_t* __restrict__ ids2,
-                                                                  const uint32_t* __restrict__ map, uint32_t* fill,
+                                                                  const uint4* __restrict__ bits, uint32_t* fill,
                                                                   const uint32_t* longs, const uint32_t* nlong) {
     __shared__ uint32_t sh[33];
     const uint32_t count = *nlong;
@@ -325,10 +354,11 @@ __global__ void __launch_bounds__(LONG_THREADS) prune_move_long_k(const uint32_t
         for (uint32_t t0 = 0; t0 < n; t0 += blockDim.x) {
             const uint32_t i = t0 + threadIdx.x;
             const uint32_t c = i < n ? ids[o + i] : 0u;
-            const bool keep = i < n && !drop[c];
+            uint32_t id = c;
+            const bool keep = i < n && entry_kept(drop, bits, c, id);
             uint32_t total;
             const uint32_t pre = block_flag_scan(keep, sh, &total);
-            if (keep) ids2[o2 + kept + pre] = map ? map[c] : c;
+            if (keep) ids2[o2 + kept + pre] = id;
             kept += total;
         }
         if (threadIdx.x == 0) {
@@ -628,22 +658,21 @@ bool ot_update(Ctx& c) {
         if (!dalloc_t(c, &c.ot_ids2, cap)) { c.simpstate = PFG_OTALLOC_FAIL; c.ot_cap2 = 0; return false; }
         c.ot_cap2 = cap;
     }
-    // kept entries move to the new offsets (renumbered after a compaction, whose
-    // drop bytes are still on the old ids); the flagged clauses are appended
-    // behind them
+    // kept entries move to the new offsets (after a compaction the table is
+    // still on the old ids: which entries stay and their new ids come from
+    // c.cbits, while c.cnew is already on the new ids); the flagged clauses
+    // are appended behind them
     const unsigned lt = tuned(c.tune.list_threads, LIST_THREADS);
-    const uint8_t* drop = c.cdrop ? c.cdrop : c.cnew;
+    const uint8_t* drop = c.cbits ? nullptr : c.cnew;
     cudaMemsetAsync(&c.dc->ot_long, 0, sizeof(uint32_t), c.s);
     PFG_LAUNCH(K_FILL, prune_move_w_k, grid_for((nl + 31) / 32 * 32, lt), lt, 0, c.s, nl, c.ot_off, c.ot_size,
-               c.hist, c.ot_ids, c.elim, drop, c.ot_off2, c.ot_ids2, c.cmap, c.ot_fill, c.big_lists,
+               c.hist, c.ot_ids, c.elim, drop, c.ot_off2, c.ot_ids2, c.cbits, c.ot_fill, c.big_lists,
                &c.dc->ot_long);
     PFG_LAUNCH(K_FILL, prune_move_long_k, 2 * sm_count(), LONG_THREADS, 0, c.s, c.ot_off, c.ot_size, c.hist,
-               c.ot_ids, drop, c.ot_off2, c.ot_ids2, c.cmap, c.ot_fill, c.big_lists, &c.dc->ot_long);
+               c.ot_ids, drop, c.ot_off2, c.ot_ids2, c.cbits, c.ot_fill, c.big_lists, &c.dc->ot_long);
     PFG_LAUNCH(K_FILL, fill_new_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.cnew, c.ot_fill,
                c.ot_ids2);
     cudaMemsetAsync(c.cnew, 0, c.ncls, c.s);
-    dfree(c, c.cdrop);
-    c.cdrop = nullptr;
     std::swap(c.ot_ids, c.ot_ids2);
     std::swap(c.ot_cap, c.ot_cap2);
     std::swap(c.ot_off, c.ot_off2);
