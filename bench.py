@@ -727,7 +727,11 @@ def run_gpu_batch(a, world, rank, local):
         "served_vs_plain": (serving["value"] / plain_value) if serving else None,
         "e2e": {"value": e2e_total / e2e_max, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_max / a.steps,
-                "ms_steps": [round(1000 * t, 2) for t in e2e_steps]},
+                "ms_steps": [round(1000 * t, 2) for t in e2e_steps],
+                "ms_median": round(1000 * statistics.median(e2e_steps), 2),
+                "ms_p90": round(1000 * sorted(e2e_steps)[min(len(e2e_steps) - 1, int(0.9 * len(e2e_steps)))], 2),
+                "spread": "host-link time varies between boxes and calls; median and p90 of the steps beside the "
+                          "mean"},
         "roofline": roofline,
         "gpu_launches": int(launches),
         "kernel_ms": {k: round(v["ms"] / a.steps, 4) for k, v in prof.items() if v["launches"]},
