@@ -172,11 +172,17 @@ __global__ void bcp_propagate_k(BK k, const ClsHdr* hdr, const uint32_t* lits, c
 __global__ void bcp_apply_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls, const uint8_t* st, const uint32_t* vinst,
                             const uint8_t* bcp, const uint32_t* conflict, int multi, unsigned long long* icnt,
                             DevCounters* dc) {
+    const unsigned lane = threadIdx.x & 31u;
+    uint64_t b, e;
+    warp_chunk(ncls, b, e);   // contiguous, so the per-instance counts are run totals
     unsigned long long nc = 0, nl = 0;
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
-        ClsHdr h = hdr[c];
+    InstRun run;
+    for (uint64_t c0 = b; c0 < e; c0 += 32) {
+        const uint64_t c = c0 + lane;
+        ClsHdr h{0, 0, 0, 0};
         uint32_t inst = 0xFFFFFFFFu;
-        if (!m_deleted(h.meta)) {
+        if (c < e) h = hdr[c];
+        if (c < e && !m_deleted(h.meta)) {
             uint32_t* l = lits + h.off;
             inst = vinst[ABSV(l[0])];
             if (h.size && bcp[inst] && !conflict[inst]) {
@@ -196,16 +202,9 @@ __global__ void bcp_apply_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls, const ui
         }
         const bool live = inst != 0xFFFFFFFFu;
         if (live) { nc++; nl += h.size; }
-        if (multi) {
-            const unsigned peers = __match_any_sync(__activemask(), inst);
-            const unsigned a = __reduce_add_sync(peers, live ? 1u : 0u);
-            const unsigned b = __reduce_add_sync(peers, live ? h.size : 0u);
-            if (live && (int)(threadIdx.x & 31u) == __ffs(peers) - 1) {
-                atomicAdd(&icnt[2 * inst], (unsigned long long)a);
-                atomicAdd(&icnt[2 * inst + 1], (unsigned long long)b);
-            }
-        }
+        if (multi) inst_run_add(run, live, inst, live ? h.size : 0u, icnt, lane);
     }
+    if (multi) inst_run_flush(run, icnt, lane);
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
         nc += __shfl_down_sync(0xFFFFFFFFu, nc, d);

@@ -99,6 +99,59 @@ struct DevCounters {
     uint32_t ot_long;                        // lists the list passes hand to whole blocks
 };
 
+// Per-instance clause and literal counts from a warp walking a contiguous
+// chunk of clause ids 32 at a time. The store keeps an instance's clauses in
+// runs, so while a whole step lies in one instance the warp only adds to a
+// running total, which goes to that instance's counters when the run ends; a
+// step that mixes instances is added per instance. A dead lane (deleted
+// clause, or past the chunk) takes the step's first live instance, or the
+// running one. Every lane of the warp calls it with warp-uniform control.
+struct InstRun {
+    uint32_t run = 0xFFFFFFFFu;              // warp-uniform
+    unsigned long long ra = 0, rb = 0;       // clauses, literals of the run
+};
+
+PFG_D void inst_run_flush(InstRun& r, unsigned long long* icnt, unsigned lane) {
+    if (lane == 0 && r.run != 0xFFFFFFFFu && (r.ra || r.rb)) {
+        atomicAdd(&icnt[2 * (uint64_t)r.run], r.ra);
+        atomicAdd(&icnt[2 * (uint64_t)r.run + 1], r.rb);
+    }
+    r.run = 0xFFFFFFFFu;
+    r.ra = r.rb = 0;
+}
+
+PFG_D void inst_run_add(InstRun& r, bool live, uint32_t inst, uint32_t sz, unsigned long long* icnt,
+                        unsigned lane) {
+    constexpr uint32_t NONE = 0xFFFFFFFFu;
+    const unsigned lb = __ballot_sync(0xFFFFFFFFu, live);
+    const uint32_t first = lb ? __shfl_sync(0xFFFFFFFFu, inst, __ffs(lb) - 1) : r.run;
+    const uint32_t key = live ? inst : first;
+    if (r.run != NONE && __all_sync(0xFFFFFFFFu, key == r.run)) {
+        r.ra += __reduce_add_sync(0xFFFFFFFFu, live ? 1u : 0u);
+        r.rb += __reduce_add_sync(0xFFFFFFFFu, live ? sz : 0u);
+        return;
+    }
+    inst_run_flush(r, icnt, lane);
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
+    const unsigned ca = __reduce_add_sync(peers, live ? 1u : 0u);
+    const unsigned cb = __reduce_add_sync(peers, live ? sz : 0u);
+    if (peers == 0xFFFFFFFFu) {              // the whole step is one instance: a new run
+        if (key != NONE) { r.run = key; r.ra = ca; r.rb = cb; }
+    } else if (key != NONE && ca && (int)lane == __ffs(peers) - 1) {
+        atomicAdd(&icnt[2 * (uint64_t)key], (unsigned long long)ca);
+        atomicAdd(&icnt[2 * (uint64_t)key + 1], (unsigned long long)cb);
+    }
+}
+
+// [b, e): the contiguous chunk of n items of the calling warp, 32-aligned
+PFG_D void warp_chunk(uint64_t n, uint64_t& b, uint64_t& e) {
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t per = ((n + nwarps - 1) / nwarps + 31) & ~31ull;
+    b = warp * per;
+    e = b + per < n ? b + per : n;
+}
+
 constexpr uint32_t ERR_UNITS_OVERFLOW = 1u;
 constexpr uint32_t ERR_STACK_OVERFLOW = 2u;
 constexpr uint32_t ERR_SLOT_MISMATCH = 4u;

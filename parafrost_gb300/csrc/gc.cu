@@ -10,32 +10,38 @@
 namespace pfg {
 namespace {
 
-// totals; with several instances also per instance (the instance of a clause
-// is the instance of its literals), summed per warp over equal instances
+// Totals, and with several instances the counts per instance (the instance of
+// a clause is the instance of its literals); a warp takes a contiguous chunk
+// of clause ids so that its per-instance counts are run totals (InstRun).
 __global__ void count_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
                         const uint32_t* __restrict__ vinst, int multi, unsigned long long* icnt, DevCounters* dc) {
+    const unsigned lane = threadIdx.x & 31u;
+    uint64_t b, e;
+    warp_chunk(ncls, b, e);
     unsigned long long nc = 0, nl = 0;
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
-        const ClsHdr h = hdr[c];
-        const bool live = !m_deleted(h.meta);
-        if (live) { nc++; nl += h.size; }
-        if (multi) {
-            const uint32_t inst = live ? vinst[ABSV(lits[h.off])] : 0xFFFFFFFFu;
-            const unsigned peers = __match_any_sync(__activemask(), inst);
-            const unsigned a = __reduce_add_sync(peers, live ? 1u : 0u);
-            const unsigned b = __reduce_add_sync(peers, live ? h.size : 0u);
-            if (inst != 0xFFFFFFFFu && (int)(threadIdx.x & 31u) == __ffs(peers) - 1) {
-                atomicAdd(&icnt[2 * inst], (unsigned long long)a);
-                atomicAdd(&icnt[2 * inst + 1], (unsigned long long)b);
+    InstRun r;
+    for (uint64_t c0 = b; c0 < e; c0 += 32) {
+        const uint64_t c = c0 + lane;
+        bool live = false;
+        uint32_t sz = 0, inst = 0xFFFFFFFFu;
+        if (c < e) {
+            const ClsHdr h = hdr[c];
+            live = !m_deleted(h.meta);
+            if (live) {
+                sz = h.size;
+                if (multi) inst = vinst[ABSV(lits[h.off])];
             }
         }
+        if (live) { nc++; nl += sz; }
+        if (multi) inst_run_add(r, live, inst, sz, icnt, lane);
     }
+    if (multi) inst_run_flush(r, icnt, lane);
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
         nc += __shfl_down_sync(0xFFFFFFFFu, nc, d);
         nl += __shfl_down_sync(0xFFFFFFFFu, nl, d);
     }
-    if ((threadIdx.x & 31u) == 0 && (nc || nl)) {
+    if (lane == 0 && (nc || nl)) {
         atomicAdd(&dc->live_cls, nc);
         atomicAdd(&dc->live_lits, nl);
     }
