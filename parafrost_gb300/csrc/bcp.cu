@@ -265,7 +265,9 @@ bool bcp_prop(Ctx& c) {
     const int multi = c.ninst > 1;
     cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
     if (multi) cudaMemsetAsync(c.dout.cnt, 0, 2 * c.ninst * sizeof(unsigned long long), c.s);
-    c.prof.bytes[K_COUNT] += 8 * c.ncls;
+    // byte model of the rewrite, which also does the count: 4 (L + C), booked
+    // with the kernel under the propagation group
+    c.prof.bytes[K_BCP] += 4 * (c.numLiterals + c.numClauses);
     if (c.ncls)
         PFG_LAUNCH(K_BCP, bcp_apply_k, grid_for(c.ncls, 256, 8), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.bstate, c.vinst,
                    c.di.bcp, c.dout.conflict, multi, c.dout.cnt, c.dc);
