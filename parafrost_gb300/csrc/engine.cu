@@ -94,9 +94,14 @@ bool ensure_tmp_u32(Ctx& c, uint64_t count) {
     return true;
 }
 
+bool stream_sync(Ctx& c, const char* what) {
+    if (c.prof.on) c.prof.close();
+    return cuda_ok(c, cudaStreamSynchronize(c.s), what);
+}
+
 void sync_counters(Ctx& c) {
     cudaMemcpyAsync(c.hc, c.dc, sizeof(DevCounters), cudaMemcpyDeviceToHost, c.s);
-    cuda_ok(c, cudaStreamSynchronize(c.s), "stream synchronize");
+    stream_sync(c, "stream synchronize");
     if (c.err.empty() && c.hc->err) {
         char b[128];
         snprintf(b, sizeof(b), "device error flags 0x%x", c.hc->err);
@@ -151,7 +156,7 @@ size_t inst_out_layout(uint32_t n, char* base, InstOut* p) {
 void push_inst_in(Ctx& c) {
     // the pinned mirror may be rewritten right after this call: wait for the copy
     cudaMemcpyAsync(c.di.voff, c.hi.voff, c.in_bytes, cudaMemcpyHostToDevice, c.s);
-    cuda_ok(c, cudaStreamSynchronize(c.s), "instance inputs");
+    stream_sync(c, "instance inputs");
 }
 
 void pull_inst_out(Ctx& c) {
@@ -191,7 +196,7 @@ bool proof_collect(Ctx& c) {
     c.pf_hb.resize(nb);
     cudaMemcpyAsync(c.pf_hw.data(), c.pf_w, nw * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     cudaMemcpyAsync(c.pf_hb.data(), c.pf_b, nb * sizeof(ulonglong2), cudaMemcpyDeviceToHost, c.s);
-    if (!cuda_ok(c, cudaStreamSynchronize(c.s), "proof copy")) return false;
+    if (!stream_sync(c, "proof copy")) return false;
     // blocks tile [0, nw) in reservation order: their ends are the next starts
     std::vector<ulonglong2>& b = c.pf_hb;
     std::sort(b.begin(), b.end(), [](const ulonglong2& a, const ulonglong2& z) { return a.y < z.y; });
@@ -430,7 +435,8 @@ void free_all(pfg_ctx* o) {
     fresh.s = c.s;
     fresh.tune = c.tune;
     fresh.s_copy = c.s_copy; fresh.ev_copy = c.ev_copy;
-    fresh.ev_begin = c.ev_begin; fresh.ev_end = c.ev_end; fresh.ev_a = c.ev_a; fresh.ev_b = c.ev_b;
+    fresh.ev_begin = c.ev_begin; fresh.ev_end = c.ev_end;
+    fresh.pass_clock = c.pass_clock;
     fresh.dc = nullptr; fresh.hc = c.hc;
     fresh.launches = c.launches;
     fresh.prof = c.prof;
@@ -439,17 +445,14 @@ void free_all(pfg_ctx* o) {
     c = fresh;
 }
 
+// Device time of a pass: an event pair on the engine's stream, read when the
+// call ends (pfg_simplify), so the host does not wait for the device after
+// every pass.
 struct PassTimer {
     Ctx& c;
     int slot;
-    PassTimer(Ctx& cc, int s) : c(cc), slot(s) { cudaEventRecord(c.ev_a, c.s); }
-    ~PassTimer() {
-        cudaEventRecord(c.ev_b, c.s);
-        cudaEventSynchronize(c.ev_b);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, c.ev_a, c.ev_b);
-        c.pass_ms[slot] += ms;
-    }
+    PassTimer(Ctx& cc, int s) : c(cc), slot(s) { c.pass_clock.begin(slot, c.s); }
+    ~PassTimer() { c.pass_clock.end(slot, c.s); }
 };
 
 // Host checks of one instance (literal range, clause size >= 2, no duplicate or
@@ -683,7 +686,7 @@ int upload_impl(pfg_ctx* o, uint32_t n, const pfg_instance* in) {
         PFG_LAUNCH(K_UPLOAD, check_off_k, grid_for(Ctot, 256), 256, 0, c.s, d_off, Ctot, d_base, d_base + n + 1, n,
                    d_bad);
         cudaMemcpyAsync(hbad, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.s);
-        cuda_ok(c, cudaStreamSynchronize(c.s), "upload");
+        stream_sync(c, "upload");
         if (hbad[0] == ~0ull && c.err.empty()) {
             PFG_LAUNCH(K_UPLOAD, init_hdr_k, grid_for(Ctot, 256), 256, 0, c.s, c.hdr, d_off, Ctot, d_learnt, d_lbd,
                        d_usage, d_base, d_base + n + 1, c.di.voff, n, d_vmax, c.lits, d_bad + 1);
@@ -762,7 +765,7 @@ void retire(Ctx& c, const std::vector<uint32_t>& ids) {
                    (const uint32_t*)nullptr, m, total, dout);
         std::vector<uint32_t> all(total);
         cudaMemcpyAsync(all.data(), dout, total * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-        cuda_ok(c, cudaStreamSynchronize(c.s), "pending units");
+        stream_sync(c, "pending units");
         for (uint32_t q = 0; q < m; q++)
             std::copy(all.begin() + db[q], all.begin() + db[q + 1], c.ih[with[q]].pending.begin());
     } else {
@@ -875,7 +878,7 @@ extern "C" int pfg_create(pfg_ctx** out, const pfg_options* opts, size_t arena_b
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); delete o; return PFG_CUDA_ERROR; }
     c.device = dev;
     if (cudaStreamCreateWithFlags(&c.s, cudaStreamNonBlocking) != cudaSuccess) { cudaGetLastError(); delete o; return PFG_CUDA_ERROR; }
-    cudaEventCreate(&c.ev_begin); cudaEventCreate(&c.ev_end); cudaEventCreate(&c.ev_a); cudaEventCreate(&c.ev_b);
+    cudaEventCreate(&c.ev_begin); cudaEventCreate(&c.ev_end);
     // keep freed blocks in the device pool: the pool is the engine's arena
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
@@ -962,7 +965,7 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
     const uint64_t base_launches = g_launches;
     g_prof = &c.prof;
     c.err.clear();
-    for (double& x : c.pass_ms) x = 0;
+    c.pass_clock.reset();
     c.phase = c.multiplier = c.simpstate = 0;
     const uint32_t n = c.ninst;
     cudaEventRecord(c.ev_begin, c.s);
@@ -1205,7 +1208,8 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
     c.stats.literals_out = c.numLiterals;
     c.stats.stack_words = tot_stack;
     c.stats.device_ms = ms;
-    for (int i = 0; i < 8; i++) c.stats.pass_ms[i] = c.pass_ms[i];
+    c.pass_clock.resolve();
+    for (int i = 0; i < 8; i++) c.stats.pass_ms[i] = c.pass_clock.ms[i];
     c.stats.alg_bytes = alg;
     c.stats.kernel_launches = g_launches - base_launches;
     c.stats.eliminated = tot_e;
@@ -1336,7 +1340,7 @@ extern "C" int pfg_download(pfg_ctx* o, uint32_t* lits, uint64_t* cls_off, uint8
     }
     if (units && ntrail) cudaMemcpyAsync(units, usrc, ntrail * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     if (stack && nstack) cudaMemcpyAsync(stack, c.stack, nstack * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    const bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "download");
+    const bool synced = stream_sync(c, "download");
     dfree(c, uk0); dfree(c, uk1); dfree(c, uv0); dfree(c, uv1);
     if (!synced) return finish(c, nullptr, base_launches, PFG_CUDA_ERROR);
     if (host_sort) std::sort(units, units + ntrail);
@@ -1423,7 +1427,7 @@ int build_cache(Ctx& c) {
     PFG_LAUNCH(K_DOWNLOAD, elim_counts_k, grid_for(c.V, 256), 256, 0, c.s, c.elim, c.vinst, c.V, ecnt);
     std::vector<unsigned long long> hcnt(2 * (size_t)n);
     cudaMemcpyAsync(hcnt.data(), ecnt, hcnt.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.s);
-    const bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "batch write-back");
+    const bool synced = stream_sync(c, "batch write-back");
     release();
     dfree(c, ecnt);
     if (!synced) return PFG_CUDA_ERROR;
@@ -1504,7 +1508,7 @@ extern "C" int pfg_batch_download(pfg_ctx* o, uint32_t i, uint32_t* lits, uint64
     if (eliminated) cudaMemcpyAsync(eliminated + 1, c.elim + h.voff + 1, h.V, cudaMemcpyDeviceToHost, c.s);
     if (units && nt) cudaMemcpyAsync(units, c.trail + c.hi.tbase[i], nt * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     if (stack && ns) cudaMemcpyAsync(stack, c.stack + c.hi.sbase[i], ns * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    if (!cuda_ok(c, cudaStreamSynchronize(c.s), "batch download")) return finish(c, nullptr, base_launches, PFG_CUDA_ERROR);
+    if (!stream_sync(c, "batch download")) return finish(c, nullptr, base_launches, PFG_CUDA_ERROR);
     if (cls_off) cls_off[nc] = nl;
     if (eliminated) eliminated[0] = 0;
     if (units && nt) {
@@ -1703,7 +1707,7 @@ extern "C" int pfg_batch_download_all(pfg_ctx* o, uint32_t* lits, uint64_t* cls_
     if (eliminated) cudaMemcpyAsync(eliminated, delim, eb[n], cudaMemcpyDeviceToHost, c.s);
     if (units && ub[n]) cudaMemcpyAsync(units, units_sorted, ub[n] * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
     if (stack && sb[n]) cudaMemcpyAsync(stack, dstack, sb[n] * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    bool synced = cuda_ok(c, cudaStreamSynchronize(c.s), "batch download");
+    bool synced = stream_sync(c, "batch download");
     if (cs != c.s) synced = cuda_ok(c, cudaStreamSynchronize(cs), "batch download copies") && synced;
     release();
     dfree(c, uk1); dfree(c, uv0); dfree(c, uv1);
@@ -1780,6 +1784,7 @@ extern "C" int pfg_profile_get(pfg_ctx* o, int id, uint64_t* launches, double* m
 extern "C" void pfg_destroy(pfg_ctx* o) {
     if (!o) return;
     Ctx& c = o->c;
+    if (g_prof == &c.prof) g_prof = nullptr;   // the calling thread's launches no longer mark this profiler
     std::vector<void*> ptrs;
     for (auto& kv : o->sizes) ptrs.push_back(kv.first);
     for (void* p : ptrs) cudaFreeAsync(p, c.s);
@@ -1788,8 +1793,7 @@ extern "C" void pfg_destroy(pfg_ctx* o) {
     if (c.ev_copy) cudaEventDestroy(c.ev_copy);
     if (c.ev_begin) cudaEventDestroy(c.ev_begin);
     if (c.ev_end) cudaEventDestroy(c.ev_end);
-    if (c.ev_a) cudaEventDestroy(c.ev_a);
-    if (c.ev_b) cudaEventDestroy(c.ev_b);
+    c.pass_clock.destroy();
     if (c.hc) cudaFreeHost(c.hc);
     if (c.in_blob_h) cudaFreeHost(c.in_blob_h);
     if (c.out_blob_h) cudaFreeHost(c.out_blob_h);
@@ -1895,7 +1899,7 @@ extern "C" int pfg_download_device_noalloc(pfg_ctx* o, uint32_t* d_lits, uint64_
     } else if (ooff) {
         cudaMemsetAsync(ooff, 0, sizeof(unsigned long long), c.s);
     }
-    const bool ok = cuda_ok(c, cudaStreamSynchronize(c.s), "allocation-free download");
+    const bool ok = stream_sync(c, "allocation-free download");
     c.launches += g_launches - base_launches;
     return ok ? PFG_OK : PFG_CUDA_ERROR;
 }

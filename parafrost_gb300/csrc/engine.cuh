@@ -84,7 +84,8 @@ struct Ctx {
     cudaStream_t s = nullptr;
     cudaStream_t s_copy = nullptr;   // write-back copies that overlap the last write-back kernels
     cudaEvent_t ev_copy = nullptr;
-    cudaEvent_t ev_begin = nullptr, ev_end = nullptr, ev_a = nullptr, ev_b = nullptr;
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    Profiler pass_clock;          // event pairs around the passes of a call (pass_ms of the stats)
     std::string err;
     uint64_t launches = 0;
     bool uploaded = false;
@@ -219,7 +220,6 @@ struct Ctx {
     // host-side bounds of the device loops (0: the built-in bound from V)
     uint32_t lim_bcp_levels = 0, lim_mis_rounds = 0;
     pfg_stats stats{};
-    double pass_ms[8] = {0};
 
     // batch write-back (built on the first per-instance call): live clauses packed
     // on the device, grouped by instance, literals back in instance numbering and
@@ -254,6 +254,7 @@ inline bool dalloc_t(Ctx& c, T** p, size_t count) { return dalloc(c, (void**)p, 
 bool ensure_tmp(Ctx& c, size_t bytes);
 bool ensure_tmp_u32(Ctx& c, uint64_t count);
 void sync_counters(Ctx& c);     // D2H copy of counters + stream sync
+bool stream_sync(Ctx& c, const char* what);   // closes the profiler's open span, then waits for c.s
 void push_inst_in(Ctx& c);      // H2D copy of the per-instance inputs
 void pull_inst_out(Ctx& c);     // D2H copy of the per-instance outputs and counters + sync
 bool cuda_ok(Ctx& c, cudaError_t e, const char* what);

@@ -650,7 +650,7 @@ bool ot_update(Ctx& c) {
     exclusive_scan_u32(c.hist, c.ot_off2, nl, 0u, c.ot_off2 + nl, c.tmp, c.s);
     uint32_t total = 0;
     cudaMemcpyAsync(&total, c.ot_off2 + nl, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-    if (!cuda_ok(c, cudaStreamSynchronize(c.s), "ot_update")) return false;
+    if (!stream_sync(c, "ot_update")) return false;
     if (c.ot_cap2 < total) {   // the kept entries stay in ot_ids; only the target grows
         dfree(c, c.ot_ids2);
         c.ot_ids2 = nullptr;
@@ -729,7 +729,7 @@ bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist, uint32_t nv) {
         std::vector<uint32_t> hs(nbig + 1);
         cudaMemcpyAsync(hs.data(), bsz, nbig * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
         cudaMemcpyAsync(&hs[nbig], boff + nbig, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.s);
-        if (!cuda_ok(c, cudaStreamSynchronize(c.s), "ot_sort big sizes")) return false;
+        if (!stream_sync(c, "ot_sort big sizes")) return false;
         const uint64_t total = hs[nbig];
         uint32_t maxn = 0;
         for (uint32_t i = 0; i < nbig; i++) maxn = std::max(maxn, hs[i]);

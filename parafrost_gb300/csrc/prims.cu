@@ -12,35 +12,54 @@ const char* const kKernelNames[K_NUM] = {
     "upload", "download", "misc", "bce",
 };
 
-cudaEvent_t Profiler::next_event() {
+uint32_t Profiler::record(cudaStream_t s) {
     if (used == pool.size()) {
         cudaEvent_t e;
         cudaEventCreate(&e);
         pool.push_back(e);
     }
-    return pool[used++];
+    cudaEventRecord(pool[used], s);
+    return (uint32_t)used++;
 }
 
-void Profiler::begin(int id, cudaStream_t s) {
-    marks.push_back(id);
-    cudaEventRecord(next_event(), s);
+void Profiler::launch(int id, cudaStream_t s) {
+    if (open_id == id && open_s == s) return;
+    const uint32_t ev = record(s);
+    if (open_id >= 0) spans.push_back({open_id, open_b, open_s == s ? ev : record(open_s)});
+    open_id = id;
+    open_s = s;
+    open_b = ev;
 }
 
-void Profiler::end(int, cudaStream_t s) { cudaEventRecord(next_event(), s); }
+void Profiler::after(int id) {
+    if (id == K_UPLOAD || id == K_DOWNLOAD) close();
+}
+
+void Profiler::close() {
+    if (open_id < 0) return;
+    spans.push_back({open_id, open_b, record(open_s)});
+    open_id = -1;
+}
+
+void Profiler::begin(int, cudaStream_t s) { pair_b = record(s); }
+
+void Profiler::end(int id, cudaStream_t s) { spans.push_back({id, pair_b, record(s)}); }
 
 void Profiler::resolve() {
-    if (used) cudaEventSynchronize(pool[used - 1]);
-    for (size_t i = 0; i < marks.size(); i++) {
+    close();
+    for (const Span& sp : spans) {
         float t = 0;
-        if (cudaEventElapsedTime(&t, pool[2 * i], pool[2 * i + 1]) == cudaSuccess) ms[marks[i]] += t;
+        cudaEventSynchronize(pool[sp.e]);
+        if (cudaEventElapsedTime(&t, pool[sp.b], pool[sp.e]) == cudaSuccess) ms[sp.id] += t;
         else cudaGetLastError();
     }
-    marks.clear();
+    spans.clear();
     used = 0;
 }
 
 void Profiler::reset() {
-    marks.clear();
+    spans.clear();
+    open_id = -1;
     used = 0;
     for (int i = 0; i < K_NUM; i++) { ms[i] = 0; launches[i] = 0; bytes[i] = 0; }
 }
@@ -48,7 +67,8 @@ void Profiler::reset() {
 void Profiler::destroy() {
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
     pool.clear();
-    marks.clear();
+    spans.clear();
+    open_id = -1;
     used = 0;
 }
 
