@@ -97,6 +97,7 @@ struct DevCounters {
     uint32_t mis_done;                       // a MIS round found nothing undecided: later rounds return at once
     uint32_t steal[4];                       // next variable of the warp kernels (SUB, BVE 1, BVE 3)
     uint32_t ot_long;                        // lists the list passes hand to whole blocks
+    unsigned long long vol_ve[2], vol_ere[2];   // clauses, literals on the elected lists (byte model)
 };
 
 // Per-instance clause and literal counts from a warp walking a contiguous

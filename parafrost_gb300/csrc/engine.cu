@@ -94,9 +94,14 @@ bool ensure_tmp_u32(Ctx& c, uint64_t count) {
     return true;
 }
 
+// The host waits by polling the stream: the round loop waits for a few bytes
+// of counters dozens of times per call, and waking a blocked thread cost more
+// than the device work between two such waits.
 bool stream_sync(Ctx& c, const char* what) {
     if (c.prof.on) c.prof.close();
-    return cuda_ok(c, cudaStreamSynchronize(c.s), what);
+    cudaError_t e;
+    while ((e = cudaStreamQuery(c.s)) == cudaErrorNotReady) {}
+    return cuda_ok(c, e, what);
 }
 
 void sync_counters(Ctx& c) {
@@ -1094,21 +1099,17 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
             if (c.nve && !ot_sort(c, false, c.veset, c.nve)) break;
         }
         if (c.nere) {
-            cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
+            // byte model: the elected lists' clauses and literals, summed on the device
             PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nere, 256), 256, 0, c.s, c.ereset, c.nere, c.hdr,
-                       c.ot_off, c.ot_size, c.ot_ids, &c.dc->live_cls);
-            sync_counters(c);
-            c.prof.bytes[K_ERE] += 4 * (c.hc->live_cls + c.hc->live_lits);
+                       c.ot_off, c.ot_size, c.ot_ids, c.dc->vol_ere);
             PassTimer t(c, 5);
             if (!ere_pass(c)) break;
         }
         if (!nmode1) break;
-        // byte model: C_E, L_E of this round
-        cudaMemsetAsync(&c.dc->live_cls, 0, 2 * sizeof(unsigned long long), c.s);
+        // byte model: C_E, L_E of the round, summed over the rounds on the
+        // device and read when the call ends
         PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nve, 256), 256, 0, c.s, c.veset, c.nve, c.hdr, c.ot_off,
-                   c.ot_size, c.ot_ids, &c.dc->live_cls);
-        sync_counters(c);
-        const uint64_t CE = c.hc->live_cls, LE = c.hc->live_lits;
+                   c.ot_size, c.ot_ids, c.dc->vol_ve);
         uint64_t Cin = 0, Lin = 0;
         for (uint32_t i = 0; i < n; i++)
             if (c.ih[i].mode == 1) {
@@ -1117,8 +1118,6 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
                 c.ih[i].processed_cls += c.ih[i].numClauses;
                 c.ih[i].processed_lits += c.ih[i].numLiterals;
             }
-        c.prof.bytes[K_SUB] += 4 * (LE + CE);
-        c.prof.bytes[K_VE1] += 4 * (LE + CE);
         const uint64_t ncls0 = c.ncls, lits0 = c.lits_used;
         c.stats.clauses_processed += Cin;
         c.stats.literals_processed += Lin;
@@ -1155,8 +1154,8 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         }
         const uint64_t Cres = c.ncls - ncls0, Lres = c.lits_used - lits0;
         c.stats.resolvents += Cres;
-        c.prof.bytes[K_VE3] += 4 * (LE + CE) + 4 * (Lres + Cres);
-        alg += 4 * (Lin + Cin) + 8 * Lin + 8 * (LE + CE) + 4 * (Lres + Cres) + 4 * (c.numLiterals + c.numClauses);
+        c.prof.bytes[K_VE3] += 4 * (Lres + Cres);
+        alg += 4 * (Lin + Cin) + 8 * Lin + 4 * (Lres + Cres) + 4 * (c.numLiterals + c.numClauses);
         c.phase++; c.multiplier++;
         c.multiplier += (c.phase == c.o.phases);
     }
@@ -1187,6 +1186,14 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         }
     }
     pull_inst_out(c);
+    {   // byte model of the elected lists (elected_volume_k), summed over the rounds
+        const uint64_t CE = c.hc->vol_ve[0], LE = c.hc->vol_ve[1];
+        c.prof.bytes[K_SUB] += 4 * (LE + CE);
+        c.prof.bytes[K_VE1] += 4 * (LE + CE);
+        c.prof.bytes[K_VE3] += 4 * (LE + CE);
+        c.prof.bytes[K_ERE] += 4 * (c.hc->vol_ere[0] + c.hc->vol_ere[1]);
+        alg += 8 * (LE + CE);
+    }
     float ms = 0;
     cudaEventElapsedTime(&ms, c.ev_begin, c.ev_end);
     c.simplified = true;
