@@ -16,7 +16,9 @@ request loop (throughput, p50/p99 latency). `tseitin`, `ksat` and
   value : clauses/s with the input resident in HBM when timing starts
           (CUDA events around the engine's rounds on its own stream);
   e2e   : the same metric through the C ABI with host buffers: upload (H2D),
-          simplify and download (D2H) inside the timed region.
+          simplify and download (D2H) inside the timed region (the batch
+          through simplify_batch(streams=4): four runs of instances on four
+          contexts, so one run's copies overlap another's kernels).
 
 `--impl reference` times the reference's own CPU simplifier (Solver::sigmify
 of src/cpu, built by oracle/ref_build.py) on every instance of the same
@@ -656,15 +658,18 @@ def run_gpu_batch(a, world, rank, local):
     # page-locked host memory, uploaded and downloaded inside the timed region ----
     from parafrost_gb300 import pinned
     pcnfs = [c.pinned() for c in cnfs]
-    rbuf = pinned.ResultBuffers()
-    sim.simplify_batch(pcnfs, into=rbuf)          # sizes the result buffers (untimed)
+    # the batch goes through simplify_batch(streams=k): k runs of consecutive
+    # instances on k contexts and host threads, so one run's copies overlap
+    # another's kernels
+    rbufs = [pinned.ResultBuffers() for _ in range(a.e2e_streams)]
+    sim.simplify_batch(pcnfs, into=rbufs, streams=a.e2e_streams)   # sizes the result buffers (untimed)
     e2e_s, e2e_proc, h2d, d2h = 0.0, 0, 0, 0
     e2e_steps = []
     gc.collect()
     gc.disable()     # no collector pause of this process inside the timed calls
     for _ in range(a.steps):
         t1 = time.perf_counter()
-        outs = sim.simplify_batch(pcnfs, into=rbuf)
+        outs = sim.simplify_batch(pcnfs, into=rbufs, streams=a.e2e_streams)
         e2e_steps.append(time.perf_counter() - t1)
         e2e_s += e2e_steps[-1]
         e2e_proc += sum(int(o.stats["clauses_processed"]) for o in outs)
@@ -727,6 +732,7 @@ def run_gpu_batch(a, world, rank, local):
         "served_vs_plain": (serving["value"] / plain_value) if serving else None,
         "e2e": {"value": e2e_total / e2e_max, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_max / a.steps,
+                "streams": a.e2e_streams,
                 "ms_steps": [round(1000 * t, 2) for t in e2e_steps],
                 "ms_median": round(1000 * statistics.median(e2e_steps), 2),
                 "ms_p90": round(1000 * sorted(e2e_steps)[min(len(e2e_steps) - 1, int(0.9 * len(e2e_steps)))], 2),
@@ -768,6 +774,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="batched line: built-in launch shapes instead of the autotuner's")
     ap.add_argument("--serve-jobs", type=int, default=SERVE["jobs"])
+    ap.add_argument("--e2e-streams", type=int, default=4,
+                    help="batched e2e: simplify_batch(streams=k), k contexts overlapping copies and kernels")
     ap.add_argument("--batch-n", type=int, default=None,
                     help="with --single-step or --impl reference: only the first N instances of the batch "
                          "(a small case for profiling and tests)")

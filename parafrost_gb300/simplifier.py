@@ -12,6 +12,7 @@ Every call goes through the C ABI of include/pfgpu.h into the CUDA engine.
 from __future__ import annotations
 
 import ctypes as C
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 from typing import Optional
 
@@ -53,6 +54,24 @@ class SimplifyResult:
         return np.nonzero((e & 1) & ~((e >> 2) & 1))[0].astype(np.uint32)
 
 
+def split_runs(sizes, k: int) -> list:
+    """k runs [b, e) of consecutive indices covering `sizes`, cut where the
+    running total passes j/k of the sum; every run holds at least one index."""
+    n = len(sizes)
+    k = max(1, min(int(k), n))
+    total = float(sum(sizes)) or 1.0
+    cuts, acc, j = [0], 0.0, 1
+    for i, sz in enumerate(sizes):
+        acc += sz
+        while j < k and acc >= total * j / k and i + 1 - cuts[-1] >= 1 and n - (i + 1) >= k - j:
+            cuts.append(i + 1)
+            j += 1
+    while len(cuts) < k:          # too few cuts: split the tail one index at a time
+        cuts.append(n - (k - len(cuts)))
+    cuts.append(n)
+    return [(cuts[i], cuts[i + 1]) for i in range(k)]
+
+
 class Simplifier:
     """One device context (a `pfg_ctx`): one instance, or a batch of instances
     simplified together with per-instance results."""
@@ -61,6 +80,9 @@ class Simplifier:
         self.lib = _lib.lib()
         self.options = _abi.options_from(**options)
         self._ctx = C.c_void_p()
+        self._arena_bytes = arena_bytes
+        self._pool = None          # host threads of simplify_batch(streams > 1)
+        self._peer_ctx = []        # its other contexts
         rc = self.lib.pfg_create(C.byref(self._ctx), C.byref(self.options), arena_bytes)
         if rc != 0:
             raise SimplifyError(rc, "pfg_create failed (is a CUDA device visible?)")
@@ -270,12 +292,65 @@ class Simplifier:
                                       self._proof_of(i, int(sizes[i].proof_bytes))))
         return out
 
-    def simplify_batch(self, cnfs, var_states=None, assumeds=None, vorgs=None, into=None) -> list:
+    def simplify_batch(self, cnfs, var_states=None, assumeds=None, vorgs=None, into=None, streams: int = 1) -> list:
         """Simplify every CNF of `cnfs` in one device store; one result per
-        instance (views into `into`, a pinned.ResultBuffers, when given)."""
-        self.upload_batch(cnfs, var_states, assumeds, vorgs)
-        self.run()
-        return self.download_all(into)
+        instance (views into `into`, a pinned.ResultBuffers, when given).
+
+        streams > 1 splits the batch into that many runs of consecutive
+        instances with about equal clause counts, each simplified by its own
+        context (same options and launch shapes) on its own stream from its
+        own host thread, so one run's host copies overlap another's kernels.
+        Instances are independent, so the results are the ones of one batch.
+        `into` is then a list of pinned.ResultBuffers, one per run."""
+        streams = max(1, min(int(streams), len(cnfs) // 2))
+        if streams == 1:
+            if isinstance(into, (list, tuple)):
+                into = into[0]
+            self.upload_batch(cnfs, var_states, assumeds, vorgs)
+            self.run()
+            return self.download_all(into)
+        runs = split_runs([c.num_clauses for c in cnfs], streams)
+        sims = [self] + self._peers(streams - 1)
+        bufs = list(into) if isinstance(into, (list, tuple)) else [into] + [None] * (streams - 1)
+        if len(bufs) < streams:
+            raise ValueError(f"`into` holds {len(bufs)} result buffers for {streams} runs")
+        pick = lambda seq, b, e: None if seq is None else seq[b:e]
+
+        def work(j):
+            b, e = runs[j]
+            sim = sims[j]
+            sim.upload_batch(cnfs[b:e], pick(var_states, b, e), pick(assumeds, b, e), pick(vorgs, b, e))
+            sim.run()
+            return sim.download_all(bufs[j])
+
+        if self._pool is None or self._pool._max_workers < streams:
+            if self._pool is not None:
+                self._pool.shutdown()
+            self._pool = ThreadPoolExecutor(streams)
+        out = []
+        for part in self._pool.map(work, range(streams)):
+            out.extend(part)
+        return out
+
+    def _peers(self, k: int) -> list:
+        """k more contexts with this one's options and launch shapes (kept for
+        the next calls)."""
+        while len(self._peer_ctx) < k:
+            peer = Simplifier.__new__(Simplifier)
+            peer.lib = self.lib
+            peer.options = self.options
+            peer._ctx = C.c_void_p()
+            peer._pool = None
+            peer._peer_ctx = []
+            peer.last_stats = None
+            rc = self.lib.pfg_create(C.byref(peer._ctx), C.byref(peer.options), self._arena_bytes)
+            if rc != 0:
+                raise SimplifyError(rc, "pfg_create failed")
+            self._peer_ctx.append(peer)
+        tuning = self.tuning
+        for peer in self._peer_ctx[:k]:
+            peer.tuning = tuning
+        return self._peer_ctx[:k]
 
     def profile(self, on: bool = True) -> None:
         """Per-kernel CUDA-event timing of the following simplify calls."""
@@ -306,6 +381,12 @@ class Simplifier:
         return int(self.lib.pfg_kernel_launches(self._ctx))
 
     def close(self) -> None:
+        if getattr(self, "_pool", None) is not None:
+            self._pool.shutdown()
+            self._pool = None
+        for peer in getattr(self, "_peer_ctx", []):
+            peer.close()
+        self._peer_ctx = []
         if self._ctx:
             self.lib.pfg_destroy(self._ctx)
             self._ctx = C.c_void_p()

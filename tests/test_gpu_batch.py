@@ -175,3 +175,34 @@ def test_download_into_pinned_buffers():
                          (a.units, b.units), (a.stack, b.stack), (a.round_ends, b.round_ends)):
                 assert np.array_equal(x, y)
         assert pinned.is_pinned(got[0].cnf.lits)
+
+
+@pytest.mark.parametrize("streams", [2, 3])
+def test_batch_over_several_streams(streams):
+    """simplify_batch(streams=k): k runs of consecutive instances, each on its
+    own context, stream and host thread; every instance as in one batch."""
+    cnfs = [inst(700 + j, scale=1 + (j % 3)) for j in range(10)]
+    vstates = [None] * len(cnfs)
+    vstates[4] = np.zeros(cnfs[4].max_var + 1, dtype=np.uint8)
+    vstates[4][1] = 1
+    with pg.Simplifier() as s:
+        one = s.simplify_batch(cnfs, var_states=vstates)
+        many = s.simplify_batch(cnfs, var_states=vstates, streams=streams)
+        again = s.simplify_batch(cnfs, var_states=vstates, streams=streams)   # the contexts are reused
+    assert len(many) == len(cnfs)
+    for i in range(len(cnfs)):
+        assert not diff(canon(many[i]), canon(one[i])), f"instance {i}"
+        assert not diff(canon(again[i]), canon(one[i])), f"instance {i}"
+        assert many[i].stats["clauses_in"] == cnfs[i].num_clauses
+
+
+def test_batch_over_several_streams_into_pinned_buffers():
+    from parafrost_gb300 import pinned
+    cnfs = [inst(800 + j, scale=2).pinned() for j in range(6)]
+    bufs = [pinned.ResultBuffers() for _ in range(3)]
+    with pg.Simplifier() as s:
+        ref = s.simplify_batch(cnfs)
+        got = s.simplify_batch(cnfs, into=bufs, streams=3)
+    for a, b in zip(got, ref):
+        assert not diff(canon(a), canon(b))
+    assert all(pinned.is_pinned(r.cnf.lits) for r in got if r.cnf.lits.size)
