@@ -167,6 +167,20 @@ int  pfg_upload(pfg_ctx* ctx, uint32_t max_var, uint64_t num_clauses,
  */
 int  pfg_simplify(pfg_ctx* ctx, pfg_stats* stats);
 
+/*
+ * Simplify k uploaded contexts at once: ctxs[0] on the calling thread,
+ * ctxs[1..k) on host threads of their own, every context on its own stream,
+ * so one context's kernels use the GPU while another waits on the host or
+ * runs a narrow pass. The contexts must be distinct and on one device.
+ * stats[j] is what pfg_simplify(ctxs[j], ...) gives; *device_ms (nullable)
+ * is the device time of the whole job, from an event every stream waits on
+ * before its first kernel to the last context's end. Every context runs;
+ * the result is the first code other than PFG_OK in context order.
+ * Replaces: nothing in the reference (one instance per solver): it runs a
+ * batch cut into runs of instances (pfg_batch_upload per context) as one job.
+ */
+int  pfg_simplify_many(pfg_ctx* const* ctxs, uint32_t k, pfg_stats* stats, float* device_ms);
+
 /* Sizes needed by pfg_download. */
 int  pfg_result_sizes_get(pfg_ctx* ctx, pfg_result_sizes* sizes);
 

@@ -8,7 +8,7 @@ from ._abi import (PFG_SAT, PFG_UNKNOWN, PFG_UNSAT, PfgOptions, PfgStats, defaul
                    options_from)
 from .cnf import (Cnf, generate, lit_to_int, int_to_lit, parse_dimacs, random_ksat, read_dimacs, scale_free, tseitin,
                   write_dimacs)
-from .simplifier import SimplifyError, SimplifyResult, Simplifier, proof_text, simplify, simplify_batch
+from .simplifier import SimplifyError, SimplifyResult, Simplifier, proof_text, run_many, simplify, simplify_batch
 from .server import JobInfo, Server
 from .incremental import Incremental
 from .writeback import Mapped, map_result, reconstruct_model
@@ -16,6 +16,6 @@ from .writeback import Mapped, map_result, reconstruct_model
 __all__ = [
     "Cnf", "Simplifier", "SimplifyResult", "SimplifyError", "simplify", "generate", "random_ksat", "tseitin",
     "scale_free", "read_dimacs", "write_dimacs", "lit_to_int", "int_to_lit", "default_options", "options_from",
-    "simplify_batch", "proof_text", "Server", "JobInfo", "parse_dimacs", "Mapped", "map_result", "reconstruct_model",
+    "simplify_batch", "run_many", "proof_text", "Server", "JobInfo", "parse_dimacs", "Mapped", "map_result", "reconstruct_model",
     "options_dict", "Incremental", "PfgOptions", "PfgStats", "PFG_SAT", "PFG_UNSAT", "PFG_UNKNOWN",
 ]

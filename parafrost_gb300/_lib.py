@@ -41,6 +41,8 @@ def lib():
     L.pfg_upload.restype = C.c_int
     L.pfg_simplify.argtypes = [C.c_void_p, C.POINTER(PfgStats)]
     L.pfg_simplify.restype = C.c_int
+    L.pfg_simplify_many.argtypes = [C.POINTER(C.c_void_p), C.c_uint32, C.POINTER(PfgStats), C.POINTER(C.c_float)]
+    L.pfg_simplify_many.restype = C.c_int
     L.pfg_result_sizes_get.argtypes = [C.c_void_p, C.POINTER(PfgResultSizes)]
     L.pfg_result_sizes_get.restype = C.c_int
     L.pfg_download.argtypes = [C.c_void_p, u32p, u64p, u8p, u32p, u8p, u8p, u32p, u32p, u32p, u64p]
@@ -161,6 +163,6 @@ EXPORTED = (
     "pfg_dimacs_read", "pfg_dimacs_get_info", "pfg_dimacs_copy", "pfg_dimacs_error", "pfg_dimacs_free",
     "pfg_map_vars", "pfg_map_lits", "pfg_extend_model", "pfg_download_proof", "pfg_batch_download_proof",
     "pfg_proof_text", "pfg_host_alloc", "pfg_host_free", "pfg_tuning_get", "pfg_tuning_set", "pfg_autotune",
-    "pfg_set_loop_limits",
+    "pfg_set_loop_limits", "pfg_simplify_many",
     "pfg_server_fetch_proof",
 )

@@ -1227,6 +1227,43 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
     return finish(c, st, base_launches, rc);
 }
 
+extern "C" int pfg_simplify_many(pfg_ctx* const* ctxs, uint32_t k, pfg_stats* stats, float* device_ms) {
+    if (!ctxs || !k || !stats) return PFG_INVALID;
+    for (uint32_t j = 0; j < k; j++) {
+        if (!ctxs[j] || ctxs[j]->c.device != ctxs[0]->c.device) return PFG_INVALID;
+        for (uint32_t i = 0; i < j; i++)
+            if (ctxs[i] == ctxs[j]) return PFG_INVALID;
+    }
+    const int dev = ctxs[0]->c.device;
+    if (cudaSetDevice(dev) != cudaSuccess) { cudaGetLastError(); return PFG_CUDA_ERROR; }
+    cudaEvent_t start = nullptr;
+    if (cudaEventCreate(&start) != cudaSuccess) { cudaGetLastError(); return PFG_CUDA_ERROR; }
+    cudaEventRecord(start, ctxs[0]->c.s);
+    for (uint32_t j = 1; j < k; j++) cudaStreamWaitEvent(ctxs[j]->c.s, start, 0);
+    std::vector<int> rc(k, PFG_OK);
+    std::vector<std::thread> th;
+    th.reserve(k - 1);
+    for (uint32_t j = 1; j < k; j++)
+        th.emplace_back([&, j] {
+            if (cudaSetDevice(dev) != cudaSuccess) { cudaGetLastError(); rc[j] = PFG_CUDA_ERROR; return; }
+            rc[j] = pfg_simplify(ctxs[j], &stats[j]);
+        });
+    rc[0] = pfg_simplify(ctxs[0], &stats[0]);
+    for (std::thread& t : th) t.join();
+    float ms = 0;
+    for (uint32_t j = 0; j < k; j++) {
+        if (!ctxs[j]->c.simplified) continue;
+        float t = 0;
+        if (cudaEventElapsedTime(&t, start, ctxs[j]->c.ev_end) == cudaSuccess) ms = std::max(ms, t);
+        else cudaGetLastError();
+    }
+    cudaEventDestroy(start);
+    if (device_ms) *device_ms = ms;
+    for (uint32_t j = 0; j < k; j++)
+        if (rc[j] != PFG_OK) return rc[j];
+    return PFG_OK;
+}
+
 namespace pfg {
 namespace {
 int build_cache(Ctx& c);

@@ -404,6 +404,26 @@ class Simplifier:
             pass
 
 
+def run_many(sims) -> tuple:
+    """pfg_simplify_many over uploaded Simplifiers (distinct contexts): each
+    one's rounds on its own stream and host thread at once. Returns their
+    stats and the device time of the whole job in ms."""
+    sims = list(sims)
+    if not sims:
+        raise ValueError("no contexts")
+    lib = sims[0].lib
+    ctxs = (C.c_void_p * len(sims))(*[s._ctx.value for s in sims])
+    stats = (_abi.PfgStats * len(sims))()
+    ms = C.c_float(0)
+    rc = lib.pfg_simplify_many(ctxs, len(sims), stats, C.byref(ms))
+    for s, st in zip(sims, stats):
+        s.last_stats = st
+    if rc != 0:
+        msgs = [lib.pfg_last_error(s._ctx) for s in sims]
+        raise SimplifyError(rc, "pfg_simplify_many: " + "; ".join(m.decode() for m in msgs if m))
+    return list(stats), float(ms.value)
+
+
 def simplify(cnf: Cnf, **options) -> SimplifyResult:
     with Simplifier(**options) as s:
         return s.simplify(cnf)

@@ -206,3 +206,31 @@ def test_batch_over_several_streams_into_pinned_buffers():
     for a, b in zip(got, ref):
         assert not diff(canon(a), canon(b))
     assert all(pinned.is_pinned(r.cnf.lits) for r in got if r.cnf.lits.size)
+
+
+def test_simplify_many_contexts_at_once():
+    """pfg_simplify_many: runs of a batch uploaded into distinct contexts and
+    simplified at once give every instance's result of one batch; the job's
+    device time covers every context's own."""
+    from parafrost_gb300.simplifier import split_runs
+    cnfs = [inst(900 + j, scale=1 + (j % 2)) for j in range(9)]
+    runs = split_runs([c.num_clauses for c in cnfs], 3)
+    with pg.Simplifier() as s:
+        ref = s.simplify_batch(cnfs)
+        sims = [s] + s._peers(2)
+        for sim, (b, e) in zip(sims, runs):
+            sim.upload_batch(cnfs[b:e])
+        stats, ms = pg.run_many(sims)
+        got = []
+        for sim in sims:
+            got.extend(sim.download_all())
+        assert ms > 0 and ms >= max(st.device_ms for st in stats) - 1e-3
+        assert sum(st.clauses_processed for st in stats) == sum(int(r.stats["clauses_processed"]) for r in ref)
+        # a context named twice is refused before anything runs
+        for sim, (b, e) in zip(sims, runs):
+            sim.upload_batch(cnfs[b:e])
+        with pytest.raises(pg.SimplifyError):
+            pg.run_many([sims[0], sims[0]])
+        stats, ms = pg.run_many(sims)      # still uploaded: the refused call ran nothing
+    for a, b in zip(got, ref):
+        assert not diff(canon(a), canon(b))
