@@ -99,6 +99,20 @@ __global__ void bcp_advance_k(DevCounters* dc) {
 
 // warp per frontier literal, lanes stride its occurrence list
 constexpr uint32_t BCP_GROUP = 32;
+constexpr unsigned FULL = 0xFFFFFFFFu;
+
+// exclusive prefix sum of v over the warp; the warp's sum in `total`
+PFG_D uint32_t bcp_warp_scan(uint32_t v, uint32_t lane, uint32_t& total) {
+    uint32_t incl = v;
+#pragma unroll
+    for (uint32_t d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, incl, d);
+        if (lane >= d) incl += t;
+    }
+    total = __shfl_sync(FULL, incl, 31);
+    return incl - v;
+}
+
 constexpr uint32_t BCP_HEAD = 4;
 
 // one clause of a falsified literal's list: conflict, unit or nothing
@@ -155,14 +169,35 @@ __global__ void bcp_propagate_k(BK k, const ClsHdr* hdr, const uint32_t* lits, c
         const uint32_t o = ot_off[f], sz = ot_size[f];
         for (uint32_t j = lane; j < sz; j += BCP_GROUP) bcp_clause(k, hdr, lits, ot_ids[o + j], inst, nxt);
     }
-    // long lists: every thread of the grid takes a share of each
+    // Long lists: the grid strides over their concatenation, so the entries of
+    // many long lists spread over all threads (starting every list at thread 0
+    // gave the first threads an entry of every list and left the rest idle). A
+    // warp reads 32 lists' bounds at once; the concatenation offsets come from
+    // the list sizes alone, so every thread computes the same ones.
     const uint32_t nl = dc->bcp_lcurr;
-    for (uint32_t li = 0; li < nl; li++) {
-        const uint32_t f = lcur[li];
-        const uint32_t inst = k.vinst[ABSV(f)];
-        if (k.conflict[inst]) continue;
-        const uint32_t o = ot_off[f], sz = ot_size[f];
-        for (uint32_t j = tid; j < sz; j += nthreads) bcp_clause(k, hdr, lits, ot_ids[o + j], inst, nxt);
+    const uint32_t wlane = threadIdx.x & 31u;
+    uint64_t base = 0;
+    for (uint32_t l0 = 0; l0 < nl; l0 += 32) {
+        const uint32_t li = l0 + wlane;
+        uint32_t o = 0, sz = 0, inst = 0;
+        if (li < nl) {
+            const uint32_t f = lcur[li];
+            inst = k.vinst[ABSV(f)];
+            o = ot_off[f];
+            sz = ot_size[f];
+        }
+        uint32_t tot;
+        const uint32_t start = bcp_warp_scan(sz, wlane, tot);
+        const uint32_t cnt = min(32u, nl - l0);
+        for (uint32_t q = 0; q < cnt; q++) {
+            const uint32_t qo = __shfl_sync(FULL, o, q), qs = __shfl_sync(FULL, sz, q);
+            const uint32_t qst = __shfl_sync(FULL, start, q), qi = __shfl_sync(FULL, inst, q);
+            if (k.conflict[qi]) continue;       // this instance is UNSAT: stop propagating it
+            const uint32_t rot = (uint32_t)((base + qst) % nthreads);
+            for (uint32_t j = (tid + nthreads - rot) % nthreads; j < qs; j += nthreads)
+                bcp_clause(k, hdr, lits, ot_ids[qo + j], qi, nxt);
+        }
+        base += tot;
     }
 }
 
