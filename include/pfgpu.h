@@ -104,7 +104,9 @@ typedef struct pfg_stats {
     uint64_t stack_words;     /* model-reconstruction words produced                */
     double   device_ms;       /* cudaEvent time of all rounds (upload/download excluded) */
     double   pass_ms[8];      /* per pass: ot, bcp, lcve, sub, ve, ere, gc/count, other */
-    uint64_t alg_bytes;       /* algorithmic bytes of all rounds (4-byte literal and clause words each pass must move) */
+    uint64_t alg_bytes;       /* algorithmic bytes of all rounds (4-byte literal and clause words each pass must move);
+                                 the elected lists' term 8(L_E + C_E) takes a pass of its own and is counted only
+                                 while the profiler is on (pfg_profile_enable) */
     uint64_t kernel_launches; /* kernels launched by pfg_simplify                   */
 } pfg_stats;
 

@@ -1099,17 +1099,20 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
             if (c.nve && !ot_sort(c, false, c.veset, c.nve)) break;
         }
         if (c.nere) {
-            // byte model: the elected lists' clauses and literals, summed on the device
-            PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nere, 256), 256, 0, c.s, c.ereset, c.nere, c.hdr,
-                       c.ot_off, c.ot_size, c.ot_ids, c.dc->vol_ere);
+            // byte model: the elected lists' clauses and literals, summed on the
+            // device (a pass of its own, so only while the profiler is on)
+            if (c.prof.on)
+                PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nere, 256), 256, 0, c.s, c.ereset, c.nere, c.hdr,
+                           c.ot_off, c.ot_size, c.ot_ids, c.dc->vol_ere);
             PassTimer t(c, 5);
             if (!ere_pass(c)) break;
         }
         if (!nmode1) break;
         // byte model: C_E, L_E of the round, summed over the rounds on the
-        // device and read when the call ends
-        PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nve, 256), 256, 0, c.s, c.veset, c.nve, c.hdr, c.ot_off,
-                   c.ot_size, c.ot_ids, c.dc->vol_ve);
+        // device and read when the call ends (only while the profiler is on)
+        if (c.prof.on)
+            PFG_LAUNCH(K_MISC, elected_volume_k, grid_for(c.nve, 256), 256, 0, c.s, c.veset, c.nve, c.hdr, c.ot_off,
+                       c.ot_size, c.ot_ids, c.dc->vol_ve);
         uint64_t Cin = 0, Lin = 0;
         for (uint32_t i = 0; i < n; i++)
             if (c.ih[i].mode == 1) {

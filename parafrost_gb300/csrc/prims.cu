@@ -113,9 +113,53 @@ __device__ __forceinline__ T block_excl_scan(T v, T& total) {
     return excl;
 }
 
-// Phase 1: scan each tile locally, emit tile totals.
+// Arrays above SCAN_SINGLE_MAX_TILES tiles: reduce, then scan. Phase 1 sums
+// each tile; phase 2 scans the tile sums into tile offsets; phase 3 scans
+// each tile again with its offset. The input is read twice and the output
+// written once (a scan-then-add pass wrote it twice and read it back).
 template <typename T>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_tiles_k(const T* in, T* out, uint64_t n, T* tile_sums) {
+__global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_k(const T* in, uint64_t n, T* tile_sums) {
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    T sum = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
+        if (idx < n) sum += in[idx];
+    }
+    T total;
+    block_excl_scan<T>(sum, total);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// Phase 2: one block scans the tile sums, SCAN_ITEMS consecutive sums per
+// thread, carrying the prefix across chunks of SCAN_TILE sums.
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_sums_k(T* sums, uint64_t nt, T init, T* total_out) {
+    T carry = init;
+    for (uint64_t b = 0; b < nt; b += SCAN_TILE) {
+        const uint64_t first = b + (uint64_t)threadIdx.x * SCAN_ITEMS;
+        T loc[SCAN_ITEMS];
+        T sum = 0;
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; i++) {
+            const T v = first + i < nt ? sums[first + i] : T(0);
+            loc[i] = sum;
+            sum += v;
+        }
+        T tot;
+        const T ex = block_excl_scan<T>(sum, tot);
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; i++)
+            if (first + i < nt) sums[first + i] = carry + ex + loc[i];
+        carry += tot;
+    }
+    if (threadIdx.x == 0 && total_out) *total_out = carry;
+}
+
+// Phase 3: scan each tile locally from its offset (in and out may alias: a
+// block reads its whole tile before it writes).
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_tiles_k(const T* in, T* out, uint64_t n, const T* offsets) {
     const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
     __shared__ T sh[SCAN_TILE];
     // coalesced striped load into shared memory
@@ -133,7 +177,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_tiles_k(const T* in, T* out
         sum += sh[threadIdx.x * SCAN_ITEMS + i];
     }
     T total;
-    const T excl = block_excl_scan<T>(sum, total);
+    const T excl = block_excl_scan<T>(sum, total) + offsets[blockIdx.x];
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; i++) sh[threadIdx.x * SCAN_ITEMS + i] = loc[i] + excl;
     __syncthreads();
@@ -141,34 +185,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_tiles_k(const T* in, T* out
     for (int i = 0; i < SCAN_ITEMS; i++) {
         const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
         if (idx < n) out[idx] = sh[i * SCAN_THREADS + threadIdx.x];
-    }
-    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
-}
-
-// Phase 2: one block scans the tile totals sequentially in chunks.
-template <typename T>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_sums_k(T* sums, uint64_t nt, T init, T* total_out) {
-    T carry = init;
-    for (uint64_t b = 0; b < nt; b += SCAN_THREADS) {
-        const uint64_t i = b + threadIdx.x;
-        const T v = i < nt ? sums[i] : T(0);
-        T tot;
-        const T ex = block_excl_scan<T>(v, tot);
-        if (i < nt) sums[i] = carry + ex;
-        carry += tot;
-    }
-    if (threadIdx.x == 0 && total_out) *total_out = carry;
-}
-
-// Phase 3: add the tile offsets.
-template <typename T>
-__global__ void scan_add_k(T* out, uint64_t n, const T* sums) {
-    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
-    const T add = sums[blockIdx.x];
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; i++) {
-        const uint64_t idx = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
-        if (idx < n) out[idx] += add;
     }
 }
 
@@ -221,9 +237,9 @@ void excl_scan(const T* in, T* out, uint64_t n, T init, T* total_out, void* tmp,
         return;
     }
     T* sums = (T*)tmp;
-    PFG_LAUNCH(K_SCAN, scan_tiles_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, in, out, n, sums);
+    PFG_LAUNCH(K_SCAN, scan_reduce_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, in, n, sums);
     PFG_LAUNCH(K_SCAN, scan_sums_k<T>, 1, SCAN_THREADS, 0, s, sums, nt, init, total_out);
-    PFG_LAUNCH(K_SCAN, scan_add_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, out, n, sums);
+    PFG_LAUNCH(K_SCAN, scan_tiles_k<T>, (unsigned)nt, SCAN_THREADS, 0, s, in, out, n, sums);
 }
 
 // ---------------- radix sort ----------------
