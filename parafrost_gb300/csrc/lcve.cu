@@ -1,8 +1,10 @@
 // Least-constrained variable elections (LCVE).
 //
 // Replaces Solver::varReorder + Solver::LCVE (src/gpu/lcve.cu:221-417):
-//   - scores ps*ns (uint32, assign_scores :221) sorted by (score, var) with the
-//     engine's stable radix sort instead of thrust::sort with GPU_LCV_CMP;
+//   - scores ps*ns (uint32, assign_scores :221) ordered by (score, var) with the
+//     engine's stable radix sort instead of thrust::sort with GPU_LCV_CMP; the
+//     parallel elections order only their candidates, which keeps their
+//     relative order, the only one the rounds read;
 //   - the Luby-style MIS (mis_init_k/mis_round_k/mis_freeze_k :143-209) runs on
 //     a shrinking worklist kept in rank order, so winners are appended in
 //     (round, rank) order -- one legal order of the reference's atomic appends;
@@ -50,12 +52,15 @@ __global__ void oversize_mark_k(const ClsHdr* __restrict__ hdr, const uint32_t* 
     }
 }
 
-__global__ void mis_init_k(const uint32_t* eligible, uint32_t V, uint32_t* rank, uint8_t* mstate,
-                           const uint8_t* vstate, const uint8_t* assumed, const uint32_t* hist,
-                           const uint8_t* oversized, uint32_t pmax, uint32_t nmax, uint32_t maxoccurs, uint8_t* cand,
-                           const uint32_t* vinst, const uint8_t* active) {
-    for (uint32_t ei = blockIdx.x * blockDim.x + threadIdx.x; ei < V; ei += gridDim.x * blockDim.x) {
-        const uint32_t v = eligible[ei];
+// The candidates of an election (mis_init_k, lcve.cu:150-173), in variable
+// order: flag, state and no rank yet; the largest candidate score goes to
+// cmax (the key width of the sort that orders only the candidates).
+__global__ void cand_k(uint32_t V, const uint32_t* scores, uint8_t* mstate, uint32_t* rank, const uint8_t* vstate,
+                       const uint8_t* assumed, const uint32_t* hist, const uint8_t* oversized, uint32_t pmax,
+                       uint32_t nmax, uint32_t maxoccurs, uint8_t* cand, const uint32_t* vinst,
+                       const uint8_t* active, uint32_t* cmax) {
+    uint32_t mx = 0;
+    for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
         uint8_t st = MIS_NONE;
         if (active[vinst[v]] && !vstate[v] && !(assumed && assumed[v])) {
             const uint32_t p = 2 * v, n = p | 1;
@@ -64,9 +69,23 @@ __global__ void mis_init_k(const uint32_t* eligible, uint32_t V, uint32_t* rank,
                 st = MIS_UNDECIDED;
         }
         mstate[v] = st;
-        rank[v] = st == MIS_UNDECIDED ? ei : NO_RANK;
-        cand[ei] = st == MIS_UNDECIDED;
+        rank[v] = NO_RANK;
+        cand[v - 1] = st == MIS_UNDECIDED;
+        if (st == MIS_UNDECIDED) mx = max(mx, scores[v]);
     }
+    for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_down_sync(0xFFFFFFFFu, mx, d));
+    if ((threadIdx.x & 31u) == 0 && mx) atomicMax(cmax, mx);
+}
+
+__global__ void cand_keys_k(const uint32_t* cands, uint32_t n, const uint32_t* scores, uint32_t* keys) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        keys[i] = scores[cands[i]];
+}
+
+// rank = place in the candidates' (score, var) order
+__global__ void cand_rank_k(const uint32_t* cands, uint32_t n, uint32_t* rank) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        rank[cands[i]] = i;
 }
 
 // The first MIS_HEAD literals of a clause are loaded together, then their
@@ -364,18 +383,10 @@ __global__ void mapfrozen_k(const uint32_t* flist, uint32_t V, const uint32_t* v
 bool lcve(Ctx& c) {
     const uint32_t V = c.V;
     const uint32_t ninst = c.ninst;
-    // scores and the (score, var) order
+    // scores (and every variable in variable order in `eligible`)
     cudaMemsetAsync(&c.dc->nfrozen, 0, sizeof(uint32_t), c.s);
     PFG_LAUNCH(K_LCVE, scores_k, grid_for(V, 256), 256, 0, c.s, c.hist, V, c.scores, c.keys_a, c.eligible, c.dc);
-    sync_counters(c);
-    const uint32_t maxscore = c.hc->nfrozen;
-    int bits = 0;
-    while (bits < 32 && (maxscore >> bits)) bits += 8;
     if (!ensure_tmp(c, std::max(radix_temp_bytes(V), scan_temp_bytes(V + 1)))) return false;
-    if (bits) {
-        const int which = radix_sort_pairs(c.keys_a, c.eligible, c.keys_b, c.eligible_b, V, 0, bits, c.tmp, c.s);
-        if (which) cudaMemcpyAsync(c.eligible, c.eligible_b, V * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
-    }
     int ibits = 0;
     while (ibits < 32 && ((ninst - 1) >> ibits)) ibits += 8;
     const uint32_t maxoccurs = c.o.lcve_max_occurs;
@@ -394,11 +405,26 @@ bool lcve(Ctx& c) {
         cudaMemsetAsync(c.winv, 0, V + 1, c.s);
         PFG_LAUNCH(K_LCVE, oversize_mark_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, maxcsize,
                    c.winv);
-        PFG_LAUNCH(K_LCVE, mis_init_k, grid_for(V, 256), 256, 0, c.s, c.eligible, V, c.rank, c.mstate, c.vstate,
-                   c.assumed, c.hist, c.winv, pmax, nmax, maxoccurs, c.flag8, c.vinst, c.di.active);
+        // Only the candidates are put in (score, var) order: the rounds compare
+        // ranks of candidates alone, and the candidates taken in variable order
+        // and sorted stably by score are in the order they have among all
+        // variables sorted by (score, var) (assign_scores + thrust::sort,
+        // lcve.cu:221-300). A candidate's rank is its place in c.work.
+        cudaMemsetAsync(&c.dc->nfrozen, 0, sizeof(uint32_t), c.s);
+        PFG_LAUNCH(K_LCVE, cand_k, grid_for(V, 256), 256, 0, c.s, V, c.scores, c.mstate, c.rank, c.vstate,
+                   c.assumed, c.hist, c.winv, pmax, nmax, maxoccurs, c.flag8, c.vinst, c.di.active, &c.dc->nfrozen);
         select_flagged(c.eligible, c.flag8, c.work, V, &c.dc->nwork, c.vscan, c.tmp, c.s);
         sync_counters(c);
         const uint32_t nwork = c.hc->nwork;
+        const uint32_t cmax = c.hc->nfrozen;    // nfrozen reused as the largest candidate score
+        int cbits = 0;
+        while (cbits < 32 && (cmax >> cbits)) cbits += 8;
+        if (nwork > 1 && cbits) {
+            PFG_LAUNCH(K_LCVE, cand_keys_k, grid_for(nwork, 256), 256, 0, c.s, c.work, nwork, c.scores, c.keys_a);
+            const int which = radix_sort_pairs(c.keys_a, c.work, c.keys_b, c.eligible_b, nwork, 0, cbits, c.tmp, c.s);
+            if (which) cudaMemcpyAsync(c.work, c.eligible_b, nwork * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+        }
+        if (nwork) PFG_LAUNCH(K_LCVE, cand_rank_k, grid_for(nwork, 256), 256, 0, c.s, c.work, nwork, c.rank);
         // Rounds run without compaction; each winner records its round. The host
         // reads the undecided count only every 1, 2, 4 .. 16 rounds.
         uint32_t* mround = c.scores;     // scores are dead once the order is sorted
@@ -416,7 +442,7 @@ bool lcve(Ctx& c) {
                     PFG_LAUNCH(K_MIS_WIN, mis_win_min_k, grid_for(V, mt), mt, 0, c.s, V, c.ot_off, c.ot_size,
                                c.ot_ids, c.tmp_u32, c.rank, c.mstate, c.winv, c.flag8, &c.dc->nwin);
                     PFG_LAUNCH(K_MIS_APPLY, mis_apply_min_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits,
-                               c.ncls, c.tmp_u32, c.eligible, c.flag8, c.frozen, c.mstate, c.rank);
+                               c.ncls, c.tmp_u32, c.work, c.flag8, c.frozen, c.mstate, c.rank);
                     PFG_LAUNCH(K_MIS_APPLY, mis_elect_k, grid_for(V, 256), 256, 0, c.s, V, c.winv, r, mround, c.mstate,
                                c.rank, &c.dc->nwin);
                     continue;
@@ -478,6 +504,15 @@ bool lcve(Ctx& c) {
                        c.varcore);
         }
     } else {
+        // every variable in (score, var) order
+        sync_counters(c);
+        const uint32_t maxscore = c.hc->nfrozen;   // nfrozen reused as the largest score
+        int bits = 0;
+        while (bits < 32 && (maxscore >> bits)) bits += 8;
+        if (bits) {
+            const int which = radix_sort_pairs(c.keys_a, c.eligible, c.keys_b, c.eligible_b, V, 0, bits, c.tmp, c.s);
+            if (which) cudaMemcpyAsync(c.eligible, c.eligible_b, V * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.s);
+        }
         // eligible grouped by instance (stable), so instance i owns positions [voff[i], voff[i+1])
         if (ninst > 1) {
             PFG_LAUNCH(K_LCVE, inst_keys_k, grid_for(V, 256), 256, 0, c.s, c.eligible, V, c.vinst,
