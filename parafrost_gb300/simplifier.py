@@ -12,6 +12,7 @@ Every call goes through the C ABI of include/pfgpu.h into the CUDA engine.
 from __future__ import annotations
 
 import ctypes as C
+import threading
 from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 from typing import Optional
@@ -299,7 +300,9 @@ class Simplifier:
         streams > 1 splits the batch into that many runs of consecutive
         instances with about equal clause counts, each simplified by its own
         context (same options and launch shapes) on its own stream from its
-        own host thread, so one run's host copies overlap another's kernels.
+        own host thread, so one run's host copies overlap another's kernels
+        (the runs are uploaded one after another: the first computes while the
+        next ones are copied up).
         Instances are independent, so the results are the ones of one batch.
         `into` is then a list of pinned.ResultBuffers, one per run."""
         streams = max(1, min(int(streams), len(cnfs) // 2))
@@ -315,11 +318,20 @@ class Simplifier:
         if len(bufs) < streams:
             raise ValueError(f"`into` holds {len(bufs)} result buffers for {streams} runs")
         pick = lambda seq, b, e: None if seq is None else seq[b:e]
+        # the uploads go one after another, so the first run's rounds start while
+        # the later runs are still being copied up (together they would all wait
+        # for the whole batch to cross the host link)
+        uploaded = [threading.Event() for _ in range(streams)]
 
         def work(j):
             b, e = runs[j]
             sim = sims[j]
-            sim.upload_batch(cnfs[b:e], pick(var_states, b, e), pick(assumeds, b, e), pick(vorgs, b, e))
+            try:
+                if j:
+                    uploaded[j - 1].wait()
+                sim.upload_batch(cnfs[b:e], pick(var_states, b, e), pick(assumeds, b, e), pick(vorgs, b, e))
+            finally:
+                uploaded[j].set()
             sim.run()
             return sim.download_all(bufs[j])
 
