@@ -13,8 +13,9 @@
  * take its model back to the original formula (pfg_extend_model, as
  * MODEL::extend, src/gpu/model.cpp:101-160), which is then checked against
  * every original clause. The same CNF also goes once through a two-instance
- * batch (pfg_batch_*) and once through the serving loop (pfg_server_*); both
- * results must equal the single call's.
+ * batch (pfg_batch_*), once into two contexts simplified at once
+ * (pfg_simplify_many) and once through the serving loop (pfg_server_*); every
+ * result must equal the single call's.
  *
  * usage: pfg_solve <in.cnf> <work-dir> [solver [solver options...]]
  * The simplify input and outputs are written to <work-dir>/simp.in and
@@ -321,6 +322,30 @@ int main(int argc, char** argv) {
                   i ? "batch_instance_1" : "batch_instance_0");
         }
         pfg_destroy(b);
+    }
+
+    /* ---- two contexts simplified at once (pfg_simplify_many) ---- */
+    {
+        pfg_ctx* m[2] = {nullptr, nullptr};
+        for (auto& x : m) {
+            rc = pfg_create(&x, &opts, 0);
+            if (rc) return die("pfg_create many", rc, "");
+            rc = pfg_upload(x, cnf.max_var, cnf.size(), cnf.lits.data(), cnf.off.data(), nullptr, nullptr, nullptr,
+                            nullptr, nullptr, nullptr);
+            if (rc) return die("pfg_upload many", rc, pfg_last_error(x));
+        }
+        pfg_stats ms[2];
+        float dev_ms = 0;
+        rc = pfg_simplify_many(m, 2, ms, &dev_ms);
+        if (rc) return die("pfg_simplify_many", rc, pfg_last_error(m[0]));
+        check(dev_ms > 0.0f, "many_device_ms");
+        for (int j = 0; j < 2; j++) {
+            Result r;
+            if (!download(m[j], r)) return die("pfg_download many", 0, pfg_last_error(m[j]));
+            check(r.canonical() == single.canonical() && r.elim == single.elim && ms[j].rounds == st.rounds,
+                  j ? "many_context_1" : "many_context_0");
+            pfg_destroy(m[j]);
+        }
     }
 
     /* ---- one job through the serving loop ---- */
