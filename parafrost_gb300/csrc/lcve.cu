@@ -403,6 +403,7 @@ bool lcve(Ctx& c) {
     if (c.o.lcve_fast) {
         // winv is free until the rounds start: it holds the oversize marks here
         cudaMemsetAsync(c.winv, 0, V + 1, c.s);
+        c.prof.bytes[K_LCVE] += 4 * (c.numLiterals + c.numClauses);   // byte model of the clause-size pass
         PFG_LAUNCH(K_LCVE, oversize_mark_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, maxcsize,
                    c.winv);
         // Only the candidates are put in (score, var) order: the rounds compare

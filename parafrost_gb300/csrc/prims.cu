@@ -227,6 +227,7 @@ constexpr uint64_t SCAN_SINGLE_MAX_TILES = 16;
 
 template <typename T>
 void excl_scan(const T* in, T* out, uint64_t n, T init, T* total_out, void* tmp, cudaStream_t s) {
+    if (g_prof) g_prof->bytes[K_SCAN] += 2 * n * sizeof(T);   // byte model: the input read, the output written
     if (n == 0) {
         if (total_out) cudaMemcpyAsync(total_out, &init, sizeof(T), cudaMemcpyHostToDevice, s);
         return;
@@ -348,6 +349,8 @@ int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uin
     uint32_t* hist = (uint32_t*)tmp;
     void* stmp = (void*)(((uintptr_t)(hist + 256 * nb) + 255) & ~(uintptr_t)255);
     int cur = 0;
+    // byte model: every 8-bit pass reads and writes the (key, value) pairs once
+    if (g_prof) g_prof->bytes[K_RADIX] += 16 * n * (uint64_t)((end_bit - begin_bit + 7) / 8);
     for (int sh = begin_bit; sh < end_bit; sh += 8) {
         const uint32_t* ki = cur ? k1 : k0;
         const uint32_t* vi = cur ? v1 : v0;
@@ -367,6 +370,8 @@ void select_flagged(const uint32_t* in, const uint8_t* flags, uint32_t* out, uin
         cudaMemsetAsync(count_out, 0, sizeof(uint32_t), s);
         return;
     }
+    // byte model: flags and input read (the kept output is not known on the host)
+    if (g_prof) g_prof->bytes[K_SELECT] += 5 * n;
     PFG_LAUNCH(K_SELECT, flags_to_u32_k, grid_for(n, 256), 256, 0, s, flags, scan_buf, n);
     excl_scan<uint32_t>(scan_buf, scan_buf, n, 0u, count_out, tmp, s);
     PFG_LAUNCH(K_SELECT, select_scatter_k, grid_for(n, 256), 256, 0, s, in, flags, scan_buf, out, n);
