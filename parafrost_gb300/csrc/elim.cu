@@ -1260,11 +1260,16 @@ PFG_D bool merge_equals(const EK& k, uint32_t x, const ClsHdr& h1, const ClsHdr&
     return true;
 }
 
+// A resolvent of an instance's variable can only equal a clause of that
+// instance, so only the clauses of the instances running ERE this round
+// (mode 2) go into the table.
 __global__ void ere_table_k(const ClsHdr* __restrict__ hdr, const uint32_t* __restrict__ lits, uint64_t ncls,
-                            uint32_t* table, uint32_t mask) {
+                            const uint32_t* __restrict__ vinst, const uint8_t* __restrict__ mode, uint32_t* table,
+                            uint32_t mask) {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncls; c += (uint64_t)gridDim.x * blockDim.x) {
         const ClsHdr h = hdr[c];
         if (m_deleted(h.meta) || h.size < 2) continue;
+        if (mode[vinst[ABSV(lits[h.off])]] != 2) continue;
         uint32_t s = cls_hash(lits + h.off, h.size) & mask;
         for (uint32_t q = 0; q <= mask; q++) {   // the table has room for every clause twice over
             if (atomicCAS(&table[s], ERE_EMPTY, (uint32_t)c) == ERE_EMPTY) break;
@@ -1647,16 +1652,21 @@ bool bce_pass(Ctx& c) {
 
 bool ere_pass(Ctx& c) {
     if (!c.nere) return true;
-    // hash table of the live clauses, at least twice their number of slots
+    // hash table of the live clauses of the instances running ERE, at least
+    // twice their number of slots
+    uint64_t ncl = 0;
+    for (uint32_t i = 0; i < c.ninst; i++)
+        if (c.ih[i].mode == 2) ncl += c.ih[i].numClauses;
     uint64_t cap = 1024;
-    while (cap < 2 * c.numClauses + 2) cap <<= 1;
+    while (cap < 2 * ncl + 2) cap <<= 1;
     if (cap > (1ull << 32)) { c.err = "ERE table exceeds 2^32 slots"; c.simpstate = PFG_OTALLOC_FAIL; return false; }
     uint32_t* table = nullptr;
     if (!dalloc_t(c, &table, cap)) { c.simpstate = PFG_OTALLOC_FAIL; return false; }
     const uint32_t mask = (uint32_t)(cap - 1);
     if (c.o.proof_en && !proof_prepare(c, 2 * (c.lits_used + c.ncls))) { dfree(c, table); return false; }
     cudaMemsetAsync(table, 0xFF, cap * sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_ERE, ere_table_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, table, mask);
+    PFG_LAUNCH(K_ERE, ere_table_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.vinst, c.di.mode,
+               table, mask);
     PFG_LAUNCH(K_ERE, ere_k, grid_for((uint64_t)c.nere * 32, 128), 128, 0, c.s, make_ek(c), c.ereset, c.nere, table,
                mask);
     dfree(c, table);

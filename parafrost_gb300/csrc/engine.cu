@@ -1096,7 +1096,8 @@ extern "C" int pfg_simplify(pfg_ctx* o, pfg_stats* st) {
         if (c.nere || c.nve) {
             PassTimer t(c, 0);
             if (c.nere && !ot_sort(c, false, c.ereset, c.nere)) break;
-            if (c.nve && !ot_sort(c, false, c.veset, c.nve)) break;
+            // the ERE sort just made every clause's key and no clause changed since
+            if (c.nve && !ot_sort(c, false, c.veset, c.nve, c.nere != 0)) break;
         }
         if (c.nere) {
             // byte model: the elected lists' clauses and literals, summed on the

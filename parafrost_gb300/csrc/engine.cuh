@@ -264,7 +264,9 @@ bool cuda_ok(Ctx& c, cudaError_t e, const char* what);
 bool ot_build(Ctx& c);          // histogram + CSR offsets + unsorted fill (clause order irrelevant)
 // sort lists by OLIST_CMP (key.cuh:67-85) or by clause id: all of them, or the two
 // lists of every variable in vlist[0..nv)
-bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist = nullptr, uint32_t nv = 0);
+// keys_ready: the clause keys of the previous ot_sort call still hold (no
+// clause changed since), so they are not made again
+bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist = nullptr, uint32_t nv = 0, bool keys_ready = false);
 bool ot_filter(Ctx& c, const uint8_t* assigned);   // drop what unit propagation removed from the lists
 // Incremental table between rounds: ot_prune drops deleted and flagged clauses and
 // the lists of eliminated variables (run before a compaction, on the old ids);

@@ -679,7 +679,7 @@ bool ot_update(Ctx& c) {
     return cuda_ok(c, cudaGetLastError(), "ot_update");
 }
 
-bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist, uint32_t nv) {
+bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist, uint32_t nv, bool keys_ready) {
     const uint64_t nl = c.nlist;
     const uint64_t count = vlist ? 2ull * nv : nl;
     // worst case: every list is mid-sized
@@ -702,7 +702,8 @@ bool ot_sort(Ctx& c, bool by_id, const uint32_t* vlist, uint32_t nv) {
         if (!dalloc_t(c, &c.ckeys, cap)) { c.simpstate = PFG_OTALLOC_FAIL; c.ckeys_cap = 0; return false; }
         c.ckeys_cap = cap;
     }
-    PFG_LAUNCH(K_SORT_SMALL, ckeys_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.ckeys, by_id);
+    if (!keys_ready)
+        PFG_LAUNCH(K_SORT_SMALL, ckeys_k, grid_for(c.ncls, 256), 256, 0, c.s, c.hdr, c.lits, c.ncls, c.ckeys, by_id);
     cudaMemsetAsync(&c.dc->nwin, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->big_lists, 0, sizeof(uint32_t), c.s);
     cudaMemsetAsync(&c.dc->sort_warp, 0, sizeof(uint32_t), c.s);
