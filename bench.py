@@ -648,7 +648,7 @@ def run_gpu_batch(a, world, rank, local):
     # every stream waits on to the last context's end) ----
     from parafrost_gb300.simplifier import split_runs
     runs = split_runs([c.num_clauses for c in cnfs], a.streams)
-    sims = [sim] + sim._peers(len(runs) - 1)
+    sims = [sim] + sim.peers(len(runs) - 1)
     for _ in range(2):
         for s_, (b, e) in zip(sims, runs):
             s_.upload_batch(cnfs[b:e])

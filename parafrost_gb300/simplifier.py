@@ -313,7 +313,7 @@ class Simplifier:
             self.run()
             return self.download_all(into)
         runs = split_runs([c.num_clauses for c in cnfs], streams)
-        sims = [self] + self._peers(streams - 1)
+        sims = [self] + self.peers(streams - 1)
         bufs = list(into) if isinstance(into, (list, tuple)) else [into] + [None] * (streams - 1)
         if len(bufs) < streams:
             raise ValueError(f"`into` holds {len(bufs)} result buffers for {streams} runs")
@@ -344,9 +344,10 @@ class Simplifier:
             out.extend(part)
         return out
 
-    def _peers(self, k: int) -> list:
-        """k more contexts with this one's options and launch shapes (kept for
-        the next calls)."""
+    def peers(self, k: int) -> list:
+        """k more contexts with this one's options and launch shapes, owned by
+        this Simplifier (kept for later calls, closed with it): the other runs
+        of simplify_batch(streams=k + 1), or contexts for run_many."""
         while len(self._peer_ctx) < k:
             peer = Simplifier.__new__(Simplifier)
             peer.lib = self.lib

@@ -217,7 +217,7 @@ def test_simplify_many_contexts_at_once():
     runs = split_runs([c.num_clauses for c in cnfs], 3)
     with pg.Simplifier() as s:
         ref = s.simplify_batch(cnfs)
-        sims = [s] + s._peers(2)
+        sims = [s] + s.peers(2)
         for sim, (b, e) in zip(sims, runs):
             sim.upload_batch(cnfs[b:e])
         stats, ms = pg.run_many(sims)
