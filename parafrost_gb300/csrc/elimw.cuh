@@ -1133,6 +1133,14 @@ PFG_D void ws_proof_sub(const EK& k, WS& w, uint32_t x, unsigned lane) {
 // updateOL (subsume.cuh:293-303) on the global list, order kept
 PFG_D void ws_update_ol(const EK& k, WS& w, const Side& L, unsigned lane) {
     __syncwarp();
+    // a list without a deleted or strengthened (molten) clause keeps every
+    // entry in the order it was staged in: nothing to write back
+    bool touched = false;
+    for (uint32_t j = lane; j < L.n; j += 32) {
+        const uint32_t m = w.meta[L.b + j];
+        touched |= m_molten(m) || m_deleted(m);
+    }
+    if (!__any_sync(FULL, touched)) return;
     uint32_t* ol = OLp(k, L.lit);
     uint32_t kept = 0;
     for (uint32_t j0 = 0; j0 < L.n; j0 += 32) {
