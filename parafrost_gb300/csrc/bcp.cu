@@ -228,11 +228,12 @@ __global__ void bcp_apply_k(ClsHdr* hdr, uint32_t* lits, uint64_t ncls, const ui
                     const uint32_t ve = litval(st, lit);
                     if (ve == BCP_TRUE) { sat = true; break; }
                     if (ve == BCP_FALSE) continue;
-                    l[n++] = lit;
+                    if (n != q) l[n] = lit;      // only a clause that lost a literal is rewritten
+                    n++;
                     sig |= MAPHASH(lit);
                 }
                 if (sat) { hdr[c].meta = m_set_st(h.meta, ST_DELETED); inst = 0xFFFFFFFFu; }
-                else { hdr[c].sig = sig; hdr[c].size = n; h.size = n; }
+                else if (n != h.size) { hdr[c].sig = sig; hdr[c].size = n; h.size = n; }
             }
         }
         const bool live = inst != 0xFFFFFFFFu;

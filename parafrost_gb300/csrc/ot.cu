@@ -169,7 +169,9 @@ __global__ void ot_filter_w_k(uint64_t nlist, const uint32_t* __restrict__ off, 
             // lanes of list j in this chunk start at lane max(sj - e0, 0)
             const uint32_t first = sj > e0 ? sj - e0 : 0u;
             const unsigned mine = ((1u << lane) - 1u) & ~((1u << first) - 1u);
-            if (keep) ids[oj + kj + __popc(bal & mine)] = c;
+            // an entry with no dropped entry before it in its list stays where it is
+            const uint32_t to = oj + kj + __popc(bal & mine);
+            if (keep && to != oj + (e - sj)) ids[to] = c;
             // this lane's own list: its entries in this chunk
             const int64_t a = (int64_t)pre - (int64_t)e0, b = a + (int64_t)n;
             const int lo = a < 0 ? 0 : (a > 32 ? 32 : (int)a);
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(LONG_THREADS) ot_filter_long_k(const uint32_t*
             const bool keep = i < n && !drop[c];
             uint32_t total;
             const uint32_t pre = block_flag_scan(keep, sh, &total);   // synchronises after the reads
-            if (keep) ids[o + kept + pre] = c;
+            if (keep && kept + pre != i) ids[o + kept + pre] = c;      // moved entries only
             kept += total;
         }
         if (threadIdx.x == 0) { size[l] = kept; hist[l] = kept; }
