@@ -27,14 +27,17 @@ constexpr uint8_t MIS_NONE = 0, MIS_UNDECIDED = 1, MIS_ELECTED = 2, MIS_FROZEN =
 // neighbour of smaller rank" is one load per neighbour: rank[u] < r
 constexpr uint32_t NO_RANK = 0xFFFFFFFFu;
 
+// keys/vals (the sort's input over every variable) only when given
 __global__ void scores_k(const uint32_t* hist, uint32_t V, uint32_t* scores, uint32_t* keys, uint32_t* vals,
                          DevCounters* dc) {
     uint32_t mx = 0;
     for (uint32_t v = 1 + blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x) {
         const uint32_t s = hist[2 * v] * hist[2 * v + 1];   // uint32 product, as assign_scores
         scores[v] = s;
-        keys[v - 1] = s;
-        vals[v - 1] = v;
+        if (keys) {
+            keys[v - 1] = s;
+            vals[v - 1] = v;
+        }
         mx = max(mx, s);
     }
     for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_down_sync(0xFFFFFFFFu, mx, d));
@@ -53,8 +56,9 @@ __global__ void oversize_mark_k(const ClsHdr* __restrict__ hdr, const uint32_t* 
 }
 
 // The candidates of an election (mis_init_k, lcve.cu:150-173), in variable
-// order: flag, state and no rank yet; the largest candidate score goes to
-// cmax (the key width of the sort that orders only the candidates).
+// order: flag (cand[v], cand[0] stays clear), state and no rank yet; the
+// largest candidate score goes to cmax (the key width of the sort that orders
+// only the candidates).
 __global__ void cand_k(uint32_t V, const uint32_t* scores, uint8_t* mstate, uint32_t* rank, const uint8_t* vstate,
                        const uint8_t* assumed, const uint32_t* hist, const uint8_t* oversized, uint32_t pmax,
                        uint32_t nmax, uint32_t maxoccurs, uint8_t* cand, const uint32_t* vinst,
@@ -70,7 +74,7 @@ __global__ void cand_k(uint32_t V, const uint32_t* scores, uint8_t* mstate, uint
         }
         mstate[v] = st;
         rank[v] = NO_RANK;
-        cand[v - 1] = st == MIS_UNDECIDED;
+        cand[v] = st == MIS_UNDECIDED;
         if (st == MIS_UNDECIDED) mx = max(mx, scores[v]);
     }
     for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_down_sync(0xFFFFFFFFu, mx, d));
@@ -383,9 +387,10 @@ __global__ void mapfrozen_k(const uint32_t* flist, uint32_t V, const uint32_t* v
 bool lcve(Ctx& c) {
     const uint32_t V = c.V;
     const uint32_t ninst = c.ninst;
-    // scores (and every variable in variable order in `eligible`)
+    // scores (and, for the sequential elections, the sort input over every variable)
     cudaMemsetAsync(&c.dc->nfrozen, 0, sizeof(uint32_t), c.s);
-    PFG_LAUNCH(K_LCVE, scores_k, grid_for(V, 256), 256, 0, c.s, c.hist, V, c.scores, c.keys_a, c.eligible, c.dc);
+    PFG_LAUNCH(K_LCVE, scores_k, grid_for(V, 256), 256, 0, c.s, c.hist, V, c.scores,
+               c.o.lcve_fast ? nullptr : c.keys_a, c.o.lcve_fast ? nullptr : c.eligible, c.dc);
     if (!ensure_tmp(c, std::max(radix_temp_bytes(V), scan_temp_bytes(V + 1)))) return false;
     int ibits = 0;
     while (ibits < 32 && ((ninst - 1) >> ibits)) ibits += 8;
@@ -414,7 +419,8 @@ bool lcve(Ctx& c) {
         cudaMemsetAsync(&c.dc->nfrozen, 0, sizeof(uint32_t), c.s);
         PFG_LAUNCH(K_LCVE, cand_k, grid_for(V, 256), 256, 0, c.s, V, c.scores, c.mstate, c.rank, c.vstate,
                    c.assumed, c.hist, c.winv, pmax, nmax, maxoccurs, c.flag8, c.vinst, c.di.active, &c.dc->nfrozen);
-        select_flagged(c.eligible, c.flag8, c.work, V, &c.dc->nwork, c.vscan, c.tmp, c.s);
+        cudaMemsetAsync(c.flag8, 0, 1, c.s);   // variable 0
+        select_flagged(nullptr, c.flag8, c.work, V + 1, &c.dc->nwork, c.vscan, c.tmp, c.s);   // the flagged v
         sync_counters(c);
         const uint32_t nwork = c.hc->nwork;
         const uint32_t cmax = c.hc->nfrozen;    // nfrozen reused as the largest candidate score

@@ -87,8 +87,9 @@ void exclusive_scan_u64(const unsigned long long* in, unsigned long long* out, u
 int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint64_t n,
                      int begin_bit, int end_bit, void* tmp, cudaStream_t s);
 
-// Stable compaction: out[j] = in[i] for flags[i] != 0 in order; *count_out
-// (device) = number kept. `scan_buf` holds n+1 uint32.
+// Stable compaction: out[j] = in[i] for flags[i] != 0 in order (i itself
+// when in is null); *count_out (device) = number kept. `scan_buf` holds n+1
+// uint32.
 void select_flagged(const uint32_t* in, const uint8_t* flags, uint32_t* out, uint64_t n,
                     uint32_t* count_out, uint32_t* scan_buf, void* tmp, cudaStream_t s);
 
