@@ -1187,6 +1187,34 @@ PFG_D void ws_sub_screen(WS& w, const Side& P, const Side& N, unsigned lane) {
     __syncwarp();
 }
 
+// The candidates of one side in list order (subsume.cuh:424-455): up to the
+// first clause above SUB_MAX_CL_SIZE (the list is sorted by size), those not
+// deleted that passed the screen. Processing a candidate changes only that
+// clause (strengthened or deleted) and earlier ones (a subsuming learnt clause
+// turned original), so the candidates are known before the first one runs and
+// are taken from one ballot per 32 clauses.
+PFG_D void ws_sub_side(WS& w, const Side& L, const Side& O, uint32_t x, uint32_t fx, uint32_t& nUnits,
+                       unsigned lane) {
+    for (uint32_t i0 = 0; i0 < L.n; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        bool big = false, cand = false;
+        if (i < L.n) {
+            const uint32_t c = L.b + i;
+            big = w.size[c] > SUB_MAX_CL_SIZE;
+            cand = !big && !m_deleted(w.meta[c]) && w.outs[c];
+        }
+        const unsigned bigm = __ballot_sync(FULL, big);
+        unsigned cm = __ballot_sync(FULL, cand);
+        if (bigm) cm &= (1u << (__ffs(bigm) - 1)) - 1u;
+        for (; cm; cm &= cm - 1) {
+            const uint32_t j = i0 + (uint32_t)__ffs(cm) - 1;
+            ws_selfsubsume(w, x, fx, O, L.b + j, nUnits, lane);
+            ws_subsume(w, L, j, L.b + j, lane);
+        }
+        if (bigm) break;
+    }
+}
+
 __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* elected, uint32_t nelected,
                                                         uint32_t* big, uint32_t* nbig, uint32_t* steal) {
     __shared__ WS stage[WS_WARPS];
@@ -1204,20 +1232,8 @@ __global__ void __launch_bounds__(WS_WARPS * 32) subw_k(EK k, const uint32_t* el
         const Side P{0, w.np, p}, N{w.np, w.nn, n};
         ws_sub_screen(w, P, N, lane);
         uint32_t nPos = 0, nNeg = 0;
-        for (uint32_t i = 0; i < P.n; i++) {
-            const uint32_t c = P.b + i;
-            if (w.size[c] > SUB_MAX_CL_SIZE) break;
-            if (m_deleted(w.meta[c]) || !w.outs[c]) continue;
-            ws_selfsubsume(w, p, n, N, c, nPos, lane);
-            ws_subsume(w, P, i, c, lane);
-        }
-        for (uint32_t i = 0; i < N.n; i++) {
-            const uint32_t c = N.b + i;
-            if (w.size[c] > SUB_MAX_CL_SIZE) break;
-            if (m_deleted(w.meta[c]) || !w.outs[c]) continue;
-            ws_selfsubsume(w, n, p, P, c, nNeg, lane);
-            ws_subsume(w, N, i, c, lane);
-        }
+        ws_sub_side(w, P, N, p, n, nPos, lane);
+        ws_sub_side(w, N, P, n, p, nNeg, lane);
         __syncwarp();
         if ((nPos || nNeg) && lane == 0) {
             if (nPos) for (uint32_t i = 0; i < P.n; i++) if (w.size[P.b + i] == 1) push_unit(k, WL(w, P.b + i)[0]);
